@@ -1,0 +1,238 @@
+/*
+ * tianxin_gb300.h -- C-ABI of the GB300-native finite-element assembly path.
+ *
+ * The library replaces, for the Residual and Jacobian evaluation types, the
+ * Tianxin/Panzer volume-assembly path:
+ *
+ *   Cartesian topology      CartesianConnManager::initialize / buildConnectivity
+ *                           (dof-mgr/test/cartesian_topology/CartesianConnManager.cpp:159-331)
+ *   DOF numbering           DOFManager::buildGlobalUnknowns
+ *                           (dof-mgr/src/Panzer_DOFManager.cpp:449-716)
+ *   CRS graph               TpetraLinearObjFactory::buildGhostedGraph
+ *                           (disc-fe/src/lof/Panzer_TpetraLinearObjFactory_impl.hpp:559-651)
+ *   evaluation (f, W)       ModelEvaluator::evalModelImpl_basic -> AssemblyEngine::evaluate
+ *                           (disc-fe/src/Panzer_ModelEvaluator_impl.hpp:1714-1882,
+ *                            disc-fe/src/Panzer_AssemblyEngine_impl.hpp:65-182)
+ *   Dirichlet rows          TianXin::DirichletEvalautor<Jacobian>::evaluateFields
+ *                           (disc-fe/src/evaluators/TianXin_Dirichlet_impl.hpp:55-81)
+ *   SpMV                    Tpetra::CrsMatrix::apply as called by Belos
+ *                           (adapters-stk/example/PoissonExample/main.cpp:402-419)
+ *
+ * Conventions
+ *   - All vector/matrix pointers passed to compute entry points are DEVICE
+ *     pointers owned by the caller (like the Tpetra container views that
+ *     GatherSolution/ScatterResidual borrow in preEvaluate).  They are
+ *     borrowed for the duration of the call only.
+ *   - f and the CRS values are SUMMED INTO; the caller zeroes them first,
+ *     exactly as ModelEvaluator does before AssemblyEngine::evaluate
+ *     (disc-fe/src/Panzer_ModelEvaluator_impl.hpp:1788-1789).
+ *   - Every entry point returns 0 on success or a TX_E* status; the message
+ *     is available from tx_last_error().  A handle is not thread safe; all
+ *     work of a handle is ordered on the handle's CUDA stream.
+ *   - Row/column indices are local ids (LIDs): the position of a DOF in the
+ *     owned (+ghosted) list.  The CRS layout is Tpetra's local layout after
+ *     fillComplete: rowptr int64[N+1], colind int32[nnz] ascending per row.
+ */
+#ifndef TIANXIN_GB300_H
+#define TIANXIN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define TX_OK 0
+#define TX_EINVAL 22     /* bad argument / shape                            */
+#define TX_ERANGE 34     /* index or size out of range                      */
+#define TX_ENOMEM 12     /* device or host allocation failed                */
+#define TX_ETIMEDOUT 110 /* a bounded device wait gave up                   */
+#define TX_ECUDA 1000    /* CUDA runtime error                              */
+#define TX_ESTATE 1001   /* call out of order (e.g. eval before dof_build)  */
+
+/* ------------------------------------------------------------- limits */
+#define TX_MAX_BLOCKS 8
+#define TX_MAX_FIELDS 3
+
+/* Element topology of the bricks of a block (CartesianConnManager elemTopo:
+ * Hexahedron<8>, or Tetrahedron<4> = each brick split into 6 tets). */
+enum tx_topology { TX_TOPO_HEX = 0, TX_TOPO_TET = 1 };
+
+/* Equation sets.  POISSON follows Example::PoissonEquationSet
+ * (adapters-stk/example/PoissonExample/Example_PoissonEquationSet_impl.hpp:
+ * 135-188); MAXWELL follows mini-em's curl-curl + sigma mass
+ * (mini-em/src/eqn_sets/MiniEM_EquationSet_Maxwell_impl.hpp:74-245).
+ * ELASTICITY, HEAT (k(T) field multiplier) and ELASTODYNAMICS have no
+ * equation set in the reference; they are built from the same integrators
+ * (GradBasisDotVector with a stress/flux closure, BasisTimesScalar). */
+enum tx_physics {
+  TX_PHYS_POISSON = 1,        /* field U: k grad u.grad v + c u v - s v (+ udot v)     */
+  TX_PHYS_ELASTICITY = 2,     /* fields UX,UY,UZ: sigma(u):grad v - b.v (+ rho udd.v)  */
+  TX_PHYS_HEAT = 3,           /* field T: (k0 + k2 T^2) grad T.grad v - q v             */
+  TX_PHYS_MAXWELL = 5         /* field E (edges): curl E.curl v / mu + sigma E.v - J.v  */
+};
+
+/* Basis family per block (IntrepidBasisFactory names in brackets). */
+enum tx_basis {
+  TX_HGRAD_C1 = 1, /* HEX: HGRAD_HEX_C1 (8)  TET: HGRAD_TET_C1 (4)  */
+  TX_HGRAD_C2 = 2, /* HEX: HGRAD_HEX_C2 (27) TET: HGRAD_TET_C2 (10) */
+  TX_HCURL_I1 = 3  /* HEX: HCURL_HEX_I1 (12 edges)                  */
+};
+
+/* Brick lattice, CartesianConnManager::initialize(comm, nx,ny,nz, px,py,pz,
+ * bx,by,bz, elemTopo) on one rank.  Blocks are enumerated in the
+ * reference's getElementBlockIds order: eblock-i_j_k with i slowest. */
+typedef struct tx_mesh_desc {
+  int32_t nx, ny, nz;                   /* bricks per block per direction           */
+  int32_t bx, by, bz;                   /* blocks per direction                     */
+  int32_t block_topology[TX_MAX_BLOCKS];/* tx_topology per block                    */
+  double lx, ly, lz;                    /* domain [0,lx]x[0,ly]x[0,lz]              */
+  double jitter;                        /* interior vertices moved U(-j,j)*h        */
+  uint64_t seed;                        /* jitter seed                              */
+} tx_mesh_desc;
+
+/* Equation set: fields follow from the physics (field order is
+ * alphabetical, DOFManagerFactory, disc-fe/src/Panzer_DOFManagerFactory.cpp:82-94). */
+typedef struct tx_equation_set_desc {
+  int32_t physics;                      /* tx_physics                               */
+  int32_t block_basis[TX_MAX_BLOCKS];   /* tx_basis per block                       */
+  int32_t integration_order[TX_MAX_BLOCKS]; /* cubature degree per block; <=0: default
+                                           (HEX C1: 2, HEX C2: 4, TET: 2, HCURL: 2)  */
+  int32_t source_kind;                  /* see TX_SOURCE_*                          */
+  double params[8];                     /* physics coefficients, see below          */
+} tx_equation_set_desc;
+/* params:
+ *  POISSON        [0] k  [1] reaction c  [2] transient multiplier (udot term)
+ *                 [3] source constant
+ *  ELASTICITY     [0] E  [1] nu  [2..4] body force  [5] rho (mass term on the
+ *                 time-derivative vector, see TX_FLAG notes)
+ *  HEAT           [0] k0 [1] k2 [2] q
+ *  MAXWELL        [0] 1/mu [1] sigma   (J is read from tx_eval_args.aux)    */
+enum tx_source {
+  TX_SOURCE_CONST = 0,     /* s = params[3] (POISSON)                           */
+  TX_SOURCE_SINE = 1,      /* s = 3 pi^2 sin(pi x) sin(pi y) sin(pi z)          */
+  TX_SOURCE_AFFINE = 2     /* s = c*(1 + x + 2y + 3z)  (patch/reproduction test)*/
+};
+
+/* Evaluation flags. */
+#define TX_EVAL_MIXED 0x1u          /* FP32 element contractions, FP64 scatter   */
+#define TX_EVAL_DETERMINISTIC 0x2u  /* fixed summation order (no atomics)       */
+
+typedef struct tx_eval_args {
+  const double* x;         /* solution, LID order (GED "... - X")                       */
+  const double* x_dot;     /* time derivative (GED "... - Xdot"); may be NULL           */
+  const double* aux;       /* DOF-indexed auxiliary input (MAXWELL: J coefficients)     */
+  double alpha, beta, t;   /* d/d x_dot seed, d/d x seed, time                          */
+  double* f;               /* residual (summed into); NULL: no residual                 */
+  double* crs_vals;        /* Jacobian values (summed into); NULL: Residual type only   */
+  int32_t block;           /* -1: every block                                           */
+  int64_t elem_begin;      /* workset range inside the block (block >= 0)               */
+  int64_t elem_end;        /* -1: to the end of the block                               */
+  uint32_t flags;          /* TX_EVAL_*                                                 */
+} tx_eval_args;
+
+typedef struct tx_handle_s* tx_handle;
+
+/* -------------------------------------------------------------- setup */
+/* CartesianConnManager::initialize (CartesianConnManager.cpp:159-294). */
+int tx_mesh_create(const tx_mesh_desc* desc, tx_handle* out);
+void tx_destroy(tx_handle h);
+const char* tx_last_error(tx_handle h);
+
+/* Mesh sizes: bricks, elements, vertices (global), blocks. */
+int tx_mesh_sizes(tx_handle h, int64_t* n_elements, int64_t* n_vertices, int32_t* n_blocks);
+/* Vertex coordinates, node GID order, xyz interleaved (host array of 3*n_vertices). */
+int tx_mesh_coordinates(tx_handle h, double* xyz_host);
+/* Element ids of a block in the block's element order (ConnManager::getElementBlock). */
+int tx_mesh_block_elements(tx_handle h, int32_t block, int64_t* n, int64_t* elems_host);
+
+/* DOFManager::buildGlobalUnknowns (Panzer_DOFManager.cpp:449-716) for the
+ * fields of an equation set, plus the CRS graph pattern
+ * (TpetraLinearObjFactory::buildGhostedGraph) and the device-side maps. */
+int tx_dof_build(tx_handle h, const tx_equation_set_desc* eqset);
+
+/* N = owned DOFs, ndof_max = largest element GID count, nnz of the graph,
+ * n_fields of the equation set. */
+int tx_dof_sizes(tx_handle h, int64_t* n_dofs, int32_t* ndof_max, int64_t* nnz, int32_t* n_fields);
+/* GlobalIndexer::getOwnedIndices: owned_[LID] = GID (host array of N). */
+int tx_dof_owned_gids(tx_handle h, int64_t* gids_host);
+/* GlobalIndexer::getElementGIDs / getElementLIDs for every element of a block
+ * (host arrays n_block_elems x getElementBlockGIDCount(block)). */
+int tx_dof_element_gids(tx_handle h, int32_t block, int64_t* gids_host);
+int tx_dof_element_lids(tx_handle h, int32_t block, int32_t* lids_host);
+int tx_dof_block_gid_count(tx_handle h, int32_t block, int32_t* count);
+/* GlobalIndexer::getGIDFieldOffsets(blockId, fieldNum) (Panzer_FieldAggPattern.cpp:369-413). */
+int tx_dof_field_offsets(tx_handle h, int32_t block, int32_t field, int32_t* n, int32_t* offsets_host);
+
+/* Dirichlet DOF set: LIDs (sorted, unique; PointEvaluatorBase std::set,
+ * TianXin_PointEvaluator_impl.hpp:104,196-202) of the fields in field_mask
+ * living on entities that lie on the box sides in side_mask
+ * (bit 0 x=0, 1 x=lx, 2 y=0, 3 y=ly, 4 z=0, 5 z=lz).  Call with lids_host
+ * NULL to get the count. */
+int tx_dirichlet_dofs(tx_handle h, uint32_t side_mask, uint32_t field_mask, int64_t* n, int32_t* lids_host);
+
+/* Graph (Tpetra local layout) into caller DEVICE arrays rowptr[N+1], colind[nnz]. */
+int tx_graph_build(tx_handle h, int64_t* rowptr, int32_t* colind);
+
+/* -------------------------------------------------------------- compute */
+/* ModelEvaluator::evalModel for f and W, volume fill only
+ * (AssemblyEngine::evaluateVolume, Panzer_AssemblyEngine_impl.hpp:134-182):
+ * gather -> IntegrationValues2/BasisValues2 -> integrators -> scatter.
+ * crs_vals == NULL gives the Residual evaluation type.  Uses the handle's
+ * graph (rowptr/colind of tx_graph_build). */
+int tx_eval(tx_handle h, const tx_eval_args* args);
+
+/* DirichletEvalautor<Jacobian>/<Residual>: f[d] = x[d] - g[i];
+ * Jacobian rows d -> unit rows (columns untouched, pivot 1.0;
+ * TianXin_Dirichlet_impl.hpp:75-81, Tpetra
+ * applyDirichletBoundaryConditionToLocalMatrixRows).  lids/g are DEVICE
+ * arrays of n entries; g may be NULL (g = 0).  f or crs_vals may be NULL. */
+int tx_dirichlet_apply(tx_handle h, int64_t n, const int32_t* lids, const double* g,
+                       const double* x, double* f, double* crs_vals);
+
+/* y = alpha*A*x + beta*y over a Tpetra-layout CRS (CrsMatrix::apply).
+ * vals/x/y are FP64 (TX_SPMV_F64) or FP32 (TX_SPMV_F32). */
+#define TX_SPMV_F64 0
+#define TX_SPMV_F32 1
+int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowptr,
+            const int32_t* colind, const void* vals, const void* x, void* y,
+            double alpha, double beta);
+
+/* Solve A dx = b with FP64 iterative refinement around an FP32 Jacobi-CG
+ * inner solve.  A is the FP64 Tpetra-layout Jacobian (Dirichlet rows unit);
+ * the outer residual is either r = b - A x (FP64 SpMV) or, with
+ * TX_SOLVE_MATRIX_FREE_RESIDUAL, r = -f(x) from an FP64 Residual evaluation
+ * of the handle's equation set plus the Dirichlet residual x_d - g_d.
+ * x must satisfy the Dirichlet values on entry (the corrections at those
+ * rows are then zero); dirichlet lids (device) are eliminated symmetrically
+ * for the CG solve.  Relative residuals are taken against ||r(x0)||.
+ * On return stats[0] = outer iterations, stats[1] = total inner CG
+ * iterations, stats[2] = final ||r||/||b||. */
+#define TX_SOLVE_MATRIX_FREE_RESIDUAL 0x1u
+typedef struct tx_solve_args {
+  const int64_t* rowptr; const int32_t* colind; const double* vals;
+  const double* b;         /* right-hand side (ignored with MATRIX_FREE: b = -f(x0)) */
+  double* x;               /* in: initial guess / state, out: solution        */
+  int64_t n_dirichlet; const int32_t* dirichlet_lids;
+  const double* dirichlet_g; /* Dirichlet values (device, n_dirichlet) or NULL = 0 */
+  double rtol;             /* outer relative residual target, e.g. 1e-10      */
+  double inner_rtol;       /* inner FP32 CG relative tolerance, e.g. 1e-5     */
+  int32_t max_outer, max_inner;
+  uint32_t flags;          /* TX_SOLVE_*                                      */
+  const double* x_dot;     /* state for MATRIX_FREE residuals (may be NULL)   */
+  double alpha, beta, t;   /* coefficients for MATRIX_FREE residuals          */
+  double stats[4];
+} tx_solve_args;
+int tx_solve_cg_ir(tx_handle h, tx_solve_args* args);
+
+/* Stream the handle's work is ordered on (cudaStream_t as void*); set NULL
+ * to use the legacy default stream. */
+int tx_set_stream(tx_handle h, void* stream);
+int tx_synchronize(tx_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TIANXIN_GB300_H */

@@ -1,0 +1,143 @@
+"""The oracle against the reference's own known answers (CPU only).
+
+Each test restates one of the reference's unit tests on the oracle:
+  Q1 mass matrix       adapters-stk/test/model_evaluator/model_evaluator_mass_check.cpp:195-211
+  two-hex integrals    disc-fe/test/evaluator_tests/integrator_scalar.cpp:393-410,500-501
+  first IP coordinate  disc-fe/test/core_tests/integration_values2.cpp:103-110
+  hex27 sub-cell map   dof-mgr/test/dofmngr_test/tIntrepidFieldPattern.cpp:527-573
+  scatter pattern      adapters-stk/test/evaluator_tests/tpetra_scatter_residual.cpp:281-305
+  reproduction         dof-mgr/test/fe_assembly/test_fe_assembly_HEX.hpp:672-677 (||b-Ax|| <= 1e-10)
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tianxin_gb300 import _abi as A
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def dense(o, vals):
+    rp, ci = o.graph()
+    M = np.zeros((o.n_dofs, o.n_dofs))
+    for r in range(o.n_dofs):
+        M[r, ci[rp[r]:rp[r + 1]]] = vals[rp[r]:rp[r + 1]]
+    return M
+
+
+def unit_hex_mass():
+    # transient Poisson term only (k = 0, c = 0, udot multiplier 1): W = alpha*M with alpha=1, beta=0
+    o = O.Oracle(A.mesh_desc(1), A.equation_set(A.TX_PHYS_POISSON, params=(0.0, 0.0, 1.0, 0.0)))
+    _, v = o.evaluate(np.zeros(o.n_dofs), np.zeros(o.n_dofs), alpha=1.0, beta=0.0)
+    M = dense(o, v)
+    # node positions by LID to classify neighbours
+    X = o.dof_coordinates()
+    return M, X
+
+
+def test_mass_matrix_known_answer_3d():
+    M, X = unit_hex_mass()
+    for i in range(8):
+        for j in range(8):
+            d = int(round(np.abs(X[i] - X[j]).sum()))  # lattice distance 0..3
+            expect = {0: 1 / 27, 1: 1 / 54, 2: 1 / 108, 3: 1 / 216}[d]
+            assert abs(M[i, j] - expect) <= 1e-15 * 1 / 27
+
+
+def test_mass_matrix_known_answer_reference_2d_values():
+    # Summing the unit-cube hex mass over its two z-layers gives the unit-square
+    # Q1 mass of the reference test: 1/9 diagonal, 1/18 edge, 1/36 opposite.
+    M, X = unit_hex_mass()
+    bottom = [i for i in range(8) if X[i, 2] == 0.0]
+    top_of = {i: [j for j in range(8) if X[j, 2] == 1.0 and np.allclose(X[j, :2], X[i, :2])][0] for i in bottom}
+    g = json.load(open(os.path.join(GOLDEN, "reference_known_answers.json")))["q1_mass_2d"]
+    for i in bottom:
+        for j in bottom:
+            m2 = M[i, j] + M[i, top_of[j]] + M[top_of[i], j] + M[top_of[i], top_of[j]]
+            d = int(round(np.abs(X[i] - X[j]).sum()))
+            expect = {0: g["diag"], 1: g["edge"], 2: g["opposite"]}[d]
+            assert m2 == pytest.approx(expect, rel=1e-15, abs=0)
+
+
+def test_two_hex_integrals():
+    g = json.load(open(os.path.join(GOLDEN, "reference_known_answers.json")))["two_hex"]
+    for X, expect in zip(g["coords"], g["integral_2x_length"]):
+        wdet, _ = O.cell_values(A.TX_TOPO_HEX, g["quad_order"], np.array(X, float))
+        assert 2.0 * wdet.sum() == pytest.approx(expect, rel=1e-15)
+
+
+def test_first_integration_point():
+    X = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    _, ip = O.cell_values(A.TX_TOPO_HEX, 2, X)
+    assert len(ip) == 8
+    expect = (1.0 / np.sqrt(3.0) + 1.0) / 2.0
+    assert np.allclose(ip[0], expect, rtol=1e-8, atol=0)
+
+
+def test_hex27_subcell_map():
+    g = json.load(open(os.path.join(GOLDEN, "reference_known_answers.json")))["hex27_subcells"]
+    for dim, name in ((0, "nodes"), (1, "edges"), (2, "faces"), (3, "cell")):
+        got = [O.basis_subcell(A.TX_TOPO_HEX, A.TX_HGRAD_C2, dim, c) for c in range(len(g[name]))]
+        assert got == g[name]
+
+
+def test_partition_of_unity_and_gradients():
+    rng = np.random.default_rng(0)
+    for topo, basis in ((A.TX_TOPO_HEX, A.TX_HGRAD_C1), (A.TX_TOPO_HEX, A.TX_HGRAD_C2), (A.TX_TOPO_TET, A.TX_HGRAD_C1),
+                        (A.TX_TOPO_TET, A.TX_HGRAD_C2)):
+        for _ in range(5):
+            xi = rng.uniform(-1, 1, 3) if topo == A.TX_TOPO_HEX else rng.dirichlet([1, 1, 1, 1])[1:]
+            v, g = O.basis_eval(topo, basis, xi)
+            assert v.sum() == pytest.approx(1.0, abs=1e-14)
+            assert np.allclose(g.sum(axis=0), 0.0, atol=1e-13)
+
+
+def test_nedelec_tangential_moments():
+    # each lowest-order edge function has unit tangential moment on its own edge, zero on the others
+    edges = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7)]
+    V = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]],
+                 float)
+    s, w = np.polynomial.legendre.leggauss(3)
+    for k, (a, b) in enumerate(edges):
+        t = V[b] - V[a]
+        mom = np.zeros(12)
+        for sj, wj in zip(s, w):
+            val, _ = O.basis_eval(A.TX_TOPO_HEX, A.TX_HCURL_I1, V[a] + (sj + 1) / 2 * t)
+            mom += wj / 2 * val @ t
+        expect = np.zeros(12)
+        expect[k] = 1.0
+        assert np.allclose(mom, expect, atol=1e-14)
+
+
+def test_scatter_pattern_counts():
+    # constant source on an undistorted mesh: every hex8 basis integrates to h^3/8,
+    # so f = -s h^3/8 * (number of elements sharing the node): v, 2v, 4v or 8v
+    n = 3
+    o = O.Oracle(A.mesh_desc(n), A.equation_set(A.TX_PHYS_POISSON, params=(0.0, 0.0, 0.0, 1.0)))
+    f, _ = o.evaluate(np.zeros(o.n_dofs), jacobian=False)
+    v = -(1.0 / n) ** 3 / 8
+    ratio = f / v
+    assert set(np.round(ratio).astype(int)) == {1, 2, 4, 8}
+    assert np.allclose(ratio, np.round(ratio), rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("topo,basis", [(A.TX_TOPO_HEX, A.TX_HGRAD_C1), (A.TX_TOPO_HEX, A.TX_HGRAD_C2),
+                                        (A.TX_TOPO_TET, A.TX_HGRAD_C1), (A.TX_TOPO_TET, A.TX_HGRAD_C2)])
+def test_reproduction_of_in_space_solution(topo, basis):
+    # -lap u + u = f with u = 1 + x + 2y + 3z (in every space here), Dirichlet u on the boundary:
+    # the nodal interpolant solves the discrete system, so f(u_h) = b - A u_h = 0 (test_fe_assembly_HEX)
+    m = A.mesh_desc((2, 3, 2), topology=topo, jitter=0.15, seed=7)
+    q = A.equation_set(A.TX_PHYS_POISSON, basis, params=(1.0, 1.0, 0.0, 0.0), source_kind=A.TX_SOURCE_AFFINE,
+                       integration_order=4 if topo == A.TX_TOPO_HEX else 2)
+    if topo == A.TX_TOPO_TET and basis == A.TX_HGRAD_C1:
+        pass
+    o = O.Oracle(m, q)
+    X = o.dof_coordinates()
+    u = 1 + X[:, 0] + 2 * X[:, 1] + 3 * X[:, 2]
+    f, vals = o.evaluate(u)
+    bd = o.dirichlet_dofs(A.ALL_SIDES)
+    o.dirichlet_apply(bd, u[bd], u, f, vals)
+    assert np.linalg.norm(f) <= 1e-10 * np.linalg.norm(u)

@@ -1,0 +1,75 @@
+"""Loader for libtianxin_gb300.so (the in-tree CUDA library) and its C-ABI.
+
+There is no CPU fallback: if the library cannot be built or loaded, every
+entry point raises.
+"""
+import ctypes as C
+import os
+
+from . import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libtianxin_gb300.so")
+
+# name -> (restype, argtypes); mirrors include/tianxin_gb300.h
+P, I32, I64, U32, D = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32, C.c_double
+SIGNATURES = {
+    "tx_mesh_create": (C.c_int, [C.POINTER(_abi.MeshDesc), C.POINTER(P)]),
+    "tx_destroy": (None, [P]),
+    "tx_last_error": (C.c_char_p, [P]),
+    "tx_mesh_sizes": (C.c_int, [P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I32)]),
+    "tx_mesh_coordinates": (C.c_int, [P, P]),
+    "tx_mesh_block_elements": (C.c_int, [P, I32, C.POINTER(I64), P]),
+    "tx_dof_build": (C.c_int, [P, C.POINTER(_abi.EquationSetDesc)]),
+    "tx_dof_sizes": (C.c_int, [P, C.POINTER(I64), C.POINTER(I32), C.POINTER(I64), C.POINTER(I32)]),
+    "tx_dof_owned_gids": (C.c_int, [P, P]),
+    "tx_dof_element_gids": (C.c_int, [P, I32, P]),
+    "tx_dof_element_lids": (C.c_int, [P, I32, P]),
+    "tx_dof_block_gid_count": (C.c_int, [P, I32, C.POINTER(I32)]),
+    "tx_dof_field_offsets": (C.c_int, [P, I32, I32, C.POINTER(I32), P]),
+    "tx_dirichlet_dofs": (C.c_int, [P, U32, U32, C.POINTER(I64), P]),
+    "tx_graph_build": (C.c_int, [P, P, P]),
+    "tx_eval": (C.c_int, [P, C.POINTER(_abi.EvalArgs)]),
+    "tx_dirichlet_apply": (C.c_int, [P, I64, P, P, P, P, P]),
+    "tx_spmv": (C.c_int, [P, I32, I64, P, P, P, P, P, D, D]),
+    "tx_solve_cg_ir": (C.c_int, [P, C.POINTER(_abi.SolveArgs)]),
+    "tx_set_stream": (C.c_int, [P, P]),
+    "tx_synchronize": (C.c_int, [P]),
+}
+
+_lib = None
+
+
+class TxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"tianxin_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def load(build_if_missing=True):
+    """Load (building first if the sources are newer) the CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from . import build as _build
+        try:
+            _build.build()
+        except (OSError, RuntimeError) as e:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"libtianxin_gb300.so is missing and could not be built: {e}") from e
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libtianxin_gb300.so not found at {LIB_PATH}; run tianxin_gb300/build.py")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(h, rc, what=""):
+    if rc != 0:
+        msg = load().tx_last_error(h) if h else b""
+        raise TxError(rc, (what + ": " if what else "") + (msg.decode() if msg else ""))

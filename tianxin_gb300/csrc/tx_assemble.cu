@@ -1,0 +1,476 @@
+// tx_assemble.cu -- fused volume assembly for one element block.
+//
+// One launch replaces the reference's per-workset evaluator chain
+// (AssemblyEngine::evaluateVolume, disc-fe/src/Panzer_AssemblyEngine_impl.hpp:
+// 134-182) for the Residual and Jacobian evaluation types:
+//   GatherSolution_Tpetra      x, x_dot -> element values (LID gather)
+//   IntegrationValues2         J, det J, J^-1, weighted measure
+//   BasisValues2               grad N = J^-T grad N^, H(curl) J^-T / J/det
+//   DOF / DOFGradient / DOFCurl values at the cubature points
+//   Integrator_GradBasisDotVector, Integrator_BasisTimesScalar,
+//   Integrator_CurlBasisDotVector (+ the mass terms on the time-derivative
+//   vector)
+//   ScatterResidual_Tpetra     f += r, A(row, cols) += dr/du
+// The reference obtains dr/du by forward-mode AD (seed beta on x and alpha on
+// x_dot in the same derivative slot); here the element matrices are the
+// closed forms of those derivatives, so W = beta dR/dx + alpha dR/dx_dot.
+//
+// Work decomposition: TPE threads (next power of two >= basis count) per
+// element, EPB elements per CTA, grid-stride over the block's elements.
+// Phase 1 gathers vertex coordinates and DOF values, phase 2 builds the
+// geometry and physical basis tables of each cubature point in shared
+// memory, phase 3 evaluates the point fluxes, phase 4 gives each thread one
+// basis function a: it forms residual row a and the Jacobian block-row
+// (a, :) and scatters them with FP64 reductions at
+//   rowptr[nf*entity(a)+c] + nf*epos[e][a][b] + d
+// where epos is the precomputed position of entity b in the sorted row of
+// entity a (the element-to-row map; no column search on the GPU).
+//
+// Real = double: the FP64 path.  Real = float (TX_EVAL_MIXED): element
+// geometry and contractions in FP32 (vertex coordinates are differenced in
+// FP64 first), accumulation into f and the CRS in FP64.
+#include <cstdio>
+
+#include "tx_device.cuh"
+
+namespace tx {
+namespace {
+
+constexpr int pow2ceil(int n) { return n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32; }
+
+template <int TOPO, int BASIS>
+struct Family;
+template <> struct Family<TX_TOPO_HEX, TX_HGRAD_C1> { static constexpr int NV = 8, NB = 8; };
+template <> struct Family<TX_TOPO_HEX, TX_HGRAD_C2> { static constexpr int NV = 8, NB = 27; };
+template <> struct Family<TX_TOPO_TET, TX_HGRAD_C1> { static constexpr int NV = 4, NB = 4; };
+template <> struct Family<TX_TOPO_TET, TX_HGRAD_C2> { static constexpr int NV = 4, NB = 10; };
+template <> struct Family<TX_TOPO_HEX, TX_HCURL_I1> { static constexpr int NV = 8, NB = 12; };
+
+constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real>
+struct Cfg {
+  static constexpr int NV = Family<TOPO, BASIS>::NV;
+  static constexpr int NB = Family<TOPO, BASIS>::NB;
+  static constexpr bool HC = BASIS == TX_HCURL_I1;
+  static constexpr int NF = PHYS == TX_PHYS_ELASTICITY ? 3 : 1;
+  static constexpr int TPE = pow2ceil(NB);
+  static constexpr int THREADS = NB > 16 ? 128 : 256;
+  static constexpr int EPB = THREADS / TPE;
+  static constexpr int NQF = PHYS == TX_PHYS_ELASTICITY ? 9 : PHYS == TX_PHYS_HEAT ? 8 : PHYS == TX_PHYS_MAXWELL ? 6 : 4;
+  static constexpr int NVAL = HC ? 3 : 1;
+  // shared: reference part
+  static constexpr size_t R_GEO_GRAD = 0;
+  static constexpr size_t R_GEO_VAL = align16(R_GEO_GRAD + sizeof(double) * NQ * NV * 3);
+  static constexpr size_t R_W = align16(R_GEO_VAL + sizeof(double) * NQ * NV);
+  static constexpr size_t R_VAL = align16(R_W + sizeof(Real) * NQ);
+  static constexpr size_t R_GRAD = align16(R_VAL + sizeof(Real) * NQ * NB * NVAL);
+  static constexpr size_t R_END = align16(R_GRAD + sizeof(Real) * NQ * NB * 3);
+  // shared: per element part
+  static constexpr size_t E_X = 0;
+  static constexpr size_t E_U = align16(E_X + sizeof(double) * NV * 3);
+  static constexpr size_t E_UD = align16(E_U + sizeof(double) * NF * NB);
+  static constexpr size_t E_AUX = align16(E_UD + sizeof(double) * NF * NB);
+  static constexpr size_t E_SG = align16(E_AUX + sizeof(double) * (HC ? NB : 0));
+  static constexpr size_t E_G = align16(E_SG + sizeof(Real) * (HC ? NB : 0));
+  static constexpr size_t E_V = align16(E_G + sizeof(Real) * NQ * NB * 3);
+  static constexpr size_t E_W = align16(E_V + sizeof(Real) * (HC ? NQ * NB * 3 : 0));
+  static constexpr size_t E_QF = align16(E_W + sizeof(Real) * NQ);
+  static constexpr size_t E_SIGN = align16(E_QF + sizeof(Real) * NQ * NQF);
+  static constexpr size_t E_END = align16(E_SIGN + sizeof(Real));
+  static constexpr size_t SMEM = R_END + EPB * E_END;
+};
+
+template <typename Real>
+__device__ __forceinline__ Real source_at(int kind, double c, double s0, const double ip[3]) {
+  if (kind == TX_SOURCE_SINE) {
+    const double pi = 3.14159265358979323846;
+    return (Real)(3.0 * pi * pi * sin(pi * ip[0]) * sin(pi * ip[1]) * sin(pi * ip[2]));
+  }
+  if (kind == TX_SOURCE_AFFINE) return (Real)(c * (1.0 + ip[0] + 2.0 * ip[1] + 3.0 * ip[2]));
+  return (Real)s0;
+}
+
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC>
+__global__ void __launch_bounds__(Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS)
+k_assemble(const BlockView B, const EvalParams P) {
+  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real>;
+  constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF;
+  constexpr bool HC = C::HC;
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* r_geo_grad = reinterpret_cast<double*>(smem + C::R_GEO_GRAD);
+  double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
+  Real* r_w = reinterpret_cast<Real*>(smem + C::R_W);
+  Real* r_val = reinterpret_cast<Real*>(smem + C::R_VAL);
+  Real* r_grad = reinterpret_cast<Real*>(smem + C::R_GRAD);
+
+  // reference tables: [w | geo_val | geo_grad | val | grad] in FP64
+  {
+    const double* ref = B.ref;
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) r_w[i] = (Real)ref[i];
+    ref += NQ;
+    for (int i = threadIdx.x; i < NQ * NV; i += blockDim.x) r_geo_val[i] = ref[i];
+    ref += NQ * NV;
+    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) r_geo_grad[i] = ref[i];
+    ref += NQ * NV * 3;
+    for (int i = threadIdx.x; i < NQ * NB * C::NVAL; i += blockDim.x) r_val[i] = (Real)ref[i];
+    ref += NQ * NB * C::NVAL;
+    for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) r_grad[i] = (Real)ref[i];
+  }
+
+  const int le = threadIdx.x / TPE;
+  const int t = threadIdx.x % TPE;
+  unsigned char* eb = smem + C::R_END + (size_t)le * C::E_END;
+  double* sX = reinterpret_cast<double*>(eb + C::E_X);
+  double* sU = reinterpret_cast<double*>(eb + C::E_U);
+  double* sUD = reinterpret_cast<double*>(eb + C::E_UD);
+  double* sAUX = reinterpret_cast<double*>(eb + C::E_AUX);
+  Real* sSG = reinterpret_cast<Real*>(eb + C::E_SG);
+  Real* sG = reinterpret_cast<Real*>(eb + C::E_G);    // [q][b][3] grad (HGRAD) or curl (HCURL)
+  Real* sV = reinterpret_cast<Real*>(eb + C::E_V);    // [q][b][3] HCURL values
+  Real* sW = reinterpret_cast<Real*>(eb + C::E_W);
+  Real* sQF = reinterpret_cast<Real*>(eb + C::E_QF);
+  Real* sSign = reinterpret_cast<Real*>(eb + C::E_SIGN);
+  __syncthreads();
+
+  const double* pp = P.p;
+  for (int64_t g0 = P.e0 + (int64_t)blockIdx.x * EPB; g0 < P.e1; g0 += (int64_t)gridDim.x * EPB) {
+    const int64_t e = g0 + le;
+    const bool valid = e < P.e1;
+    // ---------------------------------------------------------- 1 gather
+    if (valid) {
+      for (int v = t; v < NV; v += TPE) {
+        const int32_t n = __ldg(B.vconn + e * NV + v);
+        sX[3 * v + 0] = __ldg(P.coords + 3 * (int64_t)n + 0);
+        sX[3 * v + 1] = __ldg(P.coords + 3 * (int64_t)n + 1);
+        sX[3 * v + 2] = __ldg(P.coords + 3 * (int64_t)n + 2);
+      }
+      for (int b = t; b < NB; b += TPE) {
+        const int64_t ent = __ldg(B.dconn + e * NB + b);
+#pragma unroll
+        for (int c = 0; c < NF; ++c) {
+          sU[c * NB + b] = __ldg(P.x + NF * ent + c);
+          sUD[c * NB + b] = P.xdot ? __ldg(P.xdot + NF * ent + c) : 0.0;
+        }
+        if constexpr (HC) {
+          sAUX[b] = P.aux ? __ldg(P.aux + ent) : 0.0;
+          sSG[b] = (Real)__ldg(B.esign + e * NB + b);
+        }
+      }
+    }
+    __syncthreads();
+    // ---------------------------------------------------------- 2 geometry
+    if (valid) {
+      for (int q = t; q < NQ; q += TPE) {
+        Real J[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) J[k] = Real(0);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          // differencing in FP64 keeps the mixed path's J accurate
+          const Real dx = (Real)(sX[3 * v + 0] - sX[0]);
+          const Real dy = (Real)(sX[3 * v + 1] - sX[1]);
+          const Real dz = (Real)(sX[3 * v + 2] - sX[2]);
+          const double* gg = r_geo_grad + (q * NV + v) * 3;
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const Real g = (Real)gg[j];
+            J[0 + j] += dx * g;
+            J[3 + j] += dy * g;
+            J[6 + j] += dz * g;
+          }
+        }
+        const Real c00 = J[4] * J[8] - J[5] * J[7];
+        const Real c01 = J[5] * J[6] - J[3] * J[8];
+        const Real c02 = J[3] * J[7] - J[4] * J[6];
+        const Real det = J[0] * c00 + J[1] * c01 + J[2] * c02;
+        const Real id = Real(1) / det;
+        Real Ji[9];
+        Ji[0] = c00 * id; Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+        Ji[3] = c01 * id; Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[5] = (J[2] * J[3] - J[0] * J[5]) * id;
+        Ji[6] = c02 * id; Ji[7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[8] = (J[0] * J[4] - J[1] * J[3]) * id;
+        sW[q] = r_w[q] * det;
+        if (q == 0) *sSign = det < Real(0) ? Real(-1) : Real(1);
+#pragma unroll 4
+        for (int b = 0; b < NB; ++b) {
+          const Real* gr = r_grad + (q * NB + b) * 3;
+          const Real g0 = gr[0], g1 = gr[1], g2 = gr[2];
+          if constexpr (!HC) {
+            // grad_i = sum_j Jinv(j,i) grad^_j
+            sG[(q * NB + b) * 3 + 0] = Ji[0] * g0 + Ji[3] * g1 + Ji[6] * g2;
+            sG[(q * NB + b) * 3 + 1] = Ji[1] * g0 + Ji[4] * g1 + Ji[7] * g2;
+            sG[(q * NB + b) * 3 + 2] = Ji[2] * g0 + Ji[5] * g1 + Ji[8] * g2;
+          } else {
+            const Real s = sSG[b];
+            const Real* vr = r_val + (q * NB + b) * 3;
+            sV[(q * NB + b) * 3 + 0] = s * (Ji[0] * vr[0] + Ji[3] * vr[1] + Ji[6] * vr[2]);
+            sV[(q * NB + b) * 3 + 1] = s * (Ji[1] * vr[0] + Ji[4] * vr[1] + Ji[7] * vr[2]);
+            sV[(q * NB + b) * 3 + 2] = s * (Ji[2] * vr[0] + Ji[5] * vr[1] + Ji[8] * vr[2]);
+            const Real sd = s * id;  // curl = J curl^ / det
+            sG[(q * NB + b) * 3 + 0] = sd * (J[0] * g0 + J[1] * g1 + J[2] * g2);
+            sG[(q * NB + b) * 3 + 1] = sd * (J[3] * g0 + J[4] * g1 + J[5] * g2);
+            sG[(q * NB + b) * 3 + 2] = sd * (J[6] * g0 + J[7] * g1 + J[8] * g2);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---------------------------------------------------------- 3 point fluxes
+    if (valid) {
+      for (int q = t; q < NQ; q += TPE) {
+        sW[q] *= *sSign;  // computeCellMeasure: |.| by the sign of the first point
+        Real* qf = sQF + q * NQF;
+        if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
+          Real u = 0, ud = 0, g[3] = {0, 0, 0};
+          for (int b = 0; b < NB; ++b) {
+            const Real n = r_val[q * NB + b];
+            const Real ub = (Real)sU[b];
+            u += n * ub;
+            ud += n * (Real)sUD[b];
+            g[0] += sG[(q * NB + b) * 3 + 0] * ub;
+            g[1] += sG[(q * NB + b) * 3 + 1] * ub;
+            g[2] += sG[(q * NB + b) * 3 + 2] * ub;
+          }
+          if constexpr (PHYS == TX_PHYS_POISSON) {
+            const Real k = (Real)pp[0], c = (Real)pp[1], m = (Real)pp[2];
+            Real s = (Real)pp[3];
+            if (P.source_kind != TX_SOURCE_CONST) {
+              double ip[3] = {0, 0, 0};
+              for (int v = 0; v < NV; ++v) {
+                const double nv = r_geo_val[q * NV + v];
+                ip[0] += nv * sX[3 * v]; ip[1] += nv * sX[3 * v + 1]; ip[2] += nv * sX[3 * v + 2];
+              }
+              s = source_at<Real>(P.source_kind, pp[1], pp[3], ip);
+            }
+            qf[0] = k * g[0]; qf[1] = k * g[1]; qf[2] = k * g[2];
+            qf[3] = c * u + m * ud - s;
+          } else {
+            const Real k = (Real)pp[0] + (Real)pp[1] * u * u;
+            const Real dk = Real(2) * (Real)pp[1] * u;
+            qf[0] = k * g[0]; qf[1] = k * g[1]; qf[2] = k * g[2];
+            qf[3] = -(Real)pp[2];
+            qf[4] = dk * g[0]; qf[5] = dk * g[1]; qf[6] = dk * g[2];
+            qf[7] = k;
+          }
+        } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
+          Real Gu[9], acc[3] = {0, 0, 0};
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Gu[k] = 0;
+          for (int b = 0; b < NB; ++b) {
+            const Real* gb = sG + (q * NB + b) * 3;
+            const Real n = r_val[q * NB + b];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const Real ub = (Real)sU[c * NB + b];
+              Gu[3 * c + 0] += gb[0] * ub;
+              Gu[3 * c + 1] += gb[1] * ub;
+              Gu[3 * c + 2] += gb[2] * ub;
+              acc[c] += n * (Real)sUD[c * NB + b];
+            }
+          }
+          const double E = pp[0], nu = pp[1];
+          const Real lam = (Real)(E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
+          const Real mu = (Real)(E / (2.0 * (1.0 + nu)));
+          const Real tr = Gu[0] + Gu[4] + Gu[8];
+          qf[0] = mu * (Gu[0] + Gu[0]) + lam * tr;  // s00
+          qf[1] = mu * (Gu[4] + Gu[4]) + lam * tr;  // s11
+          qf[2] = mu * (Gu[8] + Gu[8]) + lam * tr;  // s22
+          qf[3] = mu * (Gu[1] + Gu[3]);             // s01
+          qf[4] = mu * (Gu[2] + Gu[6]);             // s02
+          qf[5] = mu * (Gu[5] + Gu[7]);             // s12
+          const Real rho = (Real)pp[5];
+          qf[6] = rho * acc[0] - (Real)pp[2];
+          qf[7] = rho * acc[1] - (Real)pp[3];
+          qf[8] = rho * acc[2] - (Real)pp[4];
+        } else {  // MAXWELL
+          Real Ev[3] = {0, 0, 0}, cE[3] = {0, 0, 0}, Jv[3] = {0, 0, 0};
+          for (int b = 0; b < NB; ++b) {
+            const Real ub = (Real)sU[b], jb = (Real)sAUX[b];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              Ev[i] += sV[(q * NB + b) * 3 + i] * ub;
+              Jv[i] += sV[(q * NB + b) * 3 + i] * jb;
+              cE[i] += sG[(q * NB + b) * 3 + i] * ub;
+            }
+          }
+          const Real imu = (Real)pp[0], sig = (Real)pp[1];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            qf[i] = imu * cE[i];
+            qf[3 + i] = sig * Ev[i] - Jv[i];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---------------------------------------------------------- 4 rows + scatter
+    if (valid) {
+      for (int a = t; a < NB; a += TPE) {
+        const int64_t la = __ldg(B.dconn + e * NB + a);
+        // residual row a (per field)
+        Real r[NF];
+#pragma unroll
+        for (int c = 0; c < NF; ++c) r[c] = 0;
+        for (int q = 0; q < NQ; ++q) {
+          const Real w = sW[q];
+          const Real* ga = sG + (q * NB + a) * 3;
+          const Real* qf = sQF + q * NQF;
+          if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
+            r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + r_val[q * NB + a] * qf[3]);
+          } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
+            const Real n = r_val[q * NB + a];
+            r[0] += w * (ga[0] * qf[0] + ga[1] * qf[3] + ga[2] * qf[4] + n * qf[6]);
+            r[1] += w * (ga[0] * qf[3] + ga[1] * qf[1] + ga[2] * qf[5] + n * qf[7]);
+            r[2] += w * (ga[0] * qf[4] + ga[1] * qf[5] + ga[2] * qf[2] + n * qf[8]);
+          } else {
+            const Real* va = sV + (q * NB + a) * 3;
+            r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + va[0] * qf[3] + va[1] * qf[4] + va[2] * qf[5]);
+          }
+        }
+        if (P.f) {
+#pragma unroll
+          for (int c = 0; c < NF; ++c) atomicAdd(P.f + NF * la + c, (double)r[c]);
+        }
+        if constexpr (JAC) {
+          int64_t rp[NF];
+#pragma unroll
+          for (int c = 0; c < NF; ++c) rp[c] = __ldg(P.rowptr + NF * la + c);
+          const uint8_t* ep = B.epos + (e * NB + a) * NB;
+          const Real beta = (Real)P.beta, alpha = (Real)P.alpha;
+          for (int b = 0; b < NB; ++b) {
+            const int64_t pb = (int64_t)NF * __ldg(ep + b);
+            if constexpr (PHYS == TX_PHYS_POISSON) {
+              const Real ca = beta * (Real)pp[0];
+              const Real cm = beta * (Real)pp[1] + alpha * (Real)pp[2];
+              Real kg = 0, km = 0;
+              for (int q = 0; q < NQ; ++q) {
+                const Real* ga = sG + (q * NB + a) * 3;
+                const Real* gb = sG + (q * NB + b) * 3;
+                const Real w = sW[q];
+                kg += w * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
+                km += w * r_val[q * NB + a] * r_val[q * NB + b];
+              }
+              atomicAdd(P.vals + rp[0] + pb, (double)(ca * kg + cm * km));
+            } else if constexpr (PHYS == TX_PHYS_HEAT) {
+              Real kab = 0;
+              for (int q = 0; q < NQ; ++q) {
+                const Real* ga = sG + (q * NB + a) * 3;
+                const Real* gb = sG + (q * NB + b) * 3;
+                const Real* qf = sQF + q * NQF;
+                kab += sW[q] * (qf[7] * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]) +
+                                r_val[q * NB + b] * (ga[0] * qf[4] + ga[1] * qf[5] + ga[2] * qf[6]));
+              }
+              atomicAdd(P.vals + rp[0] + pb, (double)(beta * kab));
+            } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
+              Real Pm[9], M = 0;
+#pragma unroll
+              for (int k = 0; k < 9; ++k) Pm[k] = 0;
+              for (int q = 0; q < NQ; ++q) {
+                const Real* ga = sG + (q * NB + a) * 3;
+                const Real* gb = sG + (q * NB + b) * 3;
+                const Real w = sW[q];
+                const Real wa0 = w * ga[0], wa1 = w * ga[1], wa2 = w * ga[2];
+                Pm[0] += wa0 * gb[0]; Pm[1] += wa0 * gb[1]; Pm[2] += wa0 * gb[2];
+                Pm[3] += wa1 * gb[0]; Pm[4] += wa1 * gb[1]; Pm[5] += wa1 * gb[2];
+                Pm[6] += wa2 * gb[0]; Pm[7] += wa2 * gb[1]; Pm[8] += wa2 * gb[2];
+                M += w * r_val[q * NB + a] * r_val[q * NB + b];
+              }
+              const double E = pp[0], nu = pp[1];
+              const Real lam = (Real)(E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
+              const Real mu = (Real)(E / (2.0 * (1.0 + nu)));
+              const Real trP = Pm[0] + Pm[4] + Pm[8];
+              const Real mass = alpha * (Real)pp[5] * M;
+#pragma unroll
+              for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                  Real k = beta * (lam * Pm[3 * c + d] + mu * Pm[3 * d + c]);
+                  if (c == d) k += beta * mu * trP + mass;
+                  atomicAdd(P.vals + rp[c] + pb + d, (double)k);
+                }
+            } else {  // MAXWELL
+              const Real imu = (Real)pp[0], sig = (Real)pp[1];
+              Real kc = 0, kv = 0;
+              for (int q = 0; q < NQ; ++q) {
+                const Real* ca = sG + (q * NB + a) * 3;
+                const Real* cb = sG + (q * NB + b) * 3;
+                const Real* va = sV + (q * NB + a) * 3;
+                const Real* vb = sV + (q * NB + b) * 3;
+                kc += sW[q] * (ca[0] * cb[0] + ca[1] * cb[1] + ca[2] * cb[2]);
+                kv += sW[q] * (va[0] * vb[0] + va[1] * vb[1] + va[2] * vb[2]);
+              }
+              atomicAdd(P.vals + rp[0] + pb, (double)(beta * (imu * kc + sig * kv)));
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC>
+cudaError_t launch_one(const BlockView& B, const EvalParams& P, cudaStream_t s, int grid_cap) {
+  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real>;
+  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC>;
+  static int max_blocks_per_sm = -1;
+  static int num_sms = 0;
+  if (max_blocks_per_sm < 0) {
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+    if (err != cudaSuccess) return err;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks_per_sm, kern, C::THREADS, C::SMEM);
+    if (err != cudaSuccess) return err;
+    if (max_blocks_per_sm < 1) max_blocks_per_sm = 1;
+  }
+  const int64_t n = P.e1 - P.e0;
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + C::EPB - 1) / C::EPB;
+  int64_t cap = (int64_t)max_blocks_per_sm * num_sms * 4;
+  if (grid_cap > 0 && grid_cap < cap) cap = grid_cap;
+  if (blocks > cap) blocks = cap;
+  kern<<<(unsigned)blocks, C::THREADS, C::SMEM, s>>>(B, P);
+  return cudaGetLastError();
+}
+
+template <int TOPO, int BASIS, int NQ, int PHYS>
+cudaError_t launch_prec(const BlockView& B, const EvalParams& P, bool mixed, cudaStream_t s, int cap) {
+  const bool jac = P.vals != nullptr;
+  if (mixed)
+    return jac ? launch_one<TOPO, BASIS, NQ, PHYS, float, true>(B, P, s, cap)
+               : launch_one<TOPO, BASIS, NQ, PHYS, float, false>(B, P, s, cap);
+  return jac ? launch_one<TOPO, BASIS, NQ, PHYS, double, true>(B, P, s, cap)
+             : launch_one<TOPO, BASIS, NQ, PHYS, double, false>(B, P, s, cap);
+}
+
+}  // namespace
+
+cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, cudaStream_t s, int cap) {
+  const int ph = P.physics;
+  if (B.topo == TX_TOPO_HEX && B.basis == TX_HGRAD_C1 && B.nq == 8) {
+    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_POISSON>(B, P, mixed, s, cap);
+    if (ph == TX_PHYS_ELASTICITY) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_ELASTICITY>(B, P, mixed, s, cap);
+    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_HEAT>(B, P, mixed, s, cap);
+  }
+  if (B.topo == TX_TOPO_HEX && B.basis == TX_HGRAD_C2 && B.nq == 27) {
+    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_POISSON>(B, P, mixed, s, cap);
+    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_HEAT>(B, P, mixed, s, cap);
+  }
+  if (B.topo == TX_TOPO_TET && B.basis == TX_HGRAD_C1 && B.nq == 4) {
+    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_POISSON>(B, P, mixed, s, cap);
+    if (ph == TX_PHYS_ELASTICITY) return launch_prec<TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_ELASTICITY>(B, P, mixed, s, cap);
+    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_HEAT>(B, P, mixed, s, cap);
+  }
+  if (B.topo == TX_TOPO_TET && B.basis == TX_HGRAD_C2 && B.nq == 4) {
+    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_POISSON>(B, P, mixed, s, cap);
+    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_HEAT>(B, P, mixed, s, cap);
+  }
+  if (B.topo == TX_TOPO_HEX && B.basis == TX_HCURL_I1 && B.nq == 8) {
+    if (ph == TX_PHYS_MAXWELL) return launch_prec<TX_TOPO_HEX, TX_HCURL_I1, 8, TX_PHYS_MAXWELL>(B, P, mixed, s, cap);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace tx

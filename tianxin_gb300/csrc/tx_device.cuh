@@ -1,0 +1,76 @@
+// tx_device.cuh -- kernel-side declarations shared by the .cu files.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tx_internal.h"
+
+namespace tx {
+
+// Everything one assembly launch reads besides the block view.
+struct EvalParams {
+  const double* coords;      // [n_nodes][3]
+  const double* x;           // [N]
+  const double* xdot;        // [N] or nullptr
+  const double* aux;         // [N] or nullptr
+  double alpha, beta, t;
+  double* f;                 // [N] or nullptr
+  double* vals;              // [nnz] or nullptr
+  const int64_t* rowptr;     // [N+1] DOF-level Tpetra rowptr
+  int64_t e0, e1;            // element range within the block
+  int physics, source_kind;
+  double p[8];
+};
+
+// Launch the fused gather -> geometry -> integrators -> scatter kernel for
+// one block.  Returns cudaSuccess or the launch error; TX_EINVAL (as
+// cudaErrorInvalidValue) for element families without a kernel.
+cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, cudaStream_t s, int grid_cap);
+
+// ---- linear algebra (tx_linalg.cu)
+cudaError_t launch_expand_rowptr(const int64_t* erowptr, int64_t n_ent, int nf, int64_t* rowptr, cudaStream_t s);
+cudaError_t launch_expand_colind(const int64_t* erowptr, const int32_t* ecol, int64_t n_ent, int nf,
+                                 const int64_t* rowptr, int32_t* colind, cudaStream_t s);
+cudaError_t launch_dirichlet(int64_t n, const int32_t* lids, const double* g, const double* x, double* f,
+                             const int64_t* rowptr, const int64_t* erowptr, const int32_t* ecol, int nf,
+                             double* vals, cudaStream_t s);
+cudaError_t launch_spmv_f64(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* vals,
+                            const double* x, double* y, double alpha, double beta, int64_t nnz_hint, cudaStream_t s);
+cudaError_t launch_spmv_f32(int64_t n, const int64_t* rowptr, const int32_t* colind, const float* vals,
+                            const float* x, float* y, float alpha, float beta, int64_t nnz_hint, cudaStream_t s);
+
+// Work space of the iterative-refinement solver (owned by the handle).
+struct SolverWork {
+  int64_t n = 0, nnz = 0;
+  float* vals32 = nullptr;     // FP32 Jacobian with symmetric Dirichlet elimination
+  float* dinv = nullptr;       // Jacobi preconditioner
+  float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *d = nullptr;
+  double* r64 = nullptr;       // outer residual
+  uint8_t* mask = nullptr;     // Dirichlet mask
+  double* red = nullptr;       // reduction partials [kRedSlots * kRedBlocks]
+  double* scal = nullptr;      // device scalars
+  double* host_scal = nullptr; // pinned mirror
+};
+constexpr int kRedBlocks = 1024;
+constexpr int kRedSlots = 4;
+
+cudaError_t solver_alloc(SolverWork& w, int64_t n, int64_t nnz);
+void solver_free(SolverWork& w);
+
+// Outer-residual callback: r = b - A x (or -f(x)); returns 0 or a TX status.
+typedef int (*ResidualFn)(void* ctx, const double* x, double* r);
+
+// FP64 iterative refinement around FP32 Jacobi-CG.  stats as tx_solve_args.
+int solve_cg_ir(SolverWork& w, const int64_t* rowptr, const int32_t* colind, const double* vals,
+                int64_t n_dir, const int32_t* dir_lids, double* x, ResidualFn resid, void* ctx,
+                double rtol, double inner_rtol, int max_outer, int max_inner, double* stats,
+                cudaStream_t s, std::string& err);
+
+// Vector helpers used by the API layer
+cudaError_t launch_fill(double* p, double v, int64_t n, cudaStream_t s);
+cudaError_t launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t s);
+// sum of squares of x (FP64) into *out (device), using w.red as scratch
+cudaError_t launch_norm2sq(const double* x, int64_t n, double* red, double* out, cudaStream_t s);
+
+}  // namespace tx

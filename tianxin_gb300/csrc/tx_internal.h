@@ -1,0 +1,93 @@
+// tx_internal.h -- shared host/device declarations of libtianxin_gb300.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tianxin_gb300.h"
+
+namespace tx {
+
+// Maximum sizes of the element families the kernels are instantiated for.
+constexpr int kMaxNB = 27;   // basis functions per element (hex27)
+constexpr int kMaxNQ = 27;   // cubature points per element
+constexpr int kMaxNV = 8;    // geometric vertices per element
+
+// Reference element of one block: cubature and basis tables, FP64.
+//   w[q]; geo_val[q][v]; geo_grad[q][v][3]; val[q][b] (HGRAD) or
+//   val[q][b][3] (HCURL); grad[q][b][3] (HGRAD gradient / HCURL curl).
+struct RefTables {
+  int topo = 0, basis = 0, degree = 0;
+  int nq = 0, nb = 0, nv = 0;
+  bool hcurl = false;
+  std::vector<double> xi, w, geo_val, geo_grad, val, grad;
+  // pack into one contiguous array: [w | geo_val | geo_grad | val | grad]
+  std::vector<double> packed() const;
+};
+
+RefTables make_ref_tables(int topo, int basis, int degree);
+int default_degree(int topo, int basis);
+
+// Device view of one block, passed by value to kernels.
+struct BlockView {
+  int topo, basis, nq, nb, nv;
+  int64_t n_elem;
+  const int32_t* vconn;   // [E][nv]  vertex (node GID) per geometric vertex
+  const int32_t* dconn;   // [E][nb]  entity LID of the entity carrying basis b
+  const uint8_t* epos;    // [E][nb][nb] block position of entity b in row of entity a
+  const int8_t* esign;    // [E][nb]  HCURL edge signs (nullptr otherwise)
+  const double* ref;      // packed RefTables
+};
+
+struct Handle;  // defined in tx_api.cu
+
+// ----------------------------------------------------------------- setup
+// Host-side mesh + numbering state (built by tx_setup.cpp).
+struct Mesh {
+  tx_mesh_desc desc{};
+  int64_t NX = 0, NY = 0, NZ = 0;
+  int nblocks = 0;
+  int64_t n_nodes = 0, n_hex_edges = 0, n_hex_faces = 0, n_bricks = 0;
+  int64_t n_elements = 0;
+  std::vector<int64_t> elem_brick;        // element -> brick
+  std::vector<int8_t> elem_sub;           // element -> sub-element (tet)
+  std::vector<std::vector<int64_t>> block_elems;
+  std::vector<double> coords;             // node GID order, xyz
+};
+
+struct BlockDofs {
+  int topo = 0, basis = 0, degree = 0, nb = 0, nv = 0;
+  RefTables ref;
+  std::vector<int32_t> vconn, dconn;      // [E][nv], [E][nb]
+  std::vector<uint8_t> epos;              // [E][nb][nb]
+  std::vector<int8_t> esign;              // [E][nb] (HCURL)
+  std::vector<int> geom_dim, geom_sub;    // geometric pattern (dim, subcell) in order
+  std::vector<int> geom_basis;            // basis index on that sub-cell, -1 none
+  std::vector<int> basis_pos;             // basis b -> position among DOF entities
+};
+
+struct Dofs {
+  tx_equation_set_desc eq{};
+  int nf = 0;
+  int64_t n_entities = 0;                 // DOF-carrying entities
+  int64_t n_dofs = 0;
+  std::vector<BlockDofs> blocks;
+  std::vector<int64_t> ent_gid;           // entity LID -> entity GID (mesh entity id)
+  std::vector<int64_t> ent_first_gid;     // entity LID -> first DOF GID
+  std::vector<int32_t> ent_lattice;       // entity LID -> doubled lattice position (3)
+  std::vector<int64_t> erowptr;           // entity graph
+  std::vector<int32_t> ecol;
+  int64_t nnz = 0;
+};
+
+void build_mesh(Mesh& m, const tx_mesh_desc& d);
+void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q);
+// owned GIDs (LID order), element GIDs/LIDs of a block (reference geometric order)
+void dof_owned_gids(const Dofs& D, int64_t* out);
+void dof_element_gids(const Mesh& m, const Dofs& D, int block, int64_t* out);
+void dof_element_lids(const Mesh& m, const Dofs& D, int block, int32_t* out);
+int dof_block_gid_count(const Dofs& D, int block);
+int dof_field_offsets(const Dofs& D, int block, int field, int32_t* out);
+std::vector<int32_t> dirichlet_dofs(const Dofs& D, const Mesh& m, uint32_t side_mask, uint32_t field_mask);
+
+}  // namespace tx

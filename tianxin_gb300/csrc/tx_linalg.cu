@@ -1,0 +1,427 @@
+// tx_linalg.cu -- Tpetra-layout graph expansion, Dirichlet rows, CRS SpMV
+// and the FP64-refined FP32 Jacobi-CG used for the Newton-Krylov solve.
+//
+//   graph expansion   the DOF-level CRS of TpetraLinearObjFactory::
+//                     buildGhostedGraph (disc-fe/src/lof/Panzer_TpetraLinear
+//                     ObjFactory_impl.hpp:559-651) from the entity graph: row
+//                     (entity r, field c) holds, for every neighbour entity m
+//                     in ascending LID, the nf columns nf*m .. nf*m+nf-1
+//   Dirichlet         TpetraLinearObjContainer::applyDirichletBoundaryCondition
+//                     (disc-fe/src/lof/Panzer_TpetraLinearObjContainer.hpp:
+//                     228-238, 306-318): f[d] = x[d] - g, row d = e_d
+//   SpMV              Tpetra::CrsMatrix::apply (y = alpha A x + beta y)
+//   CG + refinement   Belos' role in adapters-stk/example/PoissonExample/
+//                     main.cpp:402-419, re-designed: FP32 Jacobi-PCG inner
+//                     solve on an FP32 copy of A with symmetric Dirichlet
+//                     elimination, FP64 outer residual and update.
+#include <cmath>
+#include <cstdio>
+#include <string>
+
+#include "tx_device.cuh"
+
+namespace tx {
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(int64_t n, int per_block, int64_t cap = 152 * 32) {
+  int64_t b = (n + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (unsigned)b;
+}
+
+__global__ void k_expand_rowptr(const int64_t* __restrict__ erp, int64_t n_ent, int nf, int64_t* __restrict__ rp) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_ent; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = erp[r], deg = erp[r + 1] - b;
+    for (int c = 0; c < nf; ++c) rp[nf * r + c] = (int64_t)nf * nf * b + (int64_t)c * nf * deg;
+    if (r == n_ent - 1) rp[nf * n_ent] = (int64_t)nf * nf * erp[n_ent];
+  }
+}
+
+// one warp per entity row; lanes write consecutive column indices
+__global__ void k_expand_colind(const int64_t* __restrict__ erp, const int32_t* __restrict__ ecol, int64_t n_ent,
+                                int nf, const int64_t* __restrict__ rp, int32_t* __restrict__ col) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_ent; r += nwarps) {
+    const int64_t b = erp[r], deg = erp[r + 1] - b;
+    const int64_t len = deg * nf;
+    for (int c = 0; c < nf; ++c) {
+      int32_t* out = col + rp[nf * r + c];
+      for (int64_t k = lane; k < len; k += 32) out[k] = nf * ecol[b + k / nf] + (int32_t)(k % nf);
+    }
+  }
+}
+
+// one warp per Dirichlet DOF d = nf*r + c: zero row d, put 1 on the
+// diagonal, whose block position is that of entity r in its own sorted
+// entity row
+__global__ void k_dirichlet(int64_t n, const int32_t* __restrict__ lids, const double* __restrict__ g,
+                            const double* __restrict__ x, double* __restrict__ f, const int64_t* __restrict__ rp,
+                            const int64_t* __restrict__ erp, const int32_t* __restrict__ ecol, int nf,
+                            double* __restrict__ vals) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    const int32_t d = lids[i];
+    if (f && lane == 0) f[d] = x[d] - (g ? g[i] : 0.0);
+    if (vals) {
+      const int32_t r = d / nf, c = d - (d / nf) * nf;
+      int64_t lo = erp[r], hi = erp[r + 1];
+      while (lo < hi) {  // lower_bound of r in its row
+        const int64_t mid = (lo + hi) >> 1;
+        if (ecol[mid] < r) lo = mid + 1; else hi = mid;
+      }
+      const int64_t diag = rp[d] + (int64_t)nf * (lo - erp[r]) + c;
+      for (int64_t k = rp[d] + lane; k < rp[d + 1]; k += 32) vals[k] = k == diag ? 1.0 : 0.0;
+    }
+  }
+}
+
+// Vector CSR: LANES threads per row, strided over the row, shuffle reduction.
+template <typename T, int LANES>
+__global__ void __launch_bounds__(kThreads) k_spmv(int64_t n, const int64_t* __restrict__ rp,
+                                                   const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                                   const T* __restrict__ x, T* __restrict__ y, T alpha, T beta) {
+  const int sub = threadIdx.x % LANES;
+  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES;
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / LANES;
+  for (int64_t r = grp; r < n; r += ngrp) {
+    const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+    T s = T(0);
+    for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(x + __ldcs(col + k));
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LANES);
+    if (sub == 0) y[r] = beta == T(0) ? alpha * s : alpha * s + beta * y[r];
+  }
+}
+
+template <typename T>
+cudaError_t spmv_dispatch(int64_t n, const int64_t* rp, const int32_t* col, const T* vals, const T* x, T* y, T a,
+                          T b, int64_t nnz_hint, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const double avg = nnz_hint > 0 ? (double)nnz_hint / (double)n : 32.0;
+  if (avg <= 12) k_spmv<T, 4><<<grid_for(n, kThreads / 4, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  else if (avg <= 40) k_spmv<T, 8><<<grid_for(n, kThreads / 8, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  else if (avg <= 96) k_spmv<T, 16><<<grid_for(n, kThreads / 16, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  else k_spmv<T, 32><<<grid_for(n, kThreads / 32, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ reductions
+// Block partial sums into red[slot * kRedBlocks + block]; a one-block
+// finalize kernel writes the total.  Order is fixed: results are
+// reproducible run to run.
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void k_finalize(const double* __restrict__ red, int nslots, double* __restrict__ out) {
+  __shared__ double sh[32];
+  for (int s = 0; s < nslots; ++s) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) v += red[s * kRedBlocks + i];
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) out[s] = v;
+    __syncthreads();
+  }
+}
+
+__global__ void k_norm2sq(const double* __restrict__ x, int64_t n, double* __restrict__ red) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += x[i] * x[i];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) red[blockIdx.x] = s;
+}
+
+__global__ void k_fill(double* p, double v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_axpby(double* y, const double* x, double a, double b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
+// ------------------------------------------------------------ CG kernels
+// FP32 copy of A with symmetric Dirichlet elimination + Jacobi diagonal.
+__global__ void k_make_f32(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                           const double* __restrict__ v64, const uint8_t* __restrict__ mask, float* __restrict__ v32,
+                           float* __restrict__ dinv) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps) {
+    const bool dr = mask[r];
+    double diag = 0.0;
+    for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += 32) {
+      const int32_t c = col[k];
+      double v = v64[k];
+      if (dr || mask[c]) v = (c == r) ? 1.0 : 0.0;
+      v32[k] = (float)v;
+      if (c == r) diag = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) diag += __shfl_xor_sync(0xffffffffu, diag, o);
+    if (lane == 0) dinv[r] = diag != 0.0 ? (float)(1.0 / diag) : 1.0f;
+  }
+}
+
+__global__ void k_mask(int64_t n, const int32_t* lids, uint8_t* mask) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    mask[lids[i]] = 1;
+}
+
+// r32 = r64 (Dirichlet rows zero), z = dinv r, p = z, d = 0; partials rz, rr
+__global__ void k_cg_init(int64_t n, const double* __restrict__ r64, const uint8_t* __restrict__ mask,
+                          const float* __restrict__ dinv, float* r, float* z, float* p, float* d, double* red) {
+  __shared__ double sh[32];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float ri = mask[i] ? 0.0f : (float)r64[i];
+    const float zi = dinv[i] * ri;
+    r[i] = ri; z[i] = zi; p[i] = zi; d[i] = 0.0f;
+    rz += (double)ri * zi;
+    rr += (double)ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) red[0 * kRedBlocks + blockIdx.x] = rz;
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) red[1 * kRedBlocks + blockIdx.x] = rr;
+}
+
+// q = A p and partial dot(p, q)
+template <int LANES>
+__global__ void __launch_bounds__(kThreads) k_spmv_dot(int64_t n, const int64_t* __restrict__ rp,
+                                                       const int32_t* __restrict__ col, const float* __restrict__ vals,
+                                                       const float* __restrict__ p, float* __restrict__ q,
+                                                       double* __restrict__ red) {
+  __shared__ double sh[32];
+  const int sub = threadIdx.x % LANES;
+  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES;
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / LANES;
+  double pq = 0.0;
+  for (int64_t r = grp; r < n; r += ngrp) {
+    const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+    float s = 0.0f;
+    for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(p + __ldcs(col + k));
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LANES);
+    if (sub == 0) {
+      q[r] = s;
+      pq += (double)s * p[r];
+    }
+  }
+  pq = block_sum(pq, sh);
+  if (threadIdx.x == 0) red[2 * kRedBlocks + blockIdx.x] = pq;
+}
+
+// scal: [0] rz, [1] rr, [2] pq.  d += a p, r -= a q, z = dinv r; partial rz', rr'
+__global__ void k_cg_update(int64_t n, const double* __restrict__ scal, const float* __restrict__ dinv,
+                            const float* __restrict__ p, const float* __restrict__ q, float* r, float* z, float* d,
+                            double* red) {
+  __shared__ double sh[32];
+  const double pq = scal[2];
+  const float a = pq != 0.0 ? (float)(scal[0] / pq) : 0.0f;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    d[i] += a * p[i];
+    const float ri = r[i] - a * q[i];
+    const float zi = dinv[i] * ri;
+    r[i] = ri; z[i] = zi;
+    rz += (double)ri * zi;
+    rr += (double)ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) red[3 * kRedBlocks + blockIdx.x] = rz;
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) red[1 * kRedBlocks + blockIdx.x] = rr;
+}
+
+// new scalars: rz' = sum slot 3, rr' = slot 1; beta = rz'/rz; p = z + beta p; scal[0] = rz'
+__global__ void k_cg_finish(double* scal, const double* __restrict__ red) {
+  __shared__ double sh[32];
+  double rz = 0.0, rr = 0.0;
+  for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) {
+    rz += red[3 * kRedBlocks + i];
+    rr += red[1 * kRedBlocks + i];
+  }
+  rz = block_sum(rz, sh);
+  __syncthreads();
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    scal[3] = scal[0] != 0.0 ? rz / scal[0] : 0.0;  // beta
+    scal[0] = rz;
+    scal[1] = rr;
+  }
+}
+
+__global__ void k_cg_pupdate(int64_t n, const double* __restrict__ scal, const float* __restrict__ z, float* p) {
+  const float be = (float)scal[3];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + be * p[i];
+}
+
+__global__ void k_add_f32(int64_t n, double* x, const float* d) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += (double)d[i];
+}
+
+template <typename T>
+cudaError_t cmalloc(T*& p, size_t n) {
+  return cudaMalloc((void**)&p, sizeof(T) * (n > 0 ? n : 1));
+}
+
+}  // namespace
+
+cudaError_t launch_expand_rowptr(const int64_t* erp, int64_t n_ent, int nf, int64_t* rp, cudaStream_t s) {
+  if (n_ent <= 0) return cudaSuccess;
+  k_expand_rowptr<<<grid_for(n_ent, kThreads), kThreads, 0, s>>>(erp, n_ent, nf, rp);
+  return cudaGetLastError();
+}
+cudaError_t launch_expand_colind(const int64_t* erp, const int32_t* ecol, int64_t n_ent, int nf, const int64_t* rp,
+                                 int32_t* col, cudaStream_t s) {
+  if (n_ent <= 0) return cudaSuccess;
+  k_expand_colind<<<grid_for(n_ent, kThreads / 32), kThreads, 0, s>>>(erp, ecol, n_ent, nf, rp, col);
+  return cudaGetLastError();
+}
+cudaError_t launch_dirichlet(int64_t n, const int32_t* lids, const double* g, const double* x, double* f,
+                             const int64_t* rp, const int64_t* erp, const int32_t* ecol, int nf, double* vals,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_dirichlet<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, lids, g, x, f, rp, erp, ecol, nf, vals);
+  return cudaGetLastError();
+}
+cudaError_t launch_spmv_f64(int64_t n, const int64_t* rp, const int32_t* col, const double* vals, const double* x,
+                            double* y, double a, double b, int64_t nnz_hint, cudaStream_t s) {
+  return spmv_dispatch<double>(n, rp, col, vals, x, y, a, b, nnz_hint, s);
+}
+cudaError_t launch_spmv_f32(int64_t n, const int64_t* rp, const int32_t* col, const float* vals, const float* x,
+                            float* y, float a, float b, int64_t nnz_hint, cudaStream_t s) {
+  return spmv_dispatch<float>(n, rp, col, vals, x, y, a, b, nnz_hint, s);
+}
+cudaError_t launch_fill(double* p, double v, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_fill<<<grid_for(n, kThreads), kThreads, 0, s>>>(p, v, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_axpby<<<grid_for(n, kThreads), kThreads, 0, s>>>(y, x, a, b, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_norm2sq(const double* x, int64_t n, double* red, double* out, cudaStream_t s) {
+  cudaMemsetAsync(red, 0, sizeof(double) * kRedBlocks, s);
+  k_norm2sq<<<kRedBlocks, kThreads, 0, s>>>(x, n, red);
+  k_finalize<<<1, 1024, 0, s>>>(red, 1, out);
+  return cudaGetLastError();
+}
+
+cudaError_t solver_alloc(SolverWork& w, int64_t n, int64_t nnz) {
+  if (w.n == n && w.nnz == nnz && w.vals32) return cudaSuccess;
+  solver_free(w);
+  cudaError_t e;
+  if ((e = cmalloc(w.vals32, nnz)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.dinv, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.r, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.z, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.p, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.q, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.d, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.r64, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.mask, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.red, (size_t)kRedSlots * kRedBlocks)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.scal, 8)) != cudaSuccess) return e;
+  if ((e = cudaMallocHost((void**)&w.host_scal, sizeof(double) * 8)) != cudaSuccess) return e;
+  cudaMemset(w.red, 0, sizeof(double) * kRedSlots * kRedBlocks);
+  w.n = n; w.nnz = nnz;
+  return cudaSuccess;
+}
+
+void solver_free(SolverWork& w) {
+  cudaFree(w.vals32); cudaFree(w.dinv); cudaFree(w.r); cudaFree(w.z); cudaFree(w.p); cudaFree(w.q);
+  cudaFree(w.d); cudaFree(w.r64); cudaFree(w.mask); cudaFree(w.red); cudaFree(w.scal);
+  if (w.host_scal) cudaFreeHost(w.host_scal);
+  w = SolverWork();
+}
+
+int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const double* vals, int64_t n_dir,
+                const int32_t* dir, double* x, ResidualFn resid, void* ctx, double rtol, double inner_rtol,
+                int max_outer, int max_inner, double* stats, cudaStream_t s, std::string& err) {
+  const int64_t n = w.n;
+  const unsigned gb = kRedBlocks;
+  auto cuda_fail = [&](cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return TX_ECUDA;
+  };
+  cudaError_t e;
+  // FP32 operator with symmetric Dirichlet elimination
+  cudaMemsetAsync(w.mask, 0, n, s);
+  if (n_dir > 0) k_mask<<<grid_for(n_dir, kThreads), kThreads, 0, s>>>(n_dir, dir, w.mask);
+  k_make_f32<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, rp, col, vals, w.mask, w.vals32, w.dinv);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: make_f32");
+  const double avg = (double)w.nnz / (double)(n > 0 ? n : 1);
+  auto spmv_dot = [&]() {
+    if (avg <= 12) k_spmv_dot<4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    else if (avg <= 40) k_spmv_dot<8><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    else if (avg <= 96) k_spmv_dot<16><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    else k_spmv_dot<32><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+  };
+  double r0 = -1.0, rn = 0.0;
+  int outer = 0, inner_total = 0;
+  for (;; ++outer) {
+    int rc = resid(ctx, x, w.r64);
+    if (rc) { err = "cg: residual evaluation failed"; return rc; }
+    if ((e = launch_norm2sq(w.r64, n, w.red, w.scal + 4, s)) != cudaSuccess) return cuda_fail(e, "cg: norm");
+    cudaMemcpyAsync(w.host_scal, w.scal + 4, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cg: sync");
+    rn = std::sqrt(w.host_scal[0]);
+    if (r0 < 0.0) r0 = rn > 0.0 ? rn : 1.0;
+    if (rn <= rtol * r0 || outer >= max_outer) break;
+    // inner FP32 Jacobi-PCG on A32 d = r
+    k_cg_init<<<gb, kThreads, 0, s>>>(n, w.r64, w.mask, w.dinv, w.r, w.z, w.p, w.d, w.red);
+    k_finalize<<<1, 1024, 0, s>>>(w.red, 2, w.scal);  // scal[0] = rz, scal[1] = rr
+    cudaMemcpyAsync(w.host_scal, w.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cg: init");
+    const double rr0 = w.host_scal[1];
+    const double target = inner_rtol * inner_rtol * rr0;
+    int it = 0;
+    const int check = 16;
+    while (it < max_inner) {
+      for (int k = 0; k < check && it < max_inner; ++k, ++it) {
+        spmv_dot();
+        k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2);  // pq
+        k_cg_update<<<gb, kThreads, 0, s>>>(n, w.scal, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
+        k_cg_finish<<<1, 1024, 0, s>>>(w.scal, w.red);
+        k_cg_pupdate<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, w.scal, w.z, w.p);
+      }
+      cudaMemcpyAsync(w.host_scal, w.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cg: iterate");
+      if (!(w.host_scal[1] > target)) break;  // also stops on NaN
+    }
+    inner_total += it;
+    k_add_f32<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, x, w.d);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: update");
+  }
+  if (stats) {
+    stats[0] = outer;
+    stats[1] = inner_total;
+    stats[2] = rn / r0;
+    stats[3] = r0;
+  }
+  return (rn <= rtol * r0) ? TX_OK : TX_ETIMEDOUT;
+}
+
+}  // namespace tx

@@ -1,0 +1,281 @@
+"""Panzer/Tianxin-shaped host API over the C-ABI (device memory via torch).
+
+Class and method names follow the reference so a caller of the reference's
+assembly path finds the same objects:
+
+  CartesianConnManager      dof-mgr/test/cartesian_topology/CartesianConnManager.hpp
+  DOFManager                dof-mgr/src/Panzer_DOFManager.hpp (GlobalIndexer queries)
+  TpetraLinearObjFactory    disc-fe/src/lof/Panzer_TpetraLinearObjFactory_decl.hpp
+  CrsMatrix                 Tpetra::CrsMatrix local layout (rowptr, colind, values)
+  DirichletBC               TianXin::DirichletEvalautor parameter list
+  ModelEvaluator.evalModel  disc-fe/src/Panzer_ModelEvaluator_impl.hpp:1714-1882
+  AssemblyEngine.evaluate   disc-fe/src/Panzer_AssemblyEngine_impl.hpp:65-182
+
+Errors from the library raise TxError (the reference throws std::logic_error /
+TEUCHOS_TEST_FOR_EXCEPTION in the same places).
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _abi
+from ._lib import TxError, check, load
+
+HEX, TET = _abi.TX_TOPO_HEX, _abi.TX_TOPO_TET
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class CartesianConnManager:
+    """Brick lattice on one rank; blocks named eblock-i_j_k (i slowest)."""
+
+    def __init__(self, nx, ny, nz, bx=1, by=1, bz=1, topology=HEX, lengths=(1.0, 1.0, 1.0), jitter=0.0, seed=0):
+        self.lib = load()
+        self.desc = _abi.mesh_desc((nx, ny, nz), (bx, by, bz), topology, lengths, jitter, seed)
+        h = C.c_void_p()
+        rc = self.lib.tx_mesh_create(C.byref(self.desc), C.byref(h))
+        if rc != 0:
+            raise TxError(rc, "tx_mesh_create: invalid mesh description")
+        self.h = h
+        ne, nv, nb = C.c_int64(), C.c_int64(), C.c_int32()
+        self.lib.tx_mesh_sizes(self.h, C.byref(ne), C.byref(nv), C.byref(nb))
+        self.n_elements, self.n_vertices, self.n_blocks = ne.value, nv.value, nb.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.tx_destroy(self.h)
+            self.h = None
+
+    def numElementBlocks(self):
+        return self.n_blocks
+
+    def getElementBlockIds(self):
+        d = self.desc
+        return [f"eblock-{i}_{j}_{k}" for i in range(d.bx) for j in range(d.by) for k in range(d.bz)]
+
+    def getElementBlock(self, block):
+        n = C.c_int64()
+        check(self.h, self.lib.tx_mesh_block_elements(self.h, block, C.byref(n), None))
+        out = np.zeros(n.value, np.int64)
+        check(self.h, self.lib.tx_mesh_block_elements(self.h, block, C.byref(n), _np_ptr(out)))
+        return out
+
+    def coordinates(self):
+        out = np.zeros((self.n_vertices, 3))
+        check(self.h, self.lib.tx_mesh_coordinates(self.h, _np_ptr(out)))
+        return out
+
+
+class DOFManager:
+    """buildGlobalUnknowns for the fields of one equation set on a mesh."""
+
+    def __init__(self, conn, eqset, require_device=True):
+        self.conn, self.eqset, self.lib, self.h = conn, eqset, conn.lib, conn.h
+        rc = self.lib.tx_dof_build(self.h, C.byref(eqset))
+        if rc != 0 and (require_device or rc != _abi.TX_ECUDA):
+            check(self.h, rc, "tx_dof_build")
+        self.device_ready = rc == 0
+        n, ndm, nnz, nf = C.c_int64(), C.c_int32(), C.c_int64(), C.c_int32()
+        check(self.h, self.lib.tx_dof_sizes(self.h, C.byref(n), C.byref(ndm), C.byref(nnz), C.byref(nf)))
+        self.n_dofs, self.max_gid_count, self.nnz, self.n_fields = n.value, ndm.value, nnz.value, nf.value
+        self.field_names = _abi.field_names(eqset.physics)
+
+    # GlobalIndexer queries --------------------------------------------------
+    def getFieldNum(self, name):
+        return self.field_names.index(name)
+
+    def getFieldString(self, num):
+        return self.field_names[num]
+
+    def getNumFields(self):
+        return self.n_fields
+
+    def getOwnedIndices(self):
+        out = np.zeros(self.n_dofs, np.int64)
+        check(self.h, self.lib.tx_dof_owned_gids(self.h, _np_ptr(out)))
+        return out
+
+    def getElementBlockGIDCount(self, block):
+        n = C.c_int32()
+        check(self.h, self.lib.tx_dof_block_gid_count(self.h, block, C.byref(n)))
+        return n.value
+
+    def getElementGIDs(self, block):
+        ne = len(self.conn.getElementBlock(block))
+        out = np.zeros((ne, self.getElementBlockGIDCount(block)), np.int64)
+        check(self.h, self.lib.tx_dof_element_gids(self.h, block, _np_ptr(out)))
+        return out
+
+    def getElementLIDs(self, block):
+        ne = len(self.conn.getElementBlock(block))
+        out = np.zeros((ne, self.getElementBlockGIDCount(block)), np.int32)
+        check(self.h, self.lib.tx_dof_element_lids(self.h, block, _np_ptr(out)))
+        return out
+
+    def getGIDFieldOffsets(self, block, field):
+        n = C.c_int32()
+        check(self.h, self.lib.tx_dof_field_offsets(self.h, block, field, C.byref(n), None))
+        out = np.zeros(n.value, np.int32)
+        check(self.h, self.lib.tx_dof_field_offsets(self.h, block, field, C.byref(n), _np_ptr(out)))
+        return out
+
+    def dirichletDofs(self, side_mask, field_mask=0x7):
+        """Sorted local DOF ids of the fields in field_mask on the given box sides."""
+        n = C.c_int64()
+        check(self.h, self.lib.tx_dirichlet_dofs(self.h, side_mask, field_mask, C.byref(n), None))
+        out = np.zeros(n.value, np.int32)
+        check(self.h, self.lib.tx_dirichlet_dofs(self.h, side_mask, field_mask, C.byref(n), _np_ptr(out)))
+        return out
+
+
+class CrsMatrix:
+    """Tpetra local CRS on the device: rowptr int64, colind int32, values f64."""
+
+    def __init__(self, dof, rowptr, colind, values=None):
+        self.dof, self.rowptr, self.colind = dof, rowptr, colind
+        self.values = values if values is not None else torch.zeros(colind.numel(), dtype=torch.float64,
+                                                                      device=colind.device)
+        self.n_rows = rowptr.numel() - 1
+
+    def initializeMatrix(self, v=0.0):
+        self.values.fill_(v)
+
+    def apply(self, x, y=None, alpha=1.0, beta=0.0, values=None):
+        """y = alpha A x + beta y (Tpetra::CrsMatrix::apply); f64 or f32 by dtype of values."""
+        vals = self.values if values is None else values
+        prec = _abi.TX_SPMV_F64 if vals.dtype == torch.float64 else _abi.TX_SPMV_F32
+        if y is None:
+            y = torch.zeros(self.n_rows, dtype=vals.dtype, device=vals.device)
+        lib = self.dof.lib
+        lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(self.dof.h, lib.tx_spmv(self.dof.h, prec, self.n_rows, _ptr(self.rowptr), _ptr(self.colind), _ptr(vals),
+                                      _ptr(x), _ptr(y), alpha, beta), "tx_spmv")
+        return y
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.values.cpu().numpy(), self.colind.cpu().numpy(), self.rowptr.cpu().numpy()),
+                             shape=(self.n_rows, self.n_rows))
+
+
+class TpetraLinearObjFactory:
+    """Owns the CRS graph (buildGhostedGraph; one rank: ghosted == owned)."""
+
+    def __init__(self, dof, device="cuda"):
+        self.dof, self.device = dof, device
+        self.rowptr = torch.empty(dof.n_dofs + 1, dtype=torch.int64, device=device)
+        self.colind = torch.empty(dof.nnz, dtype=torch.int32, device=device)
+        dof.lib.tx_set_stream(dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(dof.h, dof.lib.tx_graph_build(dof.h, _ptr(self.rowptr), _ptr(self.colind)), "tx_graph_build")
+
+    def buildGraph(self):
+        return self.rowptr, self.colind
+
+    def getTpetraMatrix(self):
+        return CrsMatrix(self.dof, self.rowptr, self.colind)
+
+    def getTpetraVector(self):
+        return torch.zeros(self.dof.n_dofs, dtype=torch.float64, device=self.device)
+
+
+class DirichletBC:
+    """Dirichlet parameter list: DOF Names on the box sides (a side mask), value g."""
+
+    def __init__(self, dof, side_mask, fields=None, value=0.0):
+        names = fields if fields is not None else dof.field_names
+        mask = 0
+        for n in names:
+            mask |= 1 << dof.getFieldNum(n)
+        self.lids_host = dof.dirichletDofs(side_mask, mask)
+        self.lids = torch.from_numpy(self.lids_host).to("cuda")
+        if np.isscalar(value):
+            self.g = None if value == 0.0 else torch.full((len(self.lids_host),), float(value), dtype=torch.float64,
+                                                           device="cuda")
+        else:
+            self.g = torch.as_tensor(value, dtype=torch.float64, device="cuda")
+
+
+class AssemblyEngine:
+    """Volume fill of every block (or one workset range of a block)."""
+
+    def __init__(self, lof):
+        self.lof, self.dof = lof, lof.dof
+
+    def evaluate(self, x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False,
+                 block=-1, workset=(0, -1)):
+        a = _abi.EvalArgs()
+        a.x, a.x_dot, a.aux = _ptr(x), _ptr(x_dot), _ptr(aux)
+        a.alpha, a.beta, a.t = alpha, beta, t
+        a.f = _ptr(f)
+        a.crs_vals = _ptr(W.values) if W is not None else None
+        a.block = block
+        a.elem_begin, a.elem_end = workset
+        a.flags = _abi.TX_EVAL_MIXED if mixed else 0
+        lib = self.dof.lib
+        lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(self.dof.h, lib.tx_eval(self.dof.h, C.byref(a)), "tx_eval")
+
+
+class ModelEvaluator:
+    """evalModel(inArgs{x, x_dot, alpha, beta, t}, outArgs{f, W}) on the device."""
+
+    def __init__(self, lof, dirichlet=()):
+        self.lof, self.dof = lof, lof.dof
+        self.ae = AssemblyEngine(lof)
+        self.dirichlet = list(dirichlet)
+
+    def create_W_op(self):
+        return self.lof.getTpetraMatrix()
+
+    def evalModel(self, x, x_dot=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, aux=None, mixed=False,
+                  zero=True):
+        if zero:
+            if f is not None:
+                f.zero_()
+            if W is not None:
+                W.initializeMatrix(0.0)
+        self.ae.evaluate(x, x_dot, aux, alpha, beta, t, f, W, mixed)
+        self.applyDirichlet(x, f, W)
+        return f, W
+
+    def applyDirichlet(self, x, f=None, W=None):
+        lib = self.dof.lib
+        for bc in self.dirichlet:
+            check(self.dof.h, lib.tx_dirichlet_apply(self.dof.h, len(bc.lids_host), _ptr(bc.lids), _ptr(bc.g), _ptr(x),
+                                                     _ptr(f), _ptr(W.values) if W is not None else None),
+                  "tx_dirichlet_apply")
+
+    def dirichlet_lids(self):
+        if not self.dirichlet:
+            return torch.zeros(0, dtype=torch.int32, device="cuda"), None
+        lids = torch.cat([bc.lids for bc in self.dirichlet])
+        gs = [bc.g if bc.g is not None else torch.zeros(len(bc.lids_host), dtype=torch.float64, device="cuda")
+              for bc in self.dirichlet]
+        return lids, torch.cat(gs)
+
+    def solve(self, W, x, b=None, rtol=1e-10, inner_rtol=1e-5, max_outer=50, max_inner=100000, matrix_free=False,
+              x_dot=None, alpha=0.0, beta=1.0, t=0.0):
+        """FP64 iterative refinement around FP32 Jacobi-CG; x updated in place. Returns stats."""
+        lids, g = self.dirichlet_lids()
+        a = _abi.SolveArgs()
+        a.rowptr, a.colind, a.vals = _ptr(W.rowptr), _ptr(W.colind), _ptr(W.values)
+        a.b, a.x = _ptr(b), _ptr(x)
+        a.n_dirichlet, a.dirichlet_lids, a.dirichlet_g = lids.numel(), _ptr(lids), _ptr(g)
+        a.rtol, a.inner_rtol, a.max_outer, a.max_inner = rtol, inner_rtol, max_outer, max_inner
+        a.flags = _abi.TX_SOLVE_MATRIX_FREE_RESIDUAL if matrix_free else 0
+        a.x_dot, a.alpha, a.beta, a.t = _ptr(x_dot), alpha, beta, t
+        lib = self.dof.lib
+        lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(self.dof.h, lib.tx_solve_cg_ir(self.dof.h, C.byref(a)), "tx_solve_cg_ir")
+        return {"outer": int(a.stats[0]), "inner": int(a.stats[1]), "relres": a.stats[2], "r0": a.stats[3]}
+
+
+def synchronize(dof):
+    check(dof.h, dof.lib.tx_synchronize(dof.h), "tx_synchronize")
