@@ -118,7 +118,8 @@ enum tx_source {
 
 /* Evaluation flags. */
 #define TX_EVAL_MIXED 0x1u          /* FP32 element contractions, FP64 scatter   */
-#define TX_EVAL_DETERMINISTIC 0x2u  /* fixed summation order (no atomics)       */
+#define TX_EVAL_DETERMINISTIC 0x2u  /* fixed summation order: coloured scatter, no atomics  */
+#define TX_EVAL_PERSISTENT 0x4u     /* every block's worksets in one persistent launch      */
 
 typedef struct tx_eval_args {
   const double* x;         /* solution, LID order (GED "... - X")                       */
@@ -226,6 +227,28 @@ typedef struct tx_solve_args {
   double stats[4];
 } tx_solve_args;
 int tx_solve_cg_ir(tx_handle h, tx_solve_args* args);
+
+/* Worksets (WorksetContainer::setWorksetSize, disc-fe/src/Panzer_WorksetContainer.hpp:104)
+ * of the TX_EVAL_PERSISTENT evaluation: consecutive element ranges of every
+ * block with sizes drawn uniformly in [min_size, max_size] from seed
+ * (min == max: even worksets). */
+int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t seed);
+/* Upper bound on the CTAs of assembly launches (0: occupancy-derived); the
+ * tile-shape knob the autotuner sets (HierarchicParallelism's role,
+ * disc-fe/src/Panzer_HierarchicParallelism.hpp:78-128). */
+int tx_set_grid_cap(tx_handle h, int32_t max_ctas);
+
+/* Many independent meshes in one persistent launch: the volume fill of every
+ * block of every handle, cut into worksets, is one work list.  args holds one
+ * tx_eval_args per handle (same precision and evaluation type for all).  The
+ * reference evaluates meshes one ModelEvaluator at a time; this has no
+ * single counterpart there. */
+typedef struct tx_batch_s* tx_batch;
+int tx_batch_create(const tx_handle* handles, int32_t n, tx_batch* out);
+int tx_batch_set_worksets(tx_batch b, int64_t min_size, int64_t max_size, uint64_t seed, int32_t max_ctas);
+int tx_batch_eval(tx_batch b, const tx_eval_args* args);
+const char* tx_batch_last_error(tx_batch b);
+void tx_batch_destroy(tx_batch b);
 
 /* Stream the handle's work is ordered on (cudaStream_t as void*); set NULL
  * to use the legacy default stream. */

@@ -1,0 +1,157 @@
+"""GPU parity of the fused assembly path against the oracle (run on a GB300).
+
+Bars (from the path's contract):
+  * CRS graph, numbering, element-to-row maps: bit-exact.
+  * FP64 residual and Jacobian: max|gpu - oracle| <= 1e-12 * max|oracle|.
+  * Mixed (FP32 element contractions, FP64 scatter): <= 2e-5 * max|oracle|
+    (FP32 rounding of O(10)-term element sums; the error is stated, and the
+    solve tests show FP64 refinement recovers <= 1e-10).
+"""
+import numpy as np
+import pytest
+import torch
+
+import tianxin_gb300 as tx
+from oracle import oracle as O
+from tianxin_gb300 import _abi as A
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 2e-5
+
+PARAMS = {
+    A.TX_PHYS_POISSON: (1.0, 0.5, 1.0, 2.0),
+    A.TX_PHYS_ELASTICITY: (1.0, 0.3, 0.1, -0.2, -1.0, 0.7),
+    A.TX_PHYS_HEAT: (1.0, 0.5, 1.0),
+    A.TX_PHYS_MAXWELL: (1.0, 1.0),
+}
+
+CASES = [
+    ("poisson_hex8", (4, 3, 3), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_HGRAD_C1, A.TX_SOURCE_SINE),
+    ("elasticity_hex8", (3, 3, 4), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1, 0),
+    ("heat_hex8", (3, 3, 3), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_HEAT, A.TX_HGRAD_C1, 0),
+    ("poisson_tet4", (3, 2, 3), (1, 1, 1), A.TX_TOPO_TET, A.TX_PHYS_POISSON, A.TX_HGRAD_C1, A.TX_SOURCE_AFFINE),
+    ("elasticity_tet4", (2, 3, 3), (1, 1, 1), A.TX_TOPO_TET, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1, 0),
+    ("poisson_hex27", (2, 3, 2), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_HGRAD_C2, A.TX_SOURCE_SINE),
+    ("heat_hex27", (2, 2, 3), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_HEAT, A.TX_HGRAD_C2, 0),
+    ("heat_tet10", (2, 2, 2), (1, 1, 1), A.TX_TOPO_TET, A.TX_PHYS_HEAT, A.TX_HGRAD_C2, 0),
+    ("heat_hex27_tet10", (2, 2, 2), (2, 1, 1), [A.TX_TOPO_HEX, A.TX_TOPO_TET], A.TX_PHYS_HEAT, A.TX_HGRAD_C2, 0),
+    ("maxwell_nedelec", (3, 2, 3), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_MAXWELL, A.TX_HCURL_I1, 0),
+]
+IDS = [c[0] for c in CASES]
+
+
+def build(n, blocks, topo, phys, basis, source, jitter=0.1, seed=5):
+    m = A.mesh_desc(n, blocks, topo, jitter=jitter, seed=seed)
+    q = A.equation_set(phys, basis, params=PARAMS[phys], source_kind=source)
+    o = O.Oracle(m, q)
+    conn = tx.CartesianConnManager(*n, *blocks, topology=topo, jitter=jitter, seed=seed)
+    dof = tx.DOFManager(conn, q)
+    lof = tx.TpetraLinearObjFactory(dof)
+    return o, conn, dof, lof
+
+
+def state(n, seed=11):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-1, 1, n), rng.uniform(-1, 1, n), rng.standard_normal(n)
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def gpu_eval(dof, lof, x, xd, aux, alpha, beta, mixed=False, jacobian=True, dirichlet=()):
+    me = tx.ModelEvaluator(lof, dirichlet)
+    dev = lambda a: torch.from_numpy(a).cuda()
+    f = lof.getTpetraVector()
+    W = me.create_W_op() if jacobian else None
+    me.evalModel(dev(x), dev(xd), alpha=alpha, beta=beta, f=f, W=W, aux=dev(aux), mixed=mixed)
+    torch.cuda.synchronize()
+    return f.cpu().numpy(), (W.values.cpu().numpy() if jacobian else None)
+
+
+@pytest.mark.parametrize("name,n,blocks,topo,phys,basis,source", CASES, ids=IDS)
+def test_graph_bit_exact(cuda, name, n, blocks, topo, phys, basis, source):
+    o, _, dof, lof = build(n, blocks, topo, phys, basis, source)
+    rp, ci = o.graph()
+    assert np.array_equal(lof.rowptr.cpu().numpy(), rp)
+    assert np.array_equal(lof.colind.cpu().numpy(), ci)
+
+
+@pytest.mark.parametrize("name,n,blocks,topo,phys,basis,source", CASES, ids=IDS)
+def test_fp64_residual_jacobian(cuda, name, n, blocks, topo, phys, basis, source):
+    o, _, dof, lof = build(n, blocks, topo, phys, basis, source)
+    x, xd, aux = state(o.n_dofs)
+    alpha, beta = 0.75, 1.25
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=alpha, beta=beta)
+    f, v = gpu_eval(dof, lof, x, xd, aux, alpha, beta)
+    assert rel(f, f_ref) <= FP64_TOL, rel(f, f_ref)
+    assert rel(v, v_ref) <= FP64_TOL, rel(v, v_ref)
+
+
+@pytest.mark.parametrize("name,n,blocks,topo,phys,basis,source", CASES, ids=IDS)
+def test_mixed_residual_jacobian(cuda, name, n, blocks, topo, phys, basis, source):
+    o, _, dof, lof = build(n, blocks, topo, phys, basis, source)
+    x, xd, aux = state(o.n_dofs)
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=0.5, beta=1.0)
+    f, v = gpu_eval(dof, lof, x, xd, aux, 0.5, 1.0, mixed=True)
+    assert rel(f, f_ref) <= MIXED_TOL, rel(f, f_ref)
+    assert rel(v, v_ref) <= MIXED_TOL, rel(v, v_ref)
+
+
+@pytest.mark.parametrize("name,n,blocks,topo,phys,basis,source", CASES[:3] + CASES[8:], ids=IDS[:3] + IDS[8:])
+def test_residual_type_and_worksets(cuda, name, n, blocks, topo, phys, basis, source):
+    # Residual evaluation type (no W) over uneven worksets sums to the full evaluation
+    o, conn, dof, lof = build(n, blocks, topo, phys, basis, source)
+    x, xd, aux = state(o.n_dofs, seed=3)
+    f_ref, _ = o.evaluate(x, xd, aux, alpha=0.0, beta=1.0, jacobian=False)
+    dev = lambda a: torch.from_numpy(a).cuda()
+    f = lof.getTpetraVector()
+    ae = tx.AssemblyEngine(lof)
+    for b in range(conn.n_blocks):
+        ne = len(conn.getElementBlock(b))
+        cuts = sorted({0, ne, ne // 3, (2 * ne) // 3 + 1})
+        for lo, hi in zip(cuts[:-1], cuts[1:]):
+            ae.evaluate(dev(x), dev(xd), dev(aux), 0.0, 1.0, 0.0, f, None, block=b, workset=(lo, hi))
+    torch.cuda.synchronize()
+    assert rel(f.cpu().numpy(), f_ref) <= FP64_TOL
+
+
+@pytest.mark.parametrize("name,n,blocks,topo,phys,basis,source", [CASES[0], CASES[1], CASES[7]],
+                         ids=[IDS[0], IDS[1], IDS[7]])
+def test_dirichlet_rows(cuda, name, n, blocks, topo, phys, basis, source):
+    o, _, dof, lof = build(n, blocks, topo, phys, basis, source)
+    x, xd, aux = state(o.n_dofs, seed=5)
+    bc = tx.DirichletBC(dof, A.SIDE_ZMIN | A.SIDE_XMAX, value=0.25)
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=0.0, beta=1.0)
+    o.dirichlet_apply(bc.lids_host, np.full(len(bc.lids_host), 0.25), x, f_ref, v_ref)
+    f, v = gpu_eval(dof, lof, x, xd, aux, 0.0, 1.0, dirichlet=[bc])
+    assert rel(f, f_ref) <= FP64_TOL
+    assert rel(v, v_ref) <= FP64_TOL
+
+
+def test_element_range_errors(cuda):
+    _, conn, dof, lof = build((2, 2, 2), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_HGRAD_C1, 0)
+    ae = tx.AssemblyEngine(lof)
+    x = lof.getTpetraVector()
+    with pytest.raises(tx.TxError) as e:
+        ae.evaluate(x, block=0, workset=(0, 9))
+    assert e.value.code == A.TX_ERANGE
+    with pytest.raises(tx.TxError) as e:
+        ae.evaluate(x, block=3)
+    assert e.value.code == A.TX_ERANGE
+
+
+def test_scatter_pattern_counts_gpu(cuda):
+    # per-element constant contribution: f = v * (elements sharing the node), v..8v
+    n = 3
+    m = A.mesh_desc(n)
+    q = A.equation_set(A.TX_PHYS_POISSON, params=(0.0, 0.0, 0.0, 1.0))
+    dof = tx.DOFManager(tx.CartesianConnManager(n, n, n), q)
+    lof = tx.TpetraLinearObjFactory(dof)
+    f = lof.getTpetraVector()
+    tx.AssemblyEngine(lof).evaluate(lof.getTpetraVector(), f=f)
+    ratio = f.cpu().numpy() / (-(1.0 / n) ** 3 / 8)
+    assert set(np.round(ratio).astype(int)) == {1, 2, 4, 8}
+    assert np.allclose(ratio, np.round(ratio), atol=1e-12, rtol=0)

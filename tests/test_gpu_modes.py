@@ -1,0 +1,97 @@
+"""Deterministic (coloured), persistent (one-launch worksets) and batched
+(many meshes, one launch) evaluation against the oracle on the GPU."""
+import numpy as np
+import pytest
+import torch
+
+import tianxin_gb300 as tx
+from oracle import oracle as O
+from tianxin_gb300 import _abi as A
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 2e-5
+
+PARAMS = {
+    A.TX_PHYS_POISSON: (1.0, 0.5, 1.0, 2.0),
+    A.TX_PHYS_ELASTICITY: (1.0, 0.3, 0.1, -0.2, -1.0, 0.7),
+    A.TX_PHYS_HEAT: (1.0, 0.5, 1.0),
+    A.TX_PHYS_MAXWELL: (1.0, 1.0),
+}
+
+
+def build(n, blocks, topo, phys, basis, source=0, jitter=0.1, seed=5):
+    m = A.mesh_desc(n, blocks, topo, jitter=jitter, seed=seed)
+    q = A.equation_set(phys, basis, params=PARAMS[phys], source_kind=source)
+    o = O.Oracle(m, q)
+    conn = tx.CartesianConnManager(*n, *blocks, topology=topo, jitter=jitter, seed=seed)
+    dof = tx.DOFManager(conn, q)
+    lof = tx.TpetraLinearObjFactory(dof)
+    return o, dof, lof
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def run(dof, lof, x, xd, aux, mixed=False, **kw):
+    dev = lambda a: torch.from_numpy(a).cuda()
+    f = lof.getTpetraVector()
+    W = lof.getTpetraMatrix()
+    tx.AssemblyEngine(lof).evaluate(dev(x), dev(xd), dev(aux), 0.5, 1.0, 0.0, f, W, mixed, **kw)
+    torch.cuda.synchronize()
+    return f.cpu().numpy(), W.values.cpu().numpy()
+
+
+@pytest.mark.parametrize("topo,phys,basis", [(A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1),
+                                             (A.TX_TOPO_TET, A.TX_PHYS_POISSON, A.TX_HGRAD_C1),
+                                             (A.TX_TOPO_TET, A.TX_PHYS_HEAT, A.TX_HGRAD_C2)])
+def test_deterministic_is_bitwise_reproducible(cuda, topo, phys, basis):
+    o, dof, lof = build((4, 3, 3), (1, 1, 1), topo, phys, basis)
+    rng = np.random.default_rng(1)
+    x, xd, aux = rng.uniform(-1, 1, o.n_dofs), rng.uniform(-1, 1, o.n_dofs), rng.standard_normal(o.n_dofs)
+    f1, v1 = run(dof, lof, x, xd, aux, deterministic=True)
+    f2, v2 = run(dof, lof, x, xd, aux, deterministic=True)
+    assert np.array_equal(f1, f2) and np.array_equal(v1, v2)
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=0.5, beta=1.0)
+    assert rel(f1, f_ref) <= FP64_TOL and rel(v1, v_ref) <= FP64_TOL
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_persistent_mixed_families_uneven_worksets(cuda, mixed):
+    # hex27 + tet10 blocks, worksets of 5..17 elements, one launch
+    o, dof, lof = build((2, 3, 2), (2, 1, 1), [A.TX_TOPO_HEX, A.TX_TOPO_TET], A.TX_PHYS_HEAT, A.TX_HGRAD_C2)
+    rng = np.random.default_rng(2)
+    x, xd, aux = rng.uniform(0, 1, o.n_dofs), np.zeros(o.n_dofs), np.zeros(o.n_dofs)
+    ae = tx.AssemblyEngine(lof)
+    ae.setWorksetSize(5, 17, seed=3)
+    f, v = run(dof, lof, x, xd, aux, mixed=mixed, persistent=True)
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=0.5, beta=1.0)
+    tol = MIXED_TOL if mixed else FP64_TOL
+    assert rel(f, f_ref) <= tol and rel(v, v_ref) <= tol
+
+
+def test_batch_of_meshes_one_launch(cuda):
+    cases = [((3, 2, 2), A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_HGRAD_C1),
+             ((2, 2, 3), A.TX_TOPO_TET, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1),
+             ((2, 3, 2), A.TX_TOPO_HEX, A.TX_PHYS_MAXWELL, A.TX_HCURL_I1),
+             ((4, 4, 4), A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_HGRAD_C1)]
+    rng = np.random.default_rng(4)
+    built, xs, xds, auxs, fs, Ws, refs = [], [], [], [], [], [], []
+    for i, (n, topo, phys, basis) in enumerate(cases):
+        o, dof, lof = build(n, (1, 1, 1), topo, phys, basis, seed=10 + i)
+        x, xd, aux = rng.uniform(-1, 1, o.n_dofs), rng.uniform(-1, 1, o.n_dofs), rng.standard_normal(o.n_dofs)
+        built.append((o, dof, lof))
+        xs.append(torch.from_numpy(x).cuda())
+        xds.append(torch.from_numpy(xd).cuda())
+        auxs.append(torch.from_numpy(aux).cuda())
+        fs.append(lof.getTpetraVector())
+        Ws.append(lof.getTpetraMatrix())
+        refs.append(o.evaluate(x, xd, aux, alpha=0.5, beta=1.0))
+    batch = tx.Batch([b[1] for b in built], workset=(3, 11), seed=9)
+    batch.evaluate(xs, fs, Ws, xds, auxs, alpha=0.5, beta=1.0)
+    torch.cuda.synchronize()
+    for i, (f_ref, v_ref) in enumerate(refs):
+        assert rel(fs[i].cpu().numpy(), f_ref) <= FP64_TOL, i
+        assert rel(Ws[i].values.cpu().numpy(), v_ref) <= FP64_TOL, i

@@ -30,6 +30,7 @@ TX_SOURCE_AFFINE = 2
 
 TX_EVAL_MIXED = 0x1
 TX_EVAL_DETERMINISTIC = 0x2
+TX_EVAL_PERSISTENT = 0x4
 
 TX_SPMV_F64 = 0
 TX_SPMV_F32 = 1

@@ -33,6 +33,13 @@ SIGNATURES = {
     "tx_dirichlet_apply": (C.c_int, [P, I64, P, P, P, P, P]),
     "tx_spmv": (C.c_int, [P, I32, I64, P, P, P, P, P, D, D]),
     "tx_solve_cg_ir": (C.c_int, [P, C.POINTER(_abi.SolveArgs)]),
+    "tx_set_worksets": (C.c_int, [P, I64, I64, C.c_uint64]),
+    "tx_set_grid_cap": (C.c_int, [P, I32]),
+    "tx_batch_create": (C.c_int, [P, I32, C.POINTER(P)]),
+    "tx_batch_set_worksets": (C.c_int, [P, I64, I64, C.c_uint64, I32]),
+    "tx_batch_eval": (C.c_int, [P, P]),
+    "tx_batch_last_error": (C.c_char_p, [P]),
+    "tx_batch_destroy": (None, [P]),
     "tx_set_stream": (C.c_int, [P, P]),
     "tx_synchronize": (C.c_int, [P]),
 }

@@ -15,13 +15,50 @@
 namespace {
 
 struct DevBlock {
-  int topo = 0, basis = 0, nq = 0, nb = 0, nv = 0;
+  int topo = 0, basis = 0, nq = 0, nb = 0, nv = 0, kind = -1;
   int64_t n_elem = 0;
   int32_t* vconn = nullptr;
   int32_t* dconn = nullptr;
   uint8_t* epos = nullptr;
   int8_t* esign = nullptr;
   double* ref = nullptr;
+  int32_t* color_perm = nullptr;
+  std::vector<int64_t> color_offsets;
+  tx::BlockView view() const { return tx::BlockView{topo, basis, nq, nb, nv, n_elem, vconn, dconn, epos, esign, ref}; }
+};
+
+// Pinned staging for small per-call tables (kernel parameters of batched
+// launches): the copy is stream ordered; before the host buffer is reused
+// the previous copy is waited for.
+struct Staging {
+  void* host = nullptr;
+  void* dev = nullptr;
+  size_t cap = 0;
+  cudaEvent_t ev = nullptr;
+  bool pending = false;
+  cudaError_t put(const void* src, size_t n, cudaStream_t s) {
+    cudaError_t e;
+    if (pending && (e = cudaEventSynchronize(ev)) != cudaSuccess) return e;
+    if (n > cap) {
+      cudaFreeHost(host);
+      cudaFree(dev);
+      cap = n < 4096 ? 4096 : 2 * n;
+      if ((e = cudaMallocHost(&host, cap)) != cudaSuccess) return e;
+      if ((e = cudaMalloc(&dev, cap)) != cudaSuccess) return e;
+      if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+    }
+    std::memcpy(host, src, n);
+    if ((e = cudaMemcpyAsync(dev, host, n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+    pending = true;
+    return cudaEventRecord(ev, s);
+  }
+  void release() {
+    if (pending && ev) cudaEventSynchronize(ev);
+    cudaFreeHost(host);
+    cudaFree(dev);
+    if (ev) cudaEventDestroy(ev);
+    *this = Staging();
+  }
 };
 
 template <typename T>
@@ -55,11 +92,23 @@ struct tx_handle_s {
   std::string err;
   tx::SolverWork solver;
   int grid_cap = 0;
+  // worksets of the persistent (one launch) evaluation
+  int64_t ws_min = 512, ws_max = 512;
+  uint64_t ws_seed = 0;
+  std::vector<tx::WorkItem> items;   // host copy, rebuilt when the worksets change
+  tx::WorkItem* d_items = nullptr;
+  int* d_counter = nullptr;
+  Staging stage;
 
   void free_dofs() {
     for (auto& b : blocks) {
       cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
+      cudaFree(b.color_perm);
     }
+    cudaFree(d_items); cudaFree(d_counter);
+    d_items = nullptr; d_counter = nullptr;
+    items.clear();
+    stage.release();
     blocks.clear();
     cudaFree(d_erowptr); cudaFree(d_ecol); cudaFree(d_rowptr);
     d_erowptr = nullptr; d_ecol = nullptr; d_rowptr = nullptr;
@@ -95,8 +144,7 @@ int guarded(tx_handle h, F&& body) {
   }
 }
 
-// Evaluate every requested block/range (volume fill).
-int eval_blocks(tx_handle h, const tx_eval_args& a) {
+tx::EvalParams make_params(tx_handle h, const tx_eval_args& a) {
   const tx::Dofs& D = h->dofs;
   tx::EvalParams P{};
   P.coords = h->d_coords;
@@ -107,19 +155,84 @@ int eval_blocks(tx_handle h, const tx_eval_args& a) {
   P.physics = D.eq.physics;
   P.source_kind = D.eq.source_kind;
   for (int i = 0; i < 8; ++i) P.p[i] = D.eq.params[i];
+  return P;
+}
+
+// Work list of a handle: every block cut into worksets.
+void build_items(tx_handle h, std::vector<tx::WorkItem>& out, int view_base) {
+  for (size_t b = 0; b < h->blocks.size(); ++b) {
+    const DevBlock& db = h->blocks[b];
+    std::vector<int64_t> wb = tx::workset_bounds(db.n_elem, h->ws_min, h->ws_max, h->ws_seed + 7919 * b);
+    for (size_t k = 0; k + 1 < wb.size(); ++k)
+      out.push_back(tx::WorkItem{db.kind, (int32_t)(view_base + b), wb[k], wb[k + 1]});
+  }
+}
+
+int eval_persistent(tx_handle h, const tx_eval_args& a) {
   const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
+  if (h->items.empty()) {
+    build_items(h, h->items, 0);
+    cudaFree(h->d_items);
+    if (cudaMalloc((void**)&h->d_items, sizeof(tx::WorkItem) * h->items.size()) != cudaSuccess ||
+        cudaMemcpy(h->d_items, h->items.data(), sizeof(tx::WorkItem) * h->items.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+      return fail(h, TX_ENOMEM, "tx_eval: work list allocation");
+    if (!h->d_counter && cudaMalloc((void**)&h->d_counter, sizeof(int)) != cudaSuccess)
+      return fail(h, TX_ENOMEM, "tx_eval: counter allocation");
+  }
+  const size_t nb = h->blocks.size();
+  std::vector<unsigned char> tab(nb * (sizeof(tx::BlockView) + sizeof(tx::EvalParams)));
+  size_t smem = 0;
+  tx::EvalParams P = make_params(h, a);
+  for (size_t b = 0; b < nb; ++b) {
+    tx::BlockView V = h->blocks[b].view();
+    std::memcpy(&tab[b * sizeof(tx::BlockView)], &V, sizeof V);
+    std::memcpy(&tab[nb * sizeof(tx::BlockView) + b * sizeof(tx::EvalParams)], &P, sizeof P);
+    smem = std::max(smem, tx::batched_smem_bytes(h->blocks[b].kind, mixed));
+  }
+  cudaError_t e = h->stage.put(tab.data(), tab.size(), h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: staging ") + cudaGetErrorString(e));
+  const tx::BlockView* dv = (const tx::BlockView*)h->stage.dev;
+  const tx::EvalParams* dp = (const tx::EvalParams*)((unsigned char*)h->stage.dev + nb * sizeof(tx::BlockView));
+  e = tx::launch_assemble_batched(dv, dp, h->d_items, (int)h->items.size(), h->d_counter, smem, mixed,
+                                  a.crs_vals != nullptr, h->grid_cap, h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: ") + cudaGetErrorString(e));
+  return TX_OK;
+}
+
+// Evaluate every requested block/range (volume fill).
+int eval_blocks(tx_handle h, const tx_eval_args& a) {
+  tx::EvalParams P = make_params(h, a);
+  const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
+  const bool det = (a.flags & TX_EVAL_DETERMINISTIC) != 0;
+  if ((a.flags & TX_EVAL_PERSISTENT) && !det) {
+    if (a.block >= 0) return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_PERSISTENT evaluates every block (block = -1)");
+    for (const auto& db : h->blocks)
+      if (db.kind < 0) return fail(h, TX_EINVAL, "tx_eval: no kernel for this element family / cubature");
+    return eval_persistent(h, a);
+  }
   const int b0 = a.block < 0 ? 0 : a.block;
   const int b1 = a.block < 0 ? (int)h->blocks.size() : a.block + 1;
   for (int b = b0; b < b1; ++b) {
     const DevBlock& db = h->blocks[b];
-    tx::BlockView V{db.topo, db.basis, db.nq, db.nb, db.nv, db.n_elem, db.vconn, db.dconn, db.epos, db.esign, db.ref};
-    P.e0 = 0; P.e1 = db.n_elem;
+    tx::BlockView V = db.view();
+    int64_t e0 = 0, e1 = db.n_elem;
     if (a.block >= 0) {
-      P.e0 = a.elem_begin;
-      P.e1 = a.elem_end < 0 ? db.n_elem : a.elem_end;
-      if (P.e0 < 0 || P.e1 > db.n_elem || P.e0 > P.e1) return fail(h, TX_ERANGE, "tx_eval: element range outside the block");
+      e0 = a.elem_begin;
+      e1 = a.elem_end < 0 ? db.n_elem : a.elem_end;
+      if (e0 < 0 || e1 > db.n_elem || e0 > e1) return fail(h, TX_ERANGE, "tx_eval: element range outside the block");
     }
-    cudaError_t e = tx::launch_assemble(V, P, mixed, h->stream, h->grid_cap);
+    cudaError_t e = cudaSuccess;
+    if (!det) {
+      e = tx::launch_assemble(V, P, mixed, nullptr, e0, e1, true, h->stream, h->grid_cap);
+    } else {
+      if (e0 != 0 || e1 != db.n_elem)
+        return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_DETERMINISTIC evaluates whole blocks");
+      // one launch per colour, plain read-modify-write: fixed summation order
+      for (size_t c = 0; c + 1 < db.color_offsets.size() && e == cudaSuccess; ++c)
+        e = tx::launch_assemble(V, P, mixed, db.color_perm, db.color_offsets[c], db.color_offsets[c + 1], false,
+                                h->stream, h->grid_cap);
+    }
     if (e == cudaErrorInvalidValue) return fail(h, TX_EINVAL, "tx_eval: no kernel for this element family / cubature");
     if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: ") + cudaGetErrorString(e));
   }
@@ -222,6 +335,8 @@ int tx_dof_build(tx_handle h, const tx_equation_set_desc* eq) {
       DevBlock db;
       db.topo = B.topo; db.basis = B.basis; db.nq = B.ref.nq; db.nb = B.nb; db.nv = B.nv;
       db.n_elem = (int64_t)h->mesh.block_elems[b].size();
+      db.kind = tx::assemble_kind(db.topo, db.basis, db.nq, D.eq.physics);
+      db.color_offsets = B.color_offsets;
       h->blocks.push_back(db);
       DevBlock& d = h->blocks.back();
       ck(upload(d.vconn, B.vconn), "upload vconn");
@@ -229,6 +344,7 @@ int tx_dof_build(tx_handle h, const tx_equation_set_desc* eq) {
       ck(upload(d.epos, B.epos), "upload epos");
       ck(upload(d.esign, B.esign), "upload esign");
       ck(upload(d.ref, B.ref.packed()), "upload reference tables");
+      ck(upload(d.color_perm, B.color_perm), "upload colouring");
     }
     ck(upload(h->d_erowptr, D.erowptr), "upload entity rowptr");
     ck(upload(h->d_ecol, D.ecol), "upload entity columns");
@@ -379,6 +495,20 @@ int tx_solve_cg_ir(tx_handle h, tx_solve_args* a) {
   return TX_OK;
 }
 
+int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t seed) {
+  if (!h) return TX_EINVAL;
+  if (min_size < 1 || max_size < min_size) return fail(h, TX_EINVAL, "tx_set_worksets: need 1 <= min <= max");
+  h->ws_min = min_size; h->ws_max = max_size; h->ws_seed = seed;
+  h->items.clear();  // rebuilt at the next persistent evaluation
+  return TX_OK;
+}
+
+int tx_set_grid_cap(tx_handle h, int32_t max_ctas) {
+  if (!h || max_ctas < 0) return TX_EINVAL;
+  h->grid_cap = max_ctas;
+  return TX_OK;
+}
+
 int tx_set_stream(tx_handle h, void* stream) {
   if (!h) return TX_EINVAL;
   h->stream = (cudaStream_t)stream;
@@ -389,6 +519,114 @@ int tx_synchronize(tx_handle h) {
   if (!h) return TX_EINVAL;
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_synchronize: ") + cudaGetErrorString(e));
+  return TX_OK;
+}
+
+// ---------------------------------------------------------------- batches
+struct tx_batch_s {
+  std::vector<tx_handle> hs;
+  std::vector<tx::WorkItem> items;
+  tx::WorkItem* d_items = nullptr;
+  int* d_counter = nullptr;
+  Staging stage;
+  int64_t ws_min = 512, ws_max = 512;
+  uint64_t seed = 0;
+  int grid_cap = 0;
+  std::string err;
+  ~tx_batch_s() {
+    cudaFree(d_items);
+    cudaFree(d_counter);
+    stage.release();
+  }
+};
+
+int tx_batch_create(const tx_handle* handles, int32_t n, tx_batch* out) {
+  if (!handles || n < 1 || !out) return TX_EINVAL;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (!handles[i] || !handles[i]->have_dofs) return TX_ESTATE;
+  tx_batch b = new (std::nothrow) tx_batch_s;
+  if (!b) return TX_ENOMEM;
+  b->hs.assign(handles, handles + n);
+  *out = b;
+  return TX_OK;
+}
+
+void tx_batch_destroy(tx_batch b) { delete b; }
+
+const char* tx_batch_last_error(tx_batch b) { return b ? b->err.c_str() : "null batch"; }
+
+int tx_batch_set_worksets(tx_batch b, int64_t min_size, int64_t max_size, uint64_t seed, int32_t max_ctas) {
+  if (!b || min_size < 1 || max_size < min_size || max_ctas < 0) return TX_EINVAL;
+  b->ws_min = min_size; b->ws_max = max_size; b->seed = seed; b->grid_cap = max_ctas;
+  b->items.clear();
+  return TX_OK;
+}
+
+int tx_batch_eval(tx_batch b, const tx_eval_args* args) {
+  if (!b || !args) return TX_EINVAL;
+  const int n = (int)b->hs.size();
+  const bool mixed = (args[0].flags & TX_EVAL_MIXED) != 0;
+  const bool jac = args[0].crs_vals != nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!args[i].x) { b->err = "tx_batch_eval: x is required for every instance"; return TX_EINVAL; }
+    if (((args[i].flags & TX_EVAL_MIXED) != 0) != mixed || (args[i].crs_vals != nullptr) != jac) {
+      b->err = "tx_batch_eval: every instance needs the same precision and evaluation type";
+      return TX_EINVAL;
+    }
+    for (const auto& db : b->hs[i]->blocks)
+      if (db.kind < 0) { b->err = "tx_batch_eval: no kernel for an element family of the batch"; return TX_EINVAL; }
+  }
+  cudaStream_t s = b->hs[0]->stream;
+  if (b->items.empty()) {
+    int base = 0;
+    for (int i = 0; i < n; ++i) {
+      tx_handle h = b->hs[i];
+      int64_t mn = h->ws_min, mx = h->ws_max;
+      uint64_t sd = h->ws_seed;
+      h->ws_min = b->ws_min; h->ws_max = b->ws_max; h->ws_seed = b->seed + 104729ull * i;
+      build_items(h, b->items, base);
+      h->ws_min = mn; h->ws_max = mx; h->ws_seed = sd;
+      base += (int)h->blocks.size();
+    }
+    cudaFree(b->d_items);
+    if (cudaMalloc((void**)&b->d_items, sizeof(tx::WorkItem) * b->items.size()) != cudaSuccess ||
+        cudaMemcpy(b->d_items, b->items.data(), sizeof(tx::WorkItem) * b->items.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+      b->err = "tx_batch_eval: work list allocation";
+      return TX_ENOMEM;
+    }
+    if (!b->d_counter && cudaMalloc((void**)&b->d_counter, sizeof(int)) != cudaSuccess) {
+      b->err = "tx_batch_eval: counter allocation";
+      return TX_ENOMEM;
+    }
+  }
+  size_t nviews = 0;
+  for (int i = 0; i < n; ++i) nviews += b->hs[i]->blocks.size();
+  std::vector<unsigned char> tab(nviews * (sizeof(tx::BlockView) + sizeof(tx::EvalParams)));
+  size_t smem = 0, v = 0;
+  for (int i = 0; i < n; ++i) {
+    tx_handle h = b->hs[i];
+    tx::EvalParams P = make_params(h, args[i]);
+    for (const auto& db : h->blocks) {
+      tx::BlockView V = db.view();
+      std::memcpy(&tab[v * sizeof(tx::BlockView)], &V, sizeof V);
+      std::memcpy(&tab[nviews * sizeof(tx::BlockView) + v * sizeof(tx::EvalParams)], &P, sizeof P);
+      smem = std::max(smem, tx::batched_smem_bytes(db.kind, mixed));
+      ++v;
+    }
+  }
+  cudaError_t e = b->stage.put(tab.data(), tab.size(), s);
+  if (e == cudaSuccess) {
+    const tx::BlockView* dv = (const tx::BlockView*)b->stage.dev;
+    const tx::EvalParams* dp = (const tx::EvalParams*)((unsigned char*)b->stage.dev + nviews * sizeof(tx::BlockView));
+    e = tx::launch_assemble_batched(dv, dp, b->d_items, (int)b->items.size(), b->d_counter, smem, mixed, jac,
+                                    b->grid_cap, s);
+  }
+  if (e != cudaSuccess) {
+    b->err = std::string("tx_batch_eval: ") + cudaGetErrorString(e);
+    return TX_ECUDA;
+  }
   return TX_OK;
 }
 

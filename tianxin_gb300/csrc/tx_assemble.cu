@@ -48,14 +48,14 @@ template <> struct Family<TX_TOPO_HEX, TX_HCURL_I1> { static constexpr int NV = 
 
 constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real>
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, int THREADS_ = (Family<TOPO, BASIS>::NB > 16 ? 128 : 256)>
 struct Cfg {
   static constexpr int NV = Family<TOPO, BASIS>::NV;
   static constexpr int NB = Family<TOPO, BASIS>::NB;
   static constexpr bool HC = BASIS == TX_HCURL_I1;
   static constexpr int NF = PHYS == TX_PHYS_ELASTICITY ? 3 : 1;
   static constexpr int TPE = pow2ceil(NB);
-  static constexpr int THREADS = NB > 16 ? 128 : 256;
+  static constexpr int THREADS = THREADS_;
   static constexpr int EPB = THREADS / TPE;
   static constexpr int NQF = PHYS == TX_PHYS_ELASTICITY ? 9 : PHYS == TX_PHYS_HEAT ? 8 : PHYS == TX_PHYS_MAXWELL ? 6 : 4;
   static constexpr int NVAL = HC ? 3 : 1;
@@ -81,6 +81,12 @@ struct Cfg {
   static constexpr size_t SMEM = R_END + EPB * E_END;
 };
 
+template <bool ATOMIC>
+__device__ __forceinline__ void accumulate(double* p, double v) {
+  if constexpr (ATOMIC) atomicAdd(p, v);  // red.global.add.f64
+  else *p += v;
+}
+
 template <typename Real>
 __device__ __forceinline__ Real source_at(int kind, double c, double s0, const double ip[3]) {
   if (kind == TX_SOURCE_SINE) {
@@ -91,13 +97,17 @@ __device__ __forceinline__ Real source_at(int kind, double c, double s0, const d
   return (Real)s0;
 }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC>
-__global__ void __launch_bounds__(Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS)
-k_assemble(const BlockView B, const EvalParams P) {
-  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real>;
+// Elements [e_lo, e_hi) of a block (through perm if given), element groups
+// g = grp0, grp0 + grp_stride, ... of EPB elements each.  ATOMIC=false is
+// the coloured (deterministic) scatter: no two elements processed by one
+// launch share a row, so plain read-modify-write is race free.
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, int THREADS>
+__device__ __forceinline__ void assemble_body(const BlockView& B, const EvalParams& P, const int32_t* perm,
+                                              int64_t e_lo, int64_t e_hi, int64_t grp0, int64_t grp_stride,
+                                              unsigned char* smem) {
+  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS>;
   constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF;
   constexpr bool HC = C::HC;
-  extern __shared__ __align__(16) unsigned char smem[];
   double* r_geo_grad = reinterpret_cast<double*>(smem + C::R_GEO_GRAD);
   double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
   Real* r_w = reinterpret_cast<Real*>(smem + C::R_W);
@@ -134,9 +144,10 @@ k_assemble(const BlockView B, const EvalParams P) {
   __syncthreads();
 
   const double* pp = P.p;
-  for (int64_t g0 = P.e0 + (int64_t)blockIdx.x * EPB; g0 < P.e1; g0 += (int64_t)gridDim.x * EPB) {
-    const int64_t e = g0 + le;
-    const bool valid = e < P.e1;
+  for (int64_t g0 = e_lo + grp0 * EPB; g0 < e_hi; g0 += grp_stride * EPB) {
+    const int64_t ei = g0 + le;
+    const bool valid = ei < e_hi;
+    const int64_t e = (perm && valid) ? (int64_t)__ldg(perm + ei) : ei;
     // ---------------------------------------------------------- 1 gather
     if (valid) {
       for (int v = t; v < NV; v += TPE) {
@@ -329,7 +340,7 @@ k_assemble(const BlockView B, const EvalParams P) {
         }
         if (P.f) {
 #pragma unroll
-          for (int c = 0; c < NF; ++c) atomicAdd(P.f + NF * la + c, (double)r[c]);
+          for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.f + NF * la + c, (double)r[c]);
         }
         if constexpr (JAC) {
           int64_t rp[NF];
@@ -350,7 +361,7 @@ k_assemble(const BlockView B, const EvalParams P) {
                 kg += w * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
                 km += w * r_val[q * NB + a] * r_val[q * NB + b];
               }
-              atomicAdd(P.vals + rp[0] + pb, (double)(ca * kg + cm * km));
+              accumulate<ATOMIC>(P.vals + rp[0] + pb, (double)(ca * kg + cm * km));
             } else if constexpr (PHYS == TX_PHYS_HEAT) {
               Real kab = 0;
               for (int q = 0; q < NQ; ++q) {
@@ -360,7 +371,7 @@ k_assemble(const BlockView B, const EvalParams P) {
                 kab += sW[q] * (qf[7] * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]) +
                                 r_val[q * NB + b] * (ga[0] * qf[4] + ga[1] * qf[5] + ga[2] * qf[6]));
               }
-              atomicAdd(P.vals + rp[0] + pb, (double)(beta * kab));
+              accumulate<ATOMIC>(P.vals + rp[0] + pb, (double)(beta * kab));
             } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
               Real Pm[9], M = 0;
 #pragma unroll
@@ -386,7 +397,7 @@ k_assemble(const BlockView B, const EvalParams P) {
                 for (int d = 0; d < 3; ++d) {
                   Real k = beta * (lam * Pm[3 * c + d] + mu * Pm[3 * d + c]);
                   if (c == d) k += beta * mu * trP + mass;
-                  atomicAdd(P.vals + rp[c] + pb + d, (double)k);
+                  accumulate<ATOMIC>(P.vals + rp[c] + pb + d, (double)k);
                 }
             } else {  // MAXWELL
               const Real imu = (Real)pp[0], sig = (Real)pp[1];
@@ -399,7 +410,7 @@ k_assemble(const BlockView B, const EvalParams P) {
                 kc += sW[q] * (ca[0] * cb[0] + ca[1] * cb[1] + ca[2] * cb[2]);
                 kv += sW[q] * (va[0] * vb[0] + va[1] * vb[1] + va[2] * vb[2]);
               }
-              atomicAdd(P.vals + rp[0] + pb, (double)(beta * (imu * kc + sig * kv)));
+              accumulate<ATOMIC>(P.vals + rp[0] + pb, (double)(beta * (imu * kc + sig * kv)));
             }
           }
         }
@@ -409,10 +420,20 @@ k_assemble(const BlockView B, const EvalParams P) {
   }
 }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC>
-cudaError_t launch_one(const BlockView& B, const EvalParams& P, cudaStream_t s, int grid_cap) {
+// ------------------------------------------------------------- per block
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC>
+__global__ void __launch_bounds__(Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS)
+k_assemble(const BlockView B, const EvalParams P, const int32_t* perm, int64_t e_lo, int64_t e_hi) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS>(
+      B, P, perm, e_lo, e_hi, blockIdx.x, gridDim.x, smem);
+}
+
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC>
+cudaError_t launch_one(const BlockView& B, const EvalParams& P, const int32_t* perm, int64_t e_lo, int64_t e_hi,
+                       cudaStream_t s, int grid_cap) {
   using C = Cfg<TOPO, BASIS, NQ, PHYS, Real>;
-  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC>;
+  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC>;
   static int max_blocks_per_sm = -1;
   static int num_sms = 0;
   if (max_blocks_per_sm < 0) {
@@ -425,52 +446,144 @@ cudaError_t launch_one(const BlockView& B, const EvalParams& P, cudaStream_t s, 
     if (err != cudaSuccess) return err;
     if (max_blocks_per_sm < 1) max_blocks_per_sm = 1;
   }
-  const int64_t n = P.e1 - P.e0;
+  const int64_t n = e_hi - e_lo;
   if (n <= 0) return cudaSuccess;
   int64_t blocks = (n + C::EPB - 1) / C::EPB;
   int64_t cap = (int64_t)max_blocks_per_sm * num_sms * 4;
   if (grid_cap > 0 && grid_cap < cap) cap = grid_cap;
   if (blocks > cap) blocks = cap;
-  kern<<<(unsigned)blocks, C::THREADS, C::SMEM, s>>>(B, P);
+  kern<<<(unsigned)blocks, C::THREADS, C::SMEM, s>>>(B, P, perm, e_lo, e_hi);
   return cudaGetLastError();
 }
 
 template <int TOPO, int BASIS, int NQ, int PHYS>
-cudaError_t launch_prec(const BlockView& B, const EvalParams& P, bool mixed, cudaStream_t s, int cap) {
+cudaError_t launch_prec(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,
+                        int64_t e_hi, bool atomic, cudaStream_t s, int cap) {
   const bool jac = P.vals != nullptr;
-  if (mixed)
-    return jac ? launch_one<TOPO, BASIS, NQ, PHYS, float, true>(B, P, s, cap)
-               : launch_one<TOPO, BASIS, NQ, PHYS, float, false>(B, P, s, cap);
-  return jac ? launch_one<TOPO, BASIS, NQ, PHYS, double, true>(B, P, s, cap)
-             : launch_one<TOPO, BASIS, NQ, PHYS, double, false>(B, P, s, cap);
+#define TX_L(R, J, A) launch_one<TOPO, BASIS, NQ, PHYS, R, J, A>(B, P, perm, e_lo, e_hi, s, cap)
+  if (atomic) {
+    if (mixed) return jac ? TX_L(float, true, true) : TX_L(float, false, true);
+    return jac ? TX_L(double, true, true) : TX_L(double, false, true);
+  }
+  if (mixed) return jac ? TX_L(float, true, false) : TX_L(float, false, false);
+  return jac ? TX_L(double, true, false) : TX_L(double, false, false);
+#undef TX_L
+}
+
+// ------------------------------------------------------------- batched
+// The element families the kernels are instantiated for.
+enum Kind {
+  K_HEX8_POISSON, K_HEX8_ELAST, K_HEX8_HEAT, K_HEX27_POISSON, K_HEX27_HEAT, K_TET4_POISSON, K_TET4_ELAST,
+  K_TET4_HEAT, K_TET10_POISSON, K_TET10_HEAT, K_NED_MAXWELL, K_COUNT
+};
+
+#define TX_FOR_EACH_KIND(X)                                         \
+  X(K_HEX8_POISSON, TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_POISSON)    \
+  X(K_HEX8_ELAST, TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_ELASTICITY)   \
+  X(K_HEX8_HEAT, TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_HEAT)          \
+  X(K_HEX27_POISSON, TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_POISSON)  \
+  X(K_HEX27_HEAT, TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_HEAT)        \
+  X(K_TET4_POISSON, TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_POISSON)    \
+  X(K_TET4_ELAST, TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_ELASTICITY)   \
+  X(K_TET4_HEAT, TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_HEAT)          \
+  X(K_TET10_POISSON, TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_POISSON)   \
+  X(K_TET10_HEAT, TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_HEAT)         \
+  X(K_NED_MAXWELL, TX_TOPO_HEX, TX_HCURL_I1, 8, TX_PHYS_MAXWELL)
+
+constexpr int kBatchThreads = 128;
+
+// Persistent kernel: CTAs take work items (element chunks of any block of
+// any mesh, any family) from an atomic counter until the list is empty.
+template <typename Real, bool JAC>
+__global__ void __launch_bounds__(kBatchThreads)
+k_assemble_batched(const BlockView* __restrict__ views, const EvalParams* __restrict__ params,
+                   const WorkItem* __restrict__ items, int n_items, int* counter) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= n_items) break;
+    const WorkItem w = items[it];
+    const BlockView B = views[w.view];
+    const EvalParams P = params[w.view];
+    switch (w.kind) {
+#define TX_CASE(K, T, BS, Q, PH)                                                                 \
+  case K:                                                                                        \
+    assemble_body<T, BS, Q, PH, Real, JAC, true, kBatchThreads>(B, P, nullptr, w.e0, w.e1, 0, 1, smem); \
+    break;
+      TX_FOR_EACH_KIND(TX_CASE)
+#undef TX_CASE
+      default:
+        break;
+    }
+  }
+}
+
+template <typename Real>
+size_t smem_of_kind(int kind) {
+  switch (kind) {
+#define TX_SZ(K, T, BS, Q, PH) \
+  case K:                      \
+    return Cfg<T, BS, Q, PH, Real, kBatchThreads>::SMEM;
+    TX_FOR_EACH_KIND(TX_SZ)
+#undef TX_SZ
+    default:
+      return 0;
+  }
 }
 
 }  // namespace
 
-cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, cudaStream_t s, int cap) {
-  const int ph = P.physics;
-  if (B.topo == TX_TOPO_HEX && B.basis == TX_HGRAD_C1 && B.nq == 8) {
-    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_POISSON>(B, P, mixed, s, cap);
-    if (ph == TX_PHYS_ELASTICITY) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_ELASTICITY>(B, P, mixed, s, cap);
-    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_HEAT>(B, P, mixed, s, cap);
+int assemble_kind(int topo, int basis, int nq, int physics) {
+#define TX_K(K, T, BS, Q, PH) \
+  if (topo == T && basis == BS && nq == Q && physics == PH) return K;
+  TX_FOR_EACH_KIND(TX_K)
+#undef TX_K
+  return -1;
+}
+
+size_t batched_smem_bytes(int kind, bool mixed) {
+  return mixed ? smem_of_kind<float>(kind) : smem_of_kind<double>(kind);
+}
+
+cudaError_t launch_assemble_batched(const BlockView* views, const EvalParams* params, const WorkItem* items,
+                                    int n_items, int* counter, size_t smem, bool mixed, bool jac, int grid,
+                                    cudaStream_t s) {
+  if (n_items <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  auto go = [&](auto kern) -> cudaError_t {
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBatchThreads, smem);
+    if (err != cudaSuccess) return err;
+    int g = (per_sm > 0 ? per_sm : 1) * sms;
+    if (grid > 0 && grid < g) g = grid;
+    if (g > n_items) g = n_items;
+    kern<<<g, kBatchThreads, smem, s>>>(views, params, items, n_items, counter);
+    return cudaGetLastError();
+  };
+  if (mixed) return jac ? go(k_assemble_batched<float, true>) : go(k_assemble_batched<float, false>);
+  return jac ? go(k_assemble_batched<double, true>) : go(k_assemble_batched<double, false>);
+}
+
+cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,
+                            int64_t e_hi, bool atomic, cudaStream_t s, int cap) {
+  switch (assemble_kind(B.topo, B.basis, B.nq, P.physics)) {
+#define TX_LAUNCH(K, T, BS, Q, PH) \
+  case K:                          \
+    return launch_prec<T, BS, Q, PH>(B, P, mixed, perm, e_lo, e_hi, atomic, s, cap);
+    TX_FOR_EACH_KIND(TX_LAUNCH)
+#undef TX_LAUNCH
+    default:
+      return cudaErrorInvalidValue;
   }
-  if (B.topo == TX_TOPO_HEX && B.basis == TX_HGRAD_C2 && B.nq == 27) {
-    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_POISSON>(B, P, mixed, s, cap);
-    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_HEAT>(B, P, mixed, s, cap);
-  }
-  if (B.topo == TX_TOPO_TET && B.basis == TX_HGRAD_C1 && B.nq == 4) {
-    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_POISSON>(B, P, mixed, s, cap);
-    if (ph == TX_PHYS_ELASTICITY) return launch_prec<TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_ELASTICITY>(B, P, mixed, s, cap);
-    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_HEAT>(B, P, mixed, s, cap);
-  }
-  if (B.topo == TX_TOPO_TET && B.basis == TX_HGRAD_C2 && B.nq == 4) {
-    if (ph == TX_PHYS_POISSON) return launch_prec<TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_POISSON>(B, P, mixed, s, cap);
-    if (ph == TX_PHYS_HEAT) return launch_prec<TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_HEAT>(B, P, mixed, s, cap);
-  }
-  if (B.topo == TX_TOPO_HEX && B.basis == TX_HCURL_I1 && B.nq == 8) {
-    if (ph == TX_PHYS_MAXWELL) return launch_prec<TX_TOPO_HEX, TX_HCURL_I1, 8, TX_PHYS_MAXWELL>(B, P, mixed, s, cap);
-  }
-  return cudaErrorInvalidValue;
 }
 
 }  // namespace tx

@@ -24,9 +24,26 @@ struct EvalParams {
 };
 
 // Launch the fused gather -> geometry -> integrators -> scatter kernel for
-// one block.  Returns cudaSuccess or the launch error; TX_EINVAL (as
-// cudaErrorInvalidValue) for element families without a kernel.
-cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, cudaStream_t s, int grid_cap);
+// elements [e_lo, e_hi) of one block (through perm when given).  atomic=false
+// is the coloured, deterministic scatter (one launch per colour).  Returns
+// cudaErrorInvalidValue for element families without a kernel.
+cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,
+                            int64_t e_hi, bool atomic, cudaStream_t s, int grid_cap);
+
+// One chunk of elements of one block view (views[view], params[view]).
+struct WorkItem {
+  int32_t kind;   // assemble_kind() of the view
+  int32_t view;
+  int64_t e0, e1;
+};
+// Element family id of (topology, basis, cubature points, physics); -1 if none.
+int assemble_kind(int topo, int basis, int nq, int physics);
+// Dynamic shared memory of one family in the batched kernel.
+size_t batched_smem_bytes(int kind, bool mixed);
+// Persistent launch over a work list (device arrays); counter is a device int.
+cudaError_t launch_assemble_batched(const BlockView* views, const EvalParams* params, const WorkItem* items,
+                                    int n_items, int* counter, size_t smem, bool mixed, bool jac, int grid,
+                                    cudaStream_t s);
 
 // ---- linear algebra (tx_linalg.cu)
 cudaError_t launch_expand_rowptr(const int64_t* erowptr, int64_t n_ent, int nf, int64_t* rowptr, cudaStream_t s);

@@ -64,6 +64,9 @@ struct BlockDofs {
   std::vector<int> geom_dim, geom_sub;    // geometric pattern (dim, subcell) in order
   std::vector<int> geom_basis;            // basis index on that sub-cell, -1 none
   std::vector<int> basis_pos;             // basis b -> position among DOF entities
+  // greedy colouring: elements of one colour share no DOF entity
+  std::vector<int32_t> color_perm;        // block elements ordered by colour
+  std::vector<int64_t> color_offsets;     // [ncolors + 1]
 };
 
 struct Dofs {
@@ -89,5 +92,8 @@ void dof_element_lids(const Mesh& m, const Dofs& D, int block, int32_t* out);
 int dof_block_gid_count(const Dofs& D, int block);
 int dof_field_offsets(const Dofs& D, int block, int field, int32_t* out);
 std::vector<int32_t> dirichlet_dofs(const Dofs& D, const Mesh& m, uint32_t side_mask, uint32_t field_mask);
+// Worksets of a block: consecutive element ranges with sizes drawn uniformly
+// in [min_size, max_size] from a seeded generator (min == max: even split).
+std::vector<int64_t> workset_bounds(int64_t n_elem, int64_t min_size, int64_t max_size, uint64_t seed);
 
 }  // namespace tx

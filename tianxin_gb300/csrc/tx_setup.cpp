@@ -360,6 +360,8 @@ void build_mesh(Mesh& m, const tx_mesh_desc& d) {
 }
 
 // ------------------------------------------------------------------ dofs
+static void color_block(BlockDofs& B, int64_t E, int64_t n_entities);
+
 void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q) {
   D.eq = q;
   D.nf = q.physics == TX_PHYS_ELASTICITY ? 3 : 1;
@@ -540,7 +542,47 @@ void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q) {
       }
     }
     if (overflow) throw std::runtime_error("tx_dof_build: entity row longer than 256 blocks");
+    color_block(B, E, D.n_entities);
   }
+}
+
+// Greedy element colouring per block (first fit in element order): elements
+// of one colour share no DOF entity, so a launch over one colour can scatter
+// with plain read-modify-writes.  Lattice blocks give 8 colours (hex) or
+// about 48 (tet split).
+static void color_block(BlockDofs& B, int64_t E, int64_t n_entities) {
+  std::vector<uint64_t> used(n_entities, 0);
+  std::vector<int> color(E, 0);
+  int ncolors = 0;
+  for (int64_t i = 0; i < E; ++i) {
+    uint64_t m = 0;
+    for (int a = 0; a < B.nb; ++a) m |= used[B.dconn[i * B.nb + a]];
+    if (~m == 0) throw std::runtime_error("element colouring needs more than 64 colours");
+    int c = 0;
+    while (m & (1ull << c)) ++c;
+    color[i] = c;
+    ncolors = std::max(ncolors, c + 1);
+    for (int a = 0; a < B.nb; ++a) used[B.dconn[i * B.nb + a]] |= 1ull << c;
+  }
+  B.color_offsets.assign(ncolors + 1, 0);
+  for (int64_t i = 0; i < E; ++i) B.color_offsets[color[i] + 1]++;
+  for (int c = 0; c < ncolors; ++c) B.color_offsets[c + 1] += B.color_offsets[c];
+  std::vector<int64_t> pos(B.color_offsets.begin(), B.color_offsets.end() - 1);
+  B.color_perm.assign(E, 0);
+  for (int64_t i = 0; i < E; ++i) B.color_perm[pos[color[i]]++] = (int32_t)i;
+}
+
+std::vector<int64_t> workset_bounds(int64_t n_elem, int64_t min_size, int64_t max_size, uint64_t seed) {
+  std::vector<int64_t> b{0};
+  if (min_size < 1) min_size = 1;
+  if (max_size < min_size) max_size = min_size;
+  uint64_t st = seed;
+  while (b.back() < n_elem) {
+    st = splitmix(st);
+    int64_t sz = min_size + (int64_t)(st % (uint64_t)(max_size - min_size + 1));
+    b.push_back(std::min(n_elem, b.back() + sz));
+  }
+  return b;
 }
 
 void dof_owned_gids(const Dofs& D, int64_t* out) {

@@ -202,22 +202,37 @@ class DirichletBC:
             self.g = torch.as_tensor(value, dtype=torch.float64, device="cuda")
 
 
+def eval_args(x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False, block=-1,
+              workset=(0, -1), deterministic=False, persistent=False):
+    a = _abi.EvalArgs()
+    a.x, a.x_dot, a.aux = _ptr(x), _ptr(x_dot), _ptr(aux)
+    a.alpha, a.beta, a.t = alpha, beta, t
+    a.f = _ptr(f)
+    a.crs_vals = _ptr(W.values) if W is not None else None
+    a.block = block
+    a.elem_begin, a.elem_end = workset
+    a.flags = ((_abi.TX_EVAL_MIXED if mixed else 0) | (_abi.TX_EVAL_DETERMINISTIC if deterministic else 0) |
+               (_abi.TX_EVAL_PERSISTENT if persistent else 0))
+    return a
+
+
 class AssemblyEngine:
     """Volume fill of every block (or one workset range of a block)."""
 
     def __init__(self, lof):
         self.lof, self.dof = lof, lof.dof
 
+    def setWorksetSize(self, min_size, max_size=None, seed=0):
+        """Worksets of the persistent evaluation: sizes uniform in [min_size, max_size]."""
+        check(self.dof.h, self.dof.lib.tx_set_worksets(self.dof.h, min_size, max_size or min_size, seed),
+              "tx_set_worksets")
+
+    def setGridCap(self, max_ctas):
+        check(self.dof.h, self.dof.lib.tx_set_grid_cap(self.dof.h, max_ctas), "tx_set_grid_cap")
+
     def evaluate(self, x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False,
-                 block=-1, workset=(0, -1)):
-        a = _abi.EvalArgs()
-        a.x, a.x_dot, a.aux = _ptr(x), _ptr(x_dot), _ptr(aux)
-        a.alpha, a.beta, a.t = alpha, beta, t
-        a.f = _ptr(f)
-        a.crs_vals = _ptr(W.values) if W is not None else None
-        a.block = block
-        a.elem_begin, a.elem_end = workset
-        a.flags = _abi.TX_EVAL_MIXED if mixed else 0
+                 block=-1, workset=(0, -1), deterministic=False, persistent=False):
+        a = eval_args(x, x_dot, aux, alpha, beta, t, f, W, mixed, block, workset, deterministic, persistent)
         lib = self.dof.lib
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_eval(self.dof.h, C.byref(a)), "tx_eval")
@@ -235,13 +250,14 @@ class ModelEvaluator:
         return self.lof.getTpetraMatrix()
 
     def evalModel(self, x, x_dot=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, aux=None, mixed=False,
-                  zero=True):
+                  zero=True, deterministic=False, persistent=False):
         if zero:
             if f is not None:
                 f.zero_()
             if W is not None:
                 W.initializeMatrix(0.0)
-        self.ae.evaluate(x, x_dot, aux, alpha, beta, t, f, W, mixed)
+        self.ae.evaluate(x, x_dot, aux, alpha, beta, t, f, W, mixed, deterministic=deterministic,
+                         persistent=persistent)
         self.applyDirichlet(x, f, W)
         return f, W
 
@@ -275,6 +291,42 @@ class ModelEvaluator:
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_solve_cg_ir(self.dof.h, C.byref(a)), "tx_solve_cg_ir")
         return {"outer": int(a.stats[0]), "inner": int(a.stats[1]), "relres": a.stats[2], "r0": a.stats[3]}
+
+
+class Batch:
+    """Many independent meshes (DOFManagers) evaluated by one persistent launch."""
+
+    def __init__(self, dofs, workset=(512, 512), seed=0, max_ctas=0):
+        self.dofs = list(dofs)
+        self.lib = self.dofs[0].lib
+        hs = (C.c_void_p * len(self.dofs))(*[d.h for d in self.dofs])
+        b = C.c_void_p()
+        rc = self.lib.tx_batch_create(hs, len(self.dofs), C.byref(b))
+        if rc:
+            raise TxError(rc, "tx_batch_create")
+        self.b = b
+        self.setWorksets(*workset, seed=seed, max_ctas=max_ctas)
+
+    def __del__(self):
+        if getattr(self, "b", None):
+            self.lib.tx_batch_destroy(self.b)
+            self.b = None
+
+    def setWorksets(self, min_size, max_size, seed=0, max_ctas=0):
+        rc = self.lib.tx_batch_set_worksets(self.b, min_size, max_size, seed, max_ctas)
+        if rc:
+            raise TxError(rc, "tx_batch_set_worksets")
+
+    def evaluate(self, xs, fs, Ws=None, x_dots=None, auxs=None, alpha=0.0, beta=1.0, t=0.0, mixed=False):
+        n = len(self.dofs)
+        args = (_abi.EvalArgs * n)()
+        for i in range(n):
+            args[i] = eval_args(xs[i], None if x_dots is None else x_dots[i], None if auxs is None else auxs[i],
+                                alpha, beta, t, fs[i], None if Ws is None else Ws[i], mixed)
+        self.lib.tx_set_stream(self.dofs[0].h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        rc = self.lib.tx_batch_eval(self.b, args)
+        if rc:
+            raise TxError(rc, "tx_batch_eval: " + (self.lib.tx_batch_last_error(self.b) or b"").decode())
 
 
 def synchronize(dof):
