@@ -120,6 +120,8 @@ enum tx_source {
 #define TX_EVAL_MIXED 0x1u          /* FP32 element contractions, FP64 scatter   */
 #define TX_EVAL_DETERMINISTIC 0x2u  /* fixed summation order: coloured scatter, no atomics  */
 #define TX_EVAL_PERSISTENT 0x4u     /* every block's worksets in one persistent launch      */
+#define TX_EVAL_SCATTER_DIRECT 0x8u /* per-thread row reductions instead of the staged,
+                                       row-coalesced CTA scatter (comparison / tuning)     */
 
 typedef struct tx_eval_args {
   const double* x;         /* solution, LID order (GED "... - X")                       */
@@ -212,6 +214,12 @@ int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowpt
  * On return stats[0] = outer iterations, stats[1] = total inner CG
  * iterations, stats[2] = final ||r||/||b||. */
 #define TX_SOLVE_MATRIX_FREE_RESIDUAL 0x1u
+/* Exactly max_outer x max_inner iterations with no host reads (capturable
+ * in a CUDA graph after one uncaptured call has sized the work space);
+ * statistics go to stats_device. */
+#define TX_SOLVE_FIXED_ITERATIONS 0x2u
+/* Reuse the FP32 operator of the previous solve (A unchanged). */
+#define TX_SOLVE_REUSE_OPERATOR 0x4u
 typedef struct tx_solve_args {
   const int64_t* rowptr; const int32_t* colind; const double* vals;
   const double* b;         /* right-hand side (ignored with MATRIX_FREE: b = -f(x0)) */
@@ -225,6 +233,12 @@ typedef struct tx_solve_args {
   const double* x_dot;     /* state for MATRIX_FREE residuals (may be NULL)   */
   double alpha, beta, t;   /* coefficients for MATRIX_FREE residuals          */
   double stats[4];
+  double* stats_device;    /* FIXED_ITERATIONS: device double[4] (or NULL)    */
+  /* Implicit time integration (MATRIX_FREE only): when x_pred is given the
+   * residual is evaluated with x_dot = x_dot_coef * (x - x_pred), the form a
+   * Newmark or backward-Euler wrapper presents to evalModel. */
+  const double* x_pred;
+  double x_dot_coef;
 } tx_solve_args;
 int tx_solve_cg_ir(tx_handle h, tx_solve_args* args);
 

@@ -155,3 +155,18 @@ def test_scatter_pattern_counts_gpu(cuda):
     ratio = f.cpu().numpy() / (-(1.0 / n) ** 3 / 8)
     assert set(np.round(ratio).astype(int)) == {1, 2, 4, 8}
     assert np.allclose(ratio, np.round(ratio), atol=1e-12, rtol=0)
+
+
+@pytest.mark.parametrize("name,n,blocks,topo,phys,basis,source", [CASES[1], CASES[5], CASES[9]],
+                         ids=[IDS[1], IDS[5], IDS[9]])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_direct_scatter_matches(cuda, name, n, blocks, topo, phys, basis, source, mixed):
+    # per-thread row reductions (TX_EVAL_SCATTER_DIRECT) vs the staged CTA-wide scatter
+    o, _, dof, lof = build(n, blocks, topo, phys, basis, source)
+    x, xd, aux = state(o.n_dofs, seed=9)
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=0.5, beta=1.0)
+    dev = lambda a: torch.from_numpy(a).cuda()
+    f, W = lof.getTpetraVector(), lof.getTpetraMatrix()
+    tx.AssemblyEngine(lof).evaluate(dev(x), dev(xd), dev(aux), 0.5, 1.0, 0.0, f, W, mixed, scatter_direct=True)
+    tol = MIXED_TOL if mixed else FP64_TOL
+    assert rel(f.cpu().numpy(), f_ref) <= tol and rel(W.values.cpu().numpy(), v_ref) <= tol

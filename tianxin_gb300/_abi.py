@@ -31,11 +31,14 @@ TX_SOURCE_AFFINE = 2
 TX_EVAL_MIXED = 0x1
 TX_EVAL_DETERMINISTIC = 0x2
 TX_EVAL_PERSISTENT = 0x4
+TX_EVAL_SCATTER_DIRECT = 0x8
 
 TX_SPMV_F64 = 0
 TX_SPMV_F32 = 1
 
 TX_SOLVE_MATRIX_FREE_RESIDUAL = 0x1
+TX_SOLVE_FIXED_ITERATIONS = 0x2
+TX_SOLVE_REUSE_OPERATOR = 0x4
 
 # side bits for Dirichlet sets
 SIDE_XMIN, SIDE_XMAX, SIDE_YMIN, SIDE_YMAX, SIDE_ZMIN, SIDE_ZMAX = (1 << i for i in range(6))
@@ -85,6 +88,8 @@ class SolveArgs(C.Structure):
         ("x_dot", C.c_void_p),
         ("alpha", C.c_double), ("beta", C.c_double), ("t", C.c_double),
         ("stats", C.c_double * 4),
+        ("stats_device", C.c_void_p),
+        ("x_pred", C.c_void_p), ("x_dot_coef", C.c_double),
     ]
 
 

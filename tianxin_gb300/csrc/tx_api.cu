@@ -205,6 +205,7 @@ int eval_blocks(tx_handle h, const tx_eval_args& a) {
   tx::EvalParams P = make_params(h, a);
   const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
   const bool det = (a.flags & TX_EVAL_DETERMINISTIC) != 0;
+  const bool stage = (a.flags & TX_EVAL_SCATTER_DIRECT) == 0;
   if ((a.flags & TX_EVAL_PERSISTENT) && !det) {
     if (a.block >= 0) return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_PERSISTENT evaluates every block (block = -1)");
     for (const auto& db : h->blocks)
@@ -224,14 +225,14 @@ int eval_blocks(tx_handle h, const tx_eval_args& a) {
     }
     cudaError_t e = cudaSuccess;
     if (!det) {
-      e = tx::launch_assemble(V, P, mixed, nullptr, e0, e1, true, h->stream, h->grid_cap);
+      e = tx::launch_assemble(V, P, mixed, nullptr, e0, e1, true, stage, h->stream, h->grid_cap);
     } else {
       if (e0 != 0 || e1 != db.n_elem)
         return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_DETERMINISTIC evaluates whole blocks");
       // one launch per colour, plain read-modify-write: fixed summation order
       for (size_t c = 0; c + 1 < db.color_offsets.size() && e == cudaSuccess; ++c)
         e = tx::launch_assemble(V, P, mixed, db.color_perm, db.color_offsets[c], db.color_offsets[c + 1], false,
-                                h->stream, h->grid_cap);
+                                stage, h->stream, h->grid_cap);
     }
     if (e == cudaErrorInvalidValue) return fail(h, TX_EINVAL, "tx_eval: no kernel for this element family / cubature");
     if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: ") + cudaGetErrorString(e));
@@ -251,6 +252,9 @@ struct MfCtx {
   const int32_t* colind;
   const double* vals;
   bool matrix_free;
+  const double* x_pred;      // implicit integration: x_dot = coef * (x - x_pred)
+  double coef;
+  double* xdot_work;
 };
 
 int outer_residual(void* vctx, const double* x, double* r) {
@@ -260,8 +264,13 @@ int outer_residual(void* vctx, const double* x, double* r) {
   if (c->matrix_free) {
     // r = -f(x): FP64 Residual evaluation + Dirichlet residual x_d - g_d
     if (cudaMemsetAsync(r, 0, sizeof(double) * n, h->stream) != cudaSuccess) return TX_ECUDA;
+    const double* xdot = c->x_dot;
+    if (c->x_pred) {
+      if (tx::launch_scaled_diff(c->xdot_work, x, c->x_pred, c->coef, n, h->stream) != cudaSuccess) return TX_ECUDA;
+      xdot = c->xdot_work;
+    }
     tx_eval_args a{};
-    a.x = x; a.x_dot = c->x_dot; a.alpha = c->alpha; a.beta = c->beta; a.t = c->t;
+    a.x = x; a.x_dot = xdot; a.alpha = c->alpha; a.beta = c->beta; a.t = c->t;
     a.f = r; a.crs_vals = nullptr; a.block = -1; a.elem_end = -1; a.flags = 0;
     int rc = eval_blocks(h, a);
     if (rc) return rc;
@@ -484,12 +493,15 @@ int tx_solve_cg_ir(tx_handle h, tx_solve_args* a) {
   cudaError_t e = tx::solver_alloc(h->solver, n, h->dofs.nnz);
   if (e != cudaSuccess) return fail(h, TX_ENOMEM, std::string("tx_solve_cg_ir: ") + cudaGetErrorString(e));
   MfCtx ctx{h, a->x_dot, a->alpha, a->beta, a->t, a->n_dirichlet, a->dirichlet_lids, a->dirichlet_g,
-            a->b, a->rowptr, a->colind, a->vals, mf};
+            a->b, a->rowptr, a->colind, a->vals, mf, a->x_pred, a->x_dot_coef, h->solver.xdw};
+  if (a->x_pred && !mf) return fail(h, TX_EINVAL, "tx_solve_cg_ir: x_pred needs MATRIX_FREE_RESIDUAL");
   std::string err;
   int rc = tx::solve_cg_ir(h->solver, a->rowptr, a->colind, a->vals, a->n_dirichlet, a->dirichlet_lids, a->x,
                            outer_residual, &ctx, a->rtol > 0 ? a->rtol : 1e-10,
                            a->inner_rtol > 0 ? a->inner_rtol : 1e-5, a->max_outer > 0 ? a->max_outer : 50,
-                           a->max_inner > 0 ? a->max_inner : 100000, a->stats, h->stream, err);
+                           a->max_inner > 0 ? a->max_inner : 100000, a->stats, h->stream, err,
+                           (a->flags & TX_SOLVE_FIXED_ITERATIONS) != 0, (a->flags & TX_SOLVE_REUSE_OPERATOR) != 0,
+                           a->stats_device);
   if (rc == TX_ETIMEDOUT) return fail(h, rc, "tx_solve_cg_ir: did not reach rtol within max_outer iterations");
   if (rc) return fail(h, rc, err);
   return TX_OK;

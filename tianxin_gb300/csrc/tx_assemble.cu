@@ -48,7 +48,11 @@ template <> struct Family<TX_TOPO_HEX, TX_HCURL_I1> { static constexpr int NV = 
 
 constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, int THREADS_ = (Family<TOPO, BASIS>::NB > 16 ? 128 : 256)>
+// STAGE_: element residual/Jacobian staged in shared memory, then scattered
+// by the whole CTA with consecutive threads on consecutive entries of a CRS
+// row (few L2 sectors per warp reduction) instead of one row per thread.
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, int THREADS_ = (Family<TOPO, BASIS>::NB > 16 ? 128 : 256),
+          bool STAGE_ = false>
 struct Cfg {
   static constexpr int NV = Family<TOPO, BASIS>::NV;
   static constexpr int NB = Family<TOPO, BASIS>::NB;
@@ -77,7 +81,14 @@ struct Cfg {
   static constexpr size_t E_W = align16(E_V + sizeof(Real) * (HC ? NQ * NB * 3 : 0));
   static constexpr size_t E_QF = align16(E_W + sizeof(Real) * NQ);
   static constexpr size_t E_SIGN = align16(E_QF + sizeof(Real) * NQ * NQF);
-  static constexpr size_t E_END = align16(E_SIGN + sizeof(Real));
+  static constexpr bool STAGE = STAGE_;
+  static constexpr int NE = NF * NB;  // element DOFs
+  static constexpr size_t E_K = align16(E_SIGN + sizeof(Real));
+  static constexpr size_t E_R = align16(E_K + sizeof(Real) * (STAGE ? NE * NE : 0));
+  static constexpr size_t E_RP = align16(E_R + sizeof(Real) * (STAGE ? NE : 0));
+  static constexpr size_t E_LA = align16(E_RP + sizeof(int64_t) * (STAGE ? NE : 0));
+  static constexpr size_t E_EP = align16(E_LA + sizeof(int32_t) * (STAGE ? NB : 0));
+  static constexpr size_t E_END = align16(E_EP + (STAGE ? NB * NB : 0));
   static constexpr size_t SMEM = R_END + EPB * E_END;
 };
 
@@ -101,12 +112,13 @@ __device__ __forceinline__ Real source_at(int kind, double c, double s0, const d
 // g = grp0, grp0 + grp_stride, ... of EPB elements each.  ATOMIC=false is
 // the coloured (deterministic) scatter: no two elements processed by one
 // launch share a row, so plain read-modify-write is race free.
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, int THREADS>
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, int THREADS,
+          bool STAGE = false>
 __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalParams& P, const int32_t* perm,
                                               int64_t e_lo, int64_t e_hi, int64_t grp0, int64_t grp_stride,
                                               unsigned char* smem) {
-  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS>;
-  constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF;
+  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS, STAGE>;
+  constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF, NE = C::NE;
   constexpr bool HC = C::HC;
   double* r_geo_grad = reinterpret_cast<double*>(smem + C::R_GEO_GRAD);
   double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
@@ -141,6 +153,11 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
   Real* sW = reinterpret_cast<Real*>(eb + C::E_W);
   Real* sQF = reinterpret_cast<Real*>(eb + C::E_QF);
   Real* sSign = reinterpret_cast<Real*>(eb + C::E_SIGN);
+  Real* sK = reinterpret_cast<Real*>(eb + C::E_K);          // [a*NF+c][b*NF+d] staged Jacobian
+  Real* sR = reinterpret_cast<Real*>(eb + C::E_R);          // [a*NF+c] staged residual
+  int64_t* sRP = reinterpret_cast<int64_t*>(eb + C::E_RP);  // row starts rowptr[NF*la+c]
+  int32_t* sLA = reinterpret_cast<int32_t*>(eb + C::E_LA);  // entity LIDs
+  uint8_t* sEP = reinterpret_cast<uint8_t*>(eb + C::E_EP);  // epos[a][b]
   __syncthreads();
 
   const double* pp = P.p;
@@ -166,6 +183,14 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         if constexpr (HC) {
           sAUX[b] = P.aux ? __ldg(P.aux + ent) : 0.0;
           sSG[b] = (Real)__ldg(B.esign + e * NB + b);
+        }
+        if constexpr (STAGE) {
+          sLA[b] = (int32_t)ent;
+          if constexpr (JAC) {
+#pragma unroll
+            for (int c = 0; c < NF; ++c) sRP[b * NF + c] = __ldg(P.rowptr + NF * ent + c);
+            for (int k = 0; k < NB; ++k) sEP[b * NB + k] = __ldg(B.epos + (e * NB + b) * NB + k);
+          }
         }
       }
     }
@@ -338,18 +363,28 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
             r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + va[0] * qf[3] + va[1] * qf[4] + va[2] * qf[5]);
           }
         }
-        if (P.f) {
+        if constexpr (STAGE) {
+#pragma unroll
+          for (int c = 0; c < NF; ++c) sR[a * NF + c] = r[c];
+        } else if (P.f) {
 #pragma unroll
           for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.f + NF * la + c, (double)r[c]);
         }
         if constexpr (JAC) {
           int64_t rp[NF];
-#pragma unroll
-          for (int c = 0; c < NF; ++c) rp[c] = __ldg(P.rowptr + NF * la + c);
           const uint8_t* ep = B.epos + (e * NB + a) * NB;
+          if constexpr (!STAGE) {
+#pragma unroll
+            for (int c = 0; c < NF; ++c) rp[c] = __ldg(P.rowptr + NF * la + c);
+          }
+          // Jacobian entry (row a,c; column b,d): reduce now, or stage for the CTA-wide scatter
+          auto put = [&](int c, int b, int d, int64_t pb, Real v) {
+            if constexpr (STAGE) sK[(a * NF + c) * NE + b * NF + d] = v;
+            else accumulate<ATOMIC>(P.vals + rp[c] + pb + d, (double)v);
+          };
           const Real beta = (Real)P.beta, alpha = (Real)P.alpha;
           for (int b = 0; b < NB; ++b) {
-            const int64_t pb = (int64_t)NF * __ldg(ep + b);
+            const int64_t pb = STAGE ? 0 : (int64_t)NF * __ldg(ep + b);
             if constexpr (PHYS == TX_PHYS_POISSON) {
               const Real ca = beta * (Real)pp[0];
               const Real cm = beta * (Real)pp[1] + alpha * (Real)pp[2];
@@ -361,7 +396,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 kg += w * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
                 km += w * r_val[q * NB + a] * r_val[q * NB + b];
               }
-              accumulate<ATOMIC>(P.vals + rp[0] + pb, (double)(ca * kg + cm * km));
+              put(0, b, 0, pb, ca * kg + cm * km);
             } else if constexpr (PHYS == TX_PHYS_HEAT) {
               Real kab = 0;
               for (int q = 0; q < NQ; ++q) {
@@ -371,7 +406,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 kab += sW[q] * (qf[7] * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]) +
                                 r_val[q * NB + b] * (ga[0] * qf[4] + ga[1] * qf[5] + ga[2] * qf[6]));
               }
-              accumulate<ATOMIC>(P.vals + rp[0] + pb, (double)(beta * kab));
+              put(0, b, 0, pb, beta * kab);
             } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
               Real Pm[9], M = 0;
 #pragma unroll
@@ -397,7 +432,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 for (int d = 0; d < 3; ++d) {
                   Real k = beta * (lam * Pm[3 * c + d] + mu * Pm[3 * d + c]);
                   if (c == d) k += beta * mu * trP + mass;
-                  accumulate<ATOMIC>(P.vals + rp[c] + pb + d, (double)k);
+                  put(c, b, d, pb, k);
                 }
             } else {  // MAXWELL
               const Real imu = (Real)pp[0], sig = (Real)pp[1];
@@ -410,9 +445,36 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 kc += sW[q] * (ca[0] * cb[0] + ca[1] * cb[1] + ca[2] * cb[2]);
                 kv += sW[q] * (va[0] * vb[0] + va[1] * vb[1] + va[2] * vb[2]);
               }
-              accumulate<ATOMIC>(P.vals + rp[0] + pb, (double)(beta * (imu * kc + sig * kv)));
+              put(0, b, 0, pb, beta * (imu * kc + sig * kv));
             }
           }
+        }
+      }
+    }
+    if constexpr (STAGE) {
+      // ------------------------------------------------------ 5 CTA-wide scatter
+      // consecutive threads take consecutive entries of an element row
+      __syncthreads();
+      const int nval = (int)(e_hi - g0 < EPB ? e_hi - g0 : EPB);
+      unsigned char* base = smem + C::R_END;
+      if (P.f) {
+        for (int i = threadIdx.x; i < nval * NE; i += blockDim.x) {
+          const int l2 = i / NE, row = i - l2 * NE;
+          const unsigned char* e2 = base + (size_t)l2 * C::E_END;
+          const int32_t la = reinterpret_cast<const int32_t*>(e2 + C::E_LA)[row / NF];
+          accumulate<ATOMIC>(P.f + (int64_t)NF * la + row % NF,
+                             (double)reinterpret_cast<const Real*>(e2 + C::E_R)[row]);
+        }
+      }
+      if constexpr (JAC) {
+        for (int i = threadIdx.x; i < nval * NE * NE; i += blockDim.x) {
+          const int l2 = i / (NE * NE), rem = i - l2 * (NE * NE);
+          const int row = rem / NE, col = rem - row * NE;
+          const unsigned char* e2 = base + (size_t)l2 * C::E_END;
+          const int64_t addr = reinterpret_cast<const int64_t*>(e2 + C::E_RP)[row] +
+                               (int64_t)NF * reinterpret_cast<const uint8_t*>(e2 + C::E_EP)[(row / NF) * NB + col / NF] +
+                               col % NF;
+          accumulate<ATOMIC>(P.vals + addr, (double)reinterpret_cast<const Real*>(e2 + C::E_K)[rem]);
         }
       }
     }
@@ -421,19 +483,26 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 }
 
 // ------------------------------------------------------------- per block
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC>
-__global__ void __launch_bounds__(Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS)
-k_assemble(const BlockView B, const EvalParams P, const int32_t* perm, int64_t e_lo, int64_t e_hi) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS>(
-      B, P, perm, e_lo, e_hi, blockIdx.x, gridDim.x, smem);
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool STAGE>
+constexpr int block_threads() {
+  return STAGE ? 128 : Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS;
 }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC>
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE>
+__global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>())
+k_assemble(const BlockView B, const EvalParams P, const int32_t* perm, int64_t e_lo, int64_t e_hi) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
+  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, T, STAGE>(B, P, perm, e_lo, e_hi, blockIdx.x, gridDim.x,
+                                                                    smem);
+}
+
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE>
 cudaError_t launch_one(const BlockView& B, const EvalParams& P, const int32_t* perm, int64_t e_lo, int64_t e_hi,
                        cudaStream_t s, int grid_cap) {
-  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real>;
-  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC>;
+  constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
+  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, T, STAGE>;
+  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, STAGE>;
   static int max_blocks_per_sm = -1;
   static int num_sms = 0;
   if (max_blocks_per_sm < 0) {
@@ -442,7 +511,7 @@ cudaError_t launch_one(const BlockView& B, const EvalParams& P, const int32_t* p
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks_per_sm, kern, C::THREADS, C::SMEM);
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks_per_sm, kern, T, C::SMEM);
     if (err != cudaSuccess) return err;
     if (max_blocks_per_sm < 1) max_blocks_per_sm = 1;
   }
@@ -452,21 +521,26 @@ cudaError_t launch_one(const BlockView& B, const EvalParams& P, const int32_t* p
   int64_t cap = (int64_t)max_blocks_per_sm * num_sms * 4;
   if (grid_cap > 0 && grid_cap < cap) cap = grid_cap;
   if (blocks > cap) blocks = cap;
-  kern<<<(unsigned)blocks, C::THREADS, C::SMEM, s>>>(B, P, perm, e_lo, e_hi);
+  kern<<<(unsigned)blocks, T, C::SMEM, s>>>(B, P, perm, e_lo, e_hi);
   return cudaGetLastError();
 }
 
 template <int TOPO, int BASIS, int NQ, int PHYS>
 cudaError_t launch_prec(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,
-                        int64_t e_hi, bool atomic, cudaStream_t s, int cap) {
+                        int64_t e_hi, bool atomic, bool stage, cudaStream_t s, int cap) {
   const bool jac = P.vals != nullptr;
-#define TX_L(R, J, A) launch_one<TOPO, BASIS, NQ, PHYS, R, J, A>(B, P, perm, e_lo, e_hi, s, cap)
-  if (atomic) {
-    if (mixed) return jac ? TX_L(float, true, true) : TX_L(float, false, true);
-    return jac ? TX_L(double, true, true) : TX_L(double, false, true);
+  const bool st = stage && jac;
+#define TX_L(R, J, A, S) launch_one<TOPO, BASIS, NQ, PHYS, R, J, A, S>(B, P, perm, e_lo, e_hi, s, cap)
+  if (st) {
+    if (atomic) return mixed ? TX_L(float, true, true, true) : TX_L(double, true, true, true);
+    return mixed ? TX_L(float, true, false, true) : TX_L(double, true, false, true);
   }
-  if (mixed) return jac ? TX_L(float, true, false) : TX_L(float, false, false);
-  return jac ? TX_L(double, true, false) : TX_L(double, false, false);
+  if (atomic) {
+    if (mixed) return jac ? TX_L(float, true, true, false) : TX_L(float, false, true, false);
+    return jac ? TX_L(double, true, true, false) : TX_L(double, false, true, false);
+  }
+  if (mixed) return jac ? TX_L(float, true, false, false) : TX_L(float, false, false, false);
+  return jac ? TX_L(double, true, false, false) : TX_L(double, false, false, false);
 #undef TX_L
 }
 
@@ -574,11 +648,11 @@ cudaError_t launch_assemble_batched(const BlockView* views, const EvalParams* pa
 }
 
 cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,
-                            int64_t e_hi, bool atomic, cudaStream_t s, int cap) {
+                            int64_t e_hi, bool atomic, bool stage, cudaStream_t s, int cap) {
   switch (assemble_kind(B.topo, B.basis, B.nq, P.physics)) {
 #define TX_LAUNCH(K, T, BS, Q, PH) \
   case K:                          \
-    return launch_prec<T, BS, Q, PH>(B, P, mixed, perm, e_lo, e_hi, atomic, s, cap);
+    return launch_prec<T, BS, Q, PH>(B, P, mixed, perm, e_lo, e_hi, atomic, stage, s, cap);
     TX_FOR_EACH_KIND(TX_LAUNCH)
 #undef TX_LAUNCH
     default:

@@ -28,7 +28,7 @@ struct EvalParams {
 // is the coloured, deterministic scatter (one launch per colour).  Returns
 // cudaErrorInvalidValue for element families without a kernel.
 cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,
-                            int64_t e_hi, bool atomic, cudaStream_t s, int grid_cap);
+                            int64_t e_hi, bool atomic, bool stage, cudaStream_t s, int grid_cap);
 
 // One chunk of elements of one block view (views[view], params[view]).
 struct WorkItem {
@@ -64,6 +64,7 @@ struct SolverWork {
   float* dinv = nullptr;       // Jacobi preconditioner
   float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *d = nullptr;
   double* r64 = nullptr;       // outer residual
+  double* xdw = nullptr;       // x_dot work vector of implicit integration
   uint8_t* mask = nullptr;     // Dirichlet mask
   double* red = nullptr;       // reduction partials [kRedSlots * kRedBlocks]
   double* scal = nullptr;      // device scalars
@@ -82,11 +83,13 @@ typedef int (*ResidualFn)(void* ctx, const double* x, double* r);
 int solve_cg_ir(SolverWork& w, const int64_t* rowptr, const int32_t* colind, const double* vals,
                 int64_t n_dir, const int32_t* dir_lids, double* x, ResidualFn resid, void* ctx,
                 double rtol, double inner_rtol, int max_outer, int max_inner, double* stats,
-                cudaStream_t s, std::string& err);
+                cudaStream_t s, std::string& err, bool fixed, bool reuse_op, double* stats_dev);
 
 // Vector helpers used by the API layer
 cudaError_t launch_fill(double* p, double v, int64_t n, cudaStream_t s);
 cudaError_t launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t s);
+// out = c * (x - xp)
+cudaError_t launch_scaled_diff(double* out, const double* x, const double* xp, double c, int64_t n, cudaStream_t s);
 // sum of squares of x (FP64) into *out (device), using w.red as scratch
 cudaError_t launch_norm2sq(const double* x, int64_t n, double* red, double* out, cudaStream_t s);
 

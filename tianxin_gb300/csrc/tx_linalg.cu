@@ -156,6 +156,11 @@ __global__ void k_axpby(double* y, const double* x, double a, double b, int64_t 
     y[i] = a * x[i] + b * y[i];
 }
 
+__global__ void k_scaled_diff(double* out, const double* x, const double* xp, double c, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = c * (x[i] - xp[i]);
+}
+
 // ------------------------------------------------------------ CG kernels
 // FP32 copy of A with symmetric Dirichlet elimination + Jacobi diagonal.
 __global__ void k_make_f32(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
@@ -322,6 +327,12 @@ cudaError_t launch_axpby(double* y, const double* x, double a, double b, int64_t
   k_axpby<<<grid_for(n, kThreads), kThreads, 0, s>>>(y, x, a, b, n);
   return cudaGetLastError();
 }
+cudaError_t launch_scaled_diff(double* out, const double* x, const double* xp, double c, int64_t n,
+                               cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_scaled_diff<<<grid_for(n, kThreads), kThreads, 0, s>>>(out, x, xp, c, n);
+  return cudaGetLastError();
+}
 cudaError_t launch_norm2sq(const double* x, int64_t n, double* red, double* out, cudaStream_t s) {
   cudaMemsetAsync(red, 0, sizeof(double) * kRedBlocks, s);
   k_norm2sq<<<kRedBlocks, kThreads, 0, s>>>(x, n, red);
@@ -341,6 +352,7 @@ cudaError_t solver_alloc(SolverWork& w, int64_t n, int64_t nnz) {
   if ((e = cmalloc(w.q, n)) != cudaSuccess) return e;
   if ((e = cmalloc(w.d, n)) != cudaSuccess) return e;
   if ((e = cmalloc(w.r64, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.xdw, n)) != cudaSuccess) return e;
   if ((e = cmalloc(w.mask, n)) != cudaSuccess) return e;
   if ((e = cmalloc(w.red, (size_t)kRedSlots * kRedBlocks)) != cudaSuccess) return e;
   if ((e = cmalloc(w.scal, 8)) != cudaSuccess) return e;
@@ -352,14 +364,24 @@ cudaError_t solver_alloc(SolverWork& w, int64_t n, int64_t nnz) {
 
 void solver_free(SolverWork& w) {
   cudaFree(w.vals32); cudaFree(w.dinv); cudaFree(w.r); cudaFree(w.z); cudaFree(w.p); cudaFree(w.q);
-  cudaFree(w.d); cudaFree(w.r64); cudaFree(w.mask); cudaFree(w.red); cudaFree(w.scal);
+  cudaFree(w.d); cudaFree(w.r64); cudaFree(w.xdw); cudaFree(w.mask); cudaFree(w.red); cudaFree(w.scal);
   if (w.host_scal) cudaFreeHost(w.host_scal);
   w = SolverWork();
 }
 
+__global__ void k_fixed_stats(const double* scal, int outer, int inner, double* out) {
+  // scal[4] = ||r_final||^2, scal[5] = ||r_0||^2
+  const double r0 = sqrt(scal[5]);
+  out[0] = outer;
+  out[1] = (double)outer * inner;
+  out[2] = r0 > 0.0 ? sqrt(scal[4]) / r0 : 0.0;
+  out[3] = r0;
+}
+
 int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const double* vals, int64_t n_dir,
                 const int32_t* dir, double* x, ResidualFn resid, void* ctx, double rtol, double inner_rtol,
-                int max_outer, int max_inner, double* stats, cudaStream_t s, std::string& err) {
+                int max_outer, int max_inner, double* stats, cudaStream_t s, std::string& err, bool fixed,
+                bool reuse_op, double* stats_dev) {
   const int64_t n = w.n;
   const unsigned gb = kRedBlocks;
   auto cuda_fail = [&](cudaError_t e, const char* where) {
@@ -368,10 +390,12 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
   };
   cudaError_t e;
   // FP32 operator with symmetric Dirichlet elimination
-  cudaMemsetAsync(w.mask, 0, n, s);
-  if (n_dir > 0) k_mask<<<grid_for(n_dir, kThreads), kThreads, 0, s>>>(n_dir, dir, w.mask);
-  k_make_f32<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, rp, col, vals, w.mask, w.vals32, w.dinv);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: make_f32");
+  if (!reuse_op) {
+    cudaMemsetAsync(w.mask, 0, n, s);
+    if (n_dir > 0) k_mask<<<grid_for(n_dir, kThreads), kThreads, 0, s>>>(n_dir, dir, w.mask);
+    k_make_f32<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, rp, col, vals, w.mask, w.vals32, w.dinv);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: make_f32");
+  }
   const double avg = (double)w.nnz / (double)(n > 0 ? n : 1);
   auto spmv_dot = [&]() {
     if (avg <= 12) k_spmv_dot<4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
@@ -379,6 +403,33 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     else if (avg <= 96) k_spmv_dot<16><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
     else k_spmv_dot<32><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
   };
+  auto cg_iteration = [&]() {
+    spmv_dot();
+    k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2);  // pq
+    k_cg_update<<<gb, kThreads, 0, s>>>(n, w.scal, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
+    k_cg_finish<<<1, 1024, 0, s>>>(w.scal, w.red);
+    k_cg_pupdate<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, w.scal, w.z, w.p);
+  };
+  if (fixed) {
+    // Capturable form: exact iteration counts, no host reads; statistics
+    // land in stats_dev (device) when given.
+    for (int outer = 0; outer < max_outer; ++outer) {
+      int rc = resid(ctx, x, w.r64);
+      if (rc) { err = "cg: residual evaluation failed"; return rc; }
+      if (outer == 0 && (e = launch_norm2sq(w.r64, n, w.red, w.scal + 5, s)) != cudaSuccess)
+        return cuda_fail(e, "cg: norm");
+      k_cg_init<<<gb, kThreads, 0, s>>>(n, w.r64, w.mask, w.dinv, w.r, w.z, w.p, w.d, w.red);
+      k_finalize<<<1, 1024, 0, s>>>(w.red, 2, w.scal);
+      for (int it = 0; it < max_inner; ++it) cg_iteration();
+      k_add_f32<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, x, w.d);
+    }
+    int rc = resid(ctx, x, w.r64);
+    if (rc) { err = "cg: residual evaluation failed"; return rc; }
+    if ((e = launch_norm2sq(w.r64, n, w.red, w.scal + 4, s)) != cudaSuccess) return cuda_fail(e, "cg: norm");
+    if (stats_dev) k_fixed_stats<<<1, 1, 0, s>>>(w.scal, max_outer, max_inner, stats_dev);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: fixed iterations");
+    return TX_OK;
+  }
   double r0 = -1.0, rn = 0.0;
   int outer = 0, inner_total = 0;
   for (;; ++outer) {
@@ -400,13 +451,7 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     int it = 0;
     const int check = 16;
     while (it < max_inner) {
-      for (int k = 0; k < check && it < max_inner; ++k, ++it) {
-        spmv_dot();
-        k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2);  // pq
-        k_cg_update<<<gb, kThreads, 0, s>>>(n, w.scal, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
-        k_cg_finish<<<1, 1024, 0, s>>>(w.scal, w.red);
-        k_cg_pupdate<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, w.scal, w.z, w.p);
-      }
+      for (int k = 0; k < check && it < max_inner; ++k, ++it) cg_iteration();
       cudaMemcpyAsync(w.host_scal, w.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
       if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cg: iterate");
       if (!(w.host_scal[1] > target)) break;  // also stops on NaN

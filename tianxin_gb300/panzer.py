@@ -203,7 +203,7 @@ class DirichletBC:
 
 
 def eval_args(x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False, block=-1,
-              workset=(0, -1), deterministic=False, persistent=False):
+              workset=(0, -1), deterministic=False, persistent=False, scatter_direct=False):
     a = _abi.EvalArgs()
     a.x, a.x_dot, a.aux = _ptr(x), _ptr(x_dot), _ptr(aux)
     a.alpha, a.beta, a.t = alpha, beta, t
@@ -212,7 +212,8 @@ def eval_args(x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=Non
     a.block = block
     a.elem_begin, a.elem_end = workset
     a.flags = ((_abi.TX_EVAL_MIXED if mixed else 0) | (_abi.TX_EVAL_DETERMINISTIC if deterministic else 0) |
-               (_abi.TX_EVAL_PERSISTENT if persistent else 0))
+               (_abi.TX_EVAL_PERSISTENT if persistent else 0) |
+               (_abi.TX_EVAL_SCATTER_DIRECT if scatter_direct else 0))
     return a
 
 
@@ -231,8 +232,9 @@ class AssemblyEngine:
         check(self.dof.h, self.dof.lib.tx_set_grid_cap(self.dof.h, max_ctas), "tx_set_grid_cap")
 
     def evaluate(self, x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False,
-                 block=-1, workset=(0, -1), deterministic=False, persistent=False):
-        a = eval_args(x, x_dot, aux, alpha, beta, t, f, W, mixed, block, workset, deterministic, persistent)
+                 block=-1, workset=(0, -1), deterministic=False, persistent=False, scatter_direct=False):
+        a = eval_args(x, x_dot, aux, alpha, beta, t, f, W, mixed, block, workset, deterministic, persistent,
+                      scatter_direct)
         lib = self.dof.lib
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_eval(self.dof.h, C.byref(a)), "tx_eval")
@@ -277,16 +279,27 @@ class ModelEvaluator:
         return lids, torch.cat(gs)
 
     def solve(self, W, x, b=None, rtol=1e-10, inner_rtol=1e-5, max_outer=50, max_inner=100000, matrix_free=False,
-              x_dot=None, alpha=0.0, beta=1.0, t=0.0):
-        """FP64 iterative refinement around FP32 Jacobi-CG; x updated in place. Returns stats."""
-        lids, g = self.dirichlet_lids()
+              x_dot=None, alpha=0.0, beta=1.0, t=0.0, fixed=False, reuse_operator=False, stats_device=None,
+              x_pred=None, x_dot_coef=0.0):
+        """FP64 iterative refinement around FP32 Jacobi-CG; x updated in place. Returns stats.
+
+        fixed=True runs exactly max_outer x max_inner iterations without host
+        reads (capturable); its statistics go to stats_device (device f64[4]).
+        """
+        if not hasattr(self, "_dir"):
+            self._dir = self.dirichlet_lids()  # kept alive: captured graphs read these
+        lids, g = self._dir
         a = _abi.SolveArgs()
         a.rowptr, a.colind, a.vals = _ptr(W.rowptr), _ptr(W.colind), _ptr(W.values)
         a.b, a.x = _ptr(b), _ptr(x)
         a.n_dirichlet, a.dirichlet_lids, a.dirichlet_g = lids.numel(), _ptr(lids), _ptr(g)
         a.rtol, a.inner_rtol, a.max_outer, a.max_inner = rtol, inner_rtol, max_outer, max_inner
-        a.flags = _abi.TX_SOLVE_MATRIX_FREE_RESIDUAL if matrix_free else 0
+        a.flags = ((_abi.TX_SOLVE_MATRIX_FREE_RESIDUAL if matrix_free else 0) |
+                   (_abi.TX_SOLVE_FIXED_ITERATIONS if fixed else 0) |
+                   (_abi.TX_SOLVE_REUSE_OPERATOR if reuse_operator else 0))
         a.x_dot, a.alpha, a.beta, a.t = _ptr(x_dot), alpha, beta, t
+        a.stats_device = _ptr(stats_device)
+        a.x_pred, a.x_dot_coef = _ptr(x_pred), x_dot_coef
         lib = self.dof.lib
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_solve_cg_ir(self.dof.h, C.byref(a)), "tx_solve_cg_ir")

@@ -1,0 +1,93 @@
+"""The synthetic workloads of the assembly path, by name.
+
+  poisson_hex8        -lap u = 3 pi^2 sin sin sin on the unit cube, hex8 Q1, n^3 bricks,
+                      interior vertices jittered +-0.1h, homogeneous Dirichlet, 2x2x2 Gauss
+  elasticity_hex8     linear elasticity, E=1 nu=0.3, b=(0,0,-1), clamped z=0, jitter 0.05h
+  heat_hex27_tet10    k(T)=1+0.5T^2 heat, block A hex27 Q2 (27-point Gauss) on [0,1]^3,
+                      block B hex split into 6 tet10 P2 (4-point rule) on [1,2]x[0,1]^2,
+                      conforming interface, q=1
+  elastodynamics_hex8 rho=1 E=1 nu=0.25, Newmark beta=1/4 gamma=1/2, dt=1e-3
+  mixed_batch         many independent meshes, element counts log-uniform in [6^3, 40^3],
+                      each Poisson hex8, elasticity tet4 (6 per brick) or curl-curl Maxwell
+                      on lowest-order Nedelec hexes (sigma=1, J ~ N(0,1) per edge)
+
+Inputs are seeded synthetic data (no dataset is involved).
+"""
+import math
+
+import numpy as np
+import torch
+
+from . import _abi as A
+from .panzer import CartesianConnManager, DirichletBC, DOFManager, ModelEvaluator, TpetraLinearObjFactory
+
+
+class Workload:
+    def __init__(self, name, conn, dof, lof, me, mesh_desc, eqset, extras=None):
+        self.name, self.conn, self.dof, self.lof, self.me = name, conn, dof, lof, me
+        self.mesh_desc, self.eqset = mesh_desc, eqset
+        self.extras = extras or {}
+
+    @property
+    def n_elements(self):
+        return self.conn.n_elements
+
+
+def _make(name, n, blocks, topo, eqset, jitter, seed, lengths=(1.0, 1.0, 1.0), dirichlet=()):
+    m = A.mesh_desc(n, blocks, topo, lengths, jitter, seed)
+    conn = CartesianConnManager(*(n if isinstance(n, tuple) else (n, n, n)), *blocks, topology=topo, lengths=lengths,
+                                jitter=jitter, seed=seed)
+    dof = DOFManager(conn, eqset)
+    lof = TpetraLinearObjFactory(dof)
+    me = ModelEvaluator(lof, [DirichletBC(dof, sides, fields) for sides, fields in dirichlet])
+    return Workload(name, conn, dof, lof, me, m, eqset)
+
+
+def poisson_hex8(n=16, seed=1):
+    q = A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 0.0), source_kind=A.TX_SOURCE_SINE)
+    return _make("poisson_hex8", n, (1, 1, 1), A.TX_TOPO_HEX, q, 0.1, seed, dirichlet=[(A.ALL_SIDES, None)])
+
+
+def elasticity_hex8(n=128, seed=2024):
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.0))
+    return _make("elasticity_hex8", n, (1, 1, 1), A.TX_TOPO_HEX, q, 0.05, seed, dirichlet=[(A.SIDE_ZMIN, None)])
+
+
+def heat_hex27_tet10(n=48, seed=3):
+    q = A.equation_set(A.TX_PHYS_HEAT, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0), integration_order=[4, 2])
+    return _make("heat_hex27_tet10", (n, n, n), (2, 1, 1), [A.TX_TOPO_HEX, A.TX_TOPO_TET], q, 0.0, seed,
+                 lengths=(2.0, 1.0, 1.0))
+
+
+def elastodynamics_hex8(n=96, seed=4):
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.25, 0.0, 0.0, 0.0, 1.0))
+    return _make("elastodynamics_hex8", n, (1, 1, 1), A.TX_TOPO_HEX, q, 0.0, seed)
+
+
+def batch_plan(count=256, seed=5, lo=6 ** 3, hi=40 ** 3):
+    """(kind, n) per instance: n = round(N^(1/3)), N log-uniform in [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    kinds = ["poisson_hex8", "elasticity_tet4", "maxwell_nedelec"]
+    out = []
+    for _ in range(count):
+        N = math.exp(rng.uniform(math.log(lo), math.log(hi)))
+        out.append((kinds[int(rng.integers(0, 3))], max(1, int(round(N ** (1.0 / 3.0))))))
+    return out
+
+
+def batch_instance(kind, n, seed):
+    if kind == "poisson_hex8":
+        q = A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 0.0), source_kind=A.TX_SOURCE_SINE)
+        return _make(kind, n, (1, 1, 1), A.TX_TOPO_HEX, q, 0.1, seed, dirichlet=[(A.ALL_SIDES, None)])
+    if kind == "elasticity_tet4":
+        q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.0))
+        return _make(kind, n, (1, 1, 1), A.TX_TOPO_TET, q, 0.1, seed, dirichlet=[(A.SIDE_ZMIN, None)])
+    q = A.equation_set(A.TX_PHYS_MAXWELL, A.TX_HCURL_I1, params=(1.0, 1.0))
+    w = _make(kind, n, (1, 1, 1), A.TX_TOPO_HEX, q, 0.1, seed)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    w.extras["J"] = torch.randn(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g)
+    return w
+
+
+def mixed_batch(count=256, seed=5):
+    return [batch_instance(k, n, seed * 1000 + i) for i, (k, n) in enumerate(batch_plan(count, seed))]
