@@ -1,0 +1,93 @@
+"""Tile-shape autotuner for the assembly launches.
+
+The knobs play the role of Panzer's HierarchicParallelism team/vector sizes
+(disc-fe/src/Panzer_HierarchicParallelism.hpp:78-128):
+
+  * scatter   staged CTA-wide scatter vs per-thread row reductions
+  * grid_cap  CTAs of the per-block launch (0 = occupancy x SMs x 4)
+  * workset   elements per work item of the persistent / batched launch
+
+Each candidate is timed with CUDA events on the real evaluation (outputs in
+scratch vectors), the fastest is kept, and results are cached in
+_build/autotune.json keyed by GPU name, element family, physics, precision
+and size.
+"""
+import json
+import os
+
+import torch
+
+from . import _abi as A
+
+CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
+
+
+def _key(dof, mixed, mode):
+    q = dof.eqset
+    return "|".join(str(v) for v in (torch.cuda.get_device_name(), q.physics, list(q.block_basis)[:dof.conn.n_blocks],
+                                     list(dof.conn.desc.block_topology)[:dof.conn.n_blocks], dof.conn.n_elements,
+                                     int(mixed), mode))
+
+
+def _load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(d):
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    tmp = CACHE + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(d, f, indent=1, sort_keys=True)
+    os.replace(tmp, CACHE)
+
+
+def _time(fn, reps=3):
+    fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=False, verbose=False):
+    """Pick and apply the fastest configuration for ae's handle; returns it."""
+    dof = ae.dof
+    key = _key(dof, mixed, "persistent" if persistent else "block")
+    cache = _load()
+    if key in cache and not force:
+        cfg = cache[key]
+    else:
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        results = []
+        if persistent:
+            for ws in (128, 256, 512, 1024, 2048):
+                ae.setWorksetSize(ws, ws)
+                ae.setGridCap(0)
+                t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, persistent=True), reps)
+                results.append(({"workset": ws, "grid_cap": 0}, t))
+        else:
+            for direct in (False, True):
+                for cap in (0, sms * 2, sms * 4, sms * 8):
+                    ae.setGridCap(cap)
+                    t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, scatter_direct=direct), reps)
+                    results.append(({"scatter_direct": direct, "grid_cap": cap}, t))
+        best = min(results, key=lambda r: r[1])
+        cfg = dict(best[0], ms=best[1], candidates=[dict(c, ms=t) for c, t in results])
+        cache[key] = cfg
+        _save(cache)
+        if verbose:
+            for c, t in results:
+                print(f"  {c}: {t:.3f} ms")
+    ae.setGridCap(cfg.get("grid_cap", 0))
+    ae.scatter_direct = bool(cfg.get("scatter_direct", False))
+    if "workset" in cfg:
+        ae.setWorksetSize(cfg["workset"], cfg["workset"])
+    return cfg

@@ -222,6 +222,7 @@ class AssemblyEngine:
 
     def __init__(self, lof):
         self.lof, self.dof = lof, lof.dof
+        self.scatter_direct = False  # set by the autotuner
 
     def setWorksetSize(self, min_size, max_size=None, seed=0):
         """Worksets of the persistent evaluation: sizes uniform in [min_size, max_size]."""
@@ -232,7 +233,9 @@ class AssemblyEngine:
         check(self.dof.h, self.dof.lib.tx_set_grid_cap(self.dof.h, max_ctas), "tx_set_grid_cap")
 
     def evaluate(self, x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False,
-                 block=-1, workset=(0, -1), deterministic=False, persistent=False, scatter_direct=False):
+                 block=-1, workset=(0, -1), deterministic=False, persistent=False, scatter_direct=None):
+        if scatter_direct is None:
+            scatter_direct = self.scatter_direct
         a = eval_args(x, x_dot, aux, alpha, beta, t, f, W, mixed, block, workset, deterministic, persistent,
                       scatter_direct)
         lib = self.dof.lib
