@@ -83,20 +83,27 @@ __global__ void k_dirichlet(int64_t n, const int32_t* __restrict__ lids, const d
 }
 
 // Vector CSR: LANES threads per row, strided over the row, shuffle reduction.
+// The row loop advances per warp (its trip count is warp-uniform) so every
+// lane reaches the full-mask shuffles; rows past n are predicated off.
 template <typename T, int LANES>
 __global__ void __launch_bounds__(kThreads) k_spmv(int64_t n, const int64_t* __restrict__ rp,
                                                    const int32_t* __restrict__ col, const T* __restrict__ vals,
                                                    const T* __restrict__ x, T* __restrict__ y, T alpha, T beta) {
+  constexpr int GPW = 32 / LANES;  // row groups per warp
   const int sub = threadIdx.x % LANES;
-  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES;
-  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / LANES;
-  for (int64_t r = grp; r < n; r += ngrp) {
-    const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+  const int g = (threadIdx.x & 31) / LANES;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = warp * GPW; base < n; base += nwarps * GPW) {
+    const int64_t r = base + g;
     T s = T(0);
-    for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(x + __ldcs(col + k));
+    if (r < n) {
+      const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+      for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(x + __ldcs(col + k));
+    }
 #pragma unroll
     for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LANES);
-    if (sub == 0) y[r] = beta == T(0) ? alpha * s : alpha * s + beta * y[r];
+    if (r < n && sub == 0) y[r] = beta == T(0) ? alpha * s : alpha * s + beta * y[r];
   }
 }
 
@@ -214,17 +221,22 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(int64_t n, const int64_t*
                                                        const float* __restrict__ p, float* __restrict__ q,
                                                        double* __restrict__ red) {
   __shared__ double sh[32];
+  constexpr int GPW = 32 / LANES;
   const int sub = threadIdx.x % LANES;
-  const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES;
-  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / LANES;
+  const int g = (threadIdx.x & 31) / LANES;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   double pq = 0.0;
-  for (int64_t r = grp; r < n; r += ngrp) {
-    const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+  for (int64_t base = warp * GPW; base < n; base += nwarps * GPW) {  // warp-uniform trip count
+    const int64_t r = base + g;
     float s = 0.0f;
-    for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(p + __ldcs(col + k));
+    if (r < n) {
+      const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+      for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(p + __ldcs(col + k));
+    }
 #pragma unroll
     for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LANES);
-    if (sub == 0) {
+    if (r < n && sub == 0) {
       q[r] = s;
       pq += (double)s * p[r];
     }

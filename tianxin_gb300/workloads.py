@@ -91,3 +91,106 @@ def batch_instance(kind, n, seed):
 
 def mixed_batch(count=256, seed=5):
     return [batch_instance(k, n, seed * 1000 + i) for i, (k, n) in enumerate(batch_plan(count, seed))]
+
+
+# ---------------------------------------------------------------- timing
+def _events():
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def time_eval(ae, x, f, W, reps=5, **kw):
+    """Mean ms of one R+J evaluation (f, W zeroed inside the timed region)."""
+    for _ in range(2):
+        f.zero_(); W.initializeMatrix(0.0); ae.evaluate(x, f=f, W=W, **kw)
+    torch.cuda.synchronize()
+    s, e = _events()
+    s.record()
+    for _ in range(reps):
+        f.zero_(); W.initializeMatrix(0.0); ae.evaluate(x, f=f, W=W, **kw)
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def report(names=("poisson_hex8", "heat_hex27_tet10", "elastodynamics_hex8", "mixed_batch")):
+    """Elements/s of the non-headline workloads (one JSON object)."""
+    import json
+    import time
+    from .newmark import NewmarkElastodynamics
+    from .panzer import AssemblyEngine, Batch
+    out = {}
+    if "poisson_hex8" in names:
+        w = poisson_hex8(16)
+        ae, x = AssemblyEngine(w.lof), w.lof.getTpetraVector()
+        f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
+        out["poisson_hex8_16"] = {"elements": w.n_elements,
+                                  "fp64_ms": time_eval(ae, x, f, W), "mixed_ms": time_eval(ae, x, f, W, mixed=True)}
+    if "heat_hex27_tet10" in names:
+        w = heat_hex27_tet10(48)
+        ae = AssemblyEngine(w.lof)
+        ae.setWorksetSize(256, 1024, seed=11)
+        g = torch.Generator(device="cuda").manual_seed(2)
+        x = torch.rand(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g)
+        f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
+        r = {"elements": w.n_elements, "dofs": w.dof.n_dofs, "nnz": w.dof.nnz}
+        for tag, kw in (("fp64_blocks", {}), ("mixed_blocks", {"mixed": True}),
+                        ("fp64_persistent", {"persistent": True}), ("mixed_persistent", {"persistent": True, "mixed": True})):
+            r[tag + "_ms"] = time_eval(ae, x, f, W, **kw)
+        out["heat_hex27_tet10_48"] = r
+    if "elastodynamics_hex8" in names:
+        w = elastodynamics_hex8(96)
+        g = torch.Generator(device="cuda").manual_seed(4)
+        u0 = torch.randn(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g) * 1e-3
+        nm = NewmarkElastodynamics(w.me, 1e-3, 0.25, 0.5, mixed=True, outer=3, inner=24)
+        t0 = time.perf_counter()
+        nm.initialize(u0)
+        torch.cuda.synchronize()
+        t_init = time.perf_counter() - t0
+        nm.capture()
+        s, e = _events()
+        s.record()
+        rel = []
+        for _ in range(10):
+            rel.append(nm.step()[2])
+        e.record()
+        torch.cuda.synchronize()
+        out["elastodynamics_hex8_96"] = {"elements": w.n_elements, "dofs": w.dof.n_dofs, "steps": 10,
+                                         "ms_per_step": s.elapsed_time(e) / 10,
+                                         "max_step_relres": max(float(v) for v in rel),
+                                         "init_s": t_init}
+    if "mixed_batch" in names:
+        ws = mixed_batch(256)
+        g = torch.Generator(device="cuda").manual_seed(5)
+        xs = [torch.rand(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g) for w in ws]
+        auxs = [w.extras.get("J") for w in ws]
+        fs = [w.lof.getTpetraVector() for w in ws]
+        Ws = [w.lof.getTpetraMatrix() for w in ws]
+        b = Batch([w.dof for w in ws], workset=(512, 512))
+        nel = sum(w.n_elements for w in ws)
+        r = {"instances": len(ws), "elements": nel}
+        for tag, mixed in (("fp64", False), ("mixed", True)):
+            for _ in range(2):
+                b.evaluate(xs, fs, Ws, auxs=auxs, mixed=mixed)
+            torch.cuda.synchronize()
+            s, e = _events()
+            s.record()
+            for _ in range(5):
+                b.evaluate(xs, fs, Ws, auxs=auxs, mixed=mixed)
+            e.record()
+            torch.cuda.synchronize()
+            r[tag + "_one_launch_ms"] = s.elapsed_time(e) / 5
+        # the same work as one launch per mesh
+        s, e = _events()
+        s.record()
+        for i, w in enumerate(ws):
+            AssemblyEngine(w.lof).evaluate(xs[i], aux=auxs[i], f=fs[i], W=Ws[i], mixed=True)
+        e.record()
+        torch.cuda.synchronize()
+        r["mixed_per_mesh_launches_ms"] = s.elapsed_time(e)
+        out["mixed_batch_256"] = r
+    print(json.dumps(out), flush=True)
+    return out
+
+
+if __name__ == "__main__":
+    report()
