@@ -155,6 +155,11 @@ tx::EvalParams make_params(tx_handle h, const tx_eval_args& a) {
   P.physics = D.eq.physics;
   P.source_kind = D.eq.source_kind;
   for (int i = 0; i < 8; ++i) P.p[i] = D.eq.params[i];
+  if (D.eq.physics == TX_PHYS_ELASTICITY) {
+    const double E = D.eq.params[0], nu = D.eq.params[1];
+    P.lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    P.mu = E / (2.0 * (1.0 + nu));
+  }
   return P;
 }
 

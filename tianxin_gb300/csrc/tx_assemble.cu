@@ -65,17 +65,18 @@ struct Cfg {
   static constexpr int NVAL = HC ? 3 : 1;
   // shared: reference part
   static constexpr size_t R_GEO_GRAD = 0;
-  static constexpr size_t R_GEO_VAL = align16(R_GEO_GRAD + sizeof(double) * NQ * NV * 3);
+  static constexpr size_t R_GEO_VAL = align16(R_GEO_GRAD + sizeof(Real) * NQ * NV * 3);
   static constexpr size_t R_W = align16(R_GEO_VAL + sizeof(double) * NQ * NV);
   static constexpr size_t R_VAL = align16(R_W + sizeof(Real) * NQ);
   static constexpr size_t R_GRAD = align16(R_VAL + sizeof(Real) * NQ * NB * NVAL);
   static constexpr size_t R_END = align16(R_GRAD + sizeof(Real) * NQ * NB * 3);
   // shared: per element part
-  static constexpr size_t E_X = 0;
-  static constexpr size_t E_U = align16(E_X + sizeof(double) * NV * 3);
-  static constexpr size_t E_UD = align16(E_U + sizeof(double) * NF * NB);
-  static constexpr size_t E_AUX = align16(E_UD + sizeof(double) * NF * NB);
-  static constexpr size_t E_SG = align16(E_AUX + sizeof(double) * (HC ? NB : 0));
+  static constexpr size_t E_X = 0;                                      // vertex coordinates (FP64)
+  static constexpr size_t E_DX = align16(E_X + sizeof(double) * NV * 3);  // X[v] - X[0] (Real)
+  static constexpr size_t E_U = align16(E_DX + sizeof(Real) * NV * 3);
+  static constexpr size_t E_UD = align16(E_U + sizeof(Real) * NF * NB);
+  static constexpr size_t E_AUX = align16(E_UD + sizeof(Real) * NF * NB);
+  static constexpr size_t E_SG = align16(E_AUX + sizeof(Real) * (HC ? NB : 0));
   static constexpr size_t E_G = align16(E_SG + sizeof(Real) * (HC ? NB : 0));
   static constexpr size_t E_V = align16(E_G + sizeof(Real) * NQ * NB * 3);
   static constexpr size_t E_W = align16(E_V + sizeof(Real) * (HC ? NQ * NB * 3 : 0));
@@ -97,6 +98,23 @@ __device__ __forceinline__ void accumulate(double* p, double v) {
   if constexpr (ATOMIC) atomicAdd(p, v);  // red.global.add.f64
   else *p += v;
 }
+
+// Exact IEEE-754 binary32 -> binary64 widening with integer operations:
+// exponent rebiased by 1023 - 127 = 896, 23-bit fraction moved to the top of
+// the 52-bit fraction.  Keeps the mixed kernel's output conversions off the
+// FP64 pipe (a small fraction of the FP32 rate on this part); zeros,
+// subnormals, infinities and NaNs take the ordinary conversion.
+__device__ __forceinline__ double widen(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) {
+    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+    return (double)v;
+  }
+  const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+__device__ __forceinline__ double widen(double v) { return v; }
 
 template <typename Real>
 __device__ __forceinline__ Real source_at(int kind, double c, double s0, const double ip[3]) {
@@ -120,7 +138,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
   using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS, STAGE>;
   constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF, NE = C::NE;
   constexpr bool HC = C::HC;
-  double* r_geo_grad = reinterpret_cast<double*>(smem + C::R_GEO_GRAD);
+  Real* r_geo_grad = reinterpret_cast<Real*>(smem + C::R_GEO_GRAD);
   double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
   Real* r_w = reinterpret_cast<Real*>(smem + C::R_W);
   Real* r_val = reinterpret_cast<Real*>(smem + C::R_VAL);
@@ -133,7 +151,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
     ref += NQ;
     for (int i = threadIdx.x; i < NQ * NV; i += blockDim.x) r_geo_val[i] = ref[i];
     ref += NQ * NV;
-    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) r_geo_grad[i] = ref[i];
+    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) r_geo_grad[i] = (Real)ref[i];
     ref += NQ * NV * 3;
     for (int i = threadIdx.x; i < NQ * NB * C::NVAL; i += blockDim.x) r_val[i] = (Real)ref[i];
     ref += NQ * NB * C::NVAL;
@@ -144,9 +162,10 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
   const int t = threadIdx.x % TPE;
   unsigned char* eb = smem + C::R_END + (size_t)le * C::E_END;
   double* sX = reinterpret_cast<double*>(eb + C::E_X);
-  double* sU = reinterpret_cast<double*>(eb + C::E_U);
-  double* sUD = reinterpret_cast<double*>(eb + C::E_UD);
-  double* sAUX = reinterpret_cast<double*>(eb + C::E_AUX);
+  Real* sDX = reinterpret_cast<Real*>(eb + C::E_DX);
+  Real* sU = reinterpret_cast<Real*>(eb + C::E_U);
+  Real* sUD = reinterpret_cast<Real*>(eb + C::E_UD);
+  Real* sAUX = reinterpret_cast<Real*>(eb + C::E_AUX);
   Real* sSG = reinterpret_cast<Real*>(eb + C::E_SG);
   Real* sG = reinterpret_cast<Real*>(eb + C::E_G);    // [q][b][3] grad (HGRAD) or curl (HCURL)
   Real* sV = reinterpret_cast<Real*>(eb + C::E_V);    // [q][b][3] HCURL values
@@ -160,28 +179,38 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
   uint8_t* sEP = reinterpret_cast<uint8_t*>(eb + C::E_EP);  // epos[a][b]
   __syncthreads();
 
-  const double* pp = P.p;
+  // parameters in the element arithmetic's type, once per thread
+  Real pr[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) pr[i] = (Real)P.p[i];
+  const Real lam = (Real)P.lam, mu = (Real)P.mu;
+  const Real beta = (Real)P.beta, alpha = (Real)P.alpha;
   for (int64_t g0 = e_lo + grp0 * EPB; g0 < e_hi; g0 += grp_stride * EPB) {
     const int64_t ei = g0 + le;
     const bool valid = ei < e_hi;
     const int64_t e = (perm && valid) ? (int64_t)__ldg(perm + ei) : ei;
     // ---------------------------------------------------------- 1 gather
     if (valid) {
+      const int64_t n0 = __ldg(B.vconn + e * NV);
       for (int v = t; v < NV; v += TPE) {
-        const int32_t n = __ldg(B.vconn + e * NV + v);
-        sX[3 * v + 0] = __ldg(P.coords + 3 * (int64_t)n + 0);
-        sX[3 * v + 1] = __ldg(P.coords + 3 * (int64_t)n + 1);
-        sX[3 * v + 2] = __ldg(P.coords + 3 * (int64_t)n + 2);
+        const int64_t n = __ldg(B.vconn + e * NV + v);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const double xv = __ldg(P.coords + 3 * n + d);
+          sX[3 * v + d] = xv;
+          // differencing in FP64, once per vertex, keeps the mixed J accurate
+          sDX[3 * v + d] = (Real)(xv - __ldg(P.coords + 3 * n0 + d));
+        }
       }
       for (int b = t; b < NB; b += TPE) {
         const int64_t ent = __ldg(B.dconn + e * NB + b);
 #pragma unroll
         for (int c = 0; c < NF; ++c) {
-          sU[c * NB + b] = __ldg(P.x + NF * ent + c);
-          sUD[c * NB + b] = P.xdot ? __ldg(P.xdot + NF * ent + c) : 0.0;
+          sU[c * NB + b] = (Real)__ldg(P.x + NF * ent + c);
+          sUD[c * NB + b] = P.xdot ? (Real)__ldg(P.xdot + NF * ent + c) : Real(0);
         }
         if constexpr (HC) {
-          sAUX[b] = P.aux ? __ldg(P.aux + ent) : 0.0;
+          sAUX[b] = P.aux ? (Real)__ldg(P.aux + ent) : Real(0);
           sSG[b] = (Real)__ldg(B.esign + e * NB + b);
         }
         if constexpr (STAGE) {
@@ -203,14 +232,11 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         for (int k = 0; k < 9; ++k) J[k] = Real(0);
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-          // differencing in FP64 keeps the mixed path's J accurate
-          const Real dx = (Real)(sX[3 * v + 0] - sX[0]);
-          const Real dy = (Real)(sX[3 * v + 1] - sX[1]);
-          const Real dz = (Real)(sX[3 * v + 2] - sX[2]);
-          const double* gg = r_geo_grad + (q * NV + v) * 3;
+          const Real dx = sDX[3 * v + 0], dy = sDX[3 * v + 1], dz = sDX[3 * v + 2];
+          const Real* gg = r_geo_grad + (q * NV + v) * 3;
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
-            const Real g = (Real)gg[j];
+            const Real g = gg[j];
             J[0 + j] += dx * g;
             J[3 + j] += dy * g;
             J[6 + j] += dz * g;
@@ -260,31 +286,31 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           Real u = 0, ud = 0, g[3] = {0, 0, 0};
           for (int b = 0; b < NB; ++b) {
             const Real n = r_val[q * NB + b];
-            const Real ub = (Real)sU[b];
+            const Real ub = sU[b];
             u += n * ub;
-            ud += n * (Real)sUD[b];
+            ud += n * sUD[b];
             g[0] += sG[(q * NB + b) * 3 + 0] * ub;
             g[1] += sG[(q * NB + b) * 3 + 1] * ub;
             g[2] += sG[(q * NB + b) * 3 + 2] * ub;
           }
           if constexpr (PHYS == TX_PHYS_POISSON) {
-            const Real k = (Real)pp[0], c = (Real)pp[1], m = (Real)pp[2];
-            Real s = (Real)pp[3];
+            const Real k = pr[0], c = pr[1], m = pr[2];
+            Real s = pr[3];
             if (P.source_kind != TX_SOURCE_CONST) {
               double ip[3] = {0, 0, 0};
               for (int v = 0; v < NV; ++v) {
                 const double nv = r_geo_val[q * NV + v];
                 ip[0] += nv * sX[3 * v]; ip[1] += nv * sX[3 * v + 1]; ip[2] += nv * sX[3 * v + 2];
               }
-              s = source_at<Real>(P.source_kind, pp[1], pp[3], ip);
+              s = source_at<Real>(P.source_kind, P.p[1], P.p[3], ip);
             }
             qf[0] = k * g[0]; qf[1] = k * g[1]; qf[2] = k * g[2];
             qf[3] = c * u + m * ud - s;
           } else {
-            const Real k = (Real)pp[0] + (Real)pp[1] * u * u;
-            const Real dk = Real(2) * (Real)pp[1] * u;
+            const Real k = pr[0] + pr[1] * u * u;
+            const Real dk = Real(2) * pr[1] * u;
             qf[0] = k * g[0]; qf[1] = k * g[1]; qf[2] = k * g[2];
-            qf[3] = -(Real)pp[2];
+            qf[3] = -pr[2];
             qf[4] = dk * g[0]; qf[5] = dk * g[1]; qf[6] = dk * g[2];
             qf[7] = k;
           }
@@ -297,16 +323,13 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
             const Real n = r_val[q * NB + b];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              const Real ub = (Real)sU[c * NB + b];
+              const Real ub = sU[c * NB + b];
               Gu[3 * c + 0] += gb[0] * ub;
               Gu[3 * c + 1] += gb[1] * ub;
               Gu[3 * c + 2] += gb[2] * ub;
-              acc[c] += n * (Real)sUD[c * NB + b];
+              acc[c] += n * sUD[c * NB + b];
             }
           }
-          const double E = pp[0], nu = pp[1];
-          const Real lam = (Real)(E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
-          const Real mu = (Real)(E / (2.0 * (1.0 + nu)));
           const Real tr = Gu[0] + Gu[4] + Gu[8];
           qf[0] = mu * (Gu[0] + Gu[0]) + lam * tr;  // s00
           qf[1] = mu * (Gu[4] + Gu[4]) + lam * tr;  // s11
@@ -314,14 +337,14 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           qf[3] = mu * (Gu[1] + Gu[3]);             // s01
           qf[4] = mu * (Gu[2] + Gu[6]);             // s02
           qf[5] = mu * (Gu[5] + Gu[7]);             // s12
-          const Real rho = (Real)pp[5];
-          qf[6] = rho * acc[0] - (Real)pp[2];
-          qf[7] = rho * acc[1] - (Real)pp[3];
-          qf[8] = rho * acc[2] - (Real)pp[4];
+          const Real rho = pr[5];
+          qf[6] = rho * acc[0] - pr[2];
+          qf[7] = rho * acc[1] - pr[3];
+          qf[8] = rho * acc[2] - pr[4];
         } else {  // MAXWELL
           Real Ev[3] = {0, 0, 0}, cE[3] = {0, 0, 0}, Jv[3] = {0, 0, 0};
           for (int b = 0; b < NB; ++b) {
-            const Real ub = (Real)sU[b], jb = (Real)sAUX[b];
+            const Real ub = sU[b], jb = sAUX[b];
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
               Ev[i] += sV[(q * NB + b) * 3 + i] * ub;
@@ -329,7 +352,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               cE[i] += sG[(q * NB + b) * 3 + i] * ub;
             }
           }
-          const Real imu = (Real)pp[0], sig = (Real)pp[1];
+          const Real imu = pr[0], sig = pr[1];
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
             qf[i] = imu * cE[i];
@@ -368,7 +391,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           for (int c = 0; c < NF; ++c) sR[a * NF + c] = r[c];
         } else if (P.f) {
 #pragma unroll
-          for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.f + NF * la + c, (double)r[c]);
+          for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.f + NF * la + c, widen(r[c]));
         }
         if constexpr (JAC) {
           int64_t rp[NF];
@@ -380,14 +403,13 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           // Jacobian entry (row a,c; column b,d): reduce now, or stage for the CTA-wide scatter
           auto put = [&](int c, int b, int d, int64_t pb, Real v) {
             if constexpr (STAGE) sK[(a * NF + c) * NE + b * NF + d] = v;
-            else accumulate<ATOMIC>(P.vals + rp[c] + pb + d, (double)v);
+            else accumulate<ATOMIC>(P.vals + rp[c] + pb + d, widen(v));
           };
-          const Real beta = (Real)P.beta, alpha = (Real)P.alpha;
           for (int b = 0; b < NB; ++b) {
             const int64_t pb = STAGE ? 0 : (int64_t)NF * __ldg(ep + b);
             if constexpr (PHYS == TX_PHYS_POISSON) {
-              const Real ca = beta * (Real)pp[0];
-              const Real cm = beta * (Real)pp[1] + alpha * (Real)pp[2];
+              const Real ca = beta * pr[0];
+              const Real cm = beta * pr[1] + alpha * pr[2];
               Real kg = 0, km = 0;
               for (int q = 0; q < NQ; ++q) {
                 const Real* ga = sG + (q * NB + a) * 3;
@@ -421,11 +443,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 Pm[6] += wa2 * gb[0]; Pm[7] += wa2 * gb[1]; Pm[8] += wa2 * gb[2];
                 M += w * r_val[q * NB + a] * r_val[q * NB + b];
               }
-              const double E = pp[0], nu = pp[1];
-              const Real lam = (Real)(E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
-              const Real mu = (Real)(E / (2.0 * (1.0 + nu)));
               const Real trP = Pm[0] + Pm[4] + Pm[8];
-              const Real mass = alpha * (Real)pp[5] * M;
+              const Real mass = alpha * pr[5] * M;
 #pragma unroll
               for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -435,7 +454,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                   put(c, b, d, pb, k);
                 }
             } else {  // MAXWELL
-              const Real imu = (Real)pp[0], sig = (Real)pp[1];
+              const Real imu = pr[0], sig = pr[1];
               Real kc = 0, kv = 0;
               for (int q = 0; q < NQ; ++q) {
                 const Real* ca = sG + (q * NB + a) * 3;
@@ -463,7 +482,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           const unsigned char* e2 = base + (size_t)l2 * C::E_END;
           const int32_t la = reinterpret_cast<const int32_t*>(e2 + C::E_LA)[row / NF];
           accumulate<ATOMIC>(P.f + (int64_t)NF * la + row % NF,
-                             (double)reinterpret_cast<const Real*>(e2 + C::E_R)[row]);
+                             widen(reinterpret_cast<const Real*>(e2 + C::E_R)[row]));
         }
       }
       if constexpr (JAC) {
@@ -474,7 +493,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           const int64_t addr = reinterpret_cast<const int64_t*>(e2 + C::E_RP)[row] +
                                (int64_t)NF * reinterpret_cast<const uint8_t*>(e2 + C::E_EP)[(row / NF) * NB + col / NF] +
                                col % NF;
-          accumulate<ATOMIC>(P.vals + addr, (double)reinterpret_cast<const Real*>(e2 + C::E_K)[rem]);
+          accumulate<ATOMIC>(P.vals + addr, widen(reinterpret_cast<const Real*>(e2 + C::E_K)[rem]));
         }
       }
     }

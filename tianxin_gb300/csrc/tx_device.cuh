@@ -21,6 +21,7 @@ struct EvalParams {
   int64_t e0, e1;            // element range within the block
   int physics, source_kind;
   double p[8];
+  double lam, mu;            // Lame parameters from p[0] (E), p[1] (nu), computed in FP64 on the host
 };
 
 // Launch the fused gather -> geometry -> integrators -> scatter kernel for
