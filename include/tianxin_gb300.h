@@ -264,6 +264,22 @@ int tx_batch_eval(tx_batch b, const tx_eval_args* args);
 const char* tx_batch_last_error(tx_batch b);
 void tx_batch_destroy(tx_batch b);
 
+/* Volume fill that allocates no device memory.  It has no counterpart in the
+ * reference; it exists for callers that may not allocate: code running
+ * while a CUDA graph capture is open (cudaMalloc is not allowed then) and
+ * applications that pre-reserve all device memory in their own pool.
+ * Same result as tx_eval with TX_EVAL_PERSISTENT (every block, even
+ * worksets of the size set by tx_set_worksets' min_size; TX_EVAL_MIXED
+ * honoured, TX_EVAL_DETERMINISTIC refused, block must be -1).  Its scratch
+ * (work counter, parameter tables, workset list) is one static device array
+ * holding at most TX_NOALLOC_MAX_WORKSETS worksets (about 1.6 MB, kept by
+ * every GPU that loads the library until exit); larger work lists are
+ * rejected with TX_ERANGE.  The first call on a device looks the array up
+ * (make it before any stream capture).  All calls share the array: calls
+ * that overlap on the GPU race. */
+#define TX_NOALLOC_MAX_WORKSETS 65536
+int tx_eval_noalloc(tx_handle h, const tx_eval_args* args);
+
 /* Stream the handle's work is ordered on (cudaStream_t as void*); set NULL
  * to use the legacy default stream. */
 int tx_set_stream(tx_handle h, void* stream);

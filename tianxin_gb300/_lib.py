@@ -40,6 +40,7 @@ SIGNATURES = {
     "tx_batch_eval": (C.c_int, [P, P]),
     "tx_batch_last_error": (C.c_char_p, [P]),
     "tx_batch_destroy": (None, [P]),
+    "tx_eval_noalloc": (C.c_int, [P, C.POINTER(_abi.EvalArgs)]),
     "tx_set_stream": (C.c_int, [P, P]),
     "tx_synchronize": (C.c_int, [P]),
 }
