@@ -242,12 +242,16 @@ def run_ours(a):
         kern = [s.elapsed_time(e) / 1e3 for s, e in kev]
         return total, sum(kern) / len(kern)
 
+    # tile shapes: the project's autotuner times staged/direct scatter x CTA caps on this workload
+    from tianxin_gb300 import autotune
+    tuned = autotune.tune(me.ae, x, f, W, mixed=True, force=True)
     clocks = ClockSampler(local)
     clocks.start()
     t_mixed, k_mixed = timed_steps(True, a.steps, a.warmup)
     clk = clocks.stop()
     W_mixed = W.values.clone()
     K64 = max(3, min(a.steps, 8))
+    tuned64 = autotune.tune(me.ae, x, f, W, mixed=False, force=True, reps=1)
     t_fp64, k_fp64 = timed_steps(False, K64, 3)
     jac_diff = float((W.values - W_mixed).abs().max() / W.values.abs().max())
     del W_mixed
@@ -364,6 +368,10 @@ def run_ours(a):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": 2 * a.steps,
+            "autotune": {"mixed": {k: v for k, v in tuned.items() if k != "candidates"},
+                         "mixed_candidates_ms": [(c.get("scatter_direct"), c.get("grid_cap"), round(c["ms"], 3))
+                                                 for c in tuned.get("candidates", [])],
+                         "fp64": {k: v for k, v in tuned64.items() if k != "candidates"}},
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -89,7 +89,10 @@ struct Cfg {
   static constexpr size_t E_RP = align16(E_R + sizeof(Real) * (STAGE ? NE : 0));
   static constexpr size_t E_LA = align16(E_RP + sizeof(int64_t) * (STAGE ? NE : 0));
   static constexpr size_t E_EP = align16(E_LA + sizeof(int32_t) * (STAGE ? NB : 0));
-  static constexpr size_t E_END = align16(E_EP + (STAGE ? NB * NB : 0));
+  // per-element stride = 32 B past a multiple of 128 B: the four elements of a
+  // warp start 8 banks apart, so same-offset accesses do not conflict
+  static constexpr size_t E_RAW = align16(E_EP + (STAGE ? NB * NB : 0));
+  static constexpr size_t E_END = ((E_RAW + 127 - 32) / 128) * 128 + 32;
   static constexpr size_t SMEM = R_END + EPB * E_END;
 };
 
@@ -366,22 +369,44 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
     if (valid) {
       for (int a = t; a < NB; a += TPE) {
         const int64_t la = __ldg(B.dconn + e * NB + a);
+        // The thread's own weighted gradient W_q grad N_a(q) and W_q N_a(q):
+        // kept in registers for small rules, read from shared memory otherwise.
+        constexpr bool CACHE = NQ <= 8 && !HC;
+        Real wg[CACHE ? NQ : 1][3], wn[CACHE ? NQ : 1];
+        if constexpr (CACHE) {
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) {
+            const Real w = sW[q];
+            const Real* ga = sG + (q * NB + a) * 3;
+            wg[q][0] = w * ga[0]; wg[q][1] = w * ga[1]; wg[q][2] = w * ga[2];
+            wn[q] = w * r_val[q * NB + a];
+          }
+        }
+        auto WG = [&](int q, int i) -> Real {
+          if constexpr (CACHE) return wg[q][i];
+          else return sW[q] * sG[(q * NB + a) * 3 + i];
+        };
+        auto WN = [&](int q) -> Real {
+          if constexpr (CACHE) return wn[q];
+          else return sW[q] * r_val[q * NB + a];
+        };
         // residual row a (per field)
         Real r[NF];
 #pragma unroll
         for (int c = 0; c < NF; ++c) r[c] = 0;
+#pragma unroll(CACHE ? NQ : 1)
         for (int q = 0; q < NQ; ++q) {
-          const Real w = sW[q];
-          const Real* ga = sG + (q * NB + a) * 3;
           const Real* qf = sQF + q * NQF;
           if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
-            r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + r_val[q * NB + a] * qf[3]);
+            r[0] += WG(q, 0) * qf[0] + WG(q, 1) * qf[1] + WG(q, 2) * qf[2] + WN(q) * qf[3];
           } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
-            const Real n = r_val[q * NB + a];
-            r[0] += w * (ga[0] * qf[0] + ga[1] * qf[3] + ga[2] * qf[4] + n * qf[6]);
-            r[1] += w * (ga[0] * qf[3] + ga[1] * qf[1] + ga[2] * qf[5] + n * qf[7]);
-            r[2] += w * (ga[0] * qf[4] + ga[1] * qf[5] + ga[2] * qf[2] + n * qf[8]);
+            const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2), n = WN(q);
+            r[0] += g0 * qf[0] + g1 * qf[3] + g2 * qf[4] + n * qf[6];
+            r[1] += g0 * qf[3] + g1 * qf[1] + g2 * qf[5] + n * qf[7];
+            r[2] += g0 * qf[4] + g1 * qf[5] + g2 * qf[2] + n * qf[8];
           } else {
+            const Real w = sW[q];
+            const Real* ga = sG + (q * NB + a) * 3;
             const Real* va = sV + (q * NB + a) * 3;
             r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + va[0] * qf[3] + va[1] * qf[4] + va[2] * qf[5]);
           }
@@ -411,37 +436,37 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               const Real ca = beta * pr[0];
               const Real cm = beta * pr[1] + alpha * pr[2];
               Real kg = 0, km = 0;
+#pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
-                const Real* ga = sG + (q * NB + a) * 3;
                 const Real* gb = sG + (q * NB + b) * 3;
-                const Real w = sW[q];
-                kg += w * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
-                km += w * r_val[q * NB + a] * r_val[q * NB + b];
+                kg += WG(q, 0) * gb[0] + WG(q, 1) * gb[1] + WG(q, 2) * gb[2];
+                km += WN(q) * r_val[q * NB + b];
               }
               put(0, b, 0, pb, ca * kg + cm * km);
             } else if constexpr (PHYS == TX_PHYS_HEAT) {
               Real kab = 0;
+#pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
-                const Real* ga = sG + (q * NB + a) * 3;
                 const Real* gb = sG + (q * NB + b) * 3;
                 const Real* qf = sQF + q * NQF;
-                kab += sW[q] * (qf[7] * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]) +
-                                r_val[q * NB + b] * (ga[0] * qf[4] + ga[1] * qf[5] + ga[2] * qf[6]));
+                const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2);
+                kab += qf[7] * (g0 * gb[0] + g1 * gb[1] + g2 * gb[2]) +
+                       r_val[q * NB + b] * (g0 * qf[4] + g1 * qf[5] + g2 * qf[6]);
               }
               put(0, b, 0, pb, beta * kab);
             } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
               Real Pm[9], M = 0;
 #pragma unroll
               for (int k = 0; k < 9; ++k) Pm[k] = 0;
+#pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
-                const Real* ga = sG + (q * NB + a) * 3;
                 const Real* gb = sG + (q * NB + b) * 3;
-                const Real w = sW[q];
-                const Real wa0 = w * ga[0], wa1 = w * ga[1], wa2 = w * ga[2];
-                Pm[0] += wa0 * gb[0]; Pm[1] += wa0 * gb[1]; Pm[2] += wa0 * gb[2];
-                Pm[3] += wa1 * gb[0]; Pm[4] += wa1 * gb[1]; Pm[5] += wa1 * gb[2];
-                Pm[6] += wa2 * gb[0]; Pm[7] += wa2 * gb[1]; Pm[8] += wa2 * gb[2];
-                M += w * r_val[q * NB + a] * r_val[q * NB + b];
+                const Real b0 = gb[0], b1 = gb[1], b2 = gb[2];
+                const Real wa0 = WG(q, 0), wa1 = WG(q, 1), wa2 = WG(q, 2);
+                Pm[0] += wa0 * b0; Pm[1] += wa0 * b1; Pm[2] += wa0 * b2;
+                Pm[3] += wa1 * b0; Pm[4] += wa1 * b1; Pm[5] += wa1 * b2;
+                Pm[6] += wa2 * b0; Pm[7] += wa2 * b1; Pm[8] += wa2 * b2;
+                M += WN(q) * r_val[q * NB + b];
               }
               const Real trP = Pm[0] + Pm[4] + Pm[8];
               const Real mass = alpha * pr[5] * M;
