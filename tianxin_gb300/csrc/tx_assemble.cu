@@ -63,6 +63,12 @@ struct Cfg {
   static constexpr int EPB = THREADS / TPE;
   static constexpr int NQF = PHYS == TX_PHYS_ELASTICITY ? 9 : PHYS == TX_PHYS_HEAT ? 8 : PHYS == TX_PHYS_MAXWELL ? 6 : 4;
   static constexpr int NVAL = HC ? 3 : 1;
+  // odd word strides: threads that write one row/point each spread over all banks
+  // sG/sV: per point q and basis b one 4-vector (x, y, z, N) at q * GQS + b * 4;
+  // GQS / 4 odd: the quarter-warp of a 128-bit access covers all banks
+  static constexpr int GQS = NB * 4 + 4;
+  static constexpr int NE_ = (PHYS == TX_PHYS_ELASTICITY ? 3 : 1) * NB;
+  static constexpr int KRS = NE_ | 1;       // sK:    [row * KRS + col]
   // shared: reference part
   static constexpr size_t R_GEO_GRAD = 0;
   static constexpr size_t R_GEO_VAL = align16(R_GEO_GRAD + sizeof(Real) * NQ * NV * 3);
@@ -71,21 +77,26 @@ struct Cfg {
   static constexpr size_t R_GRAD = align16(R_VAL + sizeof(Real) * NQ * NB * NVAL);
   static constexpr size_t R_END = align16(R_GRAD + sizeof(Real) * NQ * NB * 3);
   // shared: per element part
+  static constexpr bool XABS = PHYS == TX_PHYS_POISSON;                // sources need absolute coordinates
   static constexpr size_t E_X = 0;                                      // vertex coordinates (FP64)
-  static constexpr size_t E_DX = align16(E_X + sizeof(double) * NV * 3);  // X[v] - X[0] (Real)
+  static constexpr size_t E_DX = align16(E_X + sizeof(double) * (XABS ? NV * 3 : 0));  // X[v] - X[0] (Real)
   static constexpr size_t E_U = align16(E_DX + sizeof(Real) * NV * 3);
   static constexpr size_t E_UD = align16(E_U + sizeof(Real) * NF * NB);
   static constexpr size_t E_AUX = align16(E_UD + sizeof(Real) * NF * NB);
   static constexpr size_t E_SG = align16(E_AUX + sizeof(Real) * (HC ? NB : 0));
   static constexpr size_t E_G = align16(E_SG + sizeof(Real) * (HC ? NB : 0));
-  static constexpr size_t E_V = align16(E_G + sizeof(Real) * NQ * NB * 3);
-  static constexpr size_t E_W = align16(E_V + sizeof(Real) * (HC ? NQ * NB * 3 : 0));
+  static constexpr size_t E_V = align16(E_G + sizeof(Real) * NQ * GQS);
+  static constexpr size_t E_W = align16(E_V + sizeof(Real) * (HC ? NQ * GQS : 0));
   static constexpr size_t E_QF = align16(E_W + sizeof(Real) * NQ);
   static constexpr size_t E_SIGN = align16(E_QF + sizeof(Real) * NQ * NQF);
   static constexpr bool STAGE = STAGE_;
   static constexpr int NE = NF * NB;  // element DOFs
-  static constexpr size_t E_K = align16(E_SIGN + sizeof(Real));
-  static constexpr size_t E_R = align16(E_K + sizeof(Real) * (STAGE ? NE * NE : 0));
+  // The staged Jacobian reuses the point tables (sG .. sSign): it is written
+  // from registers after every thread has finished reading them.
+  static constexpr size_t E_WORK_END = align16(E_SIGN + sizeof(Real));
+  static constexpr size_t E_K = E_G;
+  static constexpr size_t E_K_END = align16(E_K + sizeof(Real) * (STAGE ? NE * KRS : 0));
+  static constexpr size_t E_R = E_K_END > E_WORK_END ? E_K_END : E_WORK_END;
   static constexpr size_t E_RP = align16(E_R + sizeof(Real) * (STAGE ? NE : 0));
   static constexpr size_t E_LA = align16(E_RP + sizeof(int64_t) * (STAGE ? NE : 0));
   static constexpr size_t E_EP = align16(E_LA + sizeof(int32_t) * (STAGE ? NB : 0));
@@ -95,6 +106,26 @@ struct Cfg {
   static constexpr size_t E_END = ((E_RAW + 127 - 32) / 128) * 128 + 32;
   static constexpr size_t SMEM = R_END + EPB * E_END;
 };
+
+template <typename R>
+struct R4 {
+  R x, y, z, w;
+};
+__device__ __forceinline__ R4<float> ld4(const float* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ R4<double> ld4(const double* p) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  return {a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void st4(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void st4(double* p, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+  reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
 
 template <bool ATOMIC>
 __device__ __forceinline__ void accumulate(double* p, double v) {
@@ -140,6 +171,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                                               unsigned char* smem) {
   using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS, STAGE>;
   constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF, NE = C::NE;
+  constexpr int GQS = C::GQS, KRS = C::KRS;
   constexpr bool HC = C::HC;
   Real* r_geo_grad = reinterpret_cast<Real*>(smem + C::R_GEO_GRAD);
   double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
@@ -200,7 +232,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const double xv = __ldg(P.coords + 3 * n + d);
-          sX[3 * v + d] = xv;
+          if constexpr (C::XABS) sX[3 * v + d] = xv;
           // differencing in FP64, once per vertex, keeps the mixed J accurate
           sDX[3 * v + d] = (Real)(xv - __ldg(P.coords + 3 * n0 + d));
         }
@@ -262,19 +294,17 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           const Real g0 = gr[0], g1 = gr[1], g2 = gr[2];
           if constexpr (!HC) {
             // grad_i = sum_j Jinv(j,i) grad^_j
-            sG[(q * NB + b) * 3 + 0] = Ji[0] * g0 + Ji[3] * g1 + Ji[6] * g2;
-            sG[(q * NB + b) * 3 + 1] = Ji[1] * g0 + Ji[4] * g1 + Ji[7] * g2;
-            sG[(q * NB + b) * 3 + 2] = Ji[2] * g0 + Ji[5] * g1 + Ji[8] * g2;
+            st4(sG + q * GQS + b * 4, Ji[0] * g0 + Ji[3] * g1 + Ji[6] * g2, Ji[1] * g0 + Ji[4] * g1 + Ji[7] * g2,
+                Ji[2] * g0 + Ji[5] * g1 + Ji[8] * g2, r_val[q * NB + b]);
           } else {
             const Real s = sSG[b];
             const Real* vr = r_val + (q * NB + b) * 3;
-            sV[(q * NB + b) * 3 + 0] = s * (Ji[0] * vr[0] + Ji[3] * vr[1] + Ji[6] * vr[2]);
-            sV[(q * NB + b) * 3 + 1] = s * (Ji[1] * vr[0] + Ji[4] * vr[1] + Ji[7] * vr[2]);
-            sV[(q * NB + b) * 3 + 2] = s * (Ji[2] * vr[0] + Ji[5] * vr[1] + Ji[8] * vr[2]);
+            st4(sV + q * GQS + b * 4, s * (Ji[0] * vr[0] + Ji[3] * vr[1] + Ji[6] * vr[2]),
+                s * (Ji[1] * vr[0] + Ji[4] * vr[1] + Ji[7] * vr[2]), s * (Ji[2] * vr[0] + Ji[5] * vr[1] + Ji[8] * vr[2]),
+                Real(0));
             const Real sd = s * id;  // curl = J curl^ / det
-            sG[(q * NB + b) * 3 + 0] = sd * (J[0] * g0 + J[1] * g1 + J[2] * g2);
-            sG[(q * NB + b) * 3 + 1] = sd * (J[3] * g0 + J[4] * g1 + J[5] * g2);
-            sG[(q * NB + b) * 3 + 2] = sd * (J[6] * g0 + J[7] * g1 + J[8] * g2);
+            st4(sG + q * GQS + b * 4, sd * (J[0] * g0 + J[1] * g1 + J[2] * g2), sd * (J[3] * g0 + J[4] * g1 + J[5] * g2),
+                sd * (J[6] * g0 + J[7] * g1 + J[8] * g2), Real(0));
           }
         }
       }
@@ -288,13 +318,13 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
           Real u = 0, ud = 0, g[3] = {0, 0, 0};
           for (int b = 0; b < NB; ++b) {
-            const Real n = r_val[q * NB + b];
+            const R4<Real> gq = ld4(sG + q * GQS + b * 4);
             const Real ub = sU[b];
-            u += n * ub;
-            ud += n * sUD[b];
-            g[0] += sG[(q * NB + b) * 3 + 0] * ub;
-            g[1] += sG[(q * NB + b) * 3 + 1] * ub;
-            g[2] += sG[(q * NB + b) * 3 + 2] * ub;
+            u += gq.w * ub;
+            ud += gq.w * sUD[b];
+            g[0] += gq.x * ub;
+            g[1] += gq.y * ub;
+            g[2] += gq.z * ub;
           }
           if constexpr (PHYS == TX_PHYS_POISSON) {
             const Real k = pr[0], c = pr[1], m = pr[2];
@@ -322,15 +352,14 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 #pragma unroll
           for (int k = 0; k < 9; ++k) Gu[k] = 0;
           for (int b = 0; b < NB; ++b) {
-            const Real* gb = sG + (q * NB + b) * 3;
-            const Real n = r_val[q * NB + b];
+            const R4<Real> gb = ld4(sG + q * GQS + b * 4);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const Real ub = sU[c * NB + b];
-              Gu[3 * c + 0] += gb[0] * ub;
-              Gu[3 * c + 1] += gb[1] * ub;
-              Gu[3 * c + 2] += gb[2] * ub;
-              acc[c] += n * sUD[c * NB + b];
+              Gu[3 * c + 0] += gb.x * ub;
+              Gu[3 * c + 1] += gb.y * ub;
+              Gu[3 * c + 2] += gb.z * ub;
+              acc[c] += gb.w * sUD[c * NB + b];
             }
           }
           const Real tr = Gu[0] + Gu[4] + Gu[8];
@@ -348,11 +377,13 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           Real Ev[3] = {0, 0, 0}, cE[3] = {0, 0, 0}, Jv[3] = {0, 0, 0};
           for (int b = 0; b < NB; ++b) {
             const Real ub = sU[b], jb = sAUX[b];
+            const Real* vb = sV + q * GQS + b * 4;
+            const Real* cb = sG + q * GQS + b * 4;
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-              Ev[i] += sV[(q * NB + b) * 3 + i] * ub;
-              Jv[i] += sV[(q * NB + b) * 3 + i] * jb;
-              cE[i] += sG[(q * NB + b) * 3 + i] * ub;
+              Ev[i] += vb[i] * ub;
+              Jv[i] += vb[i] * jb;
+              cE[i] += cb[i] * ub;
             }
           }
           const Real imu = pr[0], sig = pr[1];
@@ -366,6 +397,10 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
     }
     __syncthreads();
     // ---------------------------------------------------------- 4 rows + scatter
+    // staged form: this thread's Jacobian block-row waits in registers until
+    // every thread of the CTA has finished reading the point tables it reuses
+    Real kreg[STAGE && JAC ? NF * NE : 1];
+    const int my_a = (valid && t < NB) ? t : -1;
     if (valid) {
       for (int a = t; a < NB; a += TPE) {
         const int64_t la = __ldg(B.dconn + e * NB + a);
@@ -377,18 +412,18 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 #pragma unroll
           for (int q = 0; q < NQ; ++q) {
             const Real w = sW[q];
-            const Real* ga = sG + (q * NB + a) * 3;
-            wg[q][0] = w * ga[0]; wg[q][1] = w * ga[1]; wg[q][2] = w * ga[2];
-            wn[q] = w * r_val[q * NB + a];
+            const R4<Real> ga = ld4(sG + q * GQS + a * 4);
+            wg[q][0] = w * ga.x; wg[q][1] = w * ga.y; wg[q][2] = w * ga.z;
+            wn[q] = w * ga.w;
           }
         }
         auto WG = [&](int q, int i) -> Real {
           if constexpr (CACHE) return wg[q][i];
-          else return sW[q] * sG[(q * NB + a) * 3 + i];
+          else return sW[q] * sG[q * GQS + a * 4 + i];
         };
         auto WN = [&](int q) -> Real {
           if constexpr (CACHE) return wn[q];
-          else return sW[q] * r_val[q * NB + a];
+          else return sW[q] * sG[q * GQS + a * 4 + 3];
         };
         // residual row a (per field)
         Real r[NF];
@@ -406,8 +441,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
             r[2] += g0 * qf[4] + g1 * qf[5] + g2 * qf[2] + n * qf[8];
           } else {
             const Real w = sW[q];
-            const Real* ga = sG + (q * NB + a) * 3;
-            const Real* va = sV + (q * NB + a) * 3;
+            const Real* ga = sG + q * GQS + a * 4;
+            const Real* va = sV + q * GQS + a * 4;
             r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + va[0] * qf[3] + va[1] * qf[4] + va[2] * qf[5]);
           }
         }
@@ -427,9 +462,10 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           }
           // Jacobian entry (row a,c; column b,d): reduce now, or stage for the CTA-wide scatter
           auto put = [&](int c, int b, int d, int64_t pb, Real v) {
-            if constexpr (STAGE) sK[(a * NF + c) * NE + b * NF + d] = v;
+            if constexpr (STAGE) kreg[c * NE + b * NF + d] = v;
             else accumulate<ATOMIC>(P.vals + rp[c] + pb + d, widen(v));
           };
+#pragma unroll(STAGE ? NB : 1)
           for (int b = 0; b < NB; ++b) {
             const int64_t pb = STAGE ? 0 : (int64_t)NF * __ldg(ep + b);
             if constexpr (PHYS == TX_PHYS_POISSON) {
@@ -438,20 +474,19 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               Real kg = 0, km = 0;
 #pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
-                const Real* gb = sG + (q * NB + b) * 3;
-                kg += WG(q, 0) * gb[0] + WG(q, 1) * gb[1] + WG(q, 2) * gb[2];
-                km += WN(q) * r_val[q * NB + b];
+                const R4<Real> gb = ld4(sG + q * GQS + b * 4);
+                kg += WG(q, 0) * gb.x + WG(q, 1) * gb.y + WG(q, 2) * gb.z;
+                km += WN(q) * gb.w;
               }
               put(0, b, 0, pb, ca * kg + cm * km);
             } else if constexpr (PHYS == TX_PHYS_HEAT) {
               Real kab = 0;
 #pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
-                const Real* gb = sG + (q * NB + b) * 3;
+                const R4<Real> gb = ld4(sG + q * GQS + b * 4);
                 const Real* qf = sQF + q * NQF;
                 const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2);
-                kab += qf[7] * (g0 * gb[0] + g1 * gb[1] + g2 * gb[2]) +
-                       r_val[q * NB + b] * (g0 * qf[4] + g1 * qf[5] + g2 * qf[6]);
+                kab += qf[7] * (g0 * gb.x + g1 * gb.y + g2 * gb.z) + gb.w * (g0 * qf[4] + g1 * qf[5] + g2 * qf[6]);
               }
               put(0, b, 0, pb, beta * kab);
             } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
@@ -460,13 +495,13 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               for (int k = 0; k < 9; ++k) Pm[k] = 0;
 #pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
-                const Real* gb = sG + (q * NB + b) * 3;
-                const Real b0 = gb[0], b1 = gb[1], b2 = gb[2];
+                const R4<Real> gb = ld4(sG + q * GQS + b * 4);
+                const Real b0 = gb.x, b1 = gb.y, b2 = gb.z;
                 const Real wa0 = WG(q, 0), wa1 = WG(q, 1), wa2 = WG(q, 2);
                 Pm[0] += wa0 * b0; Pm[1] += wa0 * b1; Pm[2] += wa0 * b2;
                 Pm[3] += wa1 * b0; Pm[4] += wa1 * b1; Pm[5] += wa1 * b2;
                 Pm[6] += wa2 * b0; Pm[7] += wa2 * b1; Pm[8] += wa2 * b2;
-                M += WN(q) * r_val[q * NB + b];
+                M += WN(q) * gb.w;
               }
               const Real trP = Pm[0] + Pm[4] + Pm[8];
               const Real mass = alpha * pr[5] * M;
@@ -482,10 +517,10 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               const Real imu = pr[0], sig = pr[1];
               Real kc = 0, kv = 0;
               for (int q = 0; q < NQ; ++q) {
-                const Real* ca = sG + (q * NB + a) * 3;
-                const Real* cb = sG + (q * NB + b) * 3;
-                const Real* va = sV + (q * NB + a) * 3;
-                const Real* vb = sV + (q * NB + b) * 3;
+                const Real* ca = sG + q * GQS + a * 4;
+                const Real* cb = sG + q * GQS + b * 4;
+                const Real* va = sV + q * GQS + a * 4;
+                const Real* vb = sV + q * GQS + b * 4;
                 kc += sW[q] * (ca[0] * cb[0] + ca[1] * cb[1] + ca[2] * cb[2]);
                 kv += sW[q] * (va[0] * vb[0] + va[1] * vb[1] + va[2] * vb[2]);
               }
@@ -497,6 +532,15 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
     }
     if constexpr (STAGE) {
       // ------------------------------------------------------ 5 CTA-wide scatter
+      if constexpr (JAC) {
+        __syncthreads();  // point tables are dead from here: the staged rows overwrite them
+        if (my_a >= 0) {
+#pragma unroll
+          for (int c = 0; c < NF; ++c)
+#pragma unroll
+            for (int k = 0; k < NE; ++k) sK[(my_a * NF + c) * KRS + k] = kreg[c * NE + k];
+        }
+      }
       // consecutive threads take consecutive entries of an element row
       __syncthreads();
       const int nval = (int)(e_hi - g0 < EPB ? e_hi - g0 : EPB);
@@ -518,7 +562,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           const int64_t addr = reinterpret_cast<const int64_t*>(e2 + C::E_RP)[row] +
                                (int64_t)NF * reinterpret_cast<const uint8_t*>(e2 + C::E_EP)[(row / NF) * NB + col / NF] +
                                col % NF;
-          accumulate<ATOMIC>(P.vals + addr, widen(reinterpret_cast<const Real*>(e2 + C::E_K)[rem]));
+          accumulate<ATOMIC>(P.vals + addr, widen(reinterpret_cast<const Real*>(e2 + C::E_K)[row * C::KRS + col]));
         }
       }
     }
