@@ -150,6 +150,27 @@ __device__ __forceinline__ double widen(float v) {
 }
 __device__ __forceinline__ double widen(double v) { return v; }
 
+// Exact IEEE-754 binary64 -> binary32 rounding to nearest, ties to even, with
+// integer operations: the 29 dropped fraction bits decide the round-up, whose
+// carry runs into the exponent.  Zero is exact; results that would be
+// subnormal, overflow, infinities and NaNs take the ordinary conversion.
+__device__ __forceinline__ float narrow(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const uint32_t hi = (uint32_t)(b >> 32);
+  if ((b << 1) == 0ull) return __uint_as_float(hi & 0x80000000u);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // rebias 1023 -> 127
+  if (e <= 0 || e >= 255) return (float)v;
+  uint32_t m = (uint32_t)((b & 0xFFFFFFFFFFFFFull) >> 29);
+  const uint32_t rest = (uint32_t)(b & 0x1FFFFFFFull);
+  m += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  return __uint_as_float((hi & 0x80000000u) | (((uint32_t)e << 23) + m));
+}
+template <typename Real>
+__device__ __forceinline__ Real to_real(double v) {
+  if constexpr (sizeof(Real) == 4) return narrow(v);
+  else return v;
+}
+
 template <typename Real>
 __device__ __forceinline__ Real source_at(int kind, double c, double s0, const double ip[3]) {
   if (kind == TX_SOURCE_SINE) {
@@ -234,18 +255,18 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           const double xv = __ldg(P.coords + 3 * n + d);
           if constexpr (C::XABS) sX[3 * v + d] = xv;
           // differencing in FP64, once per vertex, keeps the mixed J accurate
-          sDX[3 * v + d] = (Real)(xv - __ldg(P.coords + 3 * n0 + d));
+          sDX[3 * v + d] = to_real<Real>(xv - __ldg(P.coords + 3 * n0 + d));
         }
       }
       for (int b = t; b < NB; b += TPE) {
         const int64_t ent = __ldg(B.dconn + e * NB + b);
 #pragma unroll
         for (int c = 0; c < NF; ++c) {
-          sU[c * NB + b] = (Real)__ldg(P.x + NF * ent + c);
-          sUD[c * NB + b] = P.xdot ? (Real)__ldg(P.xdot + NF * ent + c) : Real(0);
+          sU[c * NB + b] = to_real<Real>(__ldg(P.x + NF * ent + c));
+          sUD[c * NB + b] = P.xdot ? to_real<Real>(__ldg(P.xdot + NF * ent + c)) : Real(0);
         }
         if constexpr (HC) {
-          sAUX[b] = P.aux ? (Real)__ldg(P.aux + ent) : Real(0);
+          sAUX[b] = P.aux ? to_real<Real>(__ldg(P.aux + ent)) : Real(0);
           sSG[b] = (Real)__ldg(B.esign + e * NB + b);
         }
         if constexpr (STAGE) {
@@ -555,14 +576,24 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         }
       }
       if constexpr (JAC) {
-        for (int i = threadIdx.x; i < nval * NE * NE; i += blockDim.x) {
-          const int l2 = i / (NE * NE), rem = i - l2 * (NE * NE);
-          const int row = rem / NE, col = rem - row * NE;
-          const unsigned char* e2 = base + (size_t)l2 * C::E_END;
-          const int64_t addr = reinterpret_cast<const int64_t*>(e2 + C::E_RP)[row] +
-                               (int64_t)NF * reinterpret_cast<const uint8_t*>(e2 + C::E_EP)[(row / NF) * NB + col / NF] +
-                               col % NF;
-          accumulate<ATOMIC>(P.vals + addr, widen(reinterpret_cast<const Real*>(e2 + C::E_K)[row * C::KRS + col]));
+        // a warp walks whole elements; its lanes sit on the columns of RPW rows
+        constexpr int RL = NE <= 4 ? 4 : NE <= 8 ? 8 : NE <= 16 ? 16 : 32;  // lanes per row
+        constexpr int RPW = 32 / RL;                                          // rows per pass
+        const int lane = threadIdx.x & 31;
+        const int col = lane % RL, sub = lane / RL;
+        const int cb = col / NF, cd = col - (col / NF) * NF;  // column's basis and field
+        if (col < NE) {
+          for (int l2 = threadIdx.x >> 5; l2 < nval; l2 += blockDim.x >> 5) {
+            const unsigned char* e2 = base + (size_t)l2 * C::E_END;
+            const int64_t* rps = reinterpret_cast<const int64_t*>(e2 + C::E_RP);
+            const uint8_t* eps = reinterpret_cast<const uint8_t*>(e2 + C::E_EP) + cb;
+            const Real* kk = reinterpret_cast<const Real*>(e2 + C::E_K) + col;
+#pragma unroll 4
+            for (int row = sub; row < NE; row += RPW) {
+              const int64_t addr = rps[row] + (int64_t)NF * eps[(row / NF) * NB] + cd;
+              accumulate<ATOMIC>(P.vals + addr, widen(kk[row * KRS]));
+            }
+          }
         }
       }
     }
