@@ -136,16 +136,15 @@ __device__ __forceinline__ void accumulate(double* p, double v) {
 // Exact IEEE-754 binary32 -> binary64 widening with integer operations:
 // exponent rebiased by 1023 - 127 = 896, 23-bit fraction moved to the top of
 // the 52-bit fraction.  Keeps the mixed kernel's output conversions off the
-// FP64 pipe (a small fraction of the FP32 rate on this part); zeros,
-// subnormals, infinities and NaNs take the ordinary conversion.
+// FP64 pipe (a small fraction of the FP32 rate on this part).  One unsigned
+// compare of |v| - 2^-126 against the normal range sends zeros, subnormals,
+// infinities and NaNs to the ordinary conversion; for the rest, |v| >> 3
+// puts exponent and fraction in place and adding 896 << 20 rebiases.
 __device__ __forceinline__ double widen(float v) {
   const uint32_t b = __float_as_uint(v);
-  const uint32_t e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) {
-    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
-    return (double)v;
-  }
-  const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+  const uint32_t a = b & 0x7fffffffu;
+  if (a - 0x00800000u >= 0x7f000000u) return (double)v;
+  const uint32_t hi = (b & 0x80000000u) | ((a >> 3) + 0x38000000u);
   return __hiloint2double((int)hi, (int)(b << 29));
 }
 __device__ __forceinline__ double widen(double v) { return v; }
@@ -582,16 +581,21 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         const int lane = threadIdx.x & 31;
         const int col = lane % RL, sub = lane / RL;
         const int cb = col / NF, cd = col - (col / NF) * NF;  // column's basis and field
+        constexpr int NR = (NE + RPW - 1) / RPW;  // passes over an element's rows
         if (col < NE) {
+          double* vals = P.vals + cd;
           for (int l2 = threadIdx.x >> 5; l2 < nval; l2 += blockDim.x >> 5) {
             const unsigned char* e2 = base + (size_t)l2 * C::E_END;
-            const int64_t* rps = reinterpret_cast<const int64_t*>(e2 + C::E_RP);
+            const int64_t* rps = reinterpret_cast<const int64_t*>(e2 + C::E_RP) + sub;
             const uint8_t* eps = reinterpret_cast<const uint8_t*>(e2 + C::E_EP) + cb;
-            const Real* kk = reinterpret_cast<const Real*>(e2 + C::E_K) + col;
-#pragma unroll 4
-            for (int row = sub; row < NE; row += RPW) {
-              const int64_t addr = rps[row] + (int64_t)NF * eps[(row / NF) * NB] + cd;
-              accumulate<ATOMIC>(P.vals + addr, widen(kk[row * KRS]));
+            const Real* kk = reinterpret_cast<const Real*>(e2 + C::E_K) + sub * KRS + col;
+#pragma unroll
+            for (int k = 0; k < NR; ++k) {
+              const int row = sub + k * RPW;
+              if (NE % RPW == 0 || row < NE) {
+                const int64_t addr = rps[k * RPW] + (int64_t)NF * eps[(row / NF) * NB];
+                accumulate<ATOMIC>(vals + addr, widen(kk[k * RPW * KRS]));
+              }
             }
           }
         }
@@ -607,8 +611,15 @@ constexpr int block_threads() {
   return STAGE ? 128 : Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS;
 }
 
+// Staged FP32 kernels ask for four resident CTAs (at most 128 registers a
+// thread): the register-staged Jacobian rows otherwise cap residency at three.
+template <typename Real, bool STAGE>
+constexpr int min_blocks() {
+  return STAGE && sizeof(Real) == 4 ? 4 : 1;
+}
+
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE>
-__global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>())
+__global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>(), min_blocks<Real, STAGE>())
 k_assemble(const BlockView B, const EvalParams P, const int32_t* perm, int64_t e_lo, int64_t e_hi) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();

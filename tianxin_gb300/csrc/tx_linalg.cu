@@ -82,10 +82,34 @@ __global__ void k_dirichlet(int64_t n, const int32_t* __restrict__ lids, const d
   }
 }
 
+// One lane's share of a CSR row product: entries b+sub, b+sub+LANES, ...
+// U entries per pass are loaded together (values and column indices
+// streamed past L1/L2, x through the read-only path) before any x gather
+// issues, so a lane keeps 2U independent loads in flight.  Entries past the
+// row end read column 0 with value 0.
+template <typename T, int LANES, int U>
+__device__ __forceinline__ T row_dot(int64_t b, int64_t e, int sub, const int32_t* __restrict__ col,
+                                     const T* __restrict__ vals, const T* __restrict__ x) {
+  T s = T(0);
+  for (int64_t k = b + sub; k < e; k += LANES * U) {
+    T v[U];
+    int32_t c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t kk = k + u * LANES;
+      v[u] = kk < e ? __ldcs(vals + kk) : T(0);
+      c[u] = kk < e ? __ldcs(col + kk) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) s += v[u] * __ldg(x + c[u]);
+  }
+  return s;
+}
+
 // Vector CSR: LANES threads per row, strided over the row, shuffle reduction.
 // The row loop advances per warp (its trip count is warp-uniform) so every
 // lane reaches the full-mask shuffles; rows past n are predicated off.
-template <typename T, int LANES>
+template <typename T, int LANES, int U>
 __global__ void __launch_bounds__(kThreads) k_spmv(int64_t n, const int64_t* __restrict__ rp,
                                                    const int32_t* __restrict__ col, const T* __restrict__ vals,
                                                    const T* __restrict__ x, T* __restrict__ y, T alpha, T beta) {
@@ -98,8 +122,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv(int64_t n, const int64_t* __r
     const int64_t r = base + g;
     T s = T(0);
     if (r < n) {
-      const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
-      for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(x + __ldcs(col + k));
+      s = row_dot<T, LANES, U>(__ldg(rp + r), __ldg(rp + r + 1), sub, col, vals, x);
     }
 #pragma unroll
     for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LANES);
@@ -112,10 +135,12 @@ cudaError_t spmv_dispatch(int64_t n, const int64_t* rp, const int32_t* col, cons
                           T b, int64_t nnz_hint, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const double avg = nnz_hint > 0 ? (double)nnz_hint / (double)n : 32.0;
-  if (avg <= 12) k_spmv<T, 4><<<grid_for(n, kThreads / 4, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  else if (avg <= 40) k_spmv<T, 8><<<grid_for(n, kThreads / 8, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  else if (avg <= 96) k_spmv<T, 16><<<grid_for(n, kThreads / 16, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  else k_spmv<T, 32><<<grid_for(n, kThreads / 32, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  // lanes per row and entries per lane per pass: a row of up to LANES*U entries is one pass
+  if (avg <= 16) k_spmv<T, 4, 4><<<grid_for(n, kThreads / 4, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  else if (avg <= 32) k_spmv<T, 8, 4><<<grid_for(n, kThreads / 8, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  else if (avg <= 64) k_spmv<T, 16, 4><<<grid_for(n, kThreads / 16, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  else if (avg <= 96) k_spmv<T, 32, 3><<<grid_for(n, kThreads / 32, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+  else k_spmv<T, 32, 4><<<grid_for(n, kThreads / 32, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
   return cudaGetLastError();
 }
 
@@ -215,7 +240,7 @@ __global__ void k_cg_init(int64_t n, const double* __restrict__ r64, const uint8
 }
 
 // q = A p and partial dot(p, q)
-template <int LANES>
+template <int LANES, int U>
 __global__ void __launch_bounds__(kThreads) k_spmv_dot(int64_t n, const int64_t* __restrict__ rp,
                                                        const int32_t* __restrict__ col, const float* __restrict__ vals,
                                                        const float* __restrict__ p, float* __restrict__ q,
@@ -231,8 +256,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(int64_t n, const int64_t*
     const int64_t r = base + g;
     float s = 0.0f;
     if (r < n) {
-      const int64_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
-      for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(p + __ldcs(col + k));
+      s = row_dot<float, LANES, U>(__ldg(rp + r), __ldg(rp + r + 1), sub, col, vals, p);
     }
 #pragma unroll
     for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LANES);
@@ -410,10 +434,11 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
   }
   const double avg = (double)w.nnz / (double)(n > 0 ? n : 1);
   auto spmv_dot = [&]() {
-    if (avg <= 12) k_spmv_dot<4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-    else if (avg <= 40) k_spmv_dot<8><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-    else if (avg <= 96) k_spmv_dot<16><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-    else k_spmv_dot<32><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    if (avg <= 16) k_spmv_dot<4, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    else if (avg <= 32) k_spmv_dot<8, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    else if (avg <= 64) k_spmv_dot<16, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    else if (avg <= 96) k_spmv_dot<32, 3><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
+    else k_spmv_dot<32, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
   };
   auto cg_iteration = [&]() {
     spmv_dot();
