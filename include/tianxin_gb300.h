@@ -15,6 +15,9 @@
  *                            disc-fe/src/Panzer_AssemblyEngine_impl.hpp:65-182)
  *   Dirichlet rows          TianXin::DirichletEvalautor<Jacobian>::evaluateFields
  *                           (disc-fe/src/evaluators/TianXin_Dirichlet_impl.hpp:55-81)
+ *   Neumann flux            AssemblyEngine::evaluateNeumannCondition -> TianXin::Flux
+ *                           (disc-fe/src/Panzer_AssemblyEngine_impl.hpp:324-364,
+ *                            disc-fe/src/evaluators/TianXin_Neumann_impl.hpp:146-166)
  *   SpMV                    Tpetra::CrsMatrix::apply as called by Belos
  *                           (adapters-stk/example/PoissonExample/main.cpp:402-419)
  *
@@ -195,6 +198,50 @@ int tx_eval(tx_handle h, const tx_eval_args* args);
 int tx_dirichlet_apply(tx_handle h, int64_t n, const int32_t* lids, const double* g,
                        const double* x, double* f, double* crs_vals);
 
+/* ------------------------------------------------------------ Neumann flux
+ * A "Neumann Conditions" entry of Type "Flux" (FieldManagerBuilder::
+ * setupNeumannFieldManagers, disc-fe/src/Panzer_FieldManagerBuilder.cpp:
+ * 417-535): on the side workset of one element block (the block's elements
+ * with a local side on the side set, panzer_stk::buildBCWorkset,
+ * adapters-stk/src/Panzer_STK_SetupUtilities.cpp:306-392), the residual of
+ * DOF field `field` gains
+ *     R_b += val(t) * sum_q N_b(xi_q) * w_q * |J t_u x J t_v|
+ * (TianXin::Flux::evaluateFields, TianXin_Neumann_impl.hpp:146-166; side
+ * cubature of the block's integration order mapped to the element's
+ * reference side, face measure = norm of the mapped tangents' cross
+ * product).  The flux does not depend on the solution, so a Jacobian
+ * evaluation leaves the matrix unchanged and sums the same values into f.
+ * Side sets are box sides (bits as tx_dirichlet_dofs).  Each side takes its
+ * own local side ordinal; the reference's single side workset uses the
+ * first cell's ordinal for all cells (Panzer_STK_SetupUtilities.cpp:383),
+ * which agrees whenever a side set's cells share one ordinal (every hex
+ * block here). */
+enum tx_value_type {       /* WorksetFunctor "Value Type"
+                              (disc-fe/src/evaluators/TianXin_WorksetFunctor_impl.hpp) */
+  TX_VALUE_CONSTANT = 1,   /* val = value                                              */
+  TX_VALUE_LINEAR = 2,     /* ramp to value; the elapse time is read from the same
+                              "Value" entry as the value, as the reference does (:67-82) */
+  TX_VALUE_TIME_TABLE = 3  /* piecewise linear in (table_t, table_v); t past the last
+                              time is an error (:88-121)                                 */
+};
+typedef struct tx_neumann_desc {
+  int32_t block;           /* "Element Block Name" (block index)                        */
+  uint32_t side_mask;      /* "SideSet Name": box sides, bit 0 x=0 ... bit 5 z=lz       */
+  int32_t field;           /* "DOF Name" (field number); HGRAD blocks                   */
+  int32_t value_type;      /* tx_value_type                                             */
+  double value;            /* CONSTANT / LINEAR "Value"                                 */
+  int32_t n_table;         /* TIME_TABLE points                                         */
+  const double* table_t;   /* "Time Values" (HOST, ascending, copied at creation)       */
+  const double* table_v;   /* "BC Values" (HOST)                                        */
+} tx_neumann_desc;
+/* The functor value at time t (host only, no handle). */
+int tx_neumann_value(const tx_neumann_desc* d, double t, double* value);
+/* Build the side workset and side tables of a Neumann set (allocates);
+ * *id names it in tx_neumann_eval, *n_sides = cells x local sides in it. */
+int tx_neumann_create(tx_handle h, const tx_neumann_desc* d, int32_t* id, int64_t* n_sides);
+/* f += the set's flux at time t (f DEVICE, LID order).  Launch only. */
+int tx_neumann_eval(tx_handle h, int32_t id, double t, double* f);
+
 /* y = alpha*A*x + beta*y over a Tpetra-layout CRS (CrsMatrix::apply).
  * vals/x/y are FP64 (TX_SPMV_F64) or FP32 (TX_SPMV_F32). */
 #define TX_SPMV_F64 0
@@ -207,7 +254,8 @@ int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowpt
  * inner solve.  A is the FP64 Tpetra-layout Jacobian (Dirichlet rows unit);
  * the outer residual is either r = b - A x (FP64 SpMV) or, with
  * TX_SOLVE_MATRIX_FREE_RESIDUAL, r = -f(x) from an FP64 Residual evaluation
- * of the handle's equation set plus the Dirichlet residual x_d - g_d.
+ * of the handle's equation set, the Neumann sets listed in neumann_ids
+ * (at time t) and the Dirichlet residual x_d - g_d.
  * x must satisfy the Dirichlet values on entry (the corrections at those
  * rows are then zero); dirichlet lids (device) are eliminated symmetrically
  * for the CG solve.  Relative residuals are taken against ||r(x0)||.
@@ -239,6 +287,10 @@ typedef struct tx_solve_args {
    * Newmark or backward-Euler wrapper presents to evalModel. */
   const double* x_pred;
   double x_dot_coef;
+  /* Neumann sets (ids from tx_neumann_create, HOST array) whose flux enters
+   * MATRIX_FREE residuals, as evalModel adds them before the Dirichlet rows. */
+  int32_t n_neumann;
+  const int32_t* neumann_ids;
 } tx_solve_args;
 int tx_solve_cg_ir(tx_handle h, tx_solve_args* args);
 
@@ -251,6 +303,11 @@ int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t se
  * tile-shape knob the autotuner sets (HierarchicParallelism's role,
  * disc-fe/src/Panzer_HierarchicParallelism.hpp:78-128). */
 int tx_set_grid_cap(tx_handle h, int32_t max_ctas);
+/* Launch shape of this handle's CRS SpMV (tx_spmv, the solver's inner and
+ * outer products): lanes per row 4/8/16/32 and entries each lane loads per
+ * pass 1/2/4; (0, 0) picks the lanes from the mean row length.  The
+ * autotuner's knob for the SpMV; results equal to rounding for every shape. */
+int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll);
 
 /* Many independent meshes in one persistent launch: the volume fill of every
  * block of every handle, cut into worksets, is one work list.  args holds one

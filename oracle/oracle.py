@@ -59,6 +59,8 @@ def lib():
         L.orc_dirichlet_dofs.restype = I64
         L.orc_dirichlet_dofs.argtypes = [P, C.c_uint32, C.c_uint32, P]
         L.orc_dirichlet_apply.argtypes = [P, I64, P, P, P, P, P]
+        L.orc_neumann.restype = I64
+        L.orc_neumann.argtypes = [P, C.c_int, C.c_uint32, C.c_int, D, P]
         L.orc_spmv.argtypes = [I64, P, P, P, P, P, D, D]
         L.orc_cg.argtypes = [I64, P, P, P, P, P, D, C.c_int, C.POINTER(D)]
         L.orc_cubature.argtypes = [C.c_int, C.c_int, P, P]
@@ -174,6 +176,42 @@ class Oracle:
         g = None if g is None else np.ascontiguousarray(g, np.float64)
         lib().orc_dirichlet_apply(self.h, len(lids), _p(lids), _p(g), _p(np.ascontiguousarray(x, np.float64)),
                                   _p(f), _p(vals))
+
+
+    def neumann(self, block, side_mask, field, value, f=None):
+        """f += the "Flux" Neumann residual of `value` on block's sides in side_mask; returns (f, #sides)."""
+        if f is None:
+            f = np.zeros(self.n_dofs)
+        n = lib().orc_neumann(self.h, block, side_mask, field, float(value), _p(f))
+        if n < 0:
+            raise RuntimeError("oracle neumann failed")
+        return f, int(n)
+
+
+def workset_functor(value_type, value=0.0, times=None, values=None, t=0.0):
+    """WorksetFunctor values (disc-fe/src/evaluators/TianXin_WorksetFunctor_impl.hpp:56-121):
+    Constant; Linear, whose elapse time is read from the same "Value" entry as the value (:67-82);
+    TimeTable, linear between the table points, an error past the last time (:88-121)."""
+    if value_type == "Constant":
+        return value
+    if value_type == "Linear":
+        elapse = value
+        if t >= elapse:
+            return value
+        if t <= 0.0:
+            return 0.0
+        return value * t / elapse
+    if value_type == "TimeTable":
+        if t > times[-1]:
+            raise ValueError("Time is growing unbounded!")
+        i = 0
+        while times[i] < t:
+            i += 1
+        if i == 0:
+            return values[0]
+        slope = (values[i] - values[i - 1]) / (times[i] - times[i - 1])
+        return values[i - 1] + slope * (t - times[i - 1])
+    raise ValueError(value_type)
 
 
 def spmv(rowptr, colind, vals, x, y=None, alpha=1.0, beta=0.0):

@@ -26,6 +26,10 @@
 //   * Dirichlet: f = x - g, Jacobian row -> unit row
 //       disc-fe/src/evaluators/TianXin_Dirichlet_impl.hpp:55-81,
 //       disc-fe/src/lof/Panzer_TpetraLinearObjContainer.hpp:228-238,306-318
+//   * Neumann flux: residual(cell, b) += val * N_b * w * |face normal| on the
+//     side workset of a block (TianXin::Flux, disc-fe/src/evaluators/
+//     TianXin_Neumann_impl.hpp:146-166; side worksets adapters-stk/src/
+//     Panzer_STK_SetupUtilities.cpp:306-392)
 //
 // Definitions the reference leaves to Intrepid2 (not in the reference tree)
 // are restated from the mathematics: tensor Gauss-Legendre cubature with the
@@ -1006,6 +1010,99 @@ static std::vector<LO> dirichlet_dofs(const Problem& P, uint32_t side_mask, uint
   return std::vector<LO>(ids.begin(), ids.end());
 }
 
+// ------------------------------------------------------------- Neumann
+// shards Tetrahedron<4> sides with their node order
+static const int kTetSideNodes[4][3] = {{0, 1, 3}, {1, 2, 3}, {0, 3, 2}, {0, 2, 1}};
+
+// Reference side rule mapped into the cell (CellTools::mapToReferenceSubcell)
+// and the side's two reference tangents.  Quad sides: Gauss n x n on
+// [-1,1]^2, x(u,v) = centre + u t_u + v t_v (the hex faces are
+// parallelograms in reference space, so this is their bilinear map).
+// Triangle sides: the 3-point degree-2 rule on the unit triangle,
+// x(u,v) = V0 + u (V1 - V0) + v (V2 - V0).
+static void side_rule(int topo, int degree, int s, std::vector<double>& xi, std::vector<double>& w,
+                      double tu[3], double tv[3]) {
+  xi.clear(); w.clear();
+  if (topo == TX_TOPO_HEX) {
+    const int* F = kHexFace[s];
+    std::vector<double> p, pw;
+    gauss_1d(degree / 2 + 1, p, pw);
+    const int n = (int)p.size();
+    double ctr[3];
+    for (int d = 0; d < 3; ++d) {
+      tu[d] = (kHexVert[F[1]][d] - kHexVert[F[0]][d]) / 2.0;
+      tv[d] = (kHexVert[F[3]][d] - kHexVert[F[0]][d]) / 2.0;
+      ctr[d] = (kHexVert[F[0]][d] + kHexVert[F[1]][d] + kHexVert[F[2]][d] + kHexVert[F[3]][d]) / 4.0;
+    }
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        for (int d = 0; d < 3; ++d) xi.push_back(ctr[d] + p[i] * tu[d] + p[j] * tv[d]);
+        w.push_back(pw[i] * pw[j]);
+      }
+  } else {
+    static const double V[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    const int* F = kTetSideNodes[s];
+    for (int d = 0; d < 3; ++d) { tu[d] = V[F[1]][d] - V[F[0]][d]; tv[d] = V[F[2]][d] - V[F[0]][d]; }
+    if (degree > 2) throw std::runtime_error("triangle side rule: degree <= 2");
+    const double uv[3][2] = {{1.0 / 6, 1.0 / 6}, {2.0 / 3, 1.0 / 6}, {1.0 / 6, 2.0 / 3}};
+    for (int q = 0; q < 3; ++q) {
+      for (int d = 0; d < 3; ++d) xi.push_back(V[F[0]][d] + uv[q][0] * tu[d] + uv[q][1] * tv[d]);
+      w.push_back(1.0 / 6);
+    }
+  }
+}
+
+// f[LID(cell, field, b)] += val * sum_q N_b(xi_q) * w_q * |(J t_u) x (J t_v)|
+// over the cells of `blk` with a side on the box sides of side_mask.
+static int64_t neumann_flux(const Problem& P, int blk, uint32_t side_mask, int field, double val, double* f) {
+  const Topology& T = P.T;
+  const DofManager& D = P.D;
+  const BasisDef& B = D.block_basis[blk];
+  if (B.hcurl) throw std::runtime_error("Neumann flux: scalar basis only");
+  const int topo = T.block_topo[blk];
+  const int nsides = topo == TX_TOPO_HEX ? 6 : 4;
+  const int nvs = topo == TX_TOPO_HEX ? 4 : 3;
+  BasisDef G;
+  geom_basis(topo, G);
+  const int nv = G.nb;
+  int64_t count = 0;
+  std::vector<double> xi, w, X(3 * nv), N(B.nb), dN(3 * B.nb), Ng(nv), dNg(3 * nv);
+  for (LO e : T.block_elems[blk]) {
+    GO I, J, K;
+    T.brick_ijk(T.elem_brick[e], I, J, K);
+    const int sub = T.elem_sub[e];
+    for (int s = 0; s < nsides; ++s) {
+      int bv[4];
+      for (int k = 0; k < nvs; ++k)
+        bv[k] = topo == TX_TOPO_HEX ? kHexFace[s][k] : kTetInHex[sub][kTetSideNodes[s][k]];
+      if (!on_sides(T, I, J, K, bv, nvs, side_mask)) continue;
+      ++count;
+      double tu[3], tv[3];
+      side_rule(topo, D.block_degree[blk], s, xi, w, tu, tv);
+      T.elem_vertices(e, nv, X.data());
+      std::vector<double> R(B.nb, 0.0);
+      for (size_t q = 0; q < w.size(); ++q) {
+        eval_hgrad(G, &xi[3 * q], Ng.data(), (double(*)[3])dNg.data());
+        double Jm[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int n = 0; n < nv; ++n)
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) Jm[3 * i + j] += X[3 * n + i] * dNg[3 * n + j];
+        double a[3], b[3];
+        for (int i = 0; i < 3; ++i) {
+          a[i] = Jm[3 * i] * tu[0] + Jm[3 * i + 1] * tu[1] + Jm[3 * i + 2] * tu[2];
+          b[i] = Jm[3 * i] * tv[0] + Jm[3 * i + 1] * tv[1] + Jm[3 * i + 2] * tv[2];
+        }
+        const double c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+        const double wm = w[q] * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        eval_hgrad(B, &xi[3 * q], N.data(), (double(*)[3])dN.data());
+        for (int bb = 0; bb < B.nb; ++bb) R[bb] += val * (N[bb] * wm);
+      }
+      for (int bb = 0; bb < B.nb; ++bb) f[D.elementLIDs[e][D.offsets[blk][field][bb]]] += R[bb];
+    }
+  }
+  return count;
+}
+
 }  // namespace orc
 
 // ====================================================================== C API
@@ -1253,6 +1350,16 @@ int orc_basis_eval(int topo, int basis, const double* xi, double* val, double* g
   }
   return b.nb;
 }
+// f += the Neumann flux of value val on block blk's sides in side_mask; returns
+// the number of (cell, side) pairs, or -1 on error.
+int64_t orc_neumann(void* h, int blk, uint32_t side_mask, int field, double val, double* f) {
+  try {
+    return neumann_flux(*(Problem*)h, blk, side_mask, field, val, f);
+  } catch (std::exception&) {
+    return -1;
+  }
+}
+
 int orc_max_threads() {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -40,3 +40,34 @@ def test_no_device_needed_to_describe_a_mesh():
     bad = _abi.mesh_desc((2, 2, 2))
     bad.bx = 0
     assert lib.tx_mesh_create(ctypes.byref(bad), ctypes.byref(h)) == _abi.TX_EINVAL
+
+
+def test_neumann_value_functors_match_the_oracle():
+    # tx_neumann_value is host logic: the WorksetFunctor values, checked
+    # against the oracle's restatement, including the reference's Linear
+    # ramp whose elapse time is its own "Value" and the TimeTable error.
+    import pytest
+    from oracle import oracle as O
+    import tianxin_gb300 as tx
+    from tianxin_gb300 import _abi as A
+    tt, tv = [0.0, 0.5, 2.0, 3.0], [1.0, -2.0, 4.0, 4.0]
+    for t in (-1.0, 0.0, 0.25, 0.5, 1.0, 2.0, 2.9, 3.0):
+        assert tx.neumann_value("TimeTable", times=tt, values=tv, t=t) == O.workset_functor("TimeTable", times=tt,
+                                                                                              values=tv, t=t)
+    for v, t in [(3.0, 1.0), (3.0, 3.0), (3.0, 7.0), (3.0, -2.0), (0.5, 0.25)]:
+        assert tx.neumann_value("Linear", v, t=t) == O.workset_functor("Linear", v, t=t)
+        assert tx.neumann_value("Constant", v, t=t) == v
+    with pytest.raises(tx.TxError) as e:
+        tx.neumann_value("TimeTable", times=tt, values=tv, t=3.5)
+    assert e.value.code == A.TX_ERANGE
+
+
+def test_spmv_shape_validation_needs_no_device():
+    import tianxin_gb300 as tx
+    from tianxin_gb300 import _abi as A
+    conn = tx.CartesianConnManager(1, 1, 1)
+    lib = _lib.load()
+    assert lib.tx_set_spmv_shape(conn.h, 16, 2) == 0
+    assert lib.tx_set_spmv_shape(conn.h, 0, 0) == 0
+    assert lib.tx_set_spmv_shape(conn.h, 12, 2) == A.TX_EINVAL
+    assert lib.tx_set_spmv_shape(conn.h, 8, 3) == A.TX_EINVAL

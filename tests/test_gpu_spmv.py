@@ -1,12 +1,12 @@
 """CRS SpMV (Tpetra::CrsMatrix::apply) on graphs of every row-length class.
 
-The kernel picks lanes per row and entries per lane from the mean row
-length, so each graph family below lands in a different configuration:
-Poisson tet4 (about 11 entries a row), Poisson hex8 (about 23), heat on
-hex27 + tet10 (about 60, vertex rows of 125 take two passes), elasticity
-hex8 (about 69).  A random CSR matrix with empty and long rows covers the
-configuration used when the mean is unknown.  Bars: FP64 within 1e-13
-relative (reassociated sums), FP32 within 1e-5.
+Without a tuned shape the kernel picks the lanes per row from the mean row
+length: Poisson tet4 (about 11 entries a row) 4 lanes, Poisson hex8 (about
+23) 8 lanes, heat on hex27 + tet10 (about 60; vertex rows of 125 take
+several passes) and elasticity hex8 (about 69) 16 lanes.  A random CSR
+matrix with empty and long rows covers the shape used when the mean is
+unknown, and every tunable shape is checked on two graphs.  Bars: FP64
+within 1e-13 relative (reassociated sums), FP32 within 1e-5.
 """
 import ctypes as C
 
@@ -86,3 +86,24 @@ def test_spmv_random_rows_with_empty_and_long_rows(cuda):
     out = y.cpu().numpy()
     assert np.abs(out - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
     assert np.all(out[lens == 0] == 0.0)  # empty rows: beta = 0 overwrites
+
+
+@pytest.mark.parametrize("name", ["poisson_hex8", "elasticity_hex8"])
+def test_spmv_every_launch_shape(cuda, name):
+    # the autotuner's knob changes only the summation order
+    g = GRAPHS[name]
+    conn = tx.CartesianConnManager(*g["n"], *g["blocks"], topology=g["topo"], jitter=0.1, seed=5)
+    dof = tx.DOFManager(conn, A.equation_set(g["phys"], g["basis"], params=g["params"]))
+    W = tx.TpetraLinearObjFactory(dof).getTpetraMatrix()
+    rng = np.random.default_rng(2)
+    vals = rng.uniform(-1, 1, dof.nnz)
+    x = rng.uniform(-1, 1, dof.n_dofs)
+    W.values.copy_(torch.from_numpy(vals))
+    y_ref = _csr_ref(W.rowptr.cpu().numpy(), W.colind.cpu().numpy(), vals, x)
+    xd = torch.from_numpy(x).cuda()
+    for lanes in (4, 8, 16, 32):
+        for unroll in (1, 2, 4):
+            W.setApplyShape(lanes, unroll)
+            y = W.apply(xd).cpu().numpy()
+            assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max(), (lanes, unroll)
+    W.setApplyShape(0, 0)

@@ -141,3 +141,71 @@ def test_reproduction_of_in_space_solution(topo, basis):
     bd = o.dirichlet_dofs(A.ALL_SIDES)
     o.dirichlet_apply(bd, u[bd], u, f, vals)
     assert np.linalg.norm(f) <= 1e-10 * np.linalg.norm(u)
+
+
+# ------------------------------------------------------------------ Neumann
+def test_neumann_flux_known_answer_reference_2d_values():
+    # The reference's flux test: value 5 on the left side of [0,2]x[0,1] (2x1
+    # quads, integration order 1) gives cell 0 the residual (2.5, 0, 0, 2.5).
+    # Extruded one brick in z, each 2-D node is a pair of hex nodes; their sum
+    # is the 2-D value.
+    g = json.load(open(os.path.join(GOLDEN, "reference_known_answers.json")))["neumann_flux_left"]
+    o = O.Oracle(A.mesh_desc((2, 1, 1), lengths=(2.0, 1.0, 1.0)),
+                 A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 0.0), integration_order=g["integration_order"]))
+    f, n = o.neumann(0, A.SIDE_XMIN, 0, g["value"])
+    assert n == 1
+    X = o.dof_coordinates()
+    quad = [(0.0, 0.0), (1.0, 0.0), (1.0, 1.0), (0.0, 1.0)]  # cell 0's nodes in quad order
+    for k, (x, y) in enumerate(quad):
+        pair = [i for i in range(o.n_dofs) if X[i, 0] == x and X[i, 1] == y]
+        assert len(pair) == 2
+        assert abs(f[pair].sum() - g["cell0_residual"][k]) <= g["tol"] * g["value"]
+    assert abs(f.sum() - g["value"] * 1.0) <= 1e-14  # the flux times the side's area
+
+
+@pytest.mark.parametrize("topo,basis,order", [(A.TX_TOPO_HEX, A.TX_HGRAD_C1, 2), (A.TX_TOPO_HEX, A.TX_HGRAD_C2, 4),
+                                              (A.TX_TOPO_TET, A.TX_HGRAD_C1, 2), (A.TX_TOPO_TET, A.TX_HGRAD_C2, 2)])
+def test_neumann_flux_closed_forms(topo, basis, order):
+    # Boundary vertices keep their lattice positions under the interior jitter,
+    # so every box side is tiled by exact rectangles (hex) or right triangles
+    # (tet), where the side rules integrate the traces exactly:
+    # sum of the flux = value * area, and the per-node shares of a rectangle
+    # (Q1: A/4; Q2 tensor weights (1,4,1)/6 squared) and of a triangle
+    # (P1: A/3; P2: 0 at vertices, A/3 at edge midpoints).
+    n, L, val = 3, (1.5, 1.0, 2.0), -0.75
+    o = O.Oracle(A.mesh_desc(n, topology=topo, lengths=L, jitter=0.2, seed=4),
+                 A.equation_set(A.TX_PHYS_POISSON, basis, params=(1.0, 0.0, 0.0, 0.0), integration_order=order))
+    f, cnt = o.neumann(0, A.SIDE_YMAX, 0, val)
+    area = L[0] * L[2]
+    assert cnt == (n * n if topo == A.TX_TOPO_HEX else 2 * n * n)
+    assert abs(f.sum() - val * area) <= 1e-13 * abs(val * area)
+    X = o.dof_coordinates()
+    on = np.abs(X[:, 1] - L[1]) < 1e-12
+    # off the side: exact zeros on hex sides (the side map keeps the fixed
+    # coordinate at exactly +-1); rounding of 1 - x - y - z on tet sides
+    assert np.abs(f[~on]).max() <= (0.0 if topo == A.TX_TOPO_HEX else 1e-16 * abs(val))
+    h = (L[0] / n, L[2] / n)
+    if topo == A.TX_TOPO_HEX and basis == A.TX_HGRAD_C1:
+        # an interior node of the side touches 4 rectangles
+        i = np.where(on & (np.abs(X[:, 0] - h[0]) < 1e-12) & (np.abs(X[:, 2] - h[1]) < 1e-12))[0]
+        assert abs(f[i[0]] - val * h[0] * h[1]) <= 1e-14
+    if topo == A.TX_TOPO_TET and basis == A.TX_HGRAD_C2:
+        verts = on & np.isclose(np.mod(X[:, 0], h[0]), 0) & np.isclose(np.mod(X[:, 2], h[1]), 0)
+        verts |= on & np.isclose(np.mod(X[:, 0], h[0]), h[0]) & np.isclose(np.mod(X[:, 2], h[1]), h[1])
+        assert np.abs(f[verts]).max() <= 1e-15
+
+
+def test_workset_functor_values():
+    # Constant; Linear with the elapse time read from "Value" (the reference's
+    # LinearWorksetFunctor); TimeTable interpolation and its error past the end.
+    assert O.workset_functor("Constant", 3.5, t=9.0) == 3.5
+    assert O.workset_functor("Linear", 4.0, t=1.0) == 1.0   # 4 * 1 / 4
+    assert O.workset_functor("Linear", 4.0, t=6.0) == 4.0
+    assert O.workset_functor("Linear", 4.0, t=-1.0) == 0.0
+    tt, tv = [0.0, 1.0, 3.0], [2.0, 4.0, 0.0]
+    assert O.workset_functor("TimeTable", times=tt, values=tv, t=0.0) == 2.0
+    assert O.workset_functor("TimeTable", times=tt, values=tv, t=0.5) == 3.0
+    assert O.workset_functor("TimeTable", times=tt, values=tv, t=2.0) == 2.0
+    assert O.workset_functor("TimeTable", times=tt, values=tv, t=-1.0) == 2.0
+    with pytest.raises(ValueError):
+        O.workset_functor("TimeTable", times=tt, values=tv, t=3.5)

@@ -40,6 +40,10 @@ TX_SOLVE_MATRIX_FREE_RESIDUAL = 0x1
 TX_SOLVE_FIXED_ITERATIONS = 0x2
 TX_SOLVE_REUSE_OPERATOR = 0x4
 
+TX_VALUE_CONSTANT = 1
+TX_VALUE_LINEAR = 2
+TX_VALUE_TIME_TABLE = 3
+
 # side bits for Dirichlet sets
 SIDE_XMIN, SIDE_XMAX, SIDE_YMIN, SIDE_YMAX, SIDE_ZMIN, SIDE_ZMAX = (1 << i for i in range(6))
 ALL_SIDES = 0x3F
@@ -90,6 +94,15 @@ class SolveArgs(C.Structure):
         ("stats", C.c_double * 4),
         ("stats_device", C.c_void_p),
         ("x_pred", C.c_void_p), ("x_dot_coef", C.c_double),
+        ("n_neumann", C.c_int32), ("neumann_ids", C.c_void_p),
+    ]
+
+
+class NeumannDesc(C.Structure):
+    _fields_ = [
+        ("block", C.c_int32), ("side_mask", C.c_uint32), ("field", C.c_int32), ("value_type", C.c_int32),
+        ("value", C.c_double),
+        ("n_table", C.c_int32), ("table_t", C.c_void_p), ("table_v", C.c_void_p),
     ]
 
 

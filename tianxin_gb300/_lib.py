@@ -33,8 +33,12 @@ SIGNATURES = {
     "tx_dirichlet_apply": (C.c_int, [P, I64, P, P, P, P, P]),
     "tx_spmv": (C.c_int, [P, I32, I64, P, P, P, P, P, D, D]),
     "tx_solve_cg_ir": (C.c_int, [P, C.POINTER(_abi.SolveArgs)]),
+    "tx_neumann_value": (C.c_int, [C.POINTER(_abi.NeumannDesc), D, C.POINTER(D)]),
+    "tx_neumann_create": (C.c_int, [P, C.POINTER(_abi.NeumannDesc), C.POINTER(I32), C.POINTER(I64)]),
+    "tx_neumann_eval": (C.c_int, [P, I32, D, P]),
     "tx_set_worksets": (C.c_int, [P, I64, I64, C.c_uint64]),
     "tx_set_grid_cap": (C.c_int, [P, I32]),
+    "tx_set_spmv_shape": (C.c_int, [P, I32, I32]),
     "tx_batch_create": (C.c_int, [P, I32, C.POINTER(P)]),
     "tx_batch_set_worksets": (C.c_int, [P, I64, I64, C.c_uint64, I32]),
     "tx_batch_eval": (C.c_int, [P, P]),

@@ -91,3 +91,20 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
     if "workset" in cfg:
         ae.setWorksetSize(cfg["workset"], cfg["workset"])
     return cfg
+
+
+SPMV_SHAPES = [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2, 4)]
+
+
+def tune_spmv(W, vals, x, y, reps=5):
+    """Time W.apply in every launch shape (lanes per row x loads per lane) and apply the fastest.
+
+    Returns {"shape": (lanes, unroll), "ms": t, "candidates": [((lanes, unroll), ms), ...]}.
+    """
+    results = []
+    for shape in SPMV_SHAPES:
+        W.setApplyShape(*shape)
+        results.append((shape, _time(lambda: W.apply(x, y, values=vals), reps)))
+    best = min(results, key=lambda r: r[1])
+    W.setApplyShape(*best[0])
+    return {"shape": best[0], "ms": best[1], "candidates": results}

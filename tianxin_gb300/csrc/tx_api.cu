@@ -78,6 +78,16 @@ inline void ck(cudaError_t e, const char* what) {
 
 }  // namespace
 
+// One Neumann "Flux" set: its side workset and side tables on the device.
+struct NeumannSet {
+  tx_neumann_desc desc{};
+  std::vector<double> table_t, table_v;  // TIME_TABLE copy
+  int64_t n_sides = 0;
+  int64_t* sides = nullptr;
+  double* tables = nullptr;
+  int stride = 0, nqf = 0;
+};
+
 struct tx_handle_s {
   tx::Mesh mesh;
   tx::Dofs dofs;
@@ -99,8 +109,12 @@ struct tx_handle_s {
   tx::WorkItem* d_items = nullptr;
   int* d_counter = nullptr;
   Staging stage;
+  std::vector<NeumannSet> neumann;
+  tx::SpmvShape spmv;  // SpMV launch shape ({0, 0}: automatic)
 
   void free_dofs() {
+    for (auto& ns : neumann) { cudaFree(ns.sides); cudaFree(ns.tables); }
+    neumann.clear();
     for (auto& b : blocks) {
       cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
       cudaFree(b.color_perm);
@@ -260,7 +274,11 @@ struct MfCtx {
   const double* x_pred;      // implicit integration: x_dot = coef * (x - x_pred)
   double coef;
   double* xdot_work;
+  int32_t n_neumann;
+  const int32_t* neumann_ids;
 };
+
+int neumann_eval(tx_handle h, int32_t id, double t, double* f);
 
 int outer_residual(void* vctx, const double* x, double* r) {
   MfCtx* c = (MfCtx*)vctx;
@@ -279,6 +297,8 @@ int outer_residual(void* vctx, const double* x, double* r) {
     a.f = r; a.crs_vals = nullptr; a.block = -1; a.elem_end = -1; a.flags = 0;
     int rc = eval_blocks(h, a);
     if (rc) return rc;
+    for (int32_t k = 0; k < c->n_neumann; ++k)
+      if ((rc = neumann_eval(h, c->neumann_ids[k], c->t, r)) != TX_OK) return rc;
     if (tx::launch_dirichlet(c->n_dir, c->dir, c->g, x, r, nullptr, nullptr, nullptr, h->dofs.nf, nullptr,
                              h->stream) != cudaSuccess)
       return TX_ECUDA;
@@ -286,8 +306,54 @@ int outer_residual(void* vctx, const double* x, double* r) {
     return TX_OK;
   }
   if (cudaMemcpyAsync(r, c->b, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess) return TX_ECUDA;
-  if (tx::launch_spmv_f64(n, c->rowptr, c->colind, c->vals, x, r, -1.0, 1.0, h->dofs.nnz, h->stream) != cudaSuccess)
+  if (tx::launch_spmv_f64(n, c->rowptr, c->colind, c->vals, x, r, -1.0, 1.0, h->dofs.nnz, h->stream, h->spmv) !=
+      cudaSuccess)
     return TX_ECUDA;
+  return TX_OK;
+}
+
+// Neumann sets
+
+// WorksetFunctor values (disc-fe/src/evaluators/TianXin_WorksetFunctor_impl.hpp).
+int neumann_value(const tx_neumann_desc& d, const double* tt, const double* tv, double t, double* out,
+                  std::string& err) {
+  switch (d.value_type) {
+    case TX_VALUE_CONSTANT:
+      *out = d.value;
+      return TX_OK;
+    case TX_VALUE_LINEAR: {
+      // the elapse time is the "Value" entry itself, as LinearWorksetFunctor reads it
+      const double elapse = d.value;
+      if (t >= elapse) *out = d.value;
+      else if (t <= 0.0) *out = 0.0;
+      else *out = d.value * t / elapse;
+      return TX_OK;
+    }
+    case TX_VALUE_TIME_TABLE: {
+      if (d.n_table < 1 || !tt || !tv) { err = "TIME_TABLE needs n_table >= 1 and both tables"; return TX_EINVAL; }
+      if (t > tt[d.n_table - 1]) { err = "time is past the last TIME_TABLE time"; return TX_ERANGE; }
+      int i = 0;
+      while (tt[i] < t) ++i;
+      if (i == 0) *out = tv[0];
+      else *out = tv[i - 1] + (tv[i] - tv[i - 1]) / (tt[i] - tt[i - 1]) * (t - tt[i - 1]);
+      return TX_OK;
+    }
+    default:
+      err = "unknown value_type";
+      return TX_EINVAL;
+  }
+}
+
+int neumann_eval(tx_handle h, int32_t id, double t, double* f) {
+  if (id < 0 || id >= (int32_t)h->neumann.size()) return fail(h, TX_ERANGE, "tx_neumann_eval: unknown set");
+  const NeumannSet& ns = h->neumann[id];
+  double val = 0.0;
+  std::string err;
+  int rc = neumann_value(ns.desc, ns.table_t.data(), ns.table_v.data(), t, &val, err);
+  if (rc) return fail(h, rc, "tx_neumann_eval: " + err);
+  cudaError_t e = tx::launch_neumann(h->blocks[ns.desc.block].view(), h->d_coords, ns.sides, ns.n_sides, ns.tables,
+                                     ns.stride, ns.nqf, h->dofs.nf, ns.desc.field, val, f, h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_neumann_eval: ") + cudaGetErrorString(e));
   return TX_OK;
 }
 
@@ -477,10 +543,10 @@ int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowpt
   cudaError_t e;
   if (precision == TX_SPMV_F64)
     e = tx::launch_spmv_f64(n_rows, rowptr, colind, (const double*)vals, (const double*)x, (double*)y, alpha, beta,
-                            hint, h->stream);
+                            hint, h->stream, h->spmv);
   else if (precision == TX_SPMV_F32)
     e = tx::launch_spmv_f32(n_rows, rowptr, colind, (const float*)vals, (const float*)x, (float*)y, (float)alpha,
-                            (float)beta, hint, h->stream);
+                            (float)beta, hint, h->stream, h->spmv);
   else
     return fail(h, TX_EINVAL, "tx_spmv: precision must be TX_SPMV_F64 or TX_SPMV_F32");
   if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_spmv: ") + cudaGetErrorString(e));
@@ -498,9 +564,16 @@ int tx_solve_cg_ir(tx_handle h, tx_solve_args* a) {
   cudaError_t e = tx::solver_alloc(h->solver, n, h->dofs.nnz);
   if (e != cudaSuccess) return fail(h, TX_ENOMEM, std::string("tx_solve_cg_ir: ") + cudaGetErrorString(e));
   MfCtx ctx{h, a->x_dot, a->alpha, a->beta, a->t, a->n_dirichlet, a->dirichlet_lids, a->dirichlet_g,
-            a->b, a->rowptr, a->colind, a->vals, mf, a->x_pred, a->x_dot_coef, h->solver.xdw};
+            a->b, a->rowptr, a->colind, a->vals, mf, a->x_pred, a->x_dot_coef, h->solver.xdw,
+            a->n_neumann, a->neumann_ids};
   if (a->x_pred && !mf) return fail(h, TX_EINVAL, "tx_solve_cg_ir: x_pred needs MATRIX_FREE_RESIDUAL");
+  if (a->n_neumann < 0 || (a->n_neumann > 0 && !a->neumann_ids))
+    return fail(h, TX_EINVAL, "tx_solve_cg_ir: neumann ids");
+  for (int32_t k = 0; k < a->n_neumann; ++k)
+    if (a->neumann_ids[k] < 0 || a->neumann_ids[k] >= (int32_t)h->neumann.size())
+      return fail(h, TX_ERANGE, "tx_solve_cg_ir: unknown Neumann set");
   std::string err;
+  h->solver.spmv = h->spmv;
   int rc = tx::solve_cg_ir(h->solver, a->rowptr, a->colind, a->vals, a->n_dirichlet, a->dirichlet_lids, a->x,
                            outer_residual, &ctx, a->rtol > 0 ? a->rtol : 1e-10,
                            a->inner_rtol > 0 ? a->inner_rtol : 1e-5, a->max_outer > 0 ? a->max_outer : 50,
@@ -512,11 +585,79 @@ int tx_solve_cg_ir(tx_handle h, tx_solve_args* a) {
   return TX_OK;
 }
 
+
+int tx_neumann_value(const tx_neumann_desc* d, double t, double* value) {
+  if (!d || !value) return TX_EINVAL;
+  std::string err;
+  return neumann_value(*d, d->table_t, d->table_v, t, value, err);
+}
+
+int tx_neumann_create(tx_handle h, const tx_neumann_desc* d, int32_t* id, int64_t* n_sides) {
+  if (!h || !d || !id) return TX_EINVAL;
+  if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_neumann_create before tx_dof_build");
+  if (d->block < 0 || d->block >= h->mesh.nblocks) return fail(h, TX_ERANGE, "tx_neumann_create: block out of range");
+  if (d->field < 0 || d->field >= h->dofs.nf) return fail(h, TX_ERANGE, "tx_neumann_create: field out of range");
+  if (d->side_mask == 0 || (d->side_mask & ~0x3fu)) return fail(h, TX_EINVAL, "tx_neumann_create: side_mask");
+  if (h->blocks[d->block].basis == TX_HCURL_I1)
+    return fail(h, TX_EINVAL, "tx_neumann_create: the flux integrates a scalar (HGRAD) basis");
+  double v0;
+  std::string verr;
+  int rc = neumann_value(*d, d->table_t, d->table_v, d->value_type == TX_VALUE_TIME_TABLE && d->table_t ?
+                         d->table_t[0] : 0.0, &v0, verr);
+  if (rc) return fail(h, rc, "tx_neumann_create: " + verr);
+  if (d->value_type == TX_VALUE_TIME_TABLE)
+    for (int32_t i = 1; i < d->n_table; ++i)
+      if (!(d->table_t[i] > d->table_t[i - 1]))
+        return fail(h, TX_EINVAL, "tx_neumann_create: TIME_TABLE times must increase");
+  return guarded(h, [&]() {
+    NeumannSet ns;
+    ns.desc = *d;
+    if (d->value_type == TX_VALUE_TIME_TABLE) {
+      ns.table_t.assign(d->table_t, d->table_t + d->n_table);
+      ns.table_v.assign(d->table_v, d->table_v + d->n_table);
+    }
+    ns.desc.table_t = nullptr;
+    ns.desc.table_v = nullptr;
+    const tx::BlockDofs& B = h->dofs.blocks[d->block];
+    std::vector<int64_t> sides = tx::side_workset(h->mesh, d->block, d->side_mask);
+    tx::SideTables S = tx::make_side_tables(B.topo, B.basis, B.degree);
+    ns.n_sides = (int64_t)sides.size();
+    ns.stride = S.stride;
+    ns.nqf = S.nqf;
+    try {
+      ck(upload(ns.sides, sides), "upload side workset");
+      ck(upload(ns.tables, S.packed), "upload side tables");
+    } catch (...) {
+      cudaFree(ns.sides); cudaFree(ns.tables);
+      throw;
+    }
+    h->neumann.push_back(ns);
+    *id = (int32_t)h->neumann.size() - 1;
+    if (n_sides) *n_sides = ns.n_sides;
+    return TX_OK;
+  });
+}
+
+int tx_neumann_eval(tx_handle h, int32_t id, double t, double* f) {
+  if (!h || !f) return TX_EINVAL;
+  if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_neumann_eval before tx_dof_build");
+  return neumann_eval(h, id, t, f);
+}
+
 int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t seed) {
   if (!h) return TX_EINVAL;
   if (min_size < 1 || max_size < min_size) return fail(h, TX_EINVAL, "tx_set_worksets: need 1 <= min <= max");
   h->ws_min = min_size; h->ws_max = max_size; h->ws_seed = seed;
   h->items.clear();  // rebuilt at the next persistent evaluation
+  return TX_OK;
+}
+
+int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll) {
+  if (!h) return TX_EINVAL;
+  const tx::SpmvShape sh{lanes, unroll};
+  if (!tx::spmv_shape_valid(sh))
+    return fail(h, TX_EINVAL, "tx_set_spmv_shape: lanes 4/8/16/32 and unroll 1/2/4, or both 0");
+  h->spmv = sh;
   return TX_OK;
 }
 

@@ -53,10 +53,23 @@ cudaError_t launch_expand_colind(const int64_t* erowptr, const int32_t* ecol, in
 cudaError_t launch_dirichlet(int64_t n, const int32_t* lids, const double* g, const double* x, double* f,
                              const int64_t* rowptr, const int64_t* erowptr, const int32_t* ecol, int nf,
                              double* vals, cudaStream_t s);
+// f[nf*dconn[e][b] + field] += val * sum_q N_b(q) w_q |J t_u x J t_v| over a
+// side workset (entries e << 3 | local side), one warp per side.
+cudaError_t launch_neumann(const BlockView& B, const double* coords, const int64_t* sides, int64_t n_sides,
+                           const double* tables, int stride, int nqf, int nf, int field, double val, double* f,
+                           cudaStream_t s);
+// CRS SpMV launch shape: lanes per row (4, 8, 16, 32) and entries each lane
+// loads per pass (1, 2, 4); {0, 0} picks lanes from the mean row length.
+struct SpmvShape {
+  int lanes = 0, unroll = 0;
+};
+bool spmv_shape_valid(SpmvShape sh);
 cudaError_t launch_spmv_f64(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* vals,
-                            const double* x, double* y, double alpha, double beta, int64_t nnz_hint, cudaStream_t s);
+                            const double* x, double* y, double alpha, double beta, int64_t nnz_hint, cudaStream_t s,
+                            SpmvShape shape = SpmvShape());
 cudaError_t launch_spmv_f32(int64_t n, const int64_t* rowptr, const int32_t* colind, const float* vals,
-                            const float* x, float* y, float alpha, float beta, int64_t nnz_hint, cudaStream_t s);
+                            const float* x, float* y, float alpha, float beta, int64_t nnz_hint, cudaStream_t s,
+                            SpmvShape shape = SpmvShape());
 
 // Work space of the iterative-refinement solver (owned by the handle).
 struct SolverWork {
@@ -70,6 +83,7 @@ struct SolverWork {
   double* red = nullptr;       // reduction partials [kRedSlots * kRedBlocks]
   double* scal = nullptr;      // device scalars
   double* host_scal = nullptr; // pinned mirror
+  SpmvShape spmv;              // shape of the inner FP32 SpMV
 };
 constexpr int kRedBlocks = 1024;
 constexpr int kRedSlots = 4;

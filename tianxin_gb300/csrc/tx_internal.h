@@ -28,6 +28,17 @@ struct RefTables {
 RefTables make_ref_tables(int topo, int basis, int degree);
 int default_degree(int topo, int basis);
 
+// Side cubature tables of a block's reference element, one group per local
+// side ordinal s (6 hex faces, 4 tet faces), each [w | geo_grad | val | tu |
+// tv]: weights of the reference side rule, geometry-basis gradients and
+// basis values at the side points mapped into the element, and the two
+// constant tangents of the side's parametrisation.
+struct SideTables {
+  int nsides = 0, nqf = 0, nb = 0, nv = 0, stride = 0;
+  std::vector<double> packed;  // [nsides][stride]
+};
+SideTables make_side_tables(int topo, int basis, int degree);
+
 // Device view of one block, passed by value to kernels.
 struct BlockView {
   int topo, basis, nq, nb, nv;
@@ -92,6 +103,10 @@ void dof_element_lids(const Mesh& m, const Dofs& D, int block, int32_t* out);
 int dof_block_gid_count(const Dofs& D, int block);
 int dof_field_offsets(const Dofs& D, int block, int field, int32_t* out);
 std::vector<int32_t> dirichlet_dofs(const Dofs& D, const Mesh& m, uint32_t side_mask, uint32_t field_mask);
+// Side workset of a block on the box sides in side_mask: (block element << 3
+// | local side ordinal) for every local side lying on one of the sides, in
+// block element order, then side ordinal.
+std::vector<int64_t> side_workset(const Mesh& m, int block, uint32_t side_mask);
 // Worksets of a block: consecutive element ranges with sizes drawn uniformly
 // in [min_size, max_size] from a seeded generator (min == max: even split).
 std::vector<int64_t> workset_bounds(int64_t n_elem, int64_t min_size, int64_t max_size, uint64_t seed);

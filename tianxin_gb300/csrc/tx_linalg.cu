@@ -130,18 +130,43 @@ __global__ void __launch_bounds__(kThreads) k_spmv(int64_t n, const int64_t* __r
   }
 }
 
+// The automatic shape: lanes from the mean row length, one entry per lane per pass.
+SpmvShape resolve_shape(SpmvShape sh, int64_t n, int64_t nnz_hint) {
+  if (sh.lanes > 0 && sh.unroll > 0) return sh;
+  const double avg = nnz_hint > 0 && n > 0 ? (double)nnz_hint / (double)n : 32.0;
+  sh.lanes = avg <= 12 ? 4 : avg <= 40 ? 8 : avg <= 96 ? 16 : 32;
+  sh.unroll = 1;
+  return sh;
+}
+
+// Calls F.template run<LANES, U>() for the shape's template arguments.
+template <typename F>
+cudaError_t with_shape(SpmvShape sh, F&& f) {
+#define TX_SHAPE(L, U) \
+  if (sh.lanes == L && sh.unroll == U) return f.template run<L, U>();
+  TX_SHAPE(4, 1) TX_SHAPE(4, 2) TX_SHAPE(4, 4)
+  TX_SHAPE(8, 1) TX_SHAPE(8, 2) TX_SHAPE(8, 4)
+  TX_SHAPE(16, 1) TX_SHAPE(16, 2) TX_SHAPE(16, 4)
+  TX_SHAPE(32, 1) TX_SHAPE(32, 2) TX_SHAPE(32, 4)
+#undef TX_SHAPE
+  return cudaErrorInvalidValue;
+}
+
+template <typename T>
+struct SpmvLaunch {
+  int64_t n; const int64_t* rp; const int32_t* col; const T* vals; const T* x; T* y; T a, b; cudaStream_t s;
+  template <int L, int U>
+  cudaError_t run() const {
+    k_spmv<T, L, U><<<grid_for(n, kThreads / L, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
+    return cudaGetLastError();
+  }
+};
+
 template <typename T>
 cudaError_t spmv_dispatch(int64_t n, const int64_t* rp, const int32_t* col, const T* vals, const T* x, T* y, T a,
-                          T b, int64_t nnz_hint, cudaStream_t s) {
+                          T b, int64_t nnz_hint, cudaStream_t s, SpmvShape shape) {
   if (n <= 0) return cudaSuccess;
-  const double avg = nnz_hint > 0 ? (double)nnz_hint / (double)n : 32.0;
-  // lanes per row and entries per lane per pass: a row of up to LANES*U entries is one pass
-  if (avg <= 16) k_spmv<T, 4, 4><<<grid_for(n, kThreads / 4, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  else if (avg <= 32) k_spmv<T, 8, 4><<<grid_for(n, kThreads / 8, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  else if (avg <= 64) k_spmv<T, 16, 4><<<grid_for(n, kThreads / 16, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  else if (avg <= 96) k_spmv<T, 32, 3><<<grid_for(n, kThreads / 32, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  else k_spmv<T, 32, 4><<<grid_for(n, kThreads / 32, 152 * 64), kThreads, 0, s>>>(n, rp, col, vals, x, y, a, b);
-  return cudaGetLastError();
+  return with_shape(resolve_shape(shape, n, nnz_hint), SpmvLaunch<T>{n, rp, col, vals, x, y, a, b, s});
 }
 
 // ------------------------------------------------------------ reductions
@@ -345,13 +370,19 @@ cudaError_t launch_dirichlet(int64_t n, const int32_t* lids, const double* g, co
   k_dirichlet<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, lids, g, x, f, rp, erp, ecol, nf, vals);
   return cudaGetLastError();
 }
+bool spmv_shape_valid(SpmvShape sh) {
+  if (sh.lanes == 0 && sh.unroll == 0) return true;
+  const bool l = sh.lanes == 4 || sh.lanes == 8 || sh.lanes == 16 || sh.lanes == 32;
+  const bool u = sh.unroll == 1 || sh.unroll == 2 || sh.unroll == 4;
+  return l && u;
+}
 cudaError_t launch_spmv_f64(int64_t n, const int64_t* rp, const int32_t* col, const double* vals, const double* x,
-                            double* y, double a, double b, int64_t nnz_hint, cudaStream_t s) {
-  return spmv_dispatch<double>(n, rp, col, vals, x, y, a, b, nnz_hint, s);
+                            double* y, double a, double b, int64_t nnz_hint, cudaStream_t s, SpmvShape shape) {
+  return spmv_dispatch<double>(n, rp, col, vals, x, y, a, b, nnz_hint, s, shape);
 }
 cudaError_t launch_spmv_f32(int64_t n, const int64_t* rp, const int32_t* col, const float* vals, const float* x,
-                            float* y, float a, float b, int64_t nnz_hint, cudaStream_t s) {
-  return spmv_dispatch<float>(n, rp, col, vals, x, y, a, b, nnz_hint, s);
+                            float* y, float a, float b, int64_t nnz_hint, cudaStream_t s, SpmvShape shape) {
+  return spmv_dispatch<float>(n, rp, col, vals, x, y, a, b, nnz_hint, s, shape);
 }
 cudaError_t launch_fill(double* p, double v, int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
@@ -414,6 +445,16 @@ __global__ void k_fixed_stats(const double* scal, int outer, int inner, double* 
   out[3] = r0;
 }
 
+// q = A p with dot(p, q) partials, in the solver's SpMV shape
+struct DotLaunch {
+  int64_t n; const int64_t* rp; const int32_t* col; const SolverWork* w; unsigned gb; cudaStream_t s;
+  template <int L, int U>
+  cudaError_t run() const {
+    k_spmv_dot<L, U><<<gb, kThreads, 0, s>>>(n, rp, col, w->vals32, w->p, w->q, w->red);
+    return cudaSuccess;
+  }
+};
+
 int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const double* vals, int64_t n_dir,
                 const int32_t* dir, double* x, ResidualFn resid, void* ctx, double rtol, double inner_rtol,
                 int max_outer, int max_inner, double* stats, cudaStream_t s, std::string& err, bool fixed,
@@ -432,14 +473,8 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     k_make_f32<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, rp, col, vals, w.mask, w.vals32, w.dinv);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: make_f32");
   }
-  const double avg = (double)w.nnz / (double)(n > 0 ? n : 1);
-  auto spmv_dot = [&]() {
-    if (avg <= 16) k_spmv_dot<4, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-    else if (avg <= 32) k_spmv_dot<8, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-    else if (avg <= 64) k_spmv_dot<16, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-    else if (avg <= 96) k_spmv_dot<32, 3><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-    else k_spmv_dot<32, 4><<<gb, kThreads, 0, s>>>(n, rp, col, w.vals32, w.p, w.q, w.red);
-  };
+  const SpmvShape shape = resolve_shape(w.spmv, n, w.nnz);
+  auto spmv_dot = [&]() { with_shape(shape, DotLaunch{n, rp, col, &w, gb, s}); };
   auto cg_iteration = [&]() {
     spmv_dot();
     k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2);  // pq

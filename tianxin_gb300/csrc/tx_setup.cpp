@@ -177,13 +177,20 @@ std::vector<double> RefTables::packed() const {
   return out;
 }
 
-RefTables make_ref_tables(int topo, int basis, int degree) {
+static void eval_tables(RefTables& R);
+
+static RefTables blank_tables(int topo, int basis, int degree) {
   RefTables R;
   R.topo = topo; R.basis = basis; R.degree = degree;
   R.nb = n_basis(topo, basis);
   if (R.nb < 0) throw std::runtime_error("unsupported topology/basis");
   R.hcurl = basis == TX_HCURL_I1;
   R.nv = topo == TX_TOPO_HEX ? 8 : 4;
+  return R;
+}
+
+RefTables make_ref_tables(int topo, int basis, int degree) {
+  RefTables R = blank_tables(topo, basis, degree);
   if (topo == TX_TOPO_HEX) {
     int n = degree / 2 + 1;
     double p[4], w[4];
@@ -200,6 +207,107 @@ RefTables make_ref_tables(int topo, int basis, int degree) {
     R.xi = {b, b, b, a, b, b, b, a, b, b, b, a};
     R.w.assign(4, 1.0 / 24.0);
   }
+  eval_tables(R);
+  return R;
+}
+
+// shards Tetrahedron<4> side (face) node order
+static const int kTetSideVtx[4][3] = {{0, 1, 3}, {1, 2, 3}, {0, 3, 2}, {0, 2, 1}};
+
+// Side rules: the reference side's cubature of the block's degree mapped to
+// the element's reference coordinates (CellTools::mapToReferenceSubcell).
+// Hex faces: n x n Gauss points on [-1,1]^2 (n = degree/2 + 1, u fastest),
+// x(u,v) = c + u t_u + v t_v with c the face centre and t_u = (V1 - V0)/2,
+// t_v = (V3 - V0)/2 over the face's vertices in shards order (the faces are
+// parallelograms, so this is the bilinear side map, and the face's fixed
+// coordinate stays exactly +-1).  Tet faces: 3-point degree-2 triangle rule
+// ((1/6,1/6), (2/3,1/6), (1/6,2/3), weights 1/6), x(u,v) = V0 + u (V1-V0) +
+// v (V2-V0).  For these flat reference sides the tangents are constants.
+SideTables make_side_tables(int topo, int basis, int degree) {
+  SideTables S;
+  S.nsides = topo == TX_TOPO_HEX ? 6 : 4;
+  if (basis == TX_HCURL_I1) throw std::runtime_error("side tables: HGRAD bases only");
+  for (int s = 0; s < S.nsides; ++s) {
+    RefTables R = blank_tables(topo, basis, degree);
+    double tu[3], tv[3];
+    if (topo == TX_TOPO_HEX) {
+      double V[4][3];
+      for (int k = 0; k < 4; ++k)
+        for (int d = 0; d < 3; ++d) V[k][d] = kVtx[kFaceVtx[s][k]][d] ? 1.0 : -1.0;
+      double c[3];
+      for (int d = 0; d < 3; ++d) {
+        tu[d] = 0.5 * (V[1][d] - V[0][d]);
+        tv[d] = 0.5 * (V[3][d] - V[0][d]);
+        c[d] = 0.25 * (V[0][d] + V[1][d] + V[2][d] + V[3][d]);
+      }
+      const int n = degree / 2 + 1;
+      double p[4], w[4];
+      gauss_points(n, p, w);
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          for (int d = 0; d < 3; ++d) R.xi.push_back(c[d] + p[i] * tu[d] + p[j] * tv[d]);
+          R.w.push_back(w[i] * w[j]);
+        }
+    } else {
+      if (degree != 2) throw std::runtime_error("tet side cubature: only degree 2");
+      static const double ref[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+      const double* V0 = ref[kTetSideVtx[s][0]];
+      const double* V1 = ref[kTetSideVtx[s][1]];
+      const double* V2 = ref[kTetSideVtx[s][2]];
+      for (int d = 0; d < 3; ++d) { tu[d] = V1[d] - V0[d]; tv[d] = V2[d] - V0[d]; }
+      const double uv[3][2] = {{1.0 / 6, 1.0 / 6}, {2.0 / 3, 1.0 / 6}, {1.0 / 6, 2.0 / 3}};
+      for (int q = 0; q < 3; ++q) {
+        for (int d = 0; d < 3; ++d) R.xi.push_back(V0[d] + uv[q][0] * tu[d] + uv[q][1] * tv[d]);
+        R.w.push_back(1.0 / 6);
+      }
+    }
+    eval_tables(R);
+    if (s == 0) {
+      S.nqf = R.nq; S.nb = R.nb; S.nv = R.nv;
+      S.stride = S.nqf * (1 + 3 * S.nv + S.nb) + 6;
+      S.packed.assign((size_t)S.nsides * S.stride, 0.0);
+    }
+    double* o = S.packed.data() + (size_t)s * S.stride;
+    o = std::copy(R.w.begin(), R.w.end(), o);
+    o = std::copy(R.geo_grad.begin(), R.geo_grad.end(), o);
+    o = std::copy(R.val.begin(), R.val.end(), o);
+    for (int d = 0; d < 3; ++d) *o++ = tu[d];
+    for (int d = 0; d < 3; ++d) *o++ = tv[d];
+  }
+  return S;
+}
+
+std::vector<int64_t> side_workset(const Mesh& m, int block, uint32_t side_mask) {
+  std::vector<int64_t> out;
+  const int topo = m.desc.block_topology[block];
+  const int nsides = topo == TX_TOPO_HEX ? 6 : 4;
+  const int64_t lim[3] = {m.NX, m.NY, m.NZ};
+  const std::vector<int64_t>& elems = m.block_elems[block];
+  for (int64_t i = 0; i < (int64_t)elems.size(); ++i) {
+    const int64_t e = elems[i];
+    const int64_t b = m.elem_brick[e];
+    const int64_t ijk[3] = {b % m.NX, (b / m.NX) % m.NY, b / (m.NX * m.NY)};
+    const int sub = m.elem_sub[e];
+    for (int s = 0; s < nsides; ++s) {
+      int bv[4], n = topo == TX_TOPO_HEX ? 4 : 3;
+      for (int k = 0; k < n; ++k) bv[k] = topo == TX_TOPO_HEX ? kFaceVtx[s][k] : kTets[sub][kTetSideVtx[s][k]];
+      bool on = false;
+      for (int side = 0; side < 6 && !on; ++side) {
+        if (!(side_mask & (1u << side))) continue;
+        const int axis = side / 2;
+        const int64_t want = (side & 1) ? lim[axis] : 0;
+        bool all = true;
+        for (int k = 0; k < n && all; ++k) all = ijk[axis] + kVtx[bv[k]][axis] == want;
+        on = all;
+      }
+      if (on) out.push_back(i * 8 + s);
+    }
+  }
+  return out;
+}
+
+static void eval_tables(RefTables& R) {
+  const int topo = R.topo, basis = R.basis;
   R.nq = (int)R.w.size();
   const int nq = R.nq, nb = R.nb, nv = R.nv;
   R.geo_val.assign(nq * nv, 0.0);
@@ -296,7 +404,6 @@ RefTables make_ref_tables(int topo, int basis, int degree) {
       }
     }
   }
-  return R;
 }
 
 // ------------------------------------------------------------------ mesh

@@ -8,6 +8,8 @@ assembly path finds the same objects:
   TpetraLinearObjFactory    disc-fe/src/lof/Panzer_TpetraLinearObjFactory_decl.hpp
   CrsMatrix                 Tpetra::CrsMatrix local layout (rowptr, colind, values)
   DirichletBC               TianXin::DirichletEvalautor parameter list
+  NeumannBC                 "Neumann Conditions" entry of Type "Flux" (TianXin::Flux,
+                            disc-fe/src/evaluators/TianXin_Neumann_impl.hpp:146-166)
   ModelEvaluator.evalModel  disc-fe/src/Panzer_ModelEvaluator_impl.hpp:1714-1882
   AssemblyEngine.evaluate   disc-fe/src/Panzer_AssemblyEngine_impl.hpp:65-182
 
@@ -159,6 +161,10 @@ class CrsMatrix:
                                       _ptr(x), _ptr(y), alpha, beta), "tx_spmv")
         return y
 
+    def setApplyShape(self, lanes=0, unroll=0):
+        """Launch shape of apply (and of the solver's SpMV) on this handle: lanes per row, loads per lane; 0, 0 = auto."""
+        check(self.dof.h, self.dof.lib.tx_set_spmv_shape(self.dof.h, lanes, unroll), "tx_set_spmv_shape")
+
     def to_scipy(self):
         import scipy.sparse as sp
         return sp.csr_matrix((self.values.cpu().numpy(), self.colind.cpu().numpy(), self.rowptr.cpu().numpy()),
@@ -200,6 +206,65 @@ class DirichletBC:
                                                            device="cuda")
         else:
             self.g = torch.as_tensor(value, dtype=torch.float64, device="cuda")
+
+
+_VALUE_TYPES = {"Constant": _abi.TX_VALUE_CONSTANT, "Linear": _abi.TX_VALUE_LINEAR,
+                "TimeTable": _abi.TX_VALUE_TIME_TABLE}
+
+
+def neumann_desc(block, side_mask, field, value_type="Constant", value=0.0, times=None, values=None):
+    """tx_neumann_desc from the reference's parameter names; the table arrays stay referenced by the result."""
+    d = _abi.NeumannDesc()
+    d.block, d.side_mask, d.field = block, side_mask, field
+    d.value_type = _VALUE_TYPES[value_type] if isinstance(value_type, str) else int(value_type)
+    d.value = float(value)
+    if times is not None:
+        tt = np.ascontiguousarray(times, dtype=np.float64)
+        tv = np.ascontiguousarray(values, dtype=np.float64)
+        if tt.shape != tv.shape:
+            raise ValueError("Time Values and BC Values differ in length")
+        d.n_table, d.table_t, d.table_v = len(tt), _np_ptr(tt), _np_ptr(tv)
+        d._keep = (tt, tv)
+    return d
+
+
+def neumann_value(value_type="Constant", value=0.0, times=None, values=None, t=0.0):
+    """WorksetFunctor value at time t (host only; TianXin_WorksetFunctor_impl.hpp)."""
+    d = neumann_desc(0, 1, 0, value_type, value, times, values)
+    out = C.c_double()
+    rc = load().tx_neumann_value(C.byref(d), t, C.byref(out))
+    if rc != 0:
+        raise TxError(rc, "tx_neumann_value")
+    return out.value
+
+
+class NeumannBC:
+    """A "Neumann Conditions" sublist of Type "Flux": Element Block Name (block), SideSet Name (side mask),
+    DOF Name, Value Type (Constant / Linear / TimeTable) and its value or table.
+
+    Creating it builds the side workset and side tables on the device; evaluate(f, t) adds the flux to f.
+    """
+
+    def __init__(self, dof, side_mask, dof_name=None, value_type="Constant", value=0.0, times=None, values=None,
+                 block=0):
+        field = dof.getFieldNum(dof_name) if dof_name is not None else 0
+        self.dof = dof
+        self.desc = neumann_desc(block, side_mask, field, value_type, value, times, values)
+        sid, ns = C.c_int32(), C.c_int64()
+        check(dof.h, dof.lib.tx_neumann_create(dof.h, C.byref(self.desc), C.byref(sid), C.byref(ns)),
+              "tx_neumann_create")
+        self.id, self.n_sides = sid.value, ns.value
+
+    def value(self, t=0.0):
+        out = C.c_double()
+        check(self.dof.h, self.dof.lib.tx_neumann_value(C.byref(self.desc), t, C.byref(out)), "tx_neumann_value")
+        return out.value
+
+    def evaluate(self, f, t=0.0):
+        lib = self.dof.lib
+        lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(self.dof.h, lib.tx_neumann_eval(self.dof.h, self.id, t, _ptr(f)), "tx_neumann_eval")
+        return f
 
 
 def eval_args(x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False, block=-1,
@@ -246,10 +311,11 @@ class AssemblyEngine:
 class ModelEvaluator:
     """evalModel(inArgs{x, x_dot, alpha, beta, t}, outArgs{f, W}) on the device."""
 
-    def __init__(self, lof, dirichlet=()):
+    def __init__(self, lof, dirichlet=(), neumann=()):
         self.lof, self.dof = lof, lof.dof
         self.ae = AssemblyEngine(lof)
         self.dirichlet = list(dirichlet)
+        self.neumann = list(neumann)
 
     def create_W_op(self):
         return self.lof.getTpetraMatrix()
@@ -263,6 +329,9 @@ class ModelEvaluator:
                 W.initializeMatrix(0.0)
         self.ae.evaluate(x, x_dot, aux, alpha, beta, t, f, W, mixed, deterministic=deterministic,
                          persistent=persistent)
+        if f is not None:  # Neumann sums into equations before Dirichlet overwrites rows
+            for bc in self.neumann:
+                bc.evaluate(f, t)
         self.applyDirichlet(x, f, W)
         return f, W
 
@@ -303,6 +372,8 @@ class ModelEvaluator:
         a.x_dot, a.alpha, a.beta, a.t = _ptr(x_dot), alpha, beta, t
         a.stats_device = _ptr(stats_device)
         a.x_pred, a.x_dot_coef = _ptr(x_pred), x_dot_coef
+        ids = np.array([bc.id for bc in self.neumann], dtype=np.int32)
+        a.n_neumann, a.neumann_ids = len(ids), _np_ptr(ids) if len(ids) else None
         lib = self.dof.lib
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_solve_cg_ir(self.dof.h, C.byref(a)), "tx_solve_cg_ir")
