@@ -294,6 +294,19 @@ typedef struct tx_solve_args {
 } tx_solve_args;
 int tx_solve_cg_ir(tx_handle h, tx_solve_args* args);
 
+/* ------------------------------------------------------------ CUDA graphs
+ * Record the handle's stream work into an executable CUDA graph owned by the
+ * handle and replay it: one time step or one Newton step (tx_eval,
+ * tx_neumann_eval, tx_dirichlet_apply, tx_spmv, and tx_solve_cg_ir with
+ * TX_SOLVE_FIXED_ITERATIONS after one uncaptured call) becomes one launch.
+ * Between begin and end only launch-only calls are legal; the captured
+ * calls' pointers and scalars are frozen into the graph.  The stream must be
+ * a non-default stream (tx_set_stream). */
+int tx_graph_capture_begin(tx_handle h);
+int tx_graph_capture_end(tx_handle h, int32_t* graph_id);
+int tx_graph_launch(tx_handle h, int32_t graph_id);
+int tx_graph_destroy(tx_handle h, int32_t graph_id);
+
 /* Worksets (WorksetContainer::setWorksetSize, disc-fe/src/Panzer_WorksetContainer.hpp:104)
  * of the TX_EVAL_PERSISTENT evaluation: consecutive element ranges of every
  * block with sizes drawn uniformly in [min_size, max_size] from seed

@@ -164,3 +164,24 @@ def test_neumann_argument_errors(cuda):
     with pytest.raises(tx.TxError) as e:
         tx.NeumannBC(dof, A.SIDE_XMIN, "U", "TimeTable", times=[0.0, 0.0], values=[1.0, 2.0])
     assert e.value.code == A.TX_EINVAL
+
+
+def test_captured_eval_model_step_replays(cuda):
+    # tx_graph_capture_begin/end around zeroing + volume fill + flux + Dirichlet;
+    # replays after x changes in place equal direct evaluations.
+    c = CASES["elasticity_traction_hex8"]
+    o, dof, lof = _setup(c)
+    me = tx.ModelEvaluator(lof, [tx.DirichletBC(dof, A.SIDE_ZMIN)], [tx.NeumannBC(dof, A.SIDE_ZMAX, "UZ", value=0.3)])
+    x = lof.getTpetraVector()
+    f, W = lof.getTpetraVector(), me.create_W_op()
+    me.evalModel(x, f=f, W=W, mixed=True)  # first launches set kernel attributes outside the capture
+    g = tx.CapturedGraph(dof, lambda: me.evalModel(x, f=f, W=W, mixed=True))
+    f2, W2 = lof.getTpetraVector(), me.create_W_op()
+    gen = torch.Generator(device="cuda").manual_seed(4)
+    for _ in range(3):
+        x.copy_(torch.rand(x.shape, dtype=torch.float64, device="cuda", generator=gen) * 0.01)
+        g.launch()
+        me.evalModel(x, f=f2, W=W2, mixed=True)
+        torch.cuda.synchronize()
+        assert float((f - f2).abs().max()) <= 1e-12 * float(f2.abs().max())
+        assert float((W.values - W2.values).abs().max()) <= 1e-12 * float(W2.values.abs().max())

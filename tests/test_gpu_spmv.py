@@ -1,11 +1,11 @@
 """CRS SpMV (Tpetra::CrsMatrix::apply) on graphs of every row-length class.
 
 Without a tuned shape the kernel picks the lanes per row from the mean row
-length: Poisson tet4 (about 11 entries a row) 4 lanes, Poisson hex8 (about
-23) 8 lanes, heat on hex27 + tet10 (about 60; vertex rows of 125 take
-several passes) and elasticity hex8 (about 69) 16 lanes.  A random CSR
-matrix with empty and long rows covers the shape used when the mean is
-unknown, and every tunable shape is checked on two graphs.  Bars: FP64
+length: Poisson tet4 (about 11 entries a row) 4 lanes; Poisson hex8 (about
+23), heat on hex27 + tet10 (about 60; vertex rows of 125 take several
+passes) and elasticity hex8 (about 69) 8 lanes.  A random CSR matrix with
+empty and long rows covers the shape used when the mean is unknown, and
+every tunable shape is checked on two graphs.  Bars: FP64
 within 1e-13 relative (reassociated sums), FP32 within 1e-5.
 """
 import ctypes as C

@@ -111,6 +111,8 @@ struct tx_handle_s {
   Staging stage;
   std::vector<NeumannSet> neumann;
   tx::SpmvShape spmv;  // SpMV launch shape ({0, 0}: automatic)
+  std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
+  bool capturing = false;
 
   void free_dofs() {
     for (auto& ns : neumann) { cudaFree(ns.sides); cudaFree(ns.tables); }
@@ -131,6 +133,8 @@ struct tx_handle_s {
     have_host_dofs = false;
   }
   ~tx_handle_s() {
+    for (auto g : graphs)
+      if (g) cudaGraphExecDestroy(g);
     free_dofs();
     cudaFree(d_coords);
   }
@@ -649,6 +653,53 @@ int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t se
   if (min_size < 1 || max_size < min_size) return fail(h, TX_EINVAL, "tx_set_worksets: need 1 <= min <= max");
   h->ws_min = min_size; h->ws_max = max_size; h->ws_seed = seed;
   h->items.clear();  // rebuilt at the next persistent evaluation
+  return TX_OK;
+}
+
+int tx_graph_capture_begin(tx_handle h) {
+  if (!h) return TX_EINVAL;
+  if (h->capturing) return fail(h, TX_ESTATE, "tx_graph_capture_begin: a capture is open");
+  if (!h->stream) return fail(h, TX_EINVAL, "tx_graph_capture_begin: set a non-default stream first");
+  cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_graph_capture_begin: ") + cudaGetErrorString(e));
+  h->capturing = true;
+  return TX_OK;
+}
+
+int tx_graph_capture_end(tx_handle h, int32_t* graph_id) {
+  if (!h || !graph_id) return TX_EINVAL;
+  if (!h->capturing) return fail(h, TX_ESTATE, "tx_graph_capture_end: no capture is open");
+  h->capturing = false;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(h, TX_ECUDA, std::string("tx_graph_capture_end: ") + cudaGetErrorString(e));
+  }
+  cudaGraphExec_t x = nullptr;
+  e = cudaGraphInstantiate(&x, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_graph_capture_end: ") + cudaGetErrorString(e));
+  h->graphs.push_back(x);
+  *graph_id = (int32_t)h->graphs.size() - 1;
+  return TX_OK;
+}
+
+int tx_graph_launch(tx_handle h, int32_t graph_id) {
+  if (!h) return TX_EINVAL;
+  if (graph_id < 0 || graph_id >= (int32_t)h->graphs.size() || !h->graphs[graph_id])
+    return fail(h, TX_ERANGE, "tx_graph_launch: unknown graph");
+  cudaError_t e = cudaGraphLaunch(h->graphs[graph_id], h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_graph_launch: ") + cudaGetErrorString(e));
+  return TX_OK;
+}
+
+int tx_graph_destroy(tx_handle h, int32_t graph_id) {
+  if (!h) return TX_EINVAL;
+  if (graph_id < 0 || graph_id >= (int32_t)h->graphs.size() || !h->graphs[graph_id])
+    return fail(h, TX_ERANGE, "tx_graph_destroy: unknown graph");
+  cudaGraphExecDestroy(h->graphs[graph_id]);
+  h->graphs[graph_id] = nullptr;
   return TX_OK;
 }
 

@@ -136,14 +136,17 @@ __device__ __forceinline__ void accumulate(double* p, double v) {
 // Exact IEEE-754 binary32 -> binary64 widening with integer operations:
 // exponent rebiased by 1023 - 127 = 896, 23-bit fraction moved to the top of
 // the 52-bit fraction.  Keeps the mixed kernel's output conversions off the
-// FP64 pipe (a small fraction of the FP32 rate on this part).  One unsigned
-// compare of |v| - 2^-126 against the normal range sends zeros, subnormals,
-// infinities and NaNs to the ordinary conversion; for the rest, |v| >> 3
-// puts exponent and fraction in place and adding 896 << 20 rebiases.
+// FP64 pipe (a small fraction of the FP32 rate on this part): |v| >> 3 puts
+// exponent and fraction in place and adding 896 << 20 rebiases; zeros keep
+// their sign.  Subnormals, infinities and NaNs (one unsigned compare of
+// |v| - 2^-126 against the normal range) call the ordinary conversion out of
+// line, so the compiler cannot if-convert it into every conversion.
+__device__ __noinline__ double widen_rare(float v) { return (double)v; }
 __device__ __forceinline__ double widen(float v) {
   const uint32_t b = __float_as_uint(v);
   const uint32_t a = b & 0x7fffffffu;
-  if (a - 0x00800000u >= 0x7f000000u) return (double)v;
+  if (a == 0u) return __hiloint2double((int)b, 0);
+  if (a - 0x00800000u >= 0x7f000000u) return widen_rare(v);
   const uint32_t hi = (b & 0x80000000u) | ((a >> 3) + 0x38000000u);
   return __hiloint2double((int)hi, (int)(b << 29));
 }
@@ -152,13 +155,15 @@ __device__ __forceinline__ double widen(double v) { return v; }
 // Exact IEEE-754 binary64 -> binary32 rounding to nearest, ties to even, with
 // integer operations: the 29 dropped fraction bits decide the round-up, whose
 // carry runs into the exponent.  Zero is exact; results that would be
-// subnormal, overflow, infinities and NaNs take the ordinary conversion.
+// subnormal, overflow, infinities and NaNs call the ordinary conversion out
+// of line (kept off the common path, as in widen).
+__device__ __noinline__ float narrow_rare(double v) { return (float)v; }
 __device__ __forceinline__ float narrow(double v) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const uint32_t hi = (uint32_t)(b >> 32);
   if ((b << 1) == 0ull) return __uint_as_float(hi & 0x80000000u);
   const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // rebias 1023 -> 127
-  if (e <= 0 || e >= 255) return (float)v;
+  if (e <= 0 || e >= 255) return narrow_rare(v);
   uint32_t m = (uint32_t)((b & 0xFFFFFFFFFFFFFull) >> 29);
   const uint32_t rest = (uint32_t)(b & 0x1FFFFFFFull);
   m += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;

@@ -380,6 +380,39 @@ class ModelEvaluator:
         return {"outer": int(a.stats[0]), "inner": int(a.stats[1]), "relres": a.stats[2], "r0": a.stats[3]}
 
 
+class CapturedGraph:
+    """fn()'s library work recorded into a CUDA graph owned by the handle (tx_graph_capture_begin/end) and
+    replayed by launch().  fn may only make launch-only calls (evalModel, NeumannBC.evaluate, apply,
+    solve(fixed=True) after one uncaptured solve) and in-place tensor ops; their pointers are frozen."""
+
+    def __init__(self, dof, fn):
+        self.dof, self.id = dof, None
+        self.stream = torch.cuda.Stream()
+        self.stream.wait_stream(torch.cuda.current_stream())
+        lib, gid = dof.lib, C.c_int32(-1)
+        with torch.cuda.stream(self.stream):
+            lib.tx_set_stream(dof.h, C.c_void_p(self.stream.cuda_stream))
+            check(dof.h, lib.tx_graph_capture_begin(dof.h), "tx_graph_capture_begin")
+            try:
+                fn()
+            finally:
+                rc = lib.tx_graph_capture_end(dof.h, C.byref(gid))
+            check(dof.h, rc, "tx_graph_capture_end")
+        self.id = gid.value
+
+    def launch(self):
+        lib = self.dof.lib
+        self.stream.wait_stream(torch.cuda.current_stream())
+        lib.tx_set_stream(self.dof.h, C.c_void_p(self.stream.cuda_stream))
+        check(self.dof.h, lib.tx_graph_launch(self.dof.h, self.id), "tx_graph_launch")
+        torch.cuda.current_stream().wait_stream(self.stream)
+
+    def __del__(self):
+        if self.id is not None:
+            self.dof.lib.tx_graph_destroy(self.dof.h, self.id)
+            self.id = None
+
+
 class Batch:
     """Many independent meshes (DOFManagers) evaluated by one persistent launch."""
 
