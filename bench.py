@@ -43,6 +43,8 @@ def args():
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
+    p.add_argument("--spmv-shape", default=None,
+                   help="LANES,UNROLL for both SpMV legs instead of autotuning them (e.g. 8,1)")
     return p.parse_args()
 
 
@@ -279,9 +281,15 @@ def run_ours(a):
 
     reps = max(10, a.steps)
     # launch shapes (lanes per row x loads per lane): the autotuner times all twelve per precision
-    sh64 = autotune.tune_spmv(W, W.values, xs, ys)
+    if a.spmv_shape:
+        fixed = tuple(int(v) for v in a.spmv_shape.split(","))
+        W.setApplyShape(*fixed)
+        sh64 = sh32 = {"shape": fixed, "candidates": []}
+    else:
+        sh64 = autotune.tune_spmv(W, W.values, xs, ys)
     t_s64 = time_spmv(W.values, xs, ys, reps)
-    sh32 = autotune.tune_spmv(W, v32, xs32, ys32)
+    if not a.spmv_shape:
+        sh32 = autotune.tune_spmv(W, v32, xs32, ys32)
     t_s32 = time_spmv(v32, xs32, ys32, reps)  # the FP32 shape stays set for the solver's inner SpMV
     b64 = 12 * nnz + 8 * (N + 1) + 16 * N
     b32 = 8 * nnz + 8 * (N + 1) + 8 * N
