@@ -242,6 +242,38 @@ int tx_neumann_create(tx_handle h, const tx_neumann_desc* d, int32_t* id, int64_
 /* f += the set's flux at time t (f DEVICE, LID order).  Launch only. */
 int tx_neumann_eval(tx_handle h, int32_t id, double t, double* f);
 
+/* ------------------------------------------------------------ responses
+ * Integral responses over element blocks: value = sum over cells and
+ * cubature points of integrand(q) * w_q * |det J_q| (TianXin::Response_Integral,
+ * disc-fe/src/responses/TianXin_Response_Integral_impl.hpp:106-130; the
+ * weighted measure of IntegrationValues2), and for the Jacobian evaluation
+ * type the gradient dvalue/dx at the field's LIDs, as panzer's functional
+ * response scatters it (disc-fe/src/responses/
+ * Panzer_ResponseScatterEvaluator_Functional_impl.hpp:143-171; TianXin's own
+ * Response_Integral<Jacobian> sums a placeholder constant instead, :186-200).
+ * The error integrands are the Poisson example's "L2 Error" / "H1 Error"
+ * functionals (adapters-stk/example/PoissonExample/main.cpp:269-295,
+ * Example_ClosureModel_Factory_impl.hpp:147-230) against the manufactured
+ * solution of TX_SOURCE_SINE, u* = sin(pi x) sin(pi y) sin(pi z) (the 3-D
+ * form of Example_SimpleSolution_impl.hpp:98-100). */
+enum tx_integrand {
+  TX_INTEGRAND_FIELD = 1,     /* u_field(q)                                          */
+  TX_INTEGRAND_L2_ERROR = 2,  /* (u(q) - u*(q))^2                                    */
+  TX_INTEGRAND_H1_ERROR = 3   /* (u(q) - u*(q))^2 + |grad u(q) - grad u*(q)|^2        */
+};
+typedef struct tx_response_desc {
+  int32_t block;           /* element block, -1: every block                          */
+  int32_t field;           /* DOF field number (HGRAD blocks)                         */
+  int32_t integrand;       /* tx_integrand                                            */
+  int32_t cubature_degree; /* <= 0: each block's integration order; hex up to 7, tet 2 */
+} tx_response_desc;
+/* Build the response (per-block cubature tables; allocates). */
+int tx_response_create(tx_handle h, const tx_response_desc* d, int32_t* id);
+/* *value (DEVICE double) = the integral at x, summed in a fixed order (the
+ * same bits on every call); dvalue_dx (DEVICE [N], may be NULL) += its
+ * gradient.  Launch only. */
+int tx_response_eval(tx_handle h, int32_t id, const double* x, double* value, double* dvalue_dx);
+
 /* y = alpha*A*x + beta*y over a Tpetra-layout CRS (CrsMatrix::apply).
  * vals/x/y are FP64 (TX_SPMV_F64) or FP32 (TX_SPMV_F32). */
 #define TX_SPMV_F64 0

@@ -59,6 +59,7 @@ def lib():
         L.orc_dirichlet_dofs.restype = I64
         L.orc_dirichlet_dofs.argtypes = [P, C.c_uint32, C.c_uint32, P]
         L.orc_dirichlet_apply.argtypes = [P, I64, P, P, P, P, P]
+        L.orc_response.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P]
         L.orc_neumann.restype = I64
         L.orc_neumann.argtypes = [P, C.c_int, C.c_uint32, C.c_int, D, P]
         L.orc_spmv.argtypes = [I64, P, P, P, P, P, D, D]
@@ -186,6 +187,22 @@ class Oracle:
         if n < 0:
             raise RuntimeError("oracle neumann failed")
         return f, int(n)
+
+
+def _response_impl(self, integrand, field=0, block=-1, degree=0, x=None, gradient=False):
+    """Integral response at x: "Field", "L2 Error" or "H1 Error" (against sin(pi x) sin(pi y) sin(pi z));
+    returns value, or (value, dvalue/dx) with gradient=True."""
+    kind = {"Field": _abi.TX_INTEGRAND_FIELD, "L2 Error": _abi.TX_INTEGRAND_L2_ERROR,
+            "H1 Error": _abi.TX_INTEGRAND_H1_ERROR}[integrand]
+    x = np.ascontiguousarray(x, np.float64)
+    val = C.c_double()
+    g = np.zeros(self.n_dofs) if gradient else None
+    if lib().orc_response(self.h, block, field, kind, degree, _p(x), C.byref(val), _p(g)):
+        raise RuntimeError("oracle response failed")
+    return (val.value, g) if gradient else val.value
+
+
+Oracle.response = _response_impl
 
 
 def workset_functor(value_type, value=0.0, times=None, values=None, t=0.0):

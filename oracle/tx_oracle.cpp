@@ -26,6 +26,12 @@
 //   * Dirichlet: f = x - g, Jacobian row -> unit row
 //       disc-fe/src/evaluators/TianXin_Dirichlet_impl.hpp:55-81,
 //       disc-fe/src/lof/Panzer_TpetraLinearObjContainer.hpp:228-238,306-318
+//   * Integral responses: sum of integrand * weighted measure over a block
+//     (TianXin Response_Integral, disc-fe/src/responses/
+//     TianXin_Response_Integral_impl.hpp:106-130) and its gradient (panzer
+//     functional, Panzer_ResponseScatterEvaluator_Functional_impl.hpp:143-171);
+//     L2/H1 error integrands of adapters-stk/example/PoissonExample/
+//     Example_ClosureModel_Factory_impl.hpp:147-230 for u* = sin sin sin
 //   * Neumann flux: residual(cell, b) += val * N_b * w * |face normal| on the
 //     side workset of a block (TianXin::Flux, disc-fe/src/evaluators/
 //     TianXin_Neumann_impl.hpp:146-166; side worksets adapters-stk/src/
@@ -1103,6 +1109,77 @@ static int64_t neumann_flux(const Problem& P, int blk, uint32_t side_mask, int f
   return count;
 }
 
+// ------------------------------------------------------------ responses
+// value += sum over the cells of block blk (all blocks: blk < 0) of
+// sum_q integrand(q) * wdet(q); dgdx (optional) += d value / d x.
+static void response_integral(const Problem& P, int blk_sel, int field, int integrand, int degree, const double* x,
+                              double* value, double* dgdx) {
+  const Topology& T = P.T;
+  const DofManager& D = P.D;
+  const double pi = 3.14159265358979323846;
+  double total = 0.0;
+  for (int blk = 0; blk < T.nblocks; ++blk) {
+    if (blk_sel >= 0 && blk != blk_sel) continue;
+    const BasisDef& B = D.block_basis[blk];
+    if (B.hcurl) throw std::runtime_error("response: scalar basis only");
+    const int topo = T.block_topo[blk];
+    const Cubature C = make_cubature(topo, degree > 0 ? degree : D.block_degree[blk]);
+    const int nv = topo == TX_TOPO_HEX ? 8 : 4;
+    std::vector<double> X(3 * nv), N(B.nb), dN(3 * B.nb);
+    ElemGeom g;
+    for (LO e : T.block_elems[blk]) {
+      T.elem_vertices(e, nv, X.data());
+      compute_geometry(topo, X.data(), C, g);
+      std::vector<double> ub(B.nb), grad_e(B.nb, 0.0);
+      std::vector<LO> lid(B.nb);
+      for (int b = 0; b < B.nb; ++b) {
+        lid[b] = D.elementLIDs[e][D.offsets[blk][field][b]];
+        ub[b] = x[lid[b]];
+      }
+      double cell = 0.0;
+      for (int q = 0; q < C.np; ++q) {
+        eval_hgrad(B, &C.xi[3 * q], N.data(), (double(*)[3])dN.data());
+        const double* Ji = &g.Jinv[9 * q];
+        double u = 0.0, gr[3] = {0, 0, 0};
+        for (int b = 0; b < B.nb; ++b) {
+          u += N[b] * ub[b];
+          for (int c = 0; c < 3; ++c) gr[c] += dN[3 * b + c] * ub[b];
+        }
+        double gu[3];
+        for (int i = 0; i < 3; ++i) gu[i] = Ji[i] * gr[0] + Ji[3 + i] * gr[1] + Ji[6 + i] * gr[2];
+        const double* xq = &g.ip[3 * q];
+        double ev = u, de[3] = {0, 0, 0};
+        if (integrand != TX_INTEGRAND_FIELD) {
+          const double sx = std::sin(pi * xq[0]), sy = std::sin(pi * xq[1]), sz = std::sin(pi * xq[2]);
+          ev = u - sx * sy * sz;
+          if (integrand == TX_INTEGRAND_H1_ERROR) {
+            de[0] = gu[0] - pi * std::cos(pi * xq[0]) * sy * sz;
+            de[1] = gu[1] - pi * sx * std::cos(pi * xq[1]) * sz;
+            de[2] = gu[2] - pi * sx * sy * std::cos(pi * xq[2]);
+          }
+        }
+        double integ = integrand == TX_INTEGRAND_FIELD ? ev : ev * ev;
+        if (integrand == TX_INTEGRAND_H1_ERROR) integ += de[0] * de[0] + de[1] * de[1] + de[2] * de[2];
+        const double wm = g.wdet[q];
+        cell += integ * wm;
+        if (dgdx) {
+          for (int b = 0; b < B.nb; ++b) {
+            double t = integrand == TX_INTEGRAND_FIELD ? N[b] : 2.0 * ev * N[b];
+            if (integrand == TX_INTEGRAND_H1_ERROR)
+              for (int i = 0; i < 3; ++i)
+                t += 2.0 * de[i] * (Ji[i] * dN[3 * b] + Ji[3 + i] * dN[3 * b + 1] + Ji[6 + i] * dN[3 * b + 2]);
+            grad_e[b] += t * wm;
+          }
+        }
+      }
+      total += cell;
+      if (dgdx)
+        for (int b = 0; b < B.nb; ++b) dgdx[lid[b]] += grad_e[b];
+    }
+  }
+  *value = total;
+}
+
 }  // namespace orc
 
 // ====================================================================== C API
@@ -1355,6 +1432,17 @@ int orc_basis_eval(int topo, int basis, const double* xi, double* val, double* g
 int64_t orc_neumann(void* h, int blk, uint32_t side_mask, int field, double val, double* f) {
   try {
     return neumann_flux(*(Problem*)h, blk, side_mask, field, val, f);
+  } catch (std::exception&) {
+    return -1;
+  }
+}
+
+// *value = the integral response; dgdx (may be NULL) += its gradient.  0 or -1.
+int orc_response(void* h, int blk, int field, int integrand, int degree, const double* x, double* value,
+                 double* dgdx) {
+  try {
+    response_integral(*(Problem*)h, blk, field, integrand, degree, x, value, dgdx);
+    return 0;
   } catch (std::exception&) {
     return -1;
   }

@@ -209,3 +209,32 @@ def test_workset_functor_values():
     assert O.workset_functor("TimeTable", times=tt, values=tv, t=-1.0) == 2.0
     with pytest.raises(ValueError):
         O.workset_functor("TimeTable", times=tt, values=tv, t=3.5)
+
+
+# ---------------------------------------------------------------- responses
+@pytest.mark.parametrize("topo,basis", [(A.TX_TOPO_HEX, A.TX_HGRAD_C1), (A.TX_TOPO_HEX, A.TX_HGRAD_C2),
+                                        (A.TX_TOPO_TET, A.TX_HGRAD_C1), (A.TX_TOPO_TET, A.TX_HGRAD_C2)])
+def test_response_closed_forms_and_gradient(topo, basis):
+    # Every basis here reproduces linear fields on the jittered (trilinear or
+    # affine) cells, so the integral of x over the box is exact; the "Field"
+    # gradient sums to the volume; the error integrands are quadratic in x, so a
+    # central difference checks their gradients to rounding.
+    L = (1.5, 1.0, 0.75)
+    o = O.Oracle(A.mesh_desc(2, topology=topo, lengths=L, jitter=0.2, seed=3),
+                 A.equation_set(A.TX_PHYS_POISSON, basis, params=(1.0, 0.0, 0.0, 0.0)))
+    X = o.dof_coordinates()
+    vol = L[0] * L[1] * L[2]
+    v, g = o.response("Field", x=np.ones(o.n_dofs), gradient=True)
+    assert abs(v - vol) <= 1e-14 and abs(g.sum() - vol) <= 1e-13
+    assert abs(o.response("Field", x=X[:, 0].copy()) - vol * L[0] / 2) <= 1e-14
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, o.n_dofs)
+    for kind in ("L2 Error", "H1 Error"):
+        v, g = o.response(kind, x=x, gradient=True)
+        for i in rng.choice(o.n_dofs, 5, replace=False):
+            h = 1e-3
+            xp, xm = x.copy(), x.copy()
+            xp[i] += h
+            xm[i] -= h
+            fd = (o.response(kind, x=xp) - o.response(kind, x=xm)) / (2 * h)
+            assert abs(fd - g[i]) <= 1e-8 * max(1.0, abs(g[i])), (kind, i)

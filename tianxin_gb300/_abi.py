@@ -40,6 +40,10 @@ TX_SOLVE_MATRIX_FREE_RESIDUAL = 0x1
 TX_SOLVE_FIXED_ITERATIONS = 0x2
 TX_SOLVE_REUSE_OPERATOR = 0x4
 
+TX_INTEGRAND_FIELD = 1
+TX_INTEGRAND_L2_ERROR = 2
+TX_INTEGRAND_H1_ERROR = 3
+
 TX_VALUE_CONSTANT = 1
 TX_VALUE_LINEAR = 2
 TX_VALUE_TIME_TABLE = 3
@@ -96,6 +100,10 @@ class SolveArgs(C.Structure):
         ("x_pred", C.c_void_p), ("x_dot_coef", C.c_double),
         ("n_neumann", C.c_int32), ("neumann_ids", C.c_void_p),
     ]
+
+
+class ResponseDesc(C.Structure):
+    _fields_ = [("block", C.c_int32), ("field", C.c_int32), ("integrand", C.c_int32), ("cubature_degree", C.c_int32)]
 
 
 class NeumannDesc(C.Structure):

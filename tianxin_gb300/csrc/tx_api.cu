@@ -88,6 +88,16 @@ struct NeumannSet {
   int stride = 0, nqf = 0;
 };
 
+// One integral response: per-block cubature tables and the partial sums.
+struct ResponseSet {
+  tx_response_desc desc{};
+  std::vector<int> blocks, nq;     // blocks it covers and their point counts
+  std::vector<double*> tables;     // packed RefTables per covered block
+  std::vector<int64_t> offset;     // first partial of each covered block
+  double* partial = nullptr;
+  int64_t n_partial = 0;
+};
+
 struct tx_handle_s {
   tx::Mesh mesh;
   tx::Dofs dofs;
@@ -110,6 +120,7 @@ struct tx_handle_s {
   int* d_counter = nullptr;
   Staging stage;
   std::vector<NeumannSet> neumann;
+  std::vector<ResponseSet> responses;
   tx::SpmvShape spmv;  // SpMV launch shape ({0, 0}: automatic)
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
@@ -117,6 +128,11 @@ struct tx_handle_s {
   void free_dofs() {
     for (auto& ns : neumann) { cudaFree(ns.sides); cudaFree(ns.tables); }
     neumann.clear();
+    for (auto& rs : responses) {
+      for (double* t : rs.tables) cudaFree(t);
+      cudaFree(rs.partial);
+    }
+    responses.clear();
     for (auto& b : blocks) {
       cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
       cudaFree(b.color_perm);
@@ -653,6 +669,62 @@ int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t se
   if (min_size < 1 || max_size < min_size) return fail(h, TX_EINVAL, "tx_set_worksets: need 1 <= min <= max");
   h->ws_min = min_size; h->ws_max = max_size; h->ws_seed = seed;
   h->items.clear();  // rebuilt at the next persistent evaluation
+  return TX_OK;
+}
+
+int tx_response_create(tx_handle h, const tx_response_desc* d, int32_t* id) {
+  if (!h || !d || !id) return TX_EINVAL;
+  if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_response_create before tx_dof_build");
+  if (d->block < -1 || d->block >= h->mesh.nblocks) return fail(h, TX_ERANGE, "tx_response_create: block");
+  if (d->field < 0 || d->field >= h->dofs.nf) return fail(h, TX_ERANGE, "tx_response_create: field");
+  if (d->integrand < TX_INTEGRAND_FIELD || d->integrand > TX_INTEGRAND_H1_ERROR)
+    return fail(h, TX_EINVAL, "tx_response_create: integrand");
+  return guarded(h, [&]() {
+    ResponseSet rs;
+    rs.desc = *d;
+    try {
+      for (int b = 0; b < h->mesh.nblocks; ++b) {
+        if (d->block >= 0 && b != d->block) continue;
+        const tx::BlockDofs& B = h->dofs.blocks[b];
+        if (B.basis == TX_HCURL_I1) throw std::invalid_argument("tx_response_create: HGRAD blocks only");
+        const int deg = d->cubature_degree > 0 ? d->cubature_degree : B.degree;
+        tx::RefTables R = tx::make_ref_tables(B.topo, B.basis, deg);
+        if (R.nq > 64) throw std::invalid_argument("tx_response_create: at most 64 cubature points");
+        double* t = nullptr;
+        ck(upload(t, R.packed()), "upload response tables");
+        rs.tables.push_back(t);
+        rs.blocks.push_back(b);
+        rs.nq.push_back(R.nq);
+        rs.offset.push_back(rs.n_partial);
+        rs.n_partial += tx::response_grid((int64_t)h->mesh.block_elems[b].size());
+      }
+      ck(cudaMalloc((void**)&rs.partial, sizeof(double) * (rs.n_partial > 0 ? rs.n_partial : 1)), "alloc partials");
+      ck(cudaMemset(rs.partial, 0, sizeof(double) * (rs.n_partial > 0 ? rs.n_partial : 1)), "zero partials");
+    } catch (...) {
+      for (double* t : rs.tables) cudaFree(t);
+      cudaFree(rs.partial);
+      throw;
+    }
+    h->responses.push_back(rs);
+    *id = (int32_t)h->responses.size() - 1;
+    return TX_OK;
+  });
+}
+
+int tx_response_eval(tx_handle h, int32_t id, const double* x, double* value, double* dvalue_dx) {
+  if (!h || !x || !value) return TX_EINVAL;
+  if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_response_eval before tx_dof_build");
+  if (id < 0 || id >= (int32_t)h->responses.size()) return fail(h, TX_ERANGE, "tx_response_eval: unknown response");
+  const ResponseSet& rs = h->responses[id];
+  cudaError_t e = cudaSuccess;
+  for (size_t k = 0; k < rs.blocks.size() && e == cudaSuccess; ++k) {
+    tx::BlockView v = h->blocks[rs.blocks[k]].view();
+    v.ref = rs.tables[k];
+    e = tx::launch_response(v, rs.nq[k], h->d_coords, x, h->dofs.nf, rs.desc.field, rs.desc.integrand,
+                            rs.partial + rs.offset[k], dvalue_dx, h->stream);
+  }
+  if (e == cudaSuccess) e = tx::launch_response_sum(rs.partial, rs.n_partial, value, h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_response_eval: ") + cudaGetErrorString(e));
   return TX_OK;
 }
 

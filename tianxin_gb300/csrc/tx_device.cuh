@@ -64,6 +64,14 @@ struct SpmvShape {
   int lanes = 0, unroll = 0;
 };
 bool spmv_shape_valid(SpmvShape sh);
+// Integral responses: one launch per block writes response_grid(n_elem)
+// partial sums (and adds the gradient into dgdx when given); the sum kernel
+// adds n partials in order into *value.
+constexpr int kResponseCtas = 1024;
+int response_grid(int64_t n_elem);
+cudaError_t launch_response(const BlockView& B, int nq, const double* coords, const double* x, int nf, int field,
+                            int integrand, double* partial, double* dgdx, cudaStream_t s);
+cudaError_t launch_response_sum(const double* partial, int64_t n, double* value, cudaStream_t s);
 cudaError_t launch_spmv_f64(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* vals,
                             const double* x, double* y, double alpha, double beta, int64_t nnz_hint, cudaStream_t s,
                             SpmvShape shape = SpmvShape());

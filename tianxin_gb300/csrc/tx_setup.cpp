@@ -164,7 +164,15 @@ static void gauss_points(int n, double* p, double* w) {
     w[0] = w[2] = 5.0 / 9.0; w[1] = 8.0 / 9.0;
     return;
   }
-  throw std::runtime_error("gauss_points: unsupported order");
+  if (n == 4) {  // roots of P4: sqrt(3/7 -+ 2/7 sqrt(6/5)), weights (18 +- sqrt(30)) / 36
+    const double a = std::sqrt(3.0 / 7.0 + 2.0 / 7.0 * std::sqrt(1.2));
+    const double b = std::sqrt(3.0 / 7.0 - 2.0 / 7.0 * std::sqrt(1.2));
+    p[0] = a; p[1] = b; p[2] = -b; p[3] = -a;
+    w[0] = w[3] = (18.0 - std::sqrt(30.0)) / 36.0;
+    w[1] = w[2] = (18.0 + std::sqrt(30.0)) / 36.0;
+    return;
+  }
+  throw std::runtime_error("gauss_points: 1 to 4 points per direction (degree <= 7)");
 }
 
 std::vector<double> RefTables::packed() const {

@@ -380,6 +380,39 @@ class ModelEvaluator:
         return {"outer": int(a.stats[0]), "inner": int(a.stats[1]), "relres": a.stats[2], "r0": a.stats[3]}
 
 
+_INTEGRANDS = {"Field": _abi.TX_INTEGRAND_FIELD, "L2 Error": _abi.TX_INTEGRAND_L2_ERROR,
+               "H1 Error": _abi.TX_INTEGRAND_H1_ERROR}
+
+
+class Response:
+    """An integral response (TianXin Response_Integral / panzer Functional): "Field" integrates a DOF
+    field, "L2 Error" and "H1 Error" the Poisson example's error integrands against the manufactured
+    solution of TX_SOURCE_SINE.  evaluate() leaves the value in a device scalar and can add the
+    gradient (the Jacobian evaluation type); value() returns it on the host."""
+
+    def __init__(self, dof, integrand="Field", dof_name=None, block=-1, cubature_degree=0):
+        self.dof = dof
+        d = _abi.ResponseDesc()
+        d.block = block
+        d.field = dof.getFieldNum(dof_name) if dof_name is not None else 0
+        d.integrand = _INTEGRANDS[integrand] if isinstance(integrand, str) else int(integrand)
+        d.cubature_degree = cubature_degree
+        rid = C.c_int32()
+        check(dof.h, dof.lib.tx_response_create(dof.h, C.byref(d), C.byref(rid)), "tx_response_create")
+        self.id = rid.value
+        self.out = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def evaluate(self, x, dgdx=None):
+        lib = self.dof.lib
+        lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(self.dof.h, lib.tx_response_eval(self.dof.h, self.id, _ptr(x), _ptr(self.out), _ptr(dgdx)),
+              "tx_response_eval")
+        return self.out
+
+    def value(self, x):
+        return float(self.evaluate(x).item())
+
+
 class CapturedGraph:
     """fn()'s library work recorded into a CUDA graph owned by the handle (tx_graph_capture_begin/end) and
     replayed by launch().  fn may only make launch-only calls (evalModel, NeumannBC.evaluate, apply,
