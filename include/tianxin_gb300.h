@@ -125,6 +125,16 @@ enum tx_source {
 #define TX_EVAL_PERSISTENT 0x4u     /* every block's worksets in one persistent launch      */
 #define TX_EVAL_SCATTER_DIRECT 0x8u /* per-thread row reductions instead of the staged,
                                        row-coalesced CTA scatter (comparison / tuning)     */
+/* Tangent evaluation type (GatherSolution_Tpetra<Tangent> seeds the
+ * derivative slots from tangent vectors, Panzer_GatherSolution_Tpetra_impl.hpp:
+ * 336-389; ScatterResidual_Tpetra<Tangent> sums the derivative slots into the
+ * dfdp vectors and leaves f alone, Panzer_ScatterResidual_Tpetra_impl.hpp:
+ * 237-270): dfdp[i] += (beta dR/dx + alpha dR/dxdot) tangent[i] for
+ * i < n_tangent, without assembling the matrix.  beta = 1, alpha = 0 gives the
+ * dx/dp tangents; beta = 0, alpha = 1 those of x_dot.  FP64; f and crs_vals
+ * are not touched (pass NULL); not with PERSISTENT or MIXED. */
+#define TX_EVAL_TANGENT 0x10u
+#define TX_MAX_TANGENTS 4
 
 typedef struct tx_eval_args {
   const double* x;         /* solution, LID order (GED "... - X")                       */
@@ -137,6 +147,9 @@ typedef struct tx_eval_args {
   int64_t elem_begin;      /* workset range inside the block (block >= 0)               */
   int64_t elem_end;        /* -1: to the end of the block                               */
   uint32_t flags;          /* TX_EVAL_*                                                 */
+  const double* tangent;   /* TX_EVAL_TANGENT: n_tangent directions, [n_tangent][N]     */
+  double* dfdp;            /* TX_EVAL_TANGENT: [n_tangent][N], summed into              */
+  int32_t n_tangent;       /* 1 .. TX_MAX_TANGENTS                                      */
 } tx_eval_args;
 
 typedef struct tx_handle_s* tx_handle;

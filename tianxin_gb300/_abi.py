@@ -32,6 +32,8 @@ TX_EVAL_MIXED = 0x1
 TX_EVAL_DETERMINISTIC = 0x2
 TX_EVAL_PERSISTENT = 0x4
 TX_EVAL_SCATTER_DIRECT = 0x8
+TX_EVAL_TANGENT = 0x10
+TX_MAX_TANGENTS = 4
 
 TX_SPMV_F64 = 0
 TX_SPMV_F32 = 1
@@ -82,6 +84,7 @@ class EvalArgs(C.Structure):
         ("block", C.c_int32),
         ("elem_begin", C.c_int64), ("elem_end", C.c_int64),
         ("flags", C.c_uint32),
+        ("tangent", C.c_void_p), ("dfdp", C.c_void_p), ("n_tangent", C.c_int32),
     ]
 
 

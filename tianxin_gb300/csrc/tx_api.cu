@@ -186,6 +186,11 @@ tx::EvalParams make_params(tx_handle h, const tx_eval_args& a) {
   P.alpha = a.alpha; P.beta = a.beta; P.t = a.t;
   P.f = a.f; P.vals = a.crs_vals;
   P.rowptr = h->d_rowptr;
+  P.n = D.n_dofs;
+  if (a.flags & TX_EVAL_TANGENT) {
+    P.tan = a.tangent; P.dfdp = a.dfdp; P.ntan = a.n_tangent;
+    P.f = nullptr; P.vals = nullptr;
+  }
   P.physics = D.eq.physics;
   P.source_kind = D.eq.source_kind;
   for (int i = 0; i < 8; ++i) P.p[i] = D.eq.params[i];
@@ -245,6 +250,12 @@ int eval_blocks(tx_handle h, const tx_eval_args& a) {
   const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
   const bool det = (a.flags & TX_EVAL_DETERMINISTIC) != 0;
   const bool stage = (a.flags & TX_EVAL_SCATTER_DIRECT) == 0;
+  if (a.flags & TX_EVAL_TANGENT) {
+    if (!a.tangent || !a.dfdp || a.n_tangent < 1 || a.n_tangent > TX_MAX_TANGENTS)
+      return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_TANGENT needs tangent, dfdp and 1 <= n_tangent <= 4");
+    if (a.flags & (TX_EVAL_PERSISTENT | TX_EVAL_MIXED))
+      return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_TANGENT is an FP64 per-block evaluation");
+  }
   if ((a.flags & TX_EVAL_PERSISTENT) && !det) {
     if (a.block >= 0) return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_PERSISTENT evaluates every block (block = -1)");
     for (const auto& db : h->blocks)
@@ -969,6 +980,7 @@ extern "C" int tx_eval_noalloc(tx_handle h, const tx_eval_args* a) {
   if (!a->x) return fail(h, TX_EINVAL, "tx_eval_noalloc: x is required");
   if (a->block != -1) return fail(h, TX_EINVAL, "tx_eval_noalloc evaluates every block (block = -1)");
   if (a->flags & TX_EVAL_DETERMINISTIC) return fail(h, TX_EINVAL, "tx_eval_noalloc: no deterministic form");
+  if (a->flags & TX_EVAL_TANGENT) return fail(h, TX_EINVAL, "tx_eval_noalloc: no tangent form");
   if (h->dofs.eq.physics == TX_PHYS_MAXWELL && !a->aux && a->f)
     return fail(h, TX_EINVAL, "tx_eval_noalloc: MAXWELL needs the current density J in aux");
   const int nb = (int)h->blocks.size();

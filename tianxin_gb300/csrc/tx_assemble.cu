@@ -190,7 +190,7 @@ __device__ __forceinline__ Real source_at(int kind, double c, double s0, const d
 // the coloured (deterministic) scatter: no two elements processed by one
 // launch share a row, so plain read-modify-write is race free.
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, int THREADS,
-          bool STAGE = false>
+          bool STAGE = false, bool TAN = false>
 __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalParams& P, const int32_t* perm,
                                               int64_t e_lo, int64_t e_hi, int64_t grp0, int64_t grp_stride,
                                               unsigned char* smem) {
@@ -481,18 +481,35 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         if constexpr (JAC) {
           int64_t rp[NF];
           const uint8_t* ep = B.epos + (e * NB + a) * NB;
-          if constexpr (!STAGE) {
+          if constexpr (!STAGE && !TAN) {
 #pragma unroll
             for (int c = 0; c < NF; ++c) rp[c] = __ldg(P.rowptr + NF * la + c);
           }
+          // Tangent: the row's products with the tangent directions (GatherSolution<Tangent>
+          // seeds dx(i) from them; ScatterResidual<Tangent> sums dx(i) into dfdp_i)
+          double rt[TAN ? kMaxTangents : 1][TAN ? NF : 1];
+          if constexpr (TAN) {
+#pragma unroll
+            for (int i = 0; i < kMaxTangents; ++i)
+#pragma unroll
+              for (int c = 0; c < NF; ++c) rt[i][c] = 0.0;
+          }
+          int64_t eb = 0;  // entity of column basis b (tangent gather)
           // Jacobian entry (row a,c; column b,d): reduce now, or stage for the CTA-wide scatter
           auto put = [&](int c, int b, int d, int64_t pb, Real v) {
-            if constexpr (STAGE) kreg[c * NE + b * NF + d] = v;
-            else accumulate<ATOMIC>(P.vals + rp[c] + pb + d, widen(v));
+            if constexpr (TAN) {
+              for (int i = 0; i < P.ntan; ++i)
+                rt[i][c] += (double)v * __ldg(P.tan + (int64_t)i * P.n + NF * eb + d);
+            } else if constexpr (STAGE) {
+              kreg[c * NE + b * NF + d] = v;
+            } else {
+              accumulate<ATOMIC>(P.vals + rp[c] + pb + d, widen(v));
+            }
           };
 #pragma unroll(STAGE ? NB : 1)
           for (int b = 0; b < NB; ++b) {
-            const int64_t pb = STAGE ? 0 : (int64_t)NF * __ldg(ep + b);
+            const int64_t pb = (STAGE || TAN) ? 0 : (int64_t)NF * __ldg(ep + b);
+            if constexpr (TAN) eb = __ldg(B.dconn + e * NB + b);
             if constexpr (PHYS == TX_PHYS_POISSON) {
               const Real ca = beta * pr[0];
               const Real cm = beta * pr[1] + alpha * pr[2];
@@ -551,6 +568,11 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               }
               put(0, b, 0, pb, beta * (imu * kc + sig * kv));
             }
+          }
+          if constexpr (TAN) {
+            for (int i = 0; i < P.ntan; ++i)
+#pragma unroll
+              for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.dfdp + (int64_t)i * P.n + NF * la + c, rt[i][c]);
           }
         }
       }
@@ -623,21 +645,21 @@ constexpr int min_blocks() {
   return STAGE && sizeof(Real) == 4 ? 4 : 1;
 }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE>
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false>
 __global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>(), min_blocks<Real, STAGE>())
 k_assemble(const BlockView B, const EvalParams P, const int32_t* perm, int64_t e_lo, int64_t e_hi) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
-  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, T, STAGE>(B, P, perm, e_lo, e_hi, blockIdx.x, gridDim.x,
-                                                                    smem);
+  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, T, STAGE, TAN>(B, P, perm, e_lo, e_hi, blockIdx.x,
+                                                                         gridDim.x, smem);
 }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE>
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false>
 cudaError_t launch_one(const BlockView& B, const EvalParams& P, const int32_t* perm, int64_t e_lo, int64_t e_hi,
                        cudaStream_t s, int grid_cap) {
   constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
   using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, T, STAGE>;
-  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, STAGE>;
+  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, STAGE, TAN>;
   static int max_blocks_per_sm = -1;
   static int num_sms = 0;
   if (max_blocks_per_sm < 0) {
@@ -666,6 +688,10 @@ cudaError_t launch_prec(const BlockView& B, const EvalParams& P, bool mixed, con
   const bool jac = P.vals != nullptr;
   const bool st = stage && jac;
 #define TX_L(R, J, A, S) launch_one<TOPO, BASIS, NQ, PHYS, R, J, A, S>(B, P, perm, e_lo, e_hi, s, cap)
+  if (P.tan) {  // Tangent: FP64 rows, atomic dfdp sums
+    if (atomic) return launch_one<TOPO, BASIS, NQ, PHYS, double, true, true, false, true>(B, P, perm, e_lo, e_hi, s, cap);
+    return launch_one<TOPO, BASIS, NQ, PHYS, double, true, false, false, true>(B, P, perm, e_lo, e_hi, s, cap);
+  }
   if (st) {
     if (atomic) return mixed ? TX_L(float, true, true, true) : TX_L(double, true, true, true);
     return mixed ? TX_L(float, true, false, true) : TX_L(double, true, false, true);

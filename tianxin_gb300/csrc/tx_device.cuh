@@ -22,7 +22,13 @@ struct EvalParams {
   int physics, source_kind;
   double p[8];
   double lam, mu;            // Lame parameters from p[0] (E), p[1] (nu), computed in FP64 on the host
+  // Tangent evaluation: dfdp[i][:] += (beta dR/dx + alpha dR/dxdot) tan[i][:], i < ntan
+  const double* tan;         // [ntan][n] or nullptr
+  double* dfdp;              // [ntan][n]
+  int ntan;
+  int64_t n;                 // DOF count (the stride of tan and dfdp)
 };
+constexpr int kMaxTangents = 4;
 
 // Launch the fused gather -> geometry -> integrators -> scatter kernel for
 // elements [e_lo, e_hi) of one block (through perm when given).  atomic=false

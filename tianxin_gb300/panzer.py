@@ -307,6 +307,18 @@ class AssemblyEngine:
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_eval(self.dof.h, C.byref(a)), "tx_eval")
 
+    def evaluateTangent(self, x, tangent, dfdp, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, block=-1,
+                        workset=(0, -1), deterministic=False):
+        """Tangent evaluation type: dfdp[i] += (beta dR/dx + alpha dR/dxdot) tangent[i] for the rows of the
+        2-D tensors tangent and dfdp ([n_tangent, N], n_tangent <= 4); f and W are not touched."""
+        a = eval_args(x, x_dot, aux, alpha, beta, t, None, None, False, block, workset, deterministic)
+        a.flags |= _abi.TX_EVAL_TANGENT
+        a.tangent, a.dfdp, a.n_tangent = _ptr(tangent), _ptr(dfdp), int(tangent.shape[0])
+        lib = self.dof.lib
+        lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(self.dof.h, lib.tx_eval(self.dof.h, C.byref(a)), "tx_eval (Tangent)")
+        return dfdp
+
 
 class ModelEvaluator:
     """evalModel(inArgs{x, x_dot, alpha, beta, t}, outArgs{f, W}) on the device."""
