@@ -299,10 +299,14 @@ def run_ours(a):
     bytes_alg = algorithmic_bytes((n + 1) ** 3, N, nnz, E)
     achieved = bytes_alg / k_mixed / 1e9
     traffic = None
+    warp_kernel = tuned.get("variant") == 2
+    kernel_name = ("k_assemble_wpe<hex8,elasticity,f32,jac>" if warp_kernel
+                   else "k_assemble<hex8,elasticity,f32,jac>")
     tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf)).get("assemble_elasticity_hex8_mixed_bytes_per_launch_128")
+            traffic = json.load(open(tf)).get(("assemble_wpe" if warp_kernel else "assemble") +
+                                              "_elasticity_hex8_mixed_bytes_per_launch_128")
         except Exception:
             traffic = None
 
@@ -376,13 +380,14 @@ def run_ours(a):
                                              "f32": [(c, round(t, 3)) for c, t in sh32["candidates"]]}},
             "solve": solve,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_source": peak_kind, "kernel": "k_assemble<hex8,elasticity,f32,jac>",
+                         "traffic": traffic, "peak_source": peak_kind, "kernel": kernel_name,
                          "algorithmic_bytes_per_launch": bytes_alg},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": 2 * a.steps,
             "autotune": {"mixed": {k: v for k, v in tuned.items() if k != "candidates"},
-                         "mixed_candidates_ms": [(c.get("scatter_direct"), c.get("grid_cap"), round(c["ms"], 3))
+                         "mixed_candidates_ms": [(c.get("variant"), c.get("scatter_direct"), c.get("grid_cap"),
+                                                  round(c["ms"], 3))
                                                  for c in tuned.get("candidates", [])],
                          "fp64": {k: v for k, v in tuned64.items() if k != "candidates"}},
             "clocks": clk,

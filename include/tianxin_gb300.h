@@ -366,6 +366,15 @@ int tx_set_grid_cap(tx_handle h, int32_t max_ctas);
  * pass 1/2/4; (0, 0) picks the lanes from the mean row length.  The
  * autotuner's knob for the SpMV; results equal to rounding for every shape. */
 int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll);
+/* Assembly kernel of the per-block mixed evaluation: 0 automatic (the
+ * warp-per-element kernel where the element family has one, hex8 elasticity;
+ * the CTA-staged kernel elsewhere), 1 always the CTA-staged kernel, 2 the
+ * warp-per-element kernel where available.  Results agree to the FP32
+ * summation order; the autotuner's third knob. */
+#define TX_VARIANT_AUTO 0
+#define TX_VARIANT_CTA 1
+#define TX_VARIANT_WARP 2
+int tx_set_assembly_variant(tx_handle h, int32_t variant);
 
 /* Many independent meshes in one persistent launch: the volume fill of every
  * block of every handle, cut into worksets, is one work list.  args holds one

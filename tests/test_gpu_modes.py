@@ -95,3 +95,42 @@ def test_batch_of_meshes_one_launch(cuda):
     for i, (f_ref, v_ref) in enumerate(refs):
         assert rel(fs[i].cpu().numpy(), f_ref) <= FP64_TOL, i
         assert rel(Ws[i].values.cpu().numpy(), v_ref) <= FP64_TOL, i
+
+
+@pytest.mark.parametrize("jitter", [0.0, 0.2])
+def test_warp_per_element_kernel_matches_cta_kernel_and_oracle(cuda, jitter):
+    # TX_VARIANT_WARP (hex8 elasticity, mixed) against the CTA-staged kernel and
+    # the FP64 oracle, with a time-derivative vector (alpha mass term) and the
+    # residual-only form; several blocks and uneven block sizes.
+    o, dof, lof = build((5, 4, 3), (2, 1, 2), A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1, jitter=jitter)
+    rng = np.random.default_rng(9)
+    x, xd, aux = (rng.uniform(-0.2, 0.2, o.n_dofs) for _ in range(3))
+    f_ref, v_ref = o.evaluate(x, xd, alpha=0.5, beta=1.0)
+    ae = tx.AssemblyEngine(lof)
+    out = {}
+    for variant in (1, 2):
+        ae.setVariant(variant)
+        out[variant] = run(dof, lof, x, xd, aux, mixed=True)
+        assert rel(out[variant][0], f_ref) <= MIXED_TOL
+        assert rel(out[variant][1], v_ref) <= MIXED_TOL
+        # residual-only evaluation
+        f = lof.getTpetraVector()
+        dev = lambda a: torch.from_numpy(a).cuda()
+        ae.evaluate(dev(x), dev(xd), None, 0.5, 1.0, 0.0, f, None, True)
+        assert rel(f.cpu().numpy(), f_ref) <= MIXED_TOL
+    assert rel(out[2][1], out[1][1]) <= 1e-5
+    ae.setVariant(0)
+
+
+def test_warp_variant_falls_back_where_no_warp_kernel(cuda):
+    o, dof, lof = build((3, 3, 3), (1, 1, 1), A.TX_TOPO_TET, A.TX_PHYS_POISSON, A.TX_HGRAD_C1)
+    rng = np.random.default_rng(1)
+    x, xd, aux = (rng.uniform(-1, 1, o.n_dofs) for _ in range(3))
+    ae = tx.AssemblyEngine(lof)
+    ae.setVariant(2)
+    f2, v2 = run(dof, lof, x, xd, aux, mixed=True)
+    ae.setVariant(1)
+    f1, v1 = run(dof, lof, x, xd, aux, mixed=True)
+    assert rel(v2, v1) <= 1e-6 and rel(f2, f1) <= 1e-6
+    with pytest.raises(tx.TxError):
+        ae.setVariant(3)

@@ -74,11 +74,14 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                 t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, persistent=True), reps)
                 results.append(({"workset": ws, "grid_cap": 0}, t))
         else:
-            for direct in (False, True):
+            # kernel variant (warp per element / CTA-staged / CTA direct scatter) x CTA cap
+            kernels = [(2, False), (1, False), (1, True)] if mixed else [(1, False), (1, True)]
+            for variant, direct in kernels:
+                ae.setVariant(variant)
                 for cap in (0, sms * 2, sms * 4, sms * 8):
                     ae.setGridCap(cap)
                     t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, scatter_direct=direct), reps)
-                    results.append(({"scatter_direct": direct, "grid_cap": cap}, t))
+                    results.append(({"variant": variant, "scatter_direct": direct, "grid_cap": cap}, t))
         best = min(results, key=lambda r: r[1])
         cfg = dict(best[0], ms=best[1], candidates=[dict(c, ms=t) for c, t in results])
         cache[key] = cfg
@@ -87,6 +90,7 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
             for c, t in results:
                 print(f"  {c}: {t:.3f} ms")
     ae.setGridCap(cfg.get("grid_cap", 0))
+    ae.setVariant(cfg.get("variant", 0))
     ae.scatter_direct = bool(cfg.get("scatter_direct", False))
     if "workset" in cfg:
         ae.setWorksetSize(cfg["workset"], cfg["workset"])

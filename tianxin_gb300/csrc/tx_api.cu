@@ -122,6 +122,7 @@ struct tx_handle_s {
   std::vector<NeumannSet> neumann;
   std::vector<ResponseSet> responses;
   tx::SpmvShape spmv;  // SpMV launch shape ({0, 0}: automatic)
+  int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
 
@@ -274,7 +275,10 @@ int eval_blocks(tx_handle h, const tx_eval_args& a) {
       if (e0 < 0 || e1 > db.n_elem || e0 > e1) return fail(h, TX_ERANGE, "tx_eval: element range outside the block");
     }
     cudaError_t e = cudaSuccess;
-    if (!det) {
+    const bool wpe = !det && mixed && stage && h->variant != 1 && tx::wpe_supported(V, P);
+    if (wpe) {
+      e = tx::launch_assemble_wpe(V, P, e0, e1, h->stream, h->grid_cap);
+    } else if (!det) {
       e = tx::launch_assemble(V, P, mixed, nullptr, e0, e1, true, stage, h->stream, h->grid_cap);
     } else {
       if (e0 != 0 || e1 != db.n_elem)
@@ -783,6 +787,13 @@ int tx_graph_destroy(tx_handle h, int32_t graph_id) {
     return fail(h, TX_ERANGE, "tx_graph_destroy: unknown graph");
   cudaGraphExecDestroy(h->graphs[graph_id]);
   h->graphs[graph_id] = nullptr;
+  return TX_OK;
+}
+
+int tx_set_assembly_variant(tx_handle h, int32_t variant) {
+  if (!h) return TX_EINVAL;
+  if (variant < 0 || variant > 2) return fail(h, TX_EINVAL, "tx_set_assembly_variant: 0, 1 or 2");
+  h->variant = variant;
   return TX_OK;
 }
 

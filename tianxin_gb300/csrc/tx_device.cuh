@@ -70,6 +70,13 @@ struct SpmvShape {
   int lanes = 0, unroll = 0;
 };
 bool spmv_shape_valid(SpmvShape sh);
+// Warp-per-element mixed assembly (hex8 elasticity, FP32 element math, atomic
+// FP64 scatter): the same results as launch_assemble's staged FP32 kernel up to
+// the summation order.
+bool wpe_supported(const BlockView& B, const EvalParams& P);
+cudaError_t launch_assemble_wpe(const BlockView& B, const EvalParams& P, int64_t e_lo, int64_t e_hi, cudaStream_t s,
+                                int grid_cap);
+
 // Integral responses: one launch per block writes response_grid(n_elem)
 // partial sums (and adds the gradient into dgdx when given); the sum kernel
 // adds n partials in order into *value.

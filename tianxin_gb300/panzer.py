@@ -297,6 +297,10 @@ class AssemblyEngine:
     def setGridCap(self, max_ctas):
         check(self.dof.h, self.dof.lib.tx_set_grid_cap(self.dof.h, max_ctas), "tx_set_grid_cap")
 
+    def setVariant(self, variant):
+        """Assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element (hex8 elasticity, mixed)."""
+        check(self.dof.h, self.dof.lib.tx_set_assembly_variant(self.dof.h, variant), "tx_set_assembly_variant")
+
     def evaluate(self, x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False,
                  block=-1, workset=(0, -1), deterministic=False, persistent=False, scatter_direct=None):
         if scatter_direct is None:
