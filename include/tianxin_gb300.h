@@ -363,7 +363,9 @@ int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t se
 int tx_set_grid_cap(tx_handle h, int32_t max_ctas);
 /* Launch shape of this handle's CRS SpMV (tx_spmv, the solver's inner and
  * outer products): lanes per row 4/8/16/32 and entries each lane loads per
- * pass 1/2/4; (0, 0) picks the lanes from the mean row length.  The
+ * pass 1/2/4, or 16 for aligned 16-byte vector loads (2 FP64 / 4 FP32
+ * entries a load; unaligned arrays fall back to 1); (0, 0) picks the lanes
+ * from the mean row length.  The
  * autotuner's knob for the SpMV; results equal to rounding for every shape. */
 int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll);
 /* Assembly kernel of the per-block mixed evaluation: 0 automatic (the

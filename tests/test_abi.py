@@ -71,3 +71,4 @@ def test_spmv_shape_validation_needs_no_device():
     assert lib.tx_set_spmv_shape(conn.h, 0, 0) == 0
     assert lib.tx_set_spmv_shape(conn.h, 12, 2) == A.TX_EINVAL
     assert lib.tx_set_spmv_shape(conn.h, 8, 3) == A.TX_EINVAL
+    assert lib.tx_set_spmv_shape(conn.h, 8, 16) == 0

@@ -101,9 +101,40 @@ def test_spmv_every_launch_shape(cuda, name):
     W.values.copy_(torch.from_numpy(vals))
     y_ref = _csr_ref(W.rowptr.cpu().numpy(), W.colind.cpu().numpy(), vals, x)
     xd = torch.from_numpy(x).cuda()
+    x32 = xd.float()
+    v32 = W.values.float()
     for lanes in (4, 8, 16, 32):
-        for unroll in (1, 2, 4):
+        for unroll in (1, 2, 4, 16):  # 16: aligned 16-byte loads
             W.setApplyShape(lanes, unroll)
             y = W.apply(xd).cpu().numpy()
             assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max(), (lanes, unroll)
+            y32 = W.apply(x32, values=v32).cpu().numpy()
+            assert np.abs(y32 - y_ref).max() <= 1e-5 * np.abs(y_ref).max(), (lanes, unroll)
     W.setApplyShape(0, 0)
+
+
+def test_spmv_vector_shape_on_unaligned_arrays(cuda):
+    # values starting 8 bytes past a 16-byte boundary: the 16-byte form falls back to single loads
+    lib = _lib.load()
+    conn = tx.CartesianConnManager(2, 2, 2)
+    dof = tx.DOFManager(conn, A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 1.0)))
+    rng = np.random.default_rng(8)
+    n = 300
+    lens = rng.integers(0, 90, n)
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    ci = rng.integers(0, n, int(rp[-1])).astype(np.int32)
+    vals = rng.uniform(-1, 1, int(rp[-1]))
+    x = rng.uniform(-1, 1, n)
+    y_ref = _csr_ref(rp, ci, vals, x)
+    vbuf = torch.zeros(len(vals) + 1, dtype=torch.float64, device="cuda")
+    vbuf[1:] = torch.from_numpy(vals).cuda()
+    cbuf = torch.zeros(len(ci) + 1, dtype=torch.int32, device="cuda")
+    cbuf[1:] = torch.from_numpy(ci).cuda()
+    d_rp, d_x = torch.from_numpy(rp).cuda(), torch.from_numpy(x).cuda()
+    y = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lib.tx_set_stream(dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert lib.tx_set_spmv_shape(dof.h, 8, 16) == 0
+    rc = lib.tx_spmv(dof.h, A.TX_SPMV_F64, n, d_rp.data_ptr(), cbuf.data_ptr() + 4, vbuf.data_ptr() + 8,
+                     d_x.data_ptr(), y.data_ptr(), 1.0, 0.0)
+    assert rc == 0
+    assert np.abs(y.cpu().numpy() - y_ref).max() <= 1e-13 * np.abs(y_ref).max()

@@ -97,7 +97,7 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
     return cfg
 
 
-SPMV_SHAPES = [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2, 4)]
+SPMV_SHAPES = [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2, 4, 16)]  # 16: 16-byte loads
 
 
 def tune_spmv(W, vals, x, y, reps=5):

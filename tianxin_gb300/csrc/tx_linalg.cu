@@ -87,10 +87,46 @@ __global__ void k_dirichlet(int64_t n, const int32_t* __restrict__ lids, const d
 // streamed past L1/L2, x through the read-only path) before any x gather
 // issues, so a lane keeps 2U independent loads in flight.  Entries past the
 // row end read column 0 with value 0.
+// 16-byte chunks of values and column indices: 2 FP64 or 4 FP32 entries.
+template <typename T> struct Chunk;
+template <> struct Chunk<double> {
+  using V = double2; using I = int2; static constexpr int N = 2;
+  static __device__ __forceinline__ double at(const V& v, int t) { return t == 0 ? v.x : v.y; }
+  static __device__ __forceinline__ int at(const I& v, int t) { return t == 0 ? v.x : v.y; }
+};
+template <> struct Chunk<float> {
+  using V = float4; using I = int4; static constexpr int N = 4;
+  static __device__ __forceinline__ float at(const V& v, int t) { return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w; }
+  static __device__ __forceinline__ int at(const I& v, int t) { return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w; }
+};
+constexpr int kSpmvVector = 16;  // the shape's "unroll" value of the chunked form
+
 template <typename T, int LANES, int U>
 __device__ __forceinline__ T row_dot(int64_t b, int64_t e, int sub, const int32_t* __restrict__ col,
                                      const T* __restrict__ vals, const T* __restrict__ x) {
   T s = T(0);
+  if constexpr (U == kSpmvVector) {
+    // Chunked form: the 16-byte chunks lying wholly inside the row are read
+    // with one vector load of values and one of column indices per lane; the
+    // row's unaligned head and tail (fewer than N entries each) are read singly.
+    // Needs vals and col 16-byte / (4N)-byte aligned (checked by the caller).
+    using CH = Chunk<T>;
+    constexpr int N = CH::N;
+    const int64_t ja = (b + N - 1) / N, jb = e / N;  // whole chunks [ja, jb)
+    if (ja >= jb) {
+      for (int64_t k = b + sub; k < e; k += LANES) s += __ldcs(vals + k) * __ldg(x + __ldcs(col + k));
+      return s;
+    }
+    if (b + sub < ja * N) s += __ldcs(vals + b + sub) * __ldg(x + __ldcs(col + b + sub));
+    if (jb * N + sub < e) s += __ldcs(vals + jb * N + sub) * __ldg(x + __ldcs(col + jb * N + sub));
+    for (int64_t j = ja + sub; j < jb; j += LANES) {
+      const typename CH::V v = __ldcs(reinterpret_cast<const typename CH::V*>(vals) + j);
+      const typename CH::I c = __ldcs(reinterpret_cast<const typename CH::I*>(col) + j);
+#pragma unroll
+      for (int t = 0; t < N; ++t) s += CH::at(v, t) * __ldg(x + CH::at(c, t));
+    }
+    return s;
+  }
   for (int64_t k = b + sub; k < e; k += LANES * U) {
     T v[U];
     int32_t c[U];
@@ -141,6 +177,12 @@ SpmvShape resolve_shape(SpmvShape sh, int64_t n, int64_t nnz_hint, bool f32) {
   return sh;
 }
 
+// The chunked form reads values and column indices as aligned 16-byte vectors.
+template <typename T>
+bool chunk_aligned(const T* vals, const int32_t* col) {
+  return ((uintptr_t)vals % 16) == 0 && ((uintptr_t)col % (4 * Chunk<T>::N)) == 0;
+}
+
 // Calls F.template run<LANES, U>() for the shape's template arguments.
 template <typename F>
 cudaError_t with_shape(SpmvShape sh, F&& f) {
@@ -150,6 +192,7 @@ cudaError_t with_shape(SpmvShape sh, F&& f) {
   TX_SHAPE(8, 1) TX_SHAPE(8, 2) TX_SHAPE(8, 4)
   TX_SHAPE(16, 1) TX_SHAPE(16, 2) TX_SHAPE(16, 4)
   TX_SHAPE(32, 1) TX_SHAPE(32, 2) TX_SHAPE(32, 4)
+  TX_SHAPE(4, kSpmvVector) TX_SHAPE(8, kSpmvVector) TX_SHAPE(16, kSpmvVector) TX_SHAPE(32, kSpmvVector)
 #undef TX_SHAPE
   return cudaErrorInvalidValue;
 }
@@ -168,7 +211,9 @@ template <typename T>
 cudaError_t spmv_dispatch(int64_t n, const int64_t* rp, const int32_t* col, const T* vals, const T* x, T* y, T a,
                           T b, int64_t nnz_hint, cudaStream_t s, SpmvShape shape) {
   if (n <= 0) return cudaSuccess;
-  return with_shape(resolve_shape(shape, n, nnz_hint, sizeof(T) == 4), SpmvLaunch<T>{n, rp, col, vals, x, y, a, b, s});
+  SpmvShape sh = resolve_shape(shape, n, nnz_hint, sizeof(T) == 4);
+  if (sh.unroll == kSpmvVector && !chunk_aligned<T>(vals, col)) sh.unroll = 1;
+  return with_shape(sh, SpmvLaunch<T>{n, rp, col, vals, x, y, a, b, s});
 }
 
 // ------------------------------------------------------------ reductions
@@ -375,7 +420,7 @@ cudaError_t launch_dirichlet(int64_t n, const int32_t* lids, const double* g, co
 bool spmv_shape_valid(SpmvShape sh) {
   if (sh.lanes == 0 && sh.unroll == 0) return true;
   const bool l = sh.lanes == 4 || sh.lanes == 8 || sh.lanes == 16 || sh.lanes == 32;
-  const bool u = sh.unroll == 1 || sh.unroll == 2 || sh.unroll == 4;
+  const bool u = sh.unroll == 1 || sh.unroll == 2 || sh.unroll == 4 || sh.unroll == kSpmvVector;
   return l && u;
 }
 cudaError_t launch_spmv_f64(int64_t n, const int64_t* rp, const int32_t* col, const double* vals, const double* x,
@@ -475,7 +520,8 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     k_make_f32<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, rp, col, vals, w.mask, w.vals32, w.dinv);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: make_f32");
   }
-  const SpmvShape shape = resolve_shape(w.spmv, n, w.nnz, true);
+  SpmvShape shape = resolve_shape(w.spmv, n, w.nnz, true);
+  if (shape.unroll == kSpmvVector && !chunk_aligned<float>(w.vals32, col)) shape.unroll = 1;
   auto spmv_dot = [&]() { with_shape(shape, DotLaunch{n, rp, col, &w, gb, s}); };
   auto cg_iteration = [&]() {
     spmv_dot();
