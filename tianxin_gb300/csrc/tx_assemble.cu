@@ -141,15 +141,16 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
   // reference tables: [w | geo_val | geo_grad | val | grad] in FP64
   {
     const double* ref = B.ref;
-    for (int i = threadIdx.x; i < NQ; i += blockDim.x) r_w[i] = (Real)ref[i];
+    // FP32 copies by integer narrowing (off the FP64 pipe)
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) r_w[i] = to_real<Real>(ref[i]);
     ref += NQ;
     for (int i = threadIdx.x; i < NQ * NV; i += blockDim.x) r_geo_val[i] = ref[i];
     ref += NQ * NV;
-    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) r_geo_grad[i] = (Real)ref[i];
+    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) r_geo_grad[i] = to_real<Real>(ref[i]);
     ref += NQ * NV * 3;
-    for (int i = threadIdx.x; i < NQ * NB * C::NVAL; i += blockDim.x) r_val[i] = (Real)ref[i];
+    for (int i = threadIdx.x; i < NQ * NB * C::NVAL; i += blockDim.x) r_val[i] = to_real<Real>(ref[i]);
     ref += NQ * NB * C::NVAL;
-    for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) r_grad[i] = (Real)ref[i];
+    for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) r_grad[i] = to_real<Real>(ref[i]);
   }
 
   const int le = threadIdx.x / TPE;
@@ -176,9 +177,9 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
   // parameters in the element arithmetic's type, once per thread
   Real pr[8];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) pr[i] = (Real)P.p[i];
-  const Real lam = (Real)P.lam, mu = (Real)P.mu;
-  const Real beta = (Real)P.beta, alpha = (Real)P.alpha;
+  for (int i = 0; i < 8; ++i) pr[i] = to_real<Real>(P.p[i]);
+  const Real lam = to_real<Real>(P.lam), mu = to_real<Real>(P.mu);
+  const Real beta = to_real<Real>(P.beta), alpha = to_real<Real>(P.alpha);
   for (int64_t g0 = e_lo + grp0 * EPB; g0 < e_hi; g0 += grp_stride * EPB) {
     const int64_t ei = g0 + le;
     const bool valid = ei < e_hi;

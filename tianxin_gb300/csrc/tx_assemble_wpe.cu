@@ -31,6 +31,7 @@ constexpr int GQS = NB * 4 + 4;    // floats per point in the (grad N, N) table
 
 struct WarpSmem {
   float g[NQ * GQS];               // (gx, gy, gz, N) per point and basis
+  float wg[NQ * GQS];              // the same times the weighted measure
   float k[NE * KRS];               // staged element Jacobian rows
   float ji[NQ * 9];                // J^-1 per point
   float qf[NQ * 9];                // stress (6) and inertia minus body force (3)
@@ -57,20 +58,21 @@ k_assemble_wpe(const BlockView B, const EvalParams P, int64_t e_lo, int64_t e_hi
   __shared__ RefSmem ref;
   {
     const double* r = B.ref;  // [w | geo_val | geo_grad | val | grad]
-    for (int i = threadIdx.x; i < NQ; i += blockDim.x) ref.w[i] = (float)r[i];
+    // integer narrowing keeps these conversions off the FP64 pipe
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) ref.w[i] = narrow(r[i]);
     r += NQ + NQ * NV;
-    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) ref.geo_grad[i] = (float)r[i];
+    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) ref.geo_grad[i] = narrow(r[i]);
     r += NQ * NV * 3;
-    for (int i = threadIdx.x; i < NQ * NB; i += blockDim.x) ref.val[i] = (float)r[i];
+    for (int i = threadIdx.x; i < NQ * NB; i += blockDim.x) ref.val[i] = narrow(r[i]);
     r += NQ * NB;
-    for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) ref.grad[i] = (float)r[i];
+    for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) ref.grad[i] = narrow(r[i]);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   WarpSmem& S = wsm[threadIdx.x >> 5];
-  const float lam = (float)P.lam, mu = (float)P.mu, beta = (float)P.beta, alpha = (float)P.alpha;
-  const float rho = (float)P.p[5];
-  const float bf[3] = {(float)P.p[2], (float)P.p[3], (float)P.p[4]};
+  const float lam = narrow(P.lam), mu = narrow(P.mu), beta = narrow(P.beta), alpha = narrow(P.alpha);
+  const float rho = narrow(P.p[5]);
+  const float bf[3] = {narrow(P.p[2]), narrow(P.p[3]), narrow(P.p[4])};
   const int64_t stride = (int64_t)gridDim.x * kWarps;
   for (int64_t e = e_lo + (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); e < e_hi; e += stride) {
     // ------------------------------------------------------------ gather
@@ -121,8 +123,11 @@ k_assemble_wpe(const BlockView B, const EvalParams P, int64_t e_lo, int64_t e_hi
       const float* ji = S.ji + 9 * q;
       const float* gr = ref.grad + (q * NB + b) * 3;
       const float g0 = gr[0], g1 = gr[1], g2 = gr[2];
-      st4(S.g + q * GQS + b * 4, ji[0] * g0 + ji[3] * g1 + ji[6] * g2, ji[1] * g0 + ji[4] * g1 + ji[7] * g2,
-          ji[2] * g0 + ji[5] * g1 + ji[8] * g2, ref.val[q * NB + b]);
+      const float px = ji[0] * g0 + ji[3] * g1 + ji[6] * g2, py = ji[1] * g0 + ji[4] * g1 + ji[7] * g2;
+      const float pz = ji[2] * g0 + ji[5] * g1 + ji[8] * g2, nv = ref.val[q * NB + b];
+      const float wq = S.w[q];
+      st4(S.g + q * GQS + b * 4, px, py, pz, nv);
+      st4(S.wg + q * GQS + b * 4, wq * px, wq * py, wq * pz, wq * nv);
     }
     __syncwarp();
     // ------------------------------------------------------- point fluxes
@@ -164,10 +169,9 @@ k_assemble_wpe(const BlockView B, const EvalParams P, int64_t e_lo, int64_t e_hi
       float r = 0.0f;
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
-        const R4<float> ga = ld4(S.g + q * GQS + a * 4);
-        const float wq = S.w[q];
+        const R4<float> wa = ld4(S.wg + q * GQS + a * 4);
         const float* qf = S.qf + 9 * q;
-        r += wq * (ga.x * qf[i0] + ga.y * qf[i1] + ga.z * qf[i2] + ga.w * qf[6 + c]);
+        r += wa.x * qf[i0] + wa.y * qf[i1] + wa.z * qf[i2] + wa.w * qf[6 + c];
       }
       atomicAdd(P.f + (int64_t)NF * S.la[a] + c, widen(r));
     }
@@ -179,14 +183,12 @@ k_assemble_wpe(const BlockView B, const EvalParams P, int64_t e_lo, int64_t e_hi
         float Pm[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, M = 0.0f;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
-          const R4<float> ga = ld4(S.g + q * GQS + a * 4);
+          const R4<float> wa = ld4(S.wg + q * GQS + a * 4);
           const R4<float> gb = ld4(S.g + q * GQS + b * 4);
-          const float wq = S.w[q];
-          const float wa0 = wq * ga.x, wa1 = wq * ga.y, wa2 = wq * ga.z;
-          Pm[0] += wa0 * gb.x; Pm[1] += wa0 * gb.y; Pm[2] += wa0 * gb.z;
-          Pm[3] += wa1 * gb.x; Pm[4] += wa1 * gb.y; Pm[5] += wa1 * gb.z;
-          Pm[6] += wa2 * gb.x; Pm[7] += wa2 * gb.y; Pm[8] += wa2 * gb.z;
-          M += wq * ga.w * gb.w;
+          Pm[0] += wa.x * gb.x; Pm[1] += wa.x * gb.y; Pm[2] += wa.x * gb.z;
+          Pm[3] += wa.y * gb.x; Pm[4] += wa.y * gb.y; Pm[5] += wa.y * gb.z;
+          Pm[6] += wa.z * gb.x; Pm[7] += wa.z * gb.y; Pm[8] += wa.z * gb.z;
+          M += wa.w * gb.w;
         }
         const float trP = Pm[0] + Pm[4] + Pm[8];
         const float diag = beta * mu * trP + alpha * rho * M;
