@@ -68,11 +68,13 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
         sms = torch.cuda.get_device_properties(0).multi_processor_count
         results = []
         if persistent:
-            for ws in (128, 256, 512, 1024, 2048):
-                ae.setWorksetSize(ws, ws)
-                ae.setGridCap(0)
-                t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, persistent=True), reps)
-                results.append(({"workset": ws, "grid_cap": 0}, t))
+            ae.setGridCap(0)
+            for direct in (False, True):  # staged or per-thread Jacobian scatter
+                for ws in (128, 256, 512, 1024, 2048):
+                    ae.setWorksetSize(ws, ws)
+                    t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, persistent=True,
+                                                  scatter_direct=direct), reps)
+                    results.append(({"workset": ws, "grid_cap": 0, "scatter_direct": direct}, t))
         else:
             # kernel variant (warp per element / CTA-staged / CTA direct scatter) x CTA cap
             kernels = [(2, False), (1, False), (1, True)] if mixed else [(1, False), (1, True)]

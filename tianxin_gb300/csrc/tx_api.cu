@@ -215,6 +215,7 @@ void build_items(tx_handle h, std::vector<tx::WorkItem>& out, int view_base) {
 
 int eval_persistent(tx_handle h, const tx_eval_args& a) {
   const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
+  const bool stage = a.crs_vals != nullptr && (a.flags & TX_EVAL_SCATTER_DIRECT) == 0;
   if (h->items.empty()) {
     build_items(h, h->items, 0);
     cudaFree(h->d_items);
@@ -233,14 +234,14 @@ int eval_persistent(tx_handle h, const tx_eval_args& a) {
     tx::BlockView V = h->blocks[b].view();
     std::memcpy(&tab[b * sizeof(tx::BlockView)], &V, sizeof V);
     std::memcpy(&tab[nb * sizeof(tx::BlockView) + b * sizeof(tx::EvalParams)], &P, sizeof P);
-    smem = std::max(smem, tx::batched_smem_bytes(h->blocks[b].kind, mixed));
+    smem = std::max(smem, tx::batched_smem_bytes(h->blocks[b].kind, mixed, stage));
   }
   cudaError_t e = h->stage.put(tab.data(), tab.size(), h->stream);
   if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: staging ") + cudaGetErrorString(e));
   const tx::BlockView* dv = (const tx::BlockView*)h->stage.dev;
   const tx::EvalParams* dp = (const tx::EvalParams*)((unsigned char*)h->stage.dev + nb * sizeof(tx::BlockView));
   e = tx::launch_assemble_batched(dv, dp, h->d_items, (int)h->items.size(), h->d_counter, smem, mixed,
-                                  a.crs_vals != nullptr, h->grid_cap, h->stream);
+                                  a.crs_vals != nullptr, stage, h->grid_cap, h->stream);
   if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: ") + cudaGetErrorString(e));
   return TX_OK;
 }
@@ -871,6 +872,7 @@ int tx_batch_eval(tx_batch b, const tx_eval_args* args) {
   const int n = (int)b->hs.size();
   const bool mixed = (args[0].flags & TX_EVAL_MIXED) != 0;
   const bool jac = args[0].crs_vals != nullptr;
+  const bool stage = jac && (args[0].flags & TX_EVAL_SCATTER_DIRECT) == 0;
   for (int i = 0; i < n; ++i) {
     if (!args[i].x) { b->err = "tx_batch_eval: x is required for every instance"; return TX_EINVAL; }
     if (((args[i].flags & TX_EVAL_MIXED) != 0) != mixed || (args[i].crs_vals != nullptr) != jac) {
@@ -915,7 +917,7 @@ int tx_batch_eval(tx_batch b, const tx_eval_args* args) {
       tx::BlockView V = db.view();
       std::memcpy(&tab[v * sizeof(tx::BlockView)], &V, sizeof V);
       std::memcpy(&tab[nviews * sizeof(tx::BlockView) + v * sizeof(tx::EvalParams)], &P, sizeof P);
-      smem = std::max(smem, tx::batched_smem_bytes(db.kind, mixed));
+      smem = std::max(smem, tx::batched_smem_bytes(db.kind, mixed, stage));
       ++v;
     }
   }
@@ -924,7 +926,7 @@ int tx_batch_eval(tx_batch b, const tx_eval_args* args) {
     const tx::BlockView* dv = (const tx::BlockView*)b->stage.dev;
     const tx::EvalParams* dp = (const tx::EvalParams*)((unsigned char*)b->stage.dev + nviews * sizeof(tx::BlockView));
     e = tx::launch_assemble_batched(dv, dp, b->d_items, (int)b->items.size(), b->d_counter, smem, mixed, jac,
-                                    b->grid_cap, s);
+                                    stage, b->grid_cap, s);
   }
   if (e != cudaSuccess) {
     b->err = std::string("tx_batch_eval: ") + cudaGetErrorString(e);
@@ -1023,13 +1025,14 @@ extern "C" int tx_eval_noalloc(tx_handle h, const tx_eval_args* a) {
   // parameter tables from the stack (a pageable source is copied before the call returns)
   unsigned char tab[(sizeof(tx::BlockView) + sizeof(tx::EvalParams)) * TX_MAX_BLOCKS];
   const bool mixed = (a->flags & TX_EVAL_MIXED) != 0;
+  const bool stage = a->crs_vals != nullptr && (a->flags & TX_EVAL_SCATTER_DIRECT) == 0;
   tx::EvalParams P = make_params(h, *a);
   size_t smem = 0;
   for (int b = 0; b < nb; ++b) {
     tx::BlockView V = h->blocks[b].view();
     std::memcpy(tab + b * sizeof(tx::BlockView), &V, sizeof V);
     std::memcpy(tab + nb * sizeof(tx::BlockView) + b * sizeof(tx::EvalParams), &P, sizeof P);
-    smem = std::max(smem, tx::batched_smem_bytes(h->blocks[b].kind, mixed));
+    smem = std::max(smem, tx::batched_smem_bytes(h->blocks[b].kind, mixed, stage));
   }
   e = cudaMemcpyAsync(base + kNaViews, tab, nb * sizeof(tx::BlockView), cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess)
@@ -1043,7 +1046,7 @@ extern "C" int tx_eval_noalloc(tx_handle h, const tx_eval_args* a) {
   if (e == cudaSuccess)  // clears the counter, then one persistent launch
     e = tx::launch_assemble_batched((const tx::BlockView*)(base + kNaViews), (const tx::EvalParams*)(base + kNaParams),
                                     (const tx::WorkItem*)(base + kNaItems), (int)n_items, (int*)(base + kNaCounter),
-                                    smem, mixed, a->crs_vals != nullptr, h->grid_cap, h->stream);
+                                    smem, mixed, a->crs_vals != nullptr, stage, h->grid_cap, h->stream);
   if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval_noalloc: ") + cudaGetErrorString(e));
   return TX_OK;
 }

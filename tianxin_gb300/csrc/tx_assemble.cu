@@ -1,584 +1,13 @@
-// tx_assemble.cu -- fused volume assembly for one element block.
-//
-// One launch replaces the reference's per-workset evaluator chain
-// (AssemblyEngine::evaluateVolume, disc-fe/src/Panzer_AssemblyEngine_impl.hpp:
-// 134-182) for the Residual and Jacobian evaluation types:
-//   GatherSolution_Tpetra      x, x_dot -> element values (LID gather)
-//   IntegrationValues2         J, det J, J^-1, weighted measure
-//   BasisValues2               grad N = J^-T grad N^, H(curl) J^-T / J/det
-//   DOF / DOFGradient / DOFCurl values at the cubature points
-//   Integrator_GradBasisDotVector, Integrator_BasisTimesScalar,
-//   Integrator_CurlBasisDotVector (+ the mass terms on the time-derivative
-//   vector)
-//   ScatterResidual_Tpetra     f += r, A(row, cols) += dr/du
-// The reference obtains dr/du by forward-mode AD (seed beta on x and alpha on
-// x_dot in the same derivative slot); here the element matrices are the
-// closed forms of those derivatives, so W = beta dR/dx + alpha dR/dx_dot.
-//
-// Work decomposition: TPE threads (next power of two >= basis count) per
-// element, EPB elements per CTA, grid-stride over the block's elements.
-// Phase 1 gathers vertex coordinates and DOF values, phase 2 builds the
-// geometry and physical basis tables of each cubature point in shared
-// memory, phase 3 evaluates the point fluxes, phase 4 gives each thread one
-// basis function a: it forms residual row a and the Jacobian block-row
-// (a, :) and scatters them with FP64 reductions at
-//   rowptr[nf*entity(a)+c] + nf*epos[e][a][b] + d
-// where epos is the precomputed position of entity b in the sorted row of
-// entity a (the element-to-row map; no column search on the GPU).
-//
-// Real = double: the FP64 path.  Real = float (TX_EVAL_MIXED): element
-// geometry and contractions in FP32 (vertex coordinates are differenced in
-// FP64 first), accumulation into f and the CRS in FP64.
+// tx_assemble.cu -- per-block launches of the fused volume assembly
+// (tx_assemble_body.cuh): one launch per block or workset range, or one per
+// colour for the deterministic scatter; FP32 or FP64 element arithmetic,
+// Residual, Jacobian or Tangent evaluation type.
 #include <cstdio>
 
-#include "tx_device.cuh"
-#include "tx_numeric.cuh"
+#include "tx_assemble_body.cuh"
 
 namespace tx {
 namespace {
-
-constexpr int pow2ceil(int n) { return n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32; }
-
-template <int TOPO, int BASIS>
-struct Family;
-template <> struct Family<TX_TOPO_HEX, TX_HGRAD_C1> { static constexpr int NV = 8, NB = 8; };
-template <> struct Family<TX_TOPO_HEX, TX_HGRAD_C2> { static constexpr int NV = 8, NB = 27; };
-template <> struct Family<TX_TOPO_TET, TX_HGRAD_C1> { static constexpr int NV = 4, NB = 4; };
-template <> struct Family<TX_TOPO_TET, TX_HGRAD_C2> { static constexpr int NV = 4, NB = 10; };
-template <> struct Family<TX_TOPO_HEX, TX_HCURL_I1> { static constexpr int NV = 8, NB = 12; };
-
-constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
-
-// STAGE_: element residual/Jacobian staged in shared memory, then scattered
-// by the whole CTA with consecutive threads on consecutive entries of a CRS
-// row (few L2 sectors per warp reduction) instead of one row per thread.
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, int THREADS_ = (Family<TOPO, BASIS>::NB > 16 ? 128 : 256),
-          bool STAGE_ = false>
-struct Cfg {
-  static constexpr int NV = Family<TOPO, BASIS>::NV;
-  static constexpr int NB = Family<TOPO, BASIS>::NB;
-  static constexpr bool HC = BASIS == TX_HCURL_I1;
-  static constexpr int NF = PHYS == TX_PHYS_ELASTICITY ? 3 : 1;
-  static constexpr int TPE = pow2ceil(NB);
-  static constexpr int THREADS = THREADS_;
-  static constexpr int EPB = THREADS / TPE;
-  static constexpr int NQF = PHYS == TX_PHYS_ELASTICITY ? 9 : PHYS == TX_PHYS_HEAT ? 8 : PHYS == TX_PHYS_MAXWELL ? 6 : 4;
-  static constexpr int NVAL = HC ? 3 : 1;
-  // odd word strides: threads that write one row/point each spread over all banks
-  // sG/sV: per point q and basis b one 4-vector (x, y, z, N) at q * GQS + b * 4;
-  // GQS / 4 odd: the quarter-warp of a 128-bit access covers all banks
-  static constexpr int GQS = NB * 4 + 4;
-  static constexpr int NE_ = (PHYS == TX_PHYS_ELASTICITY ? 3 : 1) * NB;
-  static constexpr int KRS = NE_ | 1;       // sK:    [row * KRS + col]
-  // shared: reference part
-  static constexpr size_t R_GEO_GRAD = 0;
-  static constexpr size_t R_GEO_VAL = align16(R_GEO_GRAD + sizeof(Real) * NQ * NV * 3);
-  static constexpr size_t R_W = align16(R_GEO_VAL + sizeof(double) * NQ * NV);
-  static constexpr size_t R_VAL = align16(R_W + sizeof(Real) * NQ);
-  static constexpr size_t R_GRAD = align16(R_VAL + sizeof(Real) * NQ * NB * NVAL);
-  static constexpr size_t R_END = align16(R_GRAD + sizeof(Real) * NQ * NB * 3);
-  // shared: per element part
-  static constexpr bool XABS = PHYS == TX_PHYS_POISSON;                // sources need absolute coordinates
-  static constexpr size_t E_X = 0;                                      // vertex coordinates (FP64)
-  static constexpr size_t E_DX = align16(E_X + sizeof(double) * (XABS ? NV * 3 : 0));  // X[v] - X[0] (Real)
-  static constexpr size_t E_U = align16(E_DX + sizeof(Real) * NV * 3);
-  static constexpr size_t E_UD = align16(E_U + sizeof(Real) * NF * NB);
-  static constexpr size_t E_AUX = align16(E_UD + sizeof(Real) * NF * NB);
-  static constexpr size_t E_SG = align16(E_AUX + sizeof(Real) * (HC ? NB : 0));
-  static constexpr size_t E_G = align16(E_SG + sizeof(Real) * (HC ? NB : 0));
-  static constexpr size_t E_V = align16(E_G + sizeof(Real) * NQ * GQS);
-  static constexpr size_t E_W = align16(E_V + sizeof(Real) * (HC ? NQ * GQS : 0));
-  static constexpr size_t E_QF = align16(E_W + sizeof(Real) * NQ);
-  static constexpr size_t E_SIGN = align16(E_QF + sizeof(Real) * NQ * NQF);
-  static constexpr bool STAGE = STAGE_;
-  static constexpr int NE = NF * NB;  // element DOFs
-  // The staged Jacobian reuses the point tables (sG .. sSign): it is written
-  // from registers after every thread has finished reading them.
-  static constexpr size_t E_WORK_END = align16(E_SIGN + sizeof(Real));
-  static constexpr size_t E_K = E_G;
-  static constexpr size_t E_K_END = align16(E_K + sizeof(Real) * (STAGE ? NE * KRS : 0));
-  static constexpr size_t E_R = E_K_END > E_WORK_END ? E_K_END : E_WORK_END;
-  static constexpr size_t E_RP = align16(E_R + sizeof(Real) * (STAGE ? NE : 0));
-  static constexpr size_t E_LA = align16(E_RP + sizeof(int64_t) * (STAGE ? NE : 0));
-  static constexpr size_t E_EP = align16(E_LA + sizeof(int32_t) * (STAGE ? NB : 0));
-  // per-element stride = 32 B past a multiple of 128 B: the four elements of a
-  // warp start 8 banks apart, so same-offset accesses do not conflict
-  static constexpr size_t E_RAW = align16(E_EP + (STAGE ? NB * NB : 0));
-  static constexpr size_t E_END = ((E_RAW + 127 - 32) / 128) * 128 + 32;
-  static constexpr size_t SMEM = R_END + EPB * E_END;
-};
-
-
-template <typename Real>
-__device__ __forceinline__ Real source_at(int kind, double c, double s0, const double ip[3]) {
-  if (kind == TX_SOURCE_SINE) {
-    const double pi = 3.14159265358979323846;
-    return (Real)(3.0 * pi * pi * sin(pi * ip[0]) * sin(pi * ip[1]) * sin(pi * ip[2]));
-  }
-  if (kind == TX_SOURCE_AFFINE) return (Real)(c * (1.0 + ip[0] + 2.0 * ip[1] + 3.0 * ip[2]));
-  return (Real)s0;
-}
-
-// Elements [e_lo, e_hi) of a block (through perm if given), element groups
-// g = grp0, grp0 + grp_stride, ... of EPB elements each.  ATOMIC=false is
-// the coloured (deterministic) scatter: no two elements processed by one
-// launch share a row, so plain read-modify-write is race free.
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, int THREADS,
-          bool STAGE = false, bool TAN = false>
-__device__ __forceinline__ void assemble_body(const BlockView& B, const EvalParams& P, const int32_t* perm,
-                                              int64_t e_lo, int64_t e_hi, int64_t grp0, int64_t grp_stride,
-                                              unsigned char* smem) {
-  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS, STAGE>;
-  constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF, NE = C::NE;
-  constexpr int GQS = C::GQS, KRS = C::KRS;
-  constexpr bool HC = C::HC;
-  Real* r_geo_grad = reinterpret_cast<Real*>(smem + C::R_GEO_GRAD);
-  double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
-  Real* r_w = reinterpret_cast<Real*>(smem + C::R_W);
-  Real* r_val = reinterpret_cast<Real*>(smem + C::R_VAL);
-  Real* r_grad = reinterpret_cast<Real*>(smem + C::R_GRAD);
-
-  // reference tables: [w | geo_val | geo_grad | val | grad] in FP64
-  {
-    const double* ref = B.ref;
-    // FP32 copies by integer narrowing (off the FP64 pipe)
-    for (int i = threadIdx.x; i < NQ; i += blockDim.x) r_w[i] = to_real<Real>(ref[i]);
-    ref += NQ;
-    for (int i = threadIdx.x; i < NQ * NV; i += blockDim.x) r_geo_val[i] = ref[i];
-    ref += NQ * NV;
-    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) r_geo_grad[i] = to_real<Real>(ref[i]);
-    ref += NQ * NV * 3;
-    for (int i = threadIdx.x; i < NQ * NB * C::NVAL; i += blockDim.x) r_val[i] = to_real<Real>(ref[i]);
-    ref += NQ * NB * C::NVAL;
-    for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) r_grad[i] = to_real<Real>(ref[i]);
-  }
-
-  const int le = threadIdx.x / TPE;
-  const int t = threadIdx.x % TPE;
-  unsigned char* eb = smem + C::R_END + (size_t)le * C::E_END;
-  double* sX = reinterpret_cast<double*>(eb + C::E_X);
-  Real* sDX = reinterpret_cast<Real*>(eb + C::E_DX);
-  Real* sU = reinterpret_cast<Real*>(eb + C::E_U);
-  Real* sUD = reinterpret_cast<Real*>(eb + C::E_UD);
-  Real* sAUX = reinterpret_cast<Real*>(eb + C::E_AUX);
-  Real* sSG = reinterpret_cast<Real*>(eb + C::E_SG);
-  Real* sG = reinterpret_cast<Real*>(eb + C::E_G);    // [q][b][3] grad (HGRAD) or curl (HCURL)
-  Real* sV = reinterpret_cast<Real*>(eb + C::E_V);    // [q][b][3] HCURL values
-  Real* sW = reinterpret_cast<Real*>(eb + C::E_W);
-  Real* sQF = reinterpret_cast<Real*>(eb + C::E_QF);
-  Real* sSign = reinterpret_cast<Real*>(eb + C::E_SIGN);
-  Real* sK = reinterpret_cast<Real*>(eb + C::E_K);          // [a*NF+c][b*NF+d] staged Jacobian
-  Real* sR = reinterpret_cast<Real*>(eb + C::E_R);          // [a*NF+c] staged residual
-  int64_t* sRP = reinterpret_cast<int64_t*>(eb + C::E_RP);  // row starts rowptr[NF*la+c]
-  int32_t* sLA = reinterpret_cast<int32_t*>(eb + C::E_LA);  // entity LIDs
-  uint8_t* sEP = reinterpret_cast<uint8_t*>(eb + C::E_EP);  // epos[a][b]
-  __syncthreads();
-
-  // parameters in the element arithmetic's type, once per thread
-  Real pr[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) pr[i] = to_real<Real>(P.p[i]);
-  const Real lam = to_real<Real>(P.lam), mu = to_real<Real>(P.mu);
-  const Real beta = to_real<Real>(P.beta), alpha = to_real<Real>(P.alpha);
-  for (int64_t g0 = e_lo + grp0 * EPB; g0 < e_hi; g0 += grp_stride * EPB) {
-    const int64_t ei = g0 + le;
-    const bool valid = ei < e_hi;
-    const int64_t e = (perm && valid) ? (int64_t)__ldg(perm + ei) : ei;
-    // ---------------------------------------------------------- 1 gather
-    if (valid) {
-      const int64_t n0 = __ldg(B.vconn + e * NV);
-      for (int v = t; v < NV; v += TPE) {
-        const int64_t n = __ldg(B.vconn + e * NV + v);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const double xv = __ldg(P.coords + 3 * n + d);
-          if constexpr (C::XABS) sX[3 * v + d] = xv;
-          // differencing in FP64, once per vertex, keeps the mixed J accurate
-          sDX[3 * v + d] = to_real<Real>(xv - __ldg(P.coords + 3 * n0 + d));
-        }
-      }
-      for (int b = t; b < NB; b += TPE) {
-        const int64_t ent = __ldg(B.dconn + e * NB + b);
-#pragma unroll
-        for (int c = 0; c < NF; ++c) {
-          sU[c * NB + b] = to_real<Real>(__ldg(P.x + NF * ent + c));
-          sUD[c * NB + b] = P.xdot ? to_real<Real>(__ldg(P.xdot + NF * ent + c)) : Real(0);
-        }
-        if constexpr (HC) {
-          sAUX[b] = P.aux ? to_real<Real>(__ldg(P.aux + ent)) : Real(0);
-          sSG[b] = (Real)__ldg(B.esign + e * NB + b);
-        }
-        if constexpr (STAGE) {
-          sLA[b] = (int32_t)ent;
-          if constexpr (JAC) {
-#pragma unroll
-            for (int c = 0; c < NF; ++c) sRP[b * NF + c] = __ldg(P.rowptr + NF * ent + c);
-            for (int k = 0; k < NB; ++k) sEP[b * NB + k] = __ldg(B.epos + (e * NB + b) * NB + k);
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // ---------------------------------------------------------- 2 geometry
-    if (valid) {
-      for (int q = t; q < NQ; q += TPE) {
-        Real J[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) J[k] = Real(0);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const Real dx = sDX[3 * v + 0], dy = sDX[3 * v + 1], dz = sDX[3 * v + 2];
-          const Real* gg = r_geo_grad + (q * NV + v) * 3;
-#pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            const Real g = gg[j];
-            J[0 + j] += dx * g;
-            J[3 + j] += dy * g;
-            J[6 + j] += dz * g;
-          }
-        }
-        const Real c00 = J[4] * J[8] - J[5] * J[7];
-        const Real c01 = J[5] * J[6] - J[3] * J[8];
-        const Real c02 = J[3] * J[7] - J[4] * J[6];
-        const Real det = J[0] * c00 + J[1] * c01 + J[2] * c02;
-        const Real id = Real(1) / det;
-        Real Ji[9];
-        Ji[0] = c00 * id; Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
-        Ji[3] = c01 * id; Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[5] = (J[2] * J[3] - J[0] * J[5]) * id;
-        Ji[6] = c02 * id; Ji[7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[8] = (J[0] * J[4] - J[1] * J[3]) * id;
-        sW[q] = r_w[q] * det;
-        if (q == 0) *sSign = det < Real(0) ? Real(-1) : Real(1);
-#pragma unroll 4
-        for (int b = 0; b < NB; ++b) {
-          const Real* gr = r_grad + (q * NB + b) * 3;
-          const Real g0 = gr[0], g1 = gr[1], g2 = gr[2];
-          if constexpr (!HC) {
-            // grad_i = sum_j Jinv(j,i) grad^_j
-            st4(sG + q * GQS + b * 4, Ji[0] * g0 + Ji[3] * g1 + Ji[6] * g2, Ji[1] * g0 + Ji[4] * g1 + Ji[7] * g2,
-                Ji[2] * g0 + Ji[5] * g1 + Ji[8] * g2, r_val[q * NB + b]);
-          } else {
-            const Real s = sSG[b];
-            const Real* vr = r_val + (q * NB + b) * 3;
-            st4(sV + q * GQS + b * 4, s * (Ji[0] * vr[0] + Ji[3] * vr[1] + Ji[6] * vr[2]),
-                s * (Ji[1] * vr[0] + Ji[4] * vr[1] + Ji[7] * vr[2]), s * (Ji[2] * vr[0] + Ji[5] * vr[1] + Ji[8] * vr[2]),
-                Real(0));
-            const Real sd = s * id;  // curl = J curl^ / det
-            st4(sG + q * GQS + b * 4, sd * (J[0] * g0 + J[1] * g1 + J[2] * g2), sd * (J[3] * g0 + J[4] * g1 + J[5] * g2),
-                sd * (J[6] * g0 + J[7] * g1 + J[8] * g2), Real(0));
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // ---------------------------------------------------------- 3 point fluxes
-    if (valid) {
-      for (int q = t; q < NQ; q += TPE) {
-        sW[q] *= *sSign;  // computeCellMeasure: |.| by the sign of the first point
-        Real* qf = sQF + q * NQF;
-        if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
-          Real u = 0, ud = 0, g[3] = {0, 0, 0};
-          for (int b = 0; b < NB; ++b) {
-            const R4<Real> gq = ld4(sG + q * GQS + b * 4);
-            const Real ub = sU[b];
-            u += gq.w * ub;
-            ud += gq.w * sUD[b];
-            g[0] += gq.x * ub;
-            g[1] += gq.y * ub;
-            g[2] += gq.z * ub;
-          }
-          if constexpr (PHYS == TX_PHYS_POISSON) {
-            const Real k = pr[0], c = pr[1], m = pr[2];
-            Real s = pr[3];
-            if (P.source_kind != TX_SOURCE_CONST) {
-              double ip[3] = {0, 0, 0};
-              for (int v = 0; v < NV; ++v) {
-                const double nv = r_geo_val[q * NV + v];
-                ip[0] += nv * sX[3 * v]; ip[1] += nv * sX[3 * v + 1]; ip[2] += nv * sX[3 * v + 2];
-              }
-              s = source_at<Real>(P.source_kind, P.p[1], P.p[3], ip);
-            }
-            qf[0] = k * g[0]; qf[1] = k * g[1]; qf[2] = k * g[2];
-            qf[3] = c * u + m * ud - s;
-          } else {
-            const Real k = pr[0] + pr[1] * u * u;
-            const Real dk = Real(2) * pr[1] * u;
-            qf[0] = k * g[0]; qf[1] = k * g[1]; qf[2] = k * g[2];
-            qf[3] = -pr[2];
-            qf[4] = dk * g[0]; qf[5] = dk * g[1]; qf[6] = dk * g[2];
-            qf[7] = k;
-          }
-        } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
-          Real Gu[9], acc[3] = {0, 0, 0};
-#pragma unroll
-          for (int k = 0; k < 9; ++k) Gu[k] = 0;
-          for (int b = 0; b < NB; ++b) {
-            const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              const Real ub = sU[c * NB + b];
-              Gu[3 * c + 0] += gb.x * ub;
-              Gu[3 * c + 1] += gb.y * ub;
-              Gu[3 * c + 2] += gb.z * ub;
-              acc[c] += gb.w * sUD[c * NB + b];
-            }
-          }
-          const Real tr = Gu[0] + Gu[4] + Gu[8];
-          qf[0] = mu * (Gu[0] + Gu[0]) + lam * tr;  // s00
-          qf[1] = mu * (Gu[4] + Gu[4]) + lam * tr;  // s11
-          qf[2] = mu * (Gu[8] + Gu[8]) + lam * tr;  // s22
-          qf[3] = mu * (Gu[1] + Gu[3]);             // s01
-          qf[4] = mu * (Gu[2] + Gu[6]);             // s02
-          qf[5] = mu * (Gu[5] + Gu[7]);             // s12
-          const Real rho = pr[5];
-          qf[6] = rho * acc[0] - pr[2];
-          qf[7] = rho * acc[1] - pr[3];
-          qf[8] = rho * acc[2] - pr[4];
-        } else {  // MAXWELL
-          Real Ev[3] = {0, 0, 0}, cE[3] = {0, 0, 0}, Jv[3] = {0, 0, 0};
-          for (int b = 0; b < NB; ++b) {
-            const Real ub = sU[b], jb = sAUX[b];
-            const Real* vb = sV + q * GQS + b * 4;
-            const Real* cb = sG + q * GQS + b * 4;
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-              Ev[i] += vb[i] * ub;
-              Jv[i] += vb[i] * jb;
-              cE[i] += cb[i] * ub;
-            }
-          }
-          const Real imu = pr[0], sig = pr[1];
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            qf[i] = imu * cE[i];
-            qf[3 + i] = sig * Ev[i] - Jv[i];
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // ---------------------------------------------------------- 4 rows + scatter
-    // staged form: this thread's Jacobian block-row waits in registers until
-    // every thread of the CTA has finished reading the point tables it reuses
-    Real kreg[STAGE && JAC ? NF * NE : 1];
-    const int my_a = (valid && t < NB) ? t : -1;
-    if (valid) {
-      for (int a = t; a < NB; a += TPE) {
-        const int64_t la = __ldg(B.dconn + e * NB + a);
-        // The thread's own weighted gradient W_q grad N_a(q) and W_q N_a(q):
-        // kept in registers for small rules, read from shared memory otherwise.
-        constexpr bool CACHE = NQ <= 8 && !HC;
-        Real wg[CACHE ? NQ : 1][3], wn[CACHE ? NQ : 1];
-        if constexpr (CACHE) {
-#pragma unroll
-          for (int q = 0; q < NQ; ++q) {
-            const Real w = sW[q];
-            const R4<Real> ga = ld4(sG + q * GQS + a * 4);
-            wg[q][0] = w * ga.x; wg[q][1] = w * ga.y; wg[q][2] = w * ga.z;
-            wn[q] = w * ga.w;
-          }
-        }
-        auto WG = [&](int q, int i) -> Real {
-          if constexpr (CACHE) return wg[q][i];
-          else return sW[q] * sG[q * GQS + a * 4 + i];
-        };
-        auto WN = [&](int q) -> Real {
-          if constexpr (CACHE) return wn[q];
-          else return sW[q] * sG[q * GQS + a * 4 + 3];
-        };
-        // residual row a (per field)
-        Real r[NF];
-#pragma unroll
-        for (int c = 0; c < NF; ++c) r[c] = 0;
-#pragma unroll(CACHE ? NQ : 1)
-        for (int q = 0; q < NQ; ++q) {
-          const Real* qf = sQF + q * NQF;
-          if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
-            r[0] += WG(q, 0) * qf[0] + WG(q, 1) * qf[1] + WG(q, 2) * qf[2] + WN(q) * qf[3];
-          } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
-            const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2), n = WN(q);
-            r[0] += g0 * qf[0] + g1 * qf[3] + g2 * qf[4] + n * qf[6];
-            r[1] += g0 * qf[3] + g1 * qf[1] + g2 * qf[5] + n * qf[7];
-            r[2] += g0 * qf[4] + g1 * qf[5] + g2 * qf[2] + n * qf[8];
-          } else {
-            const Real w = sW[q];
-            const Real* ga = sG + q * GQS + a * 4;
-            const Real* va = sV + q * GQS + a * 4;
-            r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + va[0] * qf[3] + va[1] * qf[4] + va[2] * qf[5]);
-          }
-        }
-        if constexpr (STAGE) {
-#pragma unroll
-          for (int c = 0; c < NF; ++c) sR[a * NF + c] = r[c];
-        } else if (P.f) {
-#pragma unroll
-          for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.f + NF * la + c, widen(r[c]));
-        }
-        if constexpr (JAC) {
-          int64_t rp[NF];
-          const uint8_t* ep = B.epos + (e * NB + a) * NB;
-          if constexpr (!STAGE && !TAN) {
-#pragma unroll
-            for (int c = 0; c < NF; ++c) rp[c] = __ldg(P.rowptr + NF * la + c);
-          }
-          // Tangent: the row's products with the tangent directions (GatherSolution<Tangent>
-          // seeds dx(i) from them; ScatterResidual<Tangent> sums dx(i) into dfdp_i)
-          double rt[TAN ? kMaxTangents : 1][TAN ? NF : 1];
-          if constexpr (TAN) {
-#pragma unroll
-            for (int i = 0; i < kMaxTangents; ++i)
-#pragma unroll
-              for (int c = 0; c < NF; ++c) rt[i][c] = 0.0;
-          }
-          int64_t eb = 0;  // entity of column basis b (tangent gather)
-          // Jacobian entry (row a,c; column b,d): reduce now, or stage for the CTA-wide scatter
-          auto put = [&](int c, int b, int d, int64_t pb, Real v) {
-            if constexpr (TAN) {
-              for (int i = 0; i < P.ntan; ++i)
-                rt[i][c] += (double)v * __ldg(P.tan + (int64_t)i * P.n + NF * eb + d);
-            } else if constexpr (STAGE) {
-              kreg[c * NE + b * NF + d] = v;
-            } else {
-              accumulate<ATOMIC>(P.vals + rp[c] + pb + d, widen(v));
-            }
-          };
-#pragma unroll(STAGE ? NB : 1)
-          for (int b = 0; b < NB; ++b) {
-            const int64_t pb = (STAGE || TAN) ? 0 : (int64_t)NF * __ldg(ep + b);
-            if constexpr (TAN) eb = __ldg(B.dconn + e * NB + b);
-            if constexpr (PHYS == TX_PHYS_POISSON) {
-              const Real ca = beta * pr[0];
-              const Real cm = beta * pr[1] + alpha * pr[2];
-              Real kg = 0, km = 0;
-#pragma unroll(CACHE ? NQ : 1)
-              for (int q = 0; q < NQ; ++q) {
-                const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                kg += WG(q, 0) * gb.x + WG(q, 1) * gb.y + WG(q, 2) * gb.z;
-                km += WN(q) * gb.w;
-              }
-              put(0, b, 0, pb, ca * kg + cm * km);
-            } else if constexpr (PHYS == TX_PHYS_HEAT) {
-              Real kab = 0;
-#pragma unroll(CACHE ? NQ : 1)
-              for (int q = 0; q < NQ; ++q) {
-                const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                const Real* qf = sQF + q * NQF;
-                const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2);
-                kab += qf[7] * (g0 * gb.x + g1 * gb.y + g2 * gb.z) + gb.w * (g0 * qf[4] + g1 * qf[5] + g2 * qf[6]);
-              }
-              put(0, b, 0, pb, beta * kab);
-            } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
-              Real Pm[9], M = 0;
-#pragma unroll
-              for (int k = 0; k < 9; ++k) Pm[k] = 0;
-#pragma unroll(CACHE ? NQ : 1)
-              for (int q = 0; q < NQ; ++q) {
-                const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                const Real b0 = gb.x, b1 = gb.y, b2 = gb.z;
-                const Real wa0 = WG(q, 0), wa1 = WG(q, 1), wa2 = WG(q, 2);
-                Pm[0] += wa0 * b0; Pm[1] += wa0 * b1; Pm[2] += wa0 * b2;
-                Pm[3] += wa1 * b0; Pm[4] += wa1 * b1; Pm[5] += wa1 * b2;
-                Pm[6] += wa2 * b0; Pm[7] += wa2 * b1; Pm[8] += wa2 * b2;
-                M += WN(q) * gb.w;
-              }
-              const Real trP = Pm[0] + Pm[4] + Pm[8];
-              const Real mass = alpha * pr[5] * M;
-#pragma unroll
-              for (int c = 0; c < 3; ++c)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                  Real k = beta * (lam * Pm[3 * c + d] + mu * Pm[3 * d + c]);
-                  if (c == d) k += beta * mu * trP + mass;
-                  put(c, b, d, pb, k);
-                }
-            } else {  // MAXWELL
-              const Real imu = pr[0], sig = pr[1];
-              Real kc = 0, kv = 0;
-              for (int q = 0; q < NQ; ++q) {
-                const Real* ca = sG + q * GQS + a * 4;
-                const Real* cb = sG + q * GQS + b * 4;
-                const Real* va = sV + q * GQS + a * 4;
-                const Real* vb = sV + q * GQS + b * 4;
-                kc += sW[q] * (ca[0] * cb[0] + ca[1] * cb[1] + ca[2] * cb[2]);
-                kv += sW[q] * (va[0] * vb[0] + va[1] * vb[1] + va[2] * vb[2]);
-              }
-              put(0, b, 0, pb, beta * (imu * kc + sig * kv));
-            }
-          }
-          if constexpr (TAN) {
-            for (int i = 0; i < P.ntan; ++i)
-#pragma unroll
-              for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.dfdp + (int64_t)i * P.n + NF * la + c, rt[i][c]);
-          }
-        }
-      }
-    }
-    if constexpr (STAGE) {
-      // ------------------------------------------------------ 5 CTA-wide scatter
-      if constexpr (JAC) {
-        __syncthreads();  // point tables are dead from here: the staged rows overwrite them
-        if (my_a >= 0) {
-#pragma unroll
-          for (int c = 0; c < NF; ++c)
-#pragma unroll
-            for (int k = 0; k < NE; ++k) sK[(my_a * NF + c) * KRS + k] = kreg[c * NE + k];
-        }
-      }
-      // consecutive threads take consecutive entries of an element row
-      __syncthreads();
-      const int nval = (int)(e_hi - g0 < EPB ? e_hi - g0 : EPB);
-      unsigned char* base = smem + C::R_END;
-      if (P.f) {
-        for (int i = threadIdx.x; i < nval * NE; i += blockDim.x) {
-          const int l2 = i / NE, row = i - l2 * NE;
-          const unsigned char* e2 = base + (size_t)l2 * C::E_END;
-          const int32_t la = reinterpret_cast<const int32_t*>(e2 + C::E_LA)[row / NF];
-          accumulate<ATOMIC>(P.f + (int64_t)NF * la + row % NF,
-                             widen(reinterpret_cast<const Real*>(e2 + C::E_R)[row]));
-        }
-      }
-      if constexpr (JAC) {
-        // a warp walks whole elements; its lanes sit on the columns of RPW rows
-        constexpr int RL = NE <= 4 ? 4 : NE <= 8 ? 8 : NE <= 16 ? 16 : 32;  // lanes per row
-        constexpr int RPW = 32 / RL;                                          // rows per pass
-        const int lane = threadIdx.x & 31;
-        const int col = lane % RL, sub = lane / RL;
-        const int cb = col / NF, cd = col - (col / NF) * NF;  // column's basis and field
-        constexpr int NR = (NE + RPW - 1) / RPW;  // passes over an element's rows
-        if (col < NE) {
-          double* vals = P.vals + cd;
-          for (int l2 = threadIdx.x >> 5; l2 < nval; l2 += blockDim.x >> 5) {
-            const unsigned char* e2 = base + (size_t)l2 * C::E_END;
-            const int64_t* rps = reinterpret_cast<const int64_t*>(e2 + C::E_RP) + sub;
-            const uint8_t* eps = reinterpret_cast<const uint8_t*>(e2 + C::E_EP) + cb;
-            const Real* kk = reinterpret_cast<const Real*>(e2 + C::E_K) + sub * KRS + col;
-#pragma unroll
-            for (int k = 0; k < NR; ++k) {
-              const int row = sub + k * RPW;
-              if (NE % RPW == 0 || row < NE) {
-                const int64_t addr = rps[k * RPW] + (int64_t)NF * eps[(row / NF) * NB];
-                accumulate<ATOMIC>(vals + addr, widen(kk[k * RPW * KRS]));
-              }
-            }
-          }
-        }
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// ------------------------------------------------------------- per block
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool STAGE>
-constexpr int block_threads() {
-  return STAGE ? 128 : Cfg<TOPO, BASIS, NQ, PHYS, Real>::THREADS;
-}
-
-// Staged FP32 kernels ask for four resident CTAs (at most 128 registers a
-// thread): the register-staged Jacobian rows otherwise cap residency at three.
-template <typename Real, bool STAGE>
-constexpr int min_blocks() {
-  return STAGE && sizeof(Real) == 4 ? 4 : 1;
-}
 
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false>
 __global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>(), min_blocks<Real, STAGE>())
@@ -640,71 +69,6 @@ cudaError_t launch_prec(const BlockView& B, const EvalParams& P, bool mixed, con
 #undef TX_L
 }
 
-// ------------------------------------------------------------- batched
-// The element families the kernels are instantiated for.
-enum Kind {
-  K_HEX8_POISSON, K_HEX8_ELAST, K_HEX8_HEAT, K_HEX27_POISSON, K_HEX27_HEAT, K_TET4_POISSON, K_TET4_ELAST,
-  K_TET4_HEAT, K_TET10_POISSON, K_TET10_HEAT, K_NED_MAXWELL, K_COUNT
-};
-
-#define TX_FOR_EACH_KIND(X)                                         \
-  X(K_HEX8_POISSON, TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_POISSON)    \
-  X(K_HEX8_ELAST, TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_ELASTICITY)   \
-  X(K_HEX8_HEAT, TX_TOPO_HEX, TX_HGRAD_C1, 8, TX_PHYS_HEAT)          \
-  X(K_HEX27_POISSON, TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_POISSON)  \
-  X(K_HEX27_HEAT, TX_TOPO_HEX, TX_HGRAD_C2, 27, TX_PHYS_HEAT)        \
-  X(K_TET4_POISSON, TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_POISSON)    \
-  X(K_TET4_ELAST, TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_ELASTICITY)   \
-  X(K_TET4_HEAT, TX_TOPO_TET, TX_HGRAD_C1, 4, TX_PHYS_HEAT)          \
-  X(K_TET10_POISSON, TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_POISSON)   \
-  X(K_TET10_HEAT, TX_TOPO_TET, TX_HGRAD_C2, 4, TX_PHYS_HEAT)         \
-  X(K_NED_MAXWELL, TX_TOPO_HEX, TX_HCURL_I1, 8, TX_PHYS_MAXWELL)
-
-constexpr int kBatchThreads = 128;
-
-// Persistent kernel: CTAs take work items (element chunks of any block of
-// any mesh, any family) from an atomic counter until the list is empty.
-template <typename Real, bool JAC>
-__global__ void __launch_bounds__(kBatchThreads)
-k_assemble_batched(const BlockView* __restrict__ views, const EvalParams* __restrict__ params,
-                   const WorkItem* __restrict__ items, int n_items, int* counter) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int s_item;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
-    __syncthreads();
-    const int it = s_item;
-    __syncthreads();
-    if (it >= n_items) break;
-    const WorkItem w = items[it];
-    const BlockView B = views[w.view];
-    const EvalParams P = params[w.view];
-    switch (w.kind) {
-#define TX_CASE(K, T, BS, Q, PH)                                                                 \
-  case K:                                                                                        \
-    assemble_body<T, BS, Q, PH, Real, JAC, true, kBatchThreads>(B, P, nullptr, w.e0, w.e1, 0, 1, smem); \
-    break;
-      TX_FOR_EACH_KIND(TX_CASE)
-#undef TX_CASE
-      default:
-        break;
-    }
-  }
-}
-
-template <typename Real>
-size_t smem_of_kind(int kind) {
-  switch (kind) {
-#define TX_SZ(K, T, BS, Q, PH) \
-  case K:                      \
-    return Cfg<T, BS, Q, PH, Real, kBatchThreads>::SMEM;
-    TX_FOR_EACH_KIND(TX_SZ)
-#undef TX_SZ
-    default:
-      return 0;
-  }
-}
-
 }  // namespace
 
 int assemble_kind(int topo, int basis, int nq, int physics) {
@@ -713,34 +77,6 @@ int assemble_kind(int topo, int basis, int nq, int physics) {
   TX_FOR_EACH_KIND(TX_K)
 #undef TX_K
   return -1;
-}
-
-size_t batched_smem_bytes(int kind, bool mixed) {
-  return mixed ? smem_of_kind<float>(kind) : smem_of_kind<double>(kind);
-}
-
-cudaError_t launch_assemble_batched(const BlockView* views, const EvalParams* params, const WorkItem* items,
-                                    int n_items, int* counter, size_t smem, bool mixed, bool jac, int grid,
-                                    cudaStream_t s) {
-  if (n_items <= 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
-  if (e != cudaSuccess) return e;
-  auto go = [&](auto kern) -> cudaError_t {
-    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return err;
-    int per_sm = 0, dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBatchThreads, smem);
-    if (err != cudaSuccess) return err;
-    int g = (per_sm > 0 ? per_sm : 1) * sms;
-    if (grid > 0 && grid < g) g = grid;
-    if (g > n_items) g = n_items;
-    kern<<<g, kBatchThreads, smem, s>>>(views, params, items, n_items, counter);
-    return cudaGetLastError();
-  };
-  if (mixed) return jac ? go(k_assemble_batched<float, true>) : go(k_assemble_batched<float, false>);
-  return jac ? go(k_assemble_batched<double, true>) : go(k_assemble_batched<double, false>);
 }
 
 cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,

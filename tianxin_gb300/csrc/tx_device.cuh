@@ -46,11 +46,11 @@ struct WorkItem {
 // Element family id of (topology, basis, cubature points, physics); -1 if none.
 int assemble_kind(int topo, int basis, int nq, int physics);
 // Dynamic shared memory of one family in the batched kernel.
-size_t batched_smem_bytes(int kind, bool mixed);
+size_t batched_smem_bytes(int kind, bool mixed, bool stage);
 // Persistent launch over a work list (device arrays); counter is a device int.
 cudaError_t launch_assemble_batched(const BlockView* views, const EvalParams* params, const WorkItem* items,
-                                    int n_items, int* counter, size_t smem, bool mixed, bool jac, int grid,
-                                    cudaStream_t s);
+                                    int n_items, int* counter, size_t smem, bool mixed, bool jac, bool stage,
+                                    int grid, cudaStream_t s);
 
 // ---- linear algebra (tx_linalg.cu)
 cudaError_t launch_expand_rowptr(const int64_t* erowptr, int64_t n_ent, int nf, int64_t* rowptr, cudaStream_t s);
