@@ -486,12 +486,15 @@ class Batch:
         if rc:
             raise TxError(rc, "tx_batch_set_worksets")
 
-    def evaluate(self, xs, fs, Ws=None, x_dots=None, auxs=None, alpha=0.0, beta=1.0, t=0.0, mixed=False):
+    def evaluate(self, xs, fs, Ws=None, x_dots=None, auxs=None, alpha=0.0, beta=1.0, t=0.0, mixed=False,
+                 scatter_direct=False):
+        """One persistent launch over every instance's worksets (staged Jacobian scatter unless scatter_direct)."""
         n = len(self.dofs)
         args = (_abi.EvalArgs * n)()
         for i in range(n):
             args[i] = eval_args(xs[i], None if x_dots is None else x_dots[i], None if auxs is None else auxs[i],
-                                alpha, beta, t, fs[i], None if Ws is None else Ws[i], mixed)
+                                alpha, beta, t, fs[i], None if Ws is None else Ws[i], mixed,
+                                scatter_direct=scatter_direct)
         self.lib.tx_set_stream(self.dofs[0].h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         rc = self.lib.tx_batch_eval(self.b, args)
         if rc:

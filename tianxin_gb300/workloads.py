@@ -134,7 +134,8 @@ def report(names=("poisson_hex8", "heat_hex27_tet10", "elastodynamics_hex8", "mi
         f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
         r = {"elements": w.n_elements, "dofs": w.dof.n_dofs, "nnz": w.dof.nnz}
         for tag, kw in (("fp64_blocks", {}), ("mixed_blocks", {"mixed": True}),
-                        ("fp64_persistent", {"persistent": True}), ("mixed_persistent", {"persistent": True, "mixed": True})):
+                        ("fp64_persistent", {"persistent": True}), ("mixed_persistent", {"persistent": True, "mixed": True}),
+                        ("mixed_persistent_direct", {"persistent": True, "mixed": True, "scatter_direct": True})):
             r[tag + "_ms"] = time_eval(ae, x, f, W, **kw)
         out["heat_hex27_tet10_48"] = r
     if "elastodynamics_hex8" in names:
@@ -168,14 +169,14 @@ def report(names=("poisson_hex8", "heat_hex27_tet10", "elastodynamics_hex8", "mi
         b = Batch([w.dof for w in ws], workset=(512, 512))
         nel = sum(w.n_elements for w in ws)
         r = {"instances": len(ws), "elements": nel}
-        for tag, mixed in (("fp64", False), ("mixed", True)):
+        for tag, mixed, direct in (("fp64", False, False), ("mixed", True, False), ("mixed_direct", True, True)):
             for _ in range(2):
-                b.evaluate(xs, fs, Ws, auxs=auxs, mixed=mixed)
+                b.evaluate(xs, fs, Ws, auxs=auxs, mixed=mixed, scatter_direct=direct)
             torch.cuda.synchronize()
             s, e = _events()
             s.record()
             for _ in range(5):
-                b.evaluate(xs, fs, Ws, auxs=auxs, mixed=mixed)
+                b.evaluate(xs, fs, Ws, auxs=auxs, mixed=mixed, scatter_direct=direct)
             e.record()
             torch.cuda.synchronize()
             r[tag + "_one_launch_ms"] = s.elapsed_time(e) / 5
