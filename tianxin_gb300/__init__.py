@@ -10,8 +10,8 @@ from ._abi import (ALL_SIDES, SIDE_XMAX, SIDE_XMIN, SIDE_YMAX, SIDE_YMIN, SIDE_Z
                    mesh_desc)
 from ._lib import TxError, load
 from .panzer import (HEX, TET, AssemblyEngine, Batch, CapturedGraph, CartesianConnManager, CrsMatrix, DirichletBC, DOFManager,
-                     ModelEvaluator, NeumannBC, Response, TpetraLinearObjFactory, neumann_value,
+                     HostEvaluator, ModelEvaluator, NeumannBC, Response, TpetraLinearObjFactory, neumann_value,
                      synchronize)
 
 __all__ = ["CartesianConnManager", "DOFManager", "TpetraLinearObjFactory", "CrsMatrix", "DirichletBC",
-           "NeumannBC", "neumann_value", "Response", "CapturedGraph", "AssemblyEngine", "ModelEvaluator", "TxError", "load", "equation_set", "mesh_desc", "synchronize"]
+           "NeumannBC", "neumann_value", "Response", "CapturedGraph", "HostEvaluator", "AssemblyEngine", "ModelEvaluator", "TxError", "load", "equation_set", "mesh_desc", "synchronize"]

@@ -429,6 +429,39 @@ class Response:
         return float(self.evaluate(x).item())
 
 
+class HostEvaluator:
+    """evalModel for a caller whose Tpetra vectors and matrix live in host memory (pinned), pipelined: step k's
+    f and CRS values are copied back on a copy stream while step k + 1 assembles into the other of two device
+    buffer sets.  Every step still copies its x in and its f and W out; synchronize() waits for the last copy.
+    The host link (about 0.2 TB/s on this machine) bounds the step, the assembly overlaps it."""
+
+    def __init__(self, me, mixed=True):
+        self.me, self.lof, self.mixed = me, me.lof, mixed
+        self.sets = [(self.lof.getTpetraVector(), self.lof.getTpetraVector(), me.create_W_op()) for _ in range(2)]
+        self.copy = torch.cuda.Stream()
+        self.done = [torch.cuda.Event(), torch.cuda.Event()]   # copy-back of set i finished
+        self.ready = [torch.cuda.Event(), torch.cuda.Event()]  # assembly of set i finished
+        self.k = 0
+
+    def step(self, x_host, f_host, W_host, **kw):
+        i = self.k & 1
+        x, f, W = self.sets[i]
+        cur = torch.cuda.current_stream()
+        cur.wait_event(self.done[i])          # the set's previous copy-back has left the device
+        x.copy_(x_host, non_blocking=True)
+        self.me.evalModel(x, f=f, W=W, mixed=self.mixed, **kw)
+        self.ready[i].record(cur)
+        with torch.cuda.stream(self.copy):
+            self.copy.wait_event(self.ready[i])
+            f_host.copy_(f, non_blocking=True)
+            W_host.copy_(W.values, non_blocking=True)
+            self.done[i].record(self.copy)
+        self.k += 1
+
+    def synchronize(self):
+        torch.cuda.current_stream().wait_stream(self.copy)
+
+
 class CapturedGraph:
     """fn()'s library work recorded into a CUDA graph owned by the handle (tx_graph_capture_begin/end) and
     replayed by launch().  fn may only make launch-only calls (evalModel, NeumannBC.evaluate, apply,
