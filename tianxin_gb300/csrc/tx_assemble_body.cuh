@@ -172,9 +172,9 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
   Real* sSign = reinterpret_cast<Real*>(eb + C::E_SIGN);
   Real* sK = reinterpret_cast<Real*>(eb + C::E_K);          // [a*NF+c][b*NF+d] staged Jacobian
   Real* sR = reinterpret_cast<Real*>(eb + C::E_R);          // [a*NF+c] staged residual
-  int64_t* sRP = reinterpret_cast<int64_t*>(eb + C::E_RP);  // row starts rowptr[NF*la+c]
+  int64_t* sRP = reinterpret_cast<int64_t*>(eb + C::E_RP);  // addresses of the rows' first values
   int32_t* sLA = reinterpret_cast<int32_t*>(eb + C::E_LA);  // entity LIDs
-  uint8_t* sEP = reinterpret_cast<uint8_t*>(eb + C::E_EP);  // epos[a][b]
+  uint8_t* sEP = reinterpret_cast<uint8_t*>(eb + C::E_EP);  // epos transposed: [b][a]
   __syncthreads();
 
   // parameters in the element arithmetic's type, once per thread
@@ -214,9 +214,11 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         if constexpr (STAGE) {
           sLA[b] = (int32_t)ent;
           if constexpr (JAC) {
+            // row starts as final addresses into the CRS values; epos transposed so
+            // that the scatter's lane (column block k) finds its row positions together
 #pragma unroll
-            for (int c = 0; c < NF; ++c) sRP[b * NF + c] = __ldg(P.rowptr + NF * ent + c);
-            for (int k = 0; k < NB; ++k) sEP[b * NB + k] = __ldg(B.epos + (e * NB + b) * NB + k);
+            for (int c = 0; c < NF; ++c) sRP[b * NF + c] = (int64_t)(P.vals + __ldg(P.rowptr + NF * ent + c));
+            for (int k = 0; k < NB; ++k) sEP[k * NB + b] = __ldg(B.epos + (e * NB + b) * NB + k);
           }
         }
       }
@@ -548,18 +550,33 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         const int cb = col / NF, cd = col - (col / NF) * NF;  // column's basis and field
         constexpr int NR = (NE + RPW - 1) / RPW;  // passes over an element's rows
         if (col < NE) {
-          double* vals = P.vals + cd;
           for (int l2 = threadIdx.x >> 5; l2 < nval; l2 += blockDim.x >> 5) {
             const unsigned char* e2 = base + (size_t)l2 * C::E_END;
             const int64_t* rps = reinterpret_cast<const int64_t*>(e2 + C::E_RP) + sub;
-            const uint8_t* eps = reinterpret_cast<const uint8_t*>(e2 + C::E_EP) + cb;
+            const uint8_t* eps = reinterpret_cast<const uint8_t*>(e2 + C::E_EP) + cb * NB;
             const Real* kk = reinterpret_cast<const Real*>(e2 + C::E_K) + sub * KRS + col;
+            if constexpr (RPW == 1 && NB == 8) {
+              // one pass per row: the lane's 8 byte offsets (one per row vertex) in registers
+              const uint2 w = *reinterpret_cast<const uint2*>(eps);
+              uint32_t off[NB];
 #pragma unroll
-            for (int k = 0; k < NR; ++k) {
-              const int row = sub + k * RPW;
-              if (NE % RPW == 0 || row < NE) {
-                const int64_t addr = rps[k * RPW] + (int64_t)NF * eps[(row / NF) * NB];
-                accumulate<ATOMIC>(vals + addr, widen(kk[k * RPW * KRS]));
+              for (int a2 = 0; a2 < NB; ++a2)
+                off[a2] = 8u * (NF * (((a2 < 4 ? w.x : w.y) >> (8 * (a2 & 3))) & 0xffu) + cd);
+#pragma unroll
+              for (int row = 0; row < NE; ++row) {
+                double* p = reinterpret_cast<double*>(rps[row] + off[row / NF]);
+                if constexpr (ATOMIC) red_global(p, widen(kk[row * KRS]));
+                else *p += widen(kk[row * KRS]);
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < NR; ++k) {
+                const int row = sub + k * RPW;
+                if (NE % RPW == 0 || row < NE) {
+                  double* p = reinterpret_cast<double*>(rps[k * RPW]) + (NF * eps[row / NF] + cd);
+                  if constexpr (ATOMIC) red_global(p, widen(kk[k * RPW * KRS]));
+                  else *p += widen(kk[k * RPW * KRS]);
+                }
               }
             }
           }

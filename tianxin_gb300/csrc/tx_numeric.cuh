@@ -30,6 +30,13 @@ __device__ __forceinline__ void st4(double* p, double a, double b, double c, dou
   reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
 }
 
+// FP64 reduction at an address known to be global memory (red.global: no
+// return value, no generic-address resolution), for addresses the compiler
+// cannot trace to a global pointer, e.g. ones read from shared memory.
+__device__ __forceinline__ void red_global(double* p, double v) {
+  asm volatile("red.global.add.f64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "d"(v) : "memory");
+}
+
 template <bool ATOMIC>
 __device__ __forceinline__ void accumulate(double* p, double v) {
   if constexpr (ATOMIC) atomicAdd(p, v);  // red.global.add.f64
@@ -40,15 +47,14 @@ __device__ __forceinline__ void accumulate(double* p, double v) {
 // exponent rebiased by 1023 - 127 = 896, 23-bit fraction moved to the top of
 // the 52-bit fraction.  Keeps the mixed kernel's output conversions off the
 // FP64 pipe (a small fraction of the FP32 rate on this part): |v| >> 3 puts
-// exponent and fraction in place and adding 896 << 20 rebiases; zeros keep
-// their sign.  Subnormals, infinities and NaNs (one unsigned compare of
-// |v| - 2^-126 against the normal range) call the ordinary conversion out of
-// line, so the compiler cannot if-convert it into every conversion.
+// exponent and fraction in place and adding 896 << 20 rebiases.  Zeros,
+// subnormals, infinities and NaNs (one unsigned compare of |v| - 2^-126
+// against the normal range) call the ordinary conversion out of line, so the
+// compiler cannot if-convert it into every conversion.
 __device__ __noinline__ double widen_rare(float v) { return (double)v; }
 __device__ __forceinline__ double widen(float v) {
   const uint32_t b = __float_as_uint(v);
   const uint32_t a = b & 0x7fffffffu;
-  if (a == 0u) return __hiloint2double((int)b, 0);
   if (a - 0x00800000u >= 0x7f000000u) return widen_rare(v);
   const uint32_t hi = (b & 0x80000000u) | ((a >> 3) + 0x38000000u);
   return __hiloint2double((int)hi, (int)(b << 29));
