@@ -203,13 +203,19 @@ tx::EvalParams make_params(tx_handle h, const tx_eval_args& a) {
   return P;
 }
 
-// Work list of a handle: every block cut into worksets.
+// Work list of a handle: every block cut into worksets, and each workset into
+// device work items of at most kItemPasses CTA passes of its element family, so
+// that a workset of heavy elements (4 hex27 per CTA pass) is shared by several
+// CTAs instead of serialising one of them.
+constexpr int kItemPasses = 8;
 void build_items(tx_handle h, std::vector<tx::WorkItem>& out, int view_base) {
   for (size_t b = 0; b < h->blocks.size(); ++b) {
     const DevBlock& db = h->blocks[b];
+    const int64_t cap = (int64_t)tx::batched_elements_per_pass(db.kind) * kItemPasses;
     std::vector<int64_t> wb = tx::workset_bounds(db.n_elem, h->ws_min, h->ws_max, h->ws_seed + 7919 * b);
     for (size_t k = 0; k + 1 < wb.size(); ++k)
-      out.push_back(tx::WorkItem{db.kind, (int32_t)(view_base + b), wb[k], wb[k + 1]});
+      for (int64_t e0 = wb[k]; e0 < wb[k + 1]; e0 += cap)
+        out.push_back(tx::WorkItem{db.kind, (int32_t)(view_base + b), e0, std::min(e0 + cap, wb[k + 1])});
   }
 }
 

@@ -67,6 +67,18 @@ size_t smem_of_kind(int kind) {
 
 }  // namespace
 
+int batched_elements_per_pass(int kind) {
+  switch (kind) {
+#define TX_EPB(K, T, BS, Q, PH) \
+  case K:                       \
+    return Cfg<T, BS, Q, PH, float, kBatchThreads>::EPB;
+    TX_FOR_EACH_KIND(TX_EPB)
+#undef TX_EPB
+    default:
+      return 1;
+  }
+}
+
 size_t batched_smem_bytes(int kind, bool mixed, bool stage) {
   if (stage) return mixed ? smem_of_kind<float, true>(kind) : smem_of_kind<double, true>(kind);
   return mixed ? smem_of_kind<float, false>(kind) : smem_of_kind<double, false>(kind);

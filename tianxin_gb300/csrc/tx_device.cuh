@@ -47,6 +47,8 @@ struct WorkItem {
 int assemble_kind(int topo, int basis, int nq, int physics);
 // Dynamic shared memory of one family in the batched kernel.
 size_t batched_smem_bytes(int kind, bool mixed, bool stage);
+// Elements one CTA of the persistent kernel assembles per pass for a family.
+int batched_elements_per_pass(int kind);
 // Persistent launch over a work list (device arrays); counter is a device int.
 cudaError_t launch_assemble_batched(const BlockView* views, const EvalParams* params, const WorkItem* items,
                                     int n_items, int* counter, size_t smem, bool mixed, bool jac, bool stage,
