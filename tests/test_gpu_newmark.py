@@ -24,7 +24,8 @@ def dense(o, vals):
     return M
 
 
-def test_newmark_graph_steps_match_oracle(cuda):
+@pytest.mark.parametrize("linear", [True, False])
+def test_newmark_graph_steps_match_oracle(cuda, linear):
     n, dt, beta, gamma = 5, 1e-3, 0.25, 0.5
     params = (1.0, 0.25, 0.0, 0.0, 0.0, 1.0)  # E, nu, body force, rho
     q = A.equation_set(A.TX_PHYS_ELASTICITY, params=params)
@@ -50,7 +51,7 @@ def test_newmark_graph_steps_match_oracle(cuda):
         a = c * (u - up)
         v = vp + gamma * dt * a
 
-    nm = NewmarkElastodynamics(me, dt, beta, gamma, mixed=True, outer=3, inner=24)
+    nm = NewmarkElastodynamics(me, dt, beta, gamma, mixed=True, outer=3, inner=24, linear=linear)
     nm.initialize(torch.from_numpy(u0).cuda())
     nm.capture()
     worst = 0.0
