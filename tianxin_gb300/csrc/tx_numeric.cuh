@@ -32,9 +32,12 @@ __device__ __forceinline__ void st4(double* p, double a, double b, double c, dou
 
 // FP64 reduction at an address known to be global memory (red.global: no
 // return value, no generic-address resolution), for addresses the compiler
-// cannot trace to a global pointer, e.g. ones read from shared memory.
+// cannot trace to a global pointer, e.g. ones read from shared memory.  No
+// memory clobber: the reduction depends only on its operands and nothing in
+// the kernels reads the reduced arrays back, so later shared-memory loads may
+// be scheduled ahead of it (CTA barriers still order everything).
 __device__ __forceinline__ void red_global(double* p, double v) {
-  asm volatile("red.global.add.f64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "d"(v) : "memory");
+  asm volatile("red.global.add.f64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "d"(v));
 }
 
 template <bool ATOMIC>
