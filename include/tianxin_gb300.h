@@ -352,6 +352,15 @@ int tx_graph_capture_end(tx_handle h, int32_t* graph_id);
 int tx_graph_launch(tx_handle h, int32_t graph_id);
 int tx_graph_destroy(tx_handle h, int32_t graph_id);
 
+/* Parameter sensitivity of the residual (the dfdp vectors that
+ * ScatterResidual_Tpetra<Tangent> fills for an active scalar parameter,
+ * Panzer_ScatterResidual_Tpetra_impl.hpp:218-270): dfdp += df/dparams[param]
+ * at args' x, x_dot, aux, t over args' blocks and element range, in FP64.
+ * param indexes tx_equation_set_desc.params; Dirichlet rows are not
+ * touched (zero them for a Dirichlet value independent of the parameter).
+ * TX_ERANGE for an index the physics does not use. */
+int tx_eval_dfdp(tx_handle h, const tx_eval_args* args, int32_t param, double* dfdp);
+
 /* Worksets (WorksetContainer::setWorksetSize, disc-fe/src/Panzer_WorksetContainer.hpp:104)
  * of the TX_EVAL_PERSISTENT evaluation: consecutive element ranges of every
  * block with sizes drawn uniformly in [min_size, max_size] from seed

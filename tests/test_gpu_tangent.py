@@ -62,3 +62,45 @@ def test_tangent_argument_errors(cuda):
     with pytest.raises(tx.TxError):
         ae.evaluateTangent(x, torch.zeros(5, dof.n_dofs, dtype=torch.float64, device="cuda"),
                            torch.zeros(5, dof.n_dofs, dtype=torch.float64, device="cuda"))
+
+
+PARAM_CASES = [
+    ("poisson_tet4", (1.0, 0.5, 2.0, 1.0), A.TX_SOURCE_CONST, A.TX_PHYS_POISSON, A.TX_TOPO_TET, A.TX_HGRAD_C1, range(4)),
+    ("poisson_affine_hex8", (1.0, 0.7, 2.0, 1.0), A.TX_SOURCE_AFFINE, A.TX_PHYS_POISSON, A.TX_TOPO_HEX, A.TX_HGRAD_C1,
+     range(4)),
+    ("elasticity_hex8", (1.3, 0.3, 0.2, -0.1, -1.0, 2.0), A.TX_SOURCE_CONST, A.TX_PHYS_ELASTICITY, A.TX_TOPO_HEX,
+     A.TX_HGRAD_C1, range(6)),
+    ("heat_hex27", (1.0, 0.5, 1.5), A.TX_SOURCE_CONST, A.TX_PHYS_HEAT, A.TX_TOPO_HEX, A.TX_HGRAD_C2, range(3)),
+    ("maxwell_hex", (1.5, 2.0), A.TX_SOURCE_CONST, A.TX_PHYS_MAXWELL, A.TX_TOPO_HEX, A.TX_HCURL_I1, range(2)),
+]
+
+
+@pytest.mark.parametrize("name,params,source,phys,topo,basis,indices", PARAM_CASES, ids=[c[0] for c in PARAM_CASES])
+def test_parameter_sensitivities_match_oracle_differences(cuda, name, params, source, phys, topo, basis, indices):
+    # df/dp_i against the oracle's residual difference: exact for the parameters the
+    # residual is affine in (unit step), a central difference for Poisson's ratio
+    n = (3, 2, 3)
+    m = A.mesh_desc(n, topology=topo, jitter=0.12, seed=5)
+    rng = np.random.default_rng(3)
+    q = A.equation_set(phys, basis, params=params, source_kind=source)
+    o = O.Oracle(m, q)
+    x, xd, aux = (rng.uniform(-1, 1, o.n_dofs) for _ in range(3))
+    dof = tx.DOFManager(tx.CartesianConnManager(*n, topology=topo, jitter=0.12, seed=5), q)
+    lof = tx.TpetraLinearObjFactory(dof)
+    cu = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    for i in indices:
+        h = 1e-4 if (phys == A.TX_PHYS_ELASTICITY and i == 1) else 1.0
+        fs = []
+        for sgn in (1.0, -1.0):
+            pp = list(params)
+            pp[i] += sgn * h
+            oo = O.Oracle(m, A.equation_set(phys, basis, params=pp, source_kind=source))
+            fs.append(oo.evaluate(x, xd, aux=aux, jacobian=False)[0])
+        ref = (fs[0] - fs[1]) / (2 * h)
+        dfdp = torch.zeros(o.n_dofs, dtype=torch.float64, device="cuda")
+        tx.AssemblyEngine(lof).evaluateDfdp(cu(x), i, dfdp, x_dot=cu(xd), aux=cu(aux))
+        got = dfdp.cpu().numpy()
+        tol = 1e-7 if h != 1.0 else 1e-12
+        assert np.abs(got - ref).max() <= tol * max(np.abs(ref).max(), 1e-300), (name, i)
+    with pytest.raises(tx.TxError):
+        tx.AssemblyEngine(lof).evaluateDfdp(cu(x), 7, torch.zeros(o.n_dofs, dtype=torch.float64, device="cuda"))

@@ -36,6 +36,7 @@ SIGNATURES = {
     "tx_neumann_value": (C.c_int, [C.POINTER(_abi.NeumannDesc), D, C.POINTER(D)]),
     "tx_neumann_create": (C.c_int, [P, C.POINTER(_abi.NeumannDesc), C.POINTER(I32), C.POINTER(I64)]),
     "tx_neumann_eval": (C.c_int, [P, I32, D, P]),
+    "tx_eval_dfdp": (C.c_int, [P, C.POINTER(_abi.EvalArgs), I32, P]),
     "tx_response_create": (C.c_int, [P, C.POINTER(_abi.ResponseDesc), C.POINTER(I32)]),
     "tx_response_eval": (C.c_int, [P, I32, P, P, P]),
     "tx_set_worksets": (C.c_int, [P, I64, I64, C.c_uint64]),

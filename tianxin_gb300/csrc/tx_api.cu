@@ -179,7 +179,15 @@ int guarded(tx_handle h, F&& body) {
   }
 }
 
-tx::EvalParams make_params(tx_handle h, const tx_eval_args& a) {
+// Coefficients that replace the equation set's in a parameter-derivative evaluation.
+struct CoefOverride {
+  double p[8];
+  double lam, mu;
+  int source_kind;
+  bool zero_aux;
+};
+
+tx::EvalParams make_params(tx_handle h, const tx_eval_args& a, const CoefOverride* ov = nullptr) {
   const tx::Dofs& D = h->dofs;
   tx::EvalParams P{};
   P.coords = h->d_coords;
@@ -200,7 +208,59 @@ tx::EvalParams make_params(tx_handle h, const tx_eval_args& a) {
     P.lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
     P.mu = E / (2.0 * (1.0 + nu));
   }
+  if (ov) {
+    for (int i = 0; i < 8; ++i) P.p[i] = ov->p[i];
+    P.lam = ov->lam; P.mu = ov->mu;
+    P.source_kind = ov->source_kind;
+    if (ov->zero_aux) P.aux = nullptr;
+  }
   return P;
+}
+
+// The residual is affine in every coefficient of these equation sets except
+// Poisson's ratio (through the Lame parameters), so dR/dp_i is the residual
+// evaluated with a derivative coefficient set: p_i -> 1 and the rest -> 0
+// (sources kept only where they scale with p_i), and for E and nu the Lame
+// derivatives.  Returns false for a parameter the physics does not use.
+bool derivative_coefficients(const tx_equation_set_desc& q, int i, CoefOverride& ov) {
+  for (int k = 0; k < 8; ++k) ov.p[k] = 0.0;
+  ov.lam = ov.mu = 0.0;
+  ov.source_kind = TX_SOURCE_CONST;
+  ov.zero_aux = false;
+  switch (q.physics) {
+    case TX_PHYS_POISSON:
+      if (i > 3) return false;
+      if (i == 3 && q.source_kind != TX_SOURCE_CONST) return true;  // the source does not scale with p3
+      ov.p[i] = 1.0;
+      if (i == 1 && q.source_kind == TX_SOURCE_AFFINE) ov.source_kind = TX_SOURCE_AFFINE;  // s = c (1 + x + 2y + 3z)
+      return true;
+    case TX_PHYS_ELASTICITY: {
+      if (i > 5) return false;
+      const double E = q.params[0], nu = q.params[1];
+      if (i == 0) {  // lambda, mu proportional to E
+        ov.lam = nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+        ov.mu = 1.0 / (2.0 * (1.0 + nu));
+      } else if (i == 1) {
+        const double d = (1.0 + nu) * (1.0 - 2.0 * nu);
+        ov.lam = E * (1.0 + 2.0 * nu * nu) / (d * d);
+        ov.mu = -E / (2.0 * (1.0 + nu) * (1.0 + nu));
+      } else {
+        ov.p[i] = 1.0;  // body force component or rho
+      }
+      return true;
+    }
+    case TX_PHYS_HEAT:
+      if (i > 2) return false;
+      ov.p[i] = 1.0;
+      return true;
+    case TX_PHYS_MAXWELL:
+      if (i > 1) return false;
+      ov.p[i] = 1.0;
+      ov.zero_aux = true;  // the current density does not scale with 1/mu or sigma
+      return true;
+    default:
+      return false;
+  }
 }
 
 // Work list of a handle: every block cut into worksets, and each workset into
@@ -253,8 +313,8 @@ int eval_persistent(tx_handle h, const tx_eval_args& a) {
 }
 
 // Evaluate every requested block/range (volume fill).
-int eval_blocks(tx_handle h, const tx_eval_args& a) {
-  tx::EvalParams P = make_params(h, a);
+int eval_blocks(tx_handle h, const tx_eval_args& a, const CoefOverride* ov = nullptr) {
+  tx::EvalParams P = make_params(h, a, ov);
   const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
   const bool det = (a.flags & TX_EVAL_DETERMINISTIC) != 0;
   const bool stage = (a.flags & TX_EVAL_SCATTER_DIRECT) == 0;
@@ -692,6 +752,21 @@ int tx_set_worksets(tx_handle h, int64_t min_size, int64_t max_size, uint64_t se
   h->ws_min = min_size; h->ws_max = max_size; h->ws_seed = seed;
   h->items.clear();  // rebuilt at the next persistent evaluation
   return TX_OK;
+}
+
+int tx_eval_dfdp(tx_handle h, const tx_eval_args* args, int32_t param, double* dfdp) {
+  if (!h || !args || !dfdp) return TX_EINVAL;
+  if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_eval_dfdp before tx_dof_build");
+  if (!args->x) return fail(h, TX_EINVAL, "tx_eval_dfdp: x is required");
+  if (args->block >= h->mesh.nblocks) return fail(h, TX_ERANGE, "tx_eval_dfdp: block out of range");
+  CoefOverride ov;
+  if (param < 0 || !derivative_coefficients(h->dofs.eq, param, ov))
+    return fail(h, TX_ERANGE, "tx_eval_dfdp: the equation set has no parameter with this index");
+  tx_eval_args a = *args;
+  a.f = dfdp;
+  a.crs_vals = nullptr;
+  a.flags &= TX_EVAL_DETERMINISTIC | TX_EVAL_SCATTER_DIRECT;  // FP64 residual type, per block
+  return eval_blocks(h, a, &ov);
 }
 
 int tx_response_create(tx_handle h, const tx_response_desc* d, int32_t* id) {

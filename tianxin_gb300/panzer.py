@@ -311,6 +311,14 @@ class AssemblyEngine:
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_eval(self.dof.h, C.byref(a)), "tx_eval")
 
+    def evaluateDfdp(self, x, param, dfdp, x_dot=None, aux=None, t=0.0, block=-1, workset=(0, -1)):
+        """dfdp += df/dp for the equation set's parameter params[param] (the Tangent type's dfdp vector)."""
+        a = eval_args(x, x_dot, aux, 0.0, 1.0, t, None, None, False, block, workset)
+        lib = self.dof.lib
+        lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(self.dof.h, lib.tx_eval_dfdp(self.dof.h, C.byref(a), int(param), _ptr(dfdp)), "tx_eval_dfdp")
+        return dfdp
+
     def evaluateTangent(self, x, tangent, dfdp, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, block=-1,
                         workset=(0, -1), deterministic=False):
         """Tangent evaluation type: dfdp[i] += (beta dR/dx + alpha dR/dxdot) tangent[i] for the rows of the
