@@ -280,19 +280,34 @@ def run_ours(a):
         return maxall(s.elapsed_time(e) / 1e3 / reps)
 
     reps = max(10, a.steps)
-    # launch shapes (lanes per row x loads per lane): the autotuner times all twelve per precision
+    # forms and launch shapes: CRS (lanes per row x loads per lane, 16 shapes) and entity-block
+    # (lanes per entity x blocks per pass, 8 shapes); the autotuner times all of them per precision
     if a.spmv_shape:
         fixed = tuple(int(v) for v in a.spmv_shape.split(","))
+        W.setApplyForm("crs")
         W.setApplyShape(*fixed)
-        sh64 = sh32 = {"shape": fixed, "candidates": []}
+        sh64 = sh32 = {"form": "crs", "shape": fixed, "candidates": []}
     else:
         sh64 = autotune.tune_spmv(W, W.values, xs, ys)
     t_s64 = time_spmv(W.values, xs, ys, reps)
     if not a.spmv_shape:
         sh32 = autotune.tune_spmv(W, v32, xs32, ys32)
-    t_s32 = time_spmv(v32, xs32, ys32, reps)  # the FP32 shape stays set for the solver's inner SpMV
-    b64 = 12 * nnz + 8 * (N + 1) + 16 * N
-    b32 = 8 * nnz + 8 * (N + 1) + 8 * N
+    t_s32 = time_spmv(v32, xs32, ys32, reps)  # the FP32 form and shape stay set for the solver's inner SpMV
+    n_ent = N // 3
+
+    def spmv_bytes(form, vbytes):
+        # CRS: values, column indices, rowptr, x once, y written; entity-block: one column index per
+        # 3x3 block and the entity rowptr instead of the DOF rowptr
+        if form == "entity":
+            return (vbytes * nnz + 4 * (nnz // 9) + 8 * (n_ent + 1) + 2 * vbytes * N)
+        return (vbytes + 4) * nnz + 8 * (N + 1) + 2 * vbytes * N
+
+    b64, b32 = spmv_bytes(sh64["form"], 8), spmv_bytes(sh32["form"], 4)
+    crs64, crs32 = spmv_bytes("crs", 8), spmv_bytes("crs", 4)
+
+    def best_crs_ms(sh):
+        ts = [t for c, t in sh["candidates"] if c[0] == "crs"]
+        return round(min(ts), 4) if ts else None
     del v32
 
     peak, peak_kind = measured_peaks()
@@ -375,7 +390,11 @@ def run_ours(a):
             "jacobian_mixed_vs_fp64_maxrel": jac_diff,
             "spmv": {"f64_gbs": b64 / t_s64 / 1e9, "f32_gbs": b32 / t_s32 / 1e9, "f64_ms": 1e3 * t_s64,
                      "f32_ms": 1e3 * t_s32, "f64_frac": b64 / t_s64 / 1e9 / peak, "f32_frac": b32 / t_s32 / 1e9 / peak,
-                     "bytes_f64": b64, "bytes_f32": b32, "shape_f64": sh64["shape"], "shape_f32": sh32["shape"],
+                     "bytes_f64": b64, "bytes_f32": b32, "form_f64": sh64["form"], "form_f32": sh32["form"],
+                     "shape_f64": sh64["shape"], "shape_f32": sh32["shape"],
+                     "crs_bytes_f64": crs64, "crs_bytes_f32": crs32,
+                     "crs_equivalent_gbs": {"f64": crs64 / t_s64 / 1e9, "f32": crs32 / t_s32 / 1e9},
+                     "best_crs_form_ms": {"f64": best_crs_ms(sh64), "f32": best_crs_ms(sh32)},
                      "shape_candidates_ms": {"f64": [(c, round(t, 3)) for c, t in sh64["candidates"]],
                                              "f32": [(c, round(t, 3)) for c, t in sh32["candidates"]]}},
             "solve": solve,

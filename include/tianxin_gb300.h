@@ -291,6 +291,13 @@ int tx_response_eval(tx_handle h, int32_t id, const double* x, double* value, do
  * vals/x/y are FP64 (TX_SPMV_F64) or FP32 (TX_SPMV_F32). */
 #define TX_SPMV_F64 0
 #define TX_SPMV_F32 1
+/* OR into precision: rowptr/colind/vals lie on the graph tx_graph_build
+ * wrote for this handle (n_rows = its DOF count, TX_EINVAL otherwise).  Its
+ * nf rows of one entity share one column pattern of nf x nf blocks, so with
+ * nf = 3 the product reads one column index per block from the handle's
+ * entity graph instead of one per entry (12 -> 8.4 bytes an FP64 entry,
+ * 8 -> 4.4 FP32); other nf use the CRS form.  Results equal to rounding. */
+#define TX_SPMV_ENTITY_BLOCKS 0x10
 int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowptr,
             const int32_t* colind, const void* vals, const void* x, void* y,
             double alpha, double beta);
@@ -313,6 +320,9 @@ int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowpt
 #define TX_SOLVE_FIXED_ITERATIONS 0x2u
 /* Reuse the FP32 operator of the previous solve (A unchanged). */
 #define TX_SOLVE_REUSE_OPERATOR 0x4u
+/* The operator lies on the handle's graph: the solver's SpMVs take the
+ * entity-block form of TX_SPMV_ENTITY_BLOCKS. */
+#define TX_SOLVE_ENTITY_BLOCKS 0x8u
 typedef struct tx_solve_args {
   const int64_t* rowptr; const int32_t* colind; const double* vals;
   const double* b;         /* right-hand side (ignored with MATRIX_FREE: b = -f(x0)) */
@@ -377,6 +387,10 @@ int tx_set_grid_cap(tx_handle h, int32_t max_ctas);
  * from the mean row length.  The
  * autotuner's knob for the SpMV; results equal to rounding for every shape. */
 int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll);
+/* Launch shape of the entity-block form (TX_SPMV_ENTITY_BLOCKS,
+ * TX_SOLVE_ENTITY_BLOCKS): lanes per entity 4/8/16/32 and blocks each lane
+ * loads per pass 1/2; (0, 0) = FP64 4 lanes, 1 block, FP32 16 lanes, 2. */
+int tx_set_spmv_entity_shape(tx_handle h, int32_t lanes, int32_t unroll);
 /* Assembly kernel of the per-block mixed evaluation: 0 automatic (the
  * warp-per-element kernel where the element family has one, hex8 elasticity;
  * the CTA-staged kernel elsewhere), 1 always the CTA-staged kernel, 2 the

@@ -5,7 +5,10 @@ length: Poisson tet4 (about 11 entries a row) 4 lanes; Poisson hex8 (about
 23), heat on hex27 + tet10 (about 60; vertex rows of 125 take several
 passes) and elasticity hex8 (about 69) 8 lanes.  A random CSR matrix with
 empty and long rows covers the shape used when the mean is unknown, and
-every tunable shape is checked on two graphs.  Bars: FP64
+every tunable shape is checked on two graphs.  Matrices on the handle's
+graph also take the entity-block form (one column index per 3 x 3 block of
+elasticity; nf = 1 graphs run the CRS form under that flag), checked in every
+shape, on a Dirichlet-modified Jacobian, and inside the solver.  Bars: FP64
 within 1e-13 relative (reassociated sums), FP32 within 1e-5.
 """
 import ctypes as C
@@ -40,13 +43,15 @@ GRAPHS = {
 }
 
 
+@pytest.mark.parametrize("form", ["crs", "entity"])
 @pytest.mark.parametrize("name", list(GRAPHS))
-def test_spmv_on_assembly_graphs(cuda, name):
+def test_spmv_on_assembly_graphs(cuda, name, form):
     g = GRAPHS[name]
     conn = tx.CartesianConnManager(*g["n"], *g["blocks"], topology=g["topo"], jitter=0.1, seed=5)
     dof = tx.DOFManager(conn, A.equation_set(g["phys"], g["basis"], params=g["params"]))
     lof = tx.TpetraLinearObjFactory(dof)
     W = lof.getTpetraMatrix()
+    W.setApplyForm(form)
     rng = np.random.default_rng(11)
     vals = rng.uniform(-1, 1, dof.nnz)
     x = rng.uniform(-1, 1, dof.n_dofs)
@@ -103,6 +108,7 @@ def test_spmv_every_launch_shape(cuda, name):
     xd = torch.from_numpy(x).cuda()
     x32 = xd.float()
     v32 = W.values.float()
+    W.setApplyForm("crs")
     for lanes in (4, 8, 16, 32):
         for unroll in (1, 2, 4, 16):  # 16: aligned 16-byte loads
             W.setApplyShape(lanes, unroll)
@@ -111,6 +117,58 @@ def test_spmv_every_launch_shape(cuda, name):
             y32 = W.apply(x32, values=v32).cpu().numpy()
             assert np.abs(y32 - y_ref).max() <= 1e-5 * np.abs(y_ref).max(), (lanes, unroll)
     W.setApplyShape(0, 0)
+    W.setApplyForm("entity")
+    for lanes in (4, 8, 16, 32):
+        for unroll in (1, 2):
+            W.setEntityApplyShape(lanes, unroll)
+            y = W.apply(xd).cpu().numpy()
+            assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max(), ("entity", lanes, unroll)
+            y32 = W.apply(x32, values=v32).cpu().numpy()
+            assert np.abs(y32 - y_ref).max() <= 1e-5 * np.abs(y_ref).max(), ("entity", lanes, unroll)
+    W.setEntityApplyShape(0, 0)
+
+
+def test_entity_form_on_assembled_dirichlet_jacobian_and_in_the_solver(cuda):
+    # tet4 elasticity: entity degrees vary (4 to about 27 neighbours); Dirichlet rows keep the pattern
+    conn = tx.CartesianConnManager(6, 5, 4, topology=A.TX_TOPO_TET, jitter=0.1, seed=4)
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.0))
+    dof = tx.DOFManager(conn, q)
+    lof = tx.TpetraLinearObjFactory(dof)
+    me = tx.ModelEvaluator(lof, [tx.DirichletBC(dof, A.SIDE_ZMIN)])
+    x, f, W = lof.getTpetraVector(), lof.getTpetraVector(), me.create_W_op()
+    me.evalModel(x, f=f, W=W)
+    vals = W.values.cpu().numpy()
+    rp, ci = W.rowptr.cpu().numpy(), W.colind.cpu().numpy()
+    xs = np.random.default_rng(9).uniform(-1, 1, dof.n_dofs)
+    y_ref = _csr_ref(rp, ci, vals, xs)
+    y = W.apply(torch.from_numpy(xs).cuda()).cpu().numpy()
+    assert W.apply_form == "entity"
+    assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
+    sols = {}
+    for form in ("crs", "entity"):
+        W.setApplyForm(form)
+        xx = lof.getTpetraVector()
+        st = me.solve(W, xx, rtol=1e-11, matrix_free=False, b=-f)
+        assert st["relres"] <= 1e-11, form
+        sols[form] = xx.cpu().numpy()
+    assert np.abs(sols["crs"] - sols["entity"]).max() <= 1e-9 * np.abs(sols["crs"]).max()
+
+
+def test_entity_form_needs_the_handle_graph(cuda):
+    lib = _lib.load()
+    g = GRAPHS["elasticity_hex8"]
+    conn = tx.CartesianConnManager(3, 3, 3)
+    dof = tx.DOFManager(conn, A.equation_set(g["phys"], g["basis"], params=g["params"]))
+    W = tx.TpetraLinearObjFactory(dof).getTpetraMatrix()
+    x = torch.ones(dof.n_dofs, dtype=torch.float64, device="cuda")
+    y = torch.zeros(dof.n_dofs, dtype=torch.float64, device="cuda")
+    rc = lib.tx_spmv(dof.h, A.TX_SPMV_F64 | A.TX_SPMV_ENTITY_BLOCKS, dof.n_dofs - 3, W.rowptr.data_ptr(),
+                     W.colind.data_ptr(), W.values.data_ptr(), x.data_ptr(), y.data_ptr(), 1.0, 0.0)
+    assert rc == A.TX_EINVAL
+    other = tx.CrsMatrix(dof, W.rowptr.clone(), W.colind.clone())
+    assert other.apply_form == "crs"
+    with pytest.raises(ValueError):
+        other.setApplyForm("entity")
 
 
 def test_spmv_vector_shape_on_unaligned_arrays(cuda):

@@ -42,6 +42,7 @@ SIGNATURES = {
     "tx_set_worksets": (C.c_int, [P, I64, I64, C.c_uint64]),
     "tx_set_grid_cap": (C.c_int, [P, I32]),
     "tx_set_spmv_shape": (C.c_int, [P, I32, I32]),
+    "tx_set_spmv_entity_shape": (C.c_int, [P, I32, I32]),
     "tx_set_assembly_variant": (C.c_int, [P, I32]),
     "tx_graph_capture_begin": (C.c_int, [P]),
     "tx_graph_capture_end": (C.c_int, [P, C.POINTER(I32)]),

@@ -100,17 +100,30 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
 
 
 SPMV_SHAPES = [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2, 4, 16)]  # 16: 16-byte loads
+ENTITY_SHAPES = [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2)]
 
 
 def tune_spmv(W, vals, x, y, reps=5):
-    """Time W.apply in every launch shape (lanes per row x loads per lane) and apply the fastest.
+    """Time W.apply in every launch shape of each form it has and apply the fastest.
 
-    Returns {"shape": (lanes, unroll), "ms": t, "candidates": [((lanes, unroll), ms), ...]}.
+    CRS form: lanes per row x loads per lane; entity-block form (matrices on
+    the handle's graph): lanes per entity x blocks per lane pass.  Returns
+    {"form": f, "shape": (lanes, unroll), "ms": t, "candidates": [((form, lanes, unroll), ms), ...]}.
     """
     results = []
+    W.setApplyForm("crs")
     for shape in SPMV_SHAPES:
         W.setApplyShape(*shape)
-        results.append((shape, _time(lambda: W.apply(x, y, values=vals), reps)))
+        results.append((("crs",) + shape, _time(lambda: W.apply(x, y, values=vals), reps)))
+    if W.on_handle_graph:
+        W.setApplyForm("entity")
+        for shape in ENTITY_SHAPES:
+            W.setEntityApplyShape(*shape)
+            results.append((("entity",) + shape, _time(lambda: W.apply(x, y, values=vals), reps)))
     best = min(results, key=lambda r: r[1])
-    W.setApplyShape(*best[0])
-    return {"shape": best[0], "ms": best[1], "candidates": results}
+    best_crs = min((r for r in results if r[0][0] == "crs"), key=lambda r: r[1])
+    W.setApplyShape(*best_crs[0][1:])
+    if best[0][0] == "entity":
+        W.setEntityApplyShape(*best[0][1:])
+    W.setApplyForm(best[0][0])
+    return {"form": best[0][0], "shape": best[0][1:], "ms": best[1], "candidates": results}

@@ -121,7 +121,8 @@ struct tx_handle_s {
   Staging stage;
   std::vector<NeumannSet> neumann;
   std::vector<ResponseSet> responses;
-  tx::SpmvShape spmv;  // SpMV launch shape ({0, 0}: automatic)
+  tx::SpmvShape spmv;     // SpMV launch shape ({0, 0}: automatic)
+  tx::SpmvShape spmv_eb;  // the same for the entity-block form
   int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
@@ -378,6 +379,7 @@ struct MfCtx {
   double* xdot_work;
   int32_t n_neumann;
   const int32_t* neumann_ids;
+  const tx::EntityGraph* eg;  // matrix-based residual in the entity-block form (or null)
 };
 
 int neumann_eval(tx_handle h, int32_t id, double t, double* f);
@@ -408,9 +410,10 @@ int outer_residual(void* vctx, const double* x, double* r) {
     return TX_OK;
   }
   if (cudaMemcpyAsync(r, c->b, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess) return TX_ECUDA;
-  if (tx::launch_spmv_f64(n, c->rowptr, c->colind, c->vals, x, r, -1.0, 1.0, h->dofs.nnz, h->stream, h->spmv) !=
-      cudaSuccess)
-    return TX_ECUDA;
+  const cudaError_t e =
+      c->eg ? tx::launch_spmv_entity_f64(*c->eg, c->vals, x, r, -1.0, 1.0, h->stream, h->spmv_eb)
+            : tx::launch_spmv_f64(n, c->rowptr, c->colind, c->vals, x, r, -1.0, 1.0, h->dofs.nnz, h->stream, h->spmv);
+  if (e != cudaSuccess) return TX_ECUDA;
   return TX_OK;
 }
 
@@ -637,13 +640,35 @@ int tx_dirichlet_apply(tx_handle h, int64_t n, const int32_t* lids, const double
   return TX_OK;
 }
 
+// The handle's entity graph when the caller declares (TX_SPMV_ENTITY_BLOCKS,
+// TX_SOLVE_ENTITY_BLOCKS) that its CRS is the one tx_graph_build wrote, the
+// DOFs carry kEntityNf fields each and the rows number n_dofs; else null (the
+// CRS form serves, e.g. for nf = 1, where both forms read the same bytes).
+const tx::EntityGraph* entity_graph(tx_handle h, int64_t n_rows, tx::EntityGraph& eg) {
+  if (!h->have_dofs || h->dofs.nf != tx::kEntityNf || n_rows != h->dofs.n_dofs || !h->d_erowptr) return nullptr;
+  eg = tx::EntityGraph{h->d_erowptr, h->d_ecol, h->dofs.n_entities};
+  return &eg;
+}
+
 int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowptr, const int32_t* colind,
             const void* vals, const void* x, void* y, double alpha, double beta) {
   if (!h || !rowptr || !colind || !vals || !x || !y) return TX_EINVAL;
   if (n_rows < 0) return fail(h, TX_EINVAL, "tx_spmv: negative row count");
   const int64_t hint = (h->have_dofs && n_rows == h->dofs.n_dofs) ? h->dofs.nnz : 0;
+  const bool entity = (precision & TX_SPMV_ENTITY_BLOCKS) != 0;
+  precision &= ~TX_SPMV_ENTITY_BLOCKS;
+  if (entity && (!h->have_dofs || n_rows != h->dofs.n_dofs))
+    return fail(h, TX_EINVAL, "tx_spmv: TX_SPMV_ENTITY_BLOCKS needs the handle's graph (n_rows = its DOF count)");
+  tx::EntityGraph egs;
+  const tx::EntityGraph* eg = entity ? entity_graph(h, n_rows, egs) : nullptr;
   cudaError_t e;
-  if (precision == TX_SPMV_F64)
+  if (eg && precision == TX_SPMV_F64)
+    e = tx::launch_spmv_entity_f64(*eg, (const double*)vals, (const double*)x, (double*)y, alpha, beta, h->stream,
+                                   h->spmv_eb);
+  else if (eg && precision == TX_SPMV_F32)
+    e = tx::launch_spmv_entity_f32(*eg, (const float*)vals, (const float*)x, (float*)y, (float)alpha, (float)beta,
+                                   h->stream, h->spmv_eb);
+  else if (precision == TX_SPMV_F64)
     e = tx::launch_spmv_f64(n_rows, rowptr, colind, (const double*)vals, (const double*)x, (double*)y, alpha, beta,
                             hint, h->stream, h->spmv);
   else if (precision == TX_SPMV_F32)
@@ -665,9 +690,11 @@ int tx_solve_cg_ir(tx_handle h, tx_solve_args* a) {
   const int64_t n = h->dofs.n_dofs;
   cudaError_t e = tx::solver_alloc(h->solver, n, h->dofs.nnz);
   if (e != cudaSuccess) return fail(h, TX_ENOMEM, std::string("tx_solve_cg_ir: ") + cudaGetErrorString(e));
+  tx::EntityGraph egs;
+  const tx::EntityGraph* eg = (a->flags & TX_SOLVE_ENTITY_BLOCKS) ? entity_graph(h, n, egs) : nullptr;
   MfCtx ctx{h, a->x_dot, a->alpha, a->beta, a->t, a->n_dirichlet, a->dirichlet_lids, a->dirichlet_g,
             a->b, a->rowptr, a->colind, a->vals, mf, a->x_pred, a->x_dot_coef, h->solver.xdw,
-            a->n_neumann, a->neumann_ids};
+            a->n_neumann, a->neumann_ids, eg};
   if (a->x_pred && !mf) return fail(h, TX_EINVAL, "tx_solve_cg_ir: x_pred needs MATRIX_FREE_RESIDUAL");
   if (a->n_neumann < 0 || (a->n_neumann > 0 && !a->neumann_ids))
     return fail(h, TX_EINVAL, "tx_solve_cg_ir: neumann ids");
@@ -676,12 +703,13 @@ int tx_solve_cg_ir(tx_handle h, tx_solve_args* a) {
       return fail(h, TX_ERANGE, "tx_solve_cg_ir: unknown Neumann set");
   std::string err;
   h->solver.spmv = h->spmv;
+  h->solver.spmv_eb = h->spmv_eb;
   int rc = tx::solve_cg_ir(h->solver, a->rowptr, a->colind, a->vals, a->n_dirichlet, a->dirichlet_lids, a->x,
                            outer_residual, &ctx, a->rtol > 0 ? a->rtol : 1e-10,
                            a->inner_rtol > 0 ? a->inner_rtol : 1e-5, a->max_outer > 0 ? a->max_outer : 50,
                            a->max_inner > 0 ? a->max_inner : 100000, a->stats, h->stream, err,
                            (a->flags & TX_SOLVE_FIXED_ITERATIONS) != 0, (a->flags & TX_SOLVE_REUSE_OPERATOR) != 0,
-                           a->stats_device);
+                           a->stats_device, eg);
   if (rc == TX_ETIMEDOUT) return fail(h, rc, "tx_solve_cg_ir: did not reach rtol within max_outer iterations");
   if (rc) return fail(h, rc, err);
   return TX_OK;
@@ -885,6 +913,15 @@ int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll) {
   if (!tx::spmv_shape_valid(sh))
     return fail(h, TX_EINVAL, "tx_set_spmv_shape: lanes 4/8/16/32 and unroll 1/2/4, or both 0");
   h->spmv = sh;
+  return TX_OK;
+}
+
+int tx_set_spmv_entity_shape(tx_handle h, int32_t lanes, int32_t unroll) {
+  if (!h) return TX_EINVAL;
+  const tx::SpmvShape sh{lanes, unroll};
+  if (!tx::entity_shape_valid(sh))
+    return fail(h, TX_EINVAL, "tx_set_spmv_entity_shape: lanes 4/8/16/32 and unroll 1/2, or both 0");
+  h->spmv_eb = sh;
   return TX_OK;
 }
 

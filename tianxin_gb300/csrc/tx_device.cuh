@@ -72,6 +72,22 @@ struct SpmvShape {
   int lanes = 0, unroll = 0;
 };
 bool spmv_shape_valid(SpmvShape sh);
+// The entity graph behind the CRS the library expands from it (row nf*r + c
+// holds the nf columns nf*m .. nf*m+nf-1 of every neighbour entity m of r, in
+// ascending m): the entity-block SpMV reads one column index per nf x nf
+// block from it.  Built for nf = kEntityNf (3D elasticity); other nf use the
+// CRS form.  Shapes: lanes per entity 4/8/16/32, blocks per lane pass 1/2.
+constexpr int kEntityNf = 3;
+struct EntityGraph {
+  const int64_t* erp = nullptr;
+  const int32_t* ecol = nullptr;
+  int64_t n_ent = 0;
+};
+bool entity_shape_valid(SpmvShape sh);
+cudaError_t launch_spmv_entity_f64(const EntityGraph& eg, const double* vals, const double* x, double* y, double a,
+                                   double b, cudaStream_t s, SpmvShape shape = SpmvShape());
+cudaError_t launch_spmv_entity_f32(const EntityGraph& eg, const float* vals, const float* x, float* y, float a,
+                                   float b, cudaStream_t s, SpmvShape shape = SpmvShape());
 // Warp-per-element mixed assembly (hex8 elasticity, FP32 element math, atomic
 // FP64 scatter): the same results as launch_assemble's staged FP32 kernel up to
 // the summation order.
@@ -107,6 +123,7 @@ struct SolverWork {
   double* scal = nullptr;      // device scalars
   double* host_scal = nullptr; // pinned mirror
   SpmvShape spmv;              // shape of the inner FP32 SpMV
+  SpmvShape spmv_eb;           // its shape in the entity-block form
 };
 constexpr int kRedBlocks = 1024;
 constexpr int kRedSlots = 4;
@@ -121,7 +138,8 @@ typedef int (*ResidualFn)(void* ctx, const double* x, double* r);
 int solve_cg_ir(SolverWork& w, const int64_t* rowptr, const int32_t* colind, const double* vals,
                 int64_t n_dir, const int32_t* dir_lids, double* x, ResidualFn resid, void* ctx,
                 double rtol, double inner_rtol, int max_outer, int max_inner, double* stats,
-                cudaStream_t s, std::string& err, bool fixed, bool reuse_op, double* stats_dev);
+                cudaStream_t s, std::string& err, bool fixed, bool reuse_op, double* stats_dev,
+                const EntityGraph* eg = nullptr);
 
 // Vector helpers used by the API layer
 cudaError_t launch_fill(double* p, double v, int64_t n, cudaStream_t s);

@@ -166,6 +166,111 @@ __global__ void __launch_bounds__(kThreads) k_spmv(int64_t n, const int64_t* __r
   }
 }
 
+// Entity-block form of the product on the graph this library expands: row
+// nf*r + c holds, for each neighbour entity m of r in ascending order, the nf
+// columns nf*m .. nf*m+nf-1, so the nf rows of entity r share one column
+// pattern, and row c's values start at nf*nf*erp[r] + c*nf*deg(r).  G lanes
+// take one entity; lane sub walks the blocks j = sub, sub+G, ..., reads the
+// block's one column index ecol[erp[r]+j] and its nf values of x, and applies
+// them to the block's nf x nf entries in all nf rows.  Index traffic falls
+// from 4 bytes an entry to 4/nf^2, and x is read once a block, not once an
+// entry.  U blocks per pass are loaded before any x gather issues.  Every
+// load address lies inside its array whatever the data: a pass slot past the
+// row end re-reads block j and zeroes its x values (a select, not an FP64
+// multiply: GB300's FP64 pipe is the scarce unit here, one FMA an entry), and
+// a column index outside [0, n_ent) reads entity 0.
+template <typename T, int NF, int G, int U>
+__device__ __forceinline__ void entity_dot(int64_t b, int64_t deg, int sub, const int32_t* __restrict__ ecol,
+                                           const T* __restrict__ vals, const T* __restrict__ x, int64_t n_ent,
+                                           T (&s)[NF]) {
+  const T* v0 = vals + (int64_t)NF * NF * b;
+  const int64_t rs = (int64_t)NF * deg;  // distance between the entity's rows
+  for (int64_t j = sub; j < deg; j += G * U) {
+    bool in[U];
+    int64_t m[U];
+    T v[U][NF][NF];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t jj = j + u * G;
+      in[u] = jj < deg;
+      const int64_t jc = in[u] ? jj : j;
+      const uint32_t mm = (uint32_t)__ldcs(ecol + b + jc);
+      m[u] = (uint64_t)mm < (uint64_t)n_ent ? (int64_t)mm : 0;
+#pragma unroll
+      for (int c = 0; c < NF; ++c)
+#pragma unroll
+        for (int d = 0; d < NF; ++d) v[u][c][d] = __ldcs(v0 + c * rs + NF * jc + d);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      T xm[NF];
+#pragma unroll
+      for (int d = 0; d < NF; ++d) {
+        const T xv = __ldg(x + NF * m[u] + d);
+        xm[d] = in[u] ? xv : T(0);
+      }
+#pragma unroll
+      for (int c = 0; c < NF; ++c)
+#pragma unroll
+        for (int d = 0; d < NF; ++d) s[c] += v[u][c][d] * xm[d];
+    }
+  }
+}
+
+// Sums the G lanes' partial rows of one entity (NF = 3) by reduce-scatter:
+// with the rows padded to 4, an exchange across lane bit 1 leaves each lane
+// two rows (sub & 2 picks which), one across bit 0 leaves one row (sub & 3),
+// and butterflies over the G/4 lanes sharing a row finish it: 3 + log2(G/4)
+// additions a lane instead of 3 log2(G) for three butterflies.  Lane sub < 3
+// returns row sub.  G >= 4.
+template <typename T, int NF, int G>
+__device__ __forceinline__ T entity_reduce(const T (&s)[NF], int sub) {
+  static_assert(NF == 3 && G >= 4, "reduce-scatter of three rows over at least four lanes");
+  const bool hi = (sub & 2) != 0, lo = (sub & 1) != 0;
+  T a0 = hi ? s[2] : s[0];
+  T a1 = hi ? T(0) : s[1];
+  const T b0 = hi ? s[0] : s[2];
+  const T b1 = hi ? s[1] : T(0);
+  a0 += __shfl_xor_sync(0xffffffffu, b0, 2, G);
+  a1 += __shfl_xor_sync(0xffffffffu, b1, 2, G);
+  T k = lo ? a1 : a0;
+  k += __shfl_xor_sync(0xffffffffu, lo ? a0 : a1, 1, G);
+#pragma unroll
+  for (int o = 4; o < G; o <<= 1) k += __shfl_xor_sync(0xffffffffu, k, o, G);
+  return k;
+}
+
+// Six resident CTAs an SM (40 registers) for up to 16 lanes an entity, four
+// (64 registers) for 32 lanes, whose FP64 form would spill at 40.
+constexpr int entity_min_blocks(int G) { return G >= 32 ? 4 : 6; }
+
+// y = alpha A x + beta y in the entity-block form; entity loop per warp as in
+// k_spmv (warp-uniform trip count for the full-mask shuffles).
+template <typename T, int NF, int G, int U>
+__global__ void __launch_bounds__(kThreads, entity_min_blocks(G)) k_spmv_eb(int64_t n_ent, const int64_t* __restrict__ erp,
+                                                      const int32_t* __restrict__ ecol, const T* __restrict__ vals,
+                                                      const T* __restrict__ x, T* __restrict__ y, T alpha, T beta) {
+  constexpr int GPW = 32 / G;  // entities per warp
+  const int sub = threadIdx.x % G;
+  const int g = (threadIdx.x & 31) / G;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = warp * GPW; base < n_ent; base += nwarps * GPW) {
+    const int64_t r = base + g;
+    T s[NF];
+#pragma unroll
+    for (int c = 0; c < NF; ++c) s[c] = T(0);
+    const int64_t rc = r < n_ent ? r : n_ent - 1;  // rows past the end read the last entity's bounds
+    const int64_t b = __ldg(erp + rc);
+    entity_dot<T, NF, G, U>(b, r < n_ent ? __ldg(erp + rc + 1) - b : 0, sub, ecol, vals, x, n_ent, s);
+    const T sc = entity_reduce<T, NF, G>(s, sub);
+    if (r < n_ent && sub < NF) {
+      const int64_t row = (int64_t)NF * r + sub;
+      y[row] = beta == T(0) ? alpha * sc : alpha * sc + beta * y[row];
+    }
+  }
+}
+
 // The automatic shape, from timings of every shape on the 128^3 elasticity
 // operator (80 entries a row): narrow row groups win (8 lanes, FP64 1.52 ms
 // against 3.84 ms for a warp per row), FP32 gains from four loads per lane.
@@ -215,6 +320,37 @@ cudaError_t spmv_dispatch(int64_t n, const int64_t* rp, const int32_t* col, cons
   if (sh.unroll == kSpmvVector && !chunk_aligned<T>(vals, col)) sh.unroll = 1;
   return with_shape(sh, SpmvLaunch<T>{n, rp, col, vals, x, y, a, b, s});
 }
+
+// Entity-block shapes: lanes per entity 4/8/16/32, blocks per lane pass 1/2.
+// {0, 0}: FP64 4 lanes, 1 block: GB300's FP64 pipe (about two FMAs a clock an
+// SM) bounds the FP64 product, and 4 lanes waste the fewest FMA slots on the
+// 27 blocks of an interior entity (28 slots) and on the row sums; FP32 16
+// lanes, 2 blocks, the fastest of the eight on the 128^3 elasticity operator.
+SpmvShape resolve_entity_shape(SpmvShape sh, bool f32) {
+  if (sh.lanes > 0 && sh.unroll > 0) return sh;
+  return f32 ? SpmvShape{16, 2} : SpmvShape{4, 1};
+}
+
+template <typename F>
+cudaError_t with_entity_shape(SpmvShape sh, F&& f) {
+#define TX_ESHAPE(L, U) \
+  if (sh.lanes == L && sh.unroll == U) return f.template run<L, U>();
+  TX_ESHAPE(4, 1) TX_ESHAPE(4, 2) TX_ESHAPE(8, 1) TX_ESHAPE(8, 2)
+  TX_ESHAPE(16, 1) TX_ESHAPE(16, 2) TX_ESHAPE(32, 1) TX_ESHAPE(32, 2)
+#undef TX_ESHAPE
+  return cudaErrorInvalidValue;
+}
+
+template <typename T>
+struct EntitySpmvLaunch {
+  EntityGraph eg; const T* vals; const T* x; T* y; T a, b; cudaStream_t s;
+  template <int L, int U>
+  cudaError_t run() const {
+    k_spmv_eb<T, kEntityNf, L, U><<<grid_for(eg.n_ent, kThreads / L, 152 * 64), kThreads, 0, s>>>(
+        eg.n_ent, eg.erp, eg.ecol, vals, x, y, a, b);
+    return cudaGetLastError();
+  }
+};
 
 // ------------------------------------------------------------ reductions
 // Block partial sums into red[slot * kRedBlocks + block]; a one-block
@@ -341,6 +477,38 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(int64_t n, const int64_t*
   if (threadIdx.x == 0) red[2 * kRedBlocks + blockIdx.x] = pq;
 }
 
+// q = A p and partial dot(p, q) in the entity-block form
+template <int NF, int G, int U>
+__global__ void __launch_bounds__(kThreads, entity_min_blocks(G)) k_spmv_dot_eb(int64_t n_ent, const int64_t* __restrict__ erp,
+                                                          const int32_t* __restrict__ ecol,
+                                                          const float* __restrict__ vals, const float* __restrict__ p,
+                                                          float* __restrict__ q, double* __restrict__ red) {
+  __shared__ double sh[32];
+  constexpr int GPW = 32 / G;
+  const int sub = threadIdx.x % G;
+  const int g = (threadIdx.x & 31) / G;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double pq = 0.0;
+  for (int64_t base = warp * GPW; base < n_ent; base += nwarps * GPW) {  // warp-uniform trip count
+    const int64_t r = base + g;
+    float s[NF];
+#pragma unroll
+    for (int c = 0; c < NF; ++c) s[c] = 0.0f;
+    const int64_t rc = r < n_ent ? r : n_ent - 1;
+    const int64_t b = __ldg(erp + rc);
+    entity_dot<float, NF, G, U>(b, r < n_ent ? __ldg(erp + rc + 1) - b : 0, sub, ecol, vals, p, n_ent, s);
+    const float sc = entity_reduce<float, NF, G>(s, sub);
+    if (r < n_ent && sub < NF) {
+      const int64_t row = (int64_t)NF * r + sub;
+      q[row] = sc;
+      pq += (double)sc * p[row];
+    }
+  }
+  pq = block_sum(pq, sh);
+  if (threadIdx.x == 0) red[2 * kRedBlocks + blockIdx.x] = pq;
+}
+
 // scal: [0] rz, [1] rr, [2] pq.  d += a p, r -= a q, z = dinv r; partial rz', rr'
 __global__ void k_cg_update(int64_t n, const double* __restrict__ scal, const float* __restrict__ dinv,
                             const float* __restrict__ p, const float* __restrict__ q, float* r, float* z, float* d,
@@ -423,6 +591,21 @@ bool spmv_shape_valid(SpmvShape sh) {
   const bool u = sh.unroll == 1 || sh.unroll == 2 || sh.unroll == 4 || sh.unroll == kSpmvVector;
   return l && u;
 }
+bool entity_shape_valid(SpmvShape sh) {
+  if (sh.lanes == 0 && sh.unroll == 0) return true;
+  const bool l = sh.lanes == 4 || sh.lanes == 8 || sh.lanes == 16 || sh.lanes == 32;
+  return l && (sh.unroll == 1 || sh.unroll == 2);
+}
+cudaError_t launch_spmv_entity_f64(const EntityGraph& eg, const double* vals, const double* x, double* y, double a,
+                                   double b, cudaStream_t s, SpmvShape shape) {
+  if (eg.n_ent <= 0) return cudaSuccess;
+  return with_entity_shape(resolve_entity_shape(shape, false), EntitySpmvLaunch<double>{eg, vals, x, y, a, b, s});
+}
+cudaError_t launch_spmv_entity_f32(const EntityGraph& eg, const float* vals, const float* x, float* y, float a,
+                                   float b, cudaStream_t s, SpmvShape shape) {
+  if (eg.n_ent <= 0) return cudaSuccess;
+  return with_entity_shape(resolve_entity_shape(shape, true), EntitySpmvLaunch<float>{eg, vals, x, y, a, b, s});
+}
 cudaError_t launch_spmv_f64(int64_t n, const int64_t* rp, const int32_t* col, const double* vals, const double* x,
                             double* y, double a, double b, int64_t nnz_hint, cudaStream_t s, SpmvShape shape) {
   return spmv_dispatch<double>(n, rp, col, vals, x, y, a, b, nnz_hint, s, shape);
@@ -502,10 +685,20 @@ struct DotLaunch {
   }
 };
 
+// the same in the entity-block form
+struct DotEntityLaunch {
+  EntityGraph eg; const SolverWork* w; unsigned gb; cudaStream_t s;
+  template <int L, int U>
+  cudaError_t run() const {
+    k_spmv_dot_eb<kEntityNf, L, U><<<gb, kThreads, 0, s>>>(eg.n_ent, eg.erp, eg.ecol, w->vals32, w->p, w->q, w->red);
+    return cudaSuccess;
+  }
+};
+
 int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const double* vals, int64_t n_dir,
                 const int32_t* dir, double* x, ResidualFn resid, void* ctx, double rtol, double inner_rtol,
                 int max_outer, int max_inner, double* stats, cudaStream_t s, std::string& err, bool fixed,
-                bool reuse_op, double* stats_dev) {
+                bool reuse_op, double* stats_dev, const EntityGraph* eg) {
   const int64_t n = w.n;
   const unsigned gb = kRedBlocks;
   auto cuda_fail = [&](cudaError_t e, const char* where) {
@@ -522,7 +715,11 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
   }
   SpmvShape shape = resolve_shape(w.spmv, n, w.nnz, true);
   if (shape.unroll == kSpmvVector && !chunk_aligned<float>(w.vals32, col)) shape.unroll = 1;
-  auto spmv_dot = [&]() { with_shape(shape, DotLaunch{n, rp, col, &w, gb, s}); };
+  const SpmvShape eshape = resolve_entity_shape(w.spmv_eb, true);
+  auto spmv_dot = [&]() {
+    if (eg) with_entity_shape(eshape, DotEntityLaunch{*eg, &w, gb, s});
+    else with_shape(shape, DotLaunch{n, rp, col, &w, gb, s});
+  };
   auto cg_iteration = [&]() {
     spmv_dot();
     k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2);  // pq

@@ -138,13 +138,21 @@ class DOFManager:
 
 
 class CrsMatrix:
-    """Tpetra local CRS on the device: rowptr int64, colind int32, values f64."""
+    """Tpetra local CRS on the device: rowptr int64, colind int32, values f64.
 
-    def __init__(self, dof, rowptr, colind, values=None):
+    on_handle_graph: rowptr/colind are the graph the DOF manager's handle
+    built (TpetraLinearObjFactory), so apply and the solver may take the
+    entity-block form (one column index per nf x nf block); apply_form is
+    "entity" or "crs".
+    """
+
+    def __init__(self, dof, rowptr, colind, values=None, on_handle_graph=False):
         self.dof, self.rowptr, self.colind = dof, rowptr, colind
         self.values = values if values is not None else torch.zeros(colind.numel(), dtype=torch.float64,
                                                                       device=colind.device)
         self.n_rows = rowptr.numel() - 1
+        self.on_handle_graph = on_handle_graph
+        self.apply_form = "entity" if on_handle_graph else "crs"
 
     def initializeMatrix(self, v=0.0):
         self.values.fill_(v)
@@ -153,6 +161,8 @@ class CrsMatrix:
         """y = alpha A x + beta y (Tpetra::CrsMatrix::apply); f64 or f32 by dtype of values."""
         vals = self.values if values is None else values
         prec = _abi.TX_SPMV_F64 if vals.dtype == torch.float64 else _abi.TX_SPMV_F32
+        if self.apply_form == "entity":
+            prec |= _abi.TX_SPMV_ENTITY_BLOCKS
         if y is None:
             y = torch.zeros(self.n_rows, dtype=vals.dtype, device=vals.device)
         lib = self.dof.lib
@@ -164,6 +174,17 @@ class CrsMatrix:
     def setApplyShape(self, lanes=0, unroll=0):
         """Launch shape of apply (and of the solver's SpMV) on this handle: lanes per row, loads per lane; 0, 0 = auto."""
         check(self.dof.h, self.dof.lib.tx_set_spmv_shape(self.dof.h, lanes, unroll), "tx_set_spmv_shape")
+
+    def setEntityApplyShape(self, lanes=0, unroll=0):
+        """Launch shape of the entity-block form: lanes per entity, blocks per lane pass; 0, 0 = auto."""
+        check(self.dof.h, self.dof.lib.tx_set_spmv_entity_shape(self.dof.h, lanes, unroll),
+              "tx_set_spmv_entity_shape")
+
+    def setApplyForm(self, form):
+        """"entity" (the handle's graph only) or "crs"."""
+        if form not in ("entity", "crs") or (form == "entity" and not self.on_handle_graph):
+            raise ValueError(f"apply form {form!r} not available for this matrix")
+        self.apply_form = form
 
     def to_scipy(self):
         import scipy.sparse as sp
@@ -185,7 +206,7 @@ class TpetraLinearObjFactory:
         return self.rowptr, self.colind
 
     def getTpetraMatrix(self):
-        return CrsMatrix(self.dof, self.rowptr, self.colind)
+        return CrsMatrix(self.dof, self.rowptr, self.colind, on_handle_graph=True)
 
     def getTpetraVector(self):
         return torch.zeros(self.dof.n_dofs, dtype=torch.float64, device=self.device)
@@ -392,7 +413,8 @@ class ModelEvaluator:
         a.rtol, a.inner_rtol, a.max_outer, a.max_inner = rtol, inner_rtol, max_outer, max_inner
         a.flags = ((_abi.TX_SOLVE_MATRIX_FREE_RESIDUAL if matrix_free else 0) |
                    (_abi.TX_SOLVE_FIXED_ITERATIONS if fixed else 0) |
-                   (_abi.TX_SOLVE_REUSE_OPERATOR if reuse_operator else 0))
+                   (_abi.TX_SOLVE_REUSE_OPERATOR if reuse_operator else 0) |
+                   (_abi.TX_SOLVE_ENTITY_BLOCKS if getattr(W, "apply_form", "crs") == "entity" else 0))
         a.x_dot, a.alpha, a.beta, a.t = _ptr(x_dot), alpha, beta, t
         a.stats_device = _ptr(stats_device)
         a.x_pred, a.x_dot_coef = _ptr(x_pred), x_dot_coef
