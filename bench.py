@@ -44,7 +44,10 @@ def args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--spmv-shape", default=None,
-                   help="LANES,UNROLL for both SpMV legs instead of autotuning them (e.g. 8,1)")
+                   help="fixed SpMV launch shape instead of the autotuner: lanes,unroll (both precisions) "
+                        "or lanes,unroll/lanes,unroll (FP64/FP32)")
+    p.add_argument("--spmv-form", default="crs", choices=["crs", "entity"],
+                   help="SpMV form used with --spmv-shape")
     return p.parse_args()
 
 
@@ -282,16 +285,18 @@ def run_ours(a):
     reps = max(10, a.steps)
     # forms and launch shapes: CRS (lanes per row x loads per lane, 16 shapes) and entity-block
     # (lanes per entity x blocks per pass, 8 shapes); the autotuner times all of them per precision
+    def fix_shape(shape):
+        W.setApplyForm(a.spmv_form)
+        (W.setApplyShape if a.spmv_form == "crs" else W.setEntityApplyShape)(*shape)
+        return {"form": a.spmv_form, "shape": shape, "candidates": []}
+
     if a.spmv_shape:
-        fixed = tuple(int(v) for v in a.spmv_shape.split(","))
-        W.setApplyForm("crs")
-        W.setApplyShape(*fixed)
-        sh64 = sh32 = {"form": "crs", "shape": fixed, "candidates": []}
+        parts = [tuple(int(v) for v in p.split(",")) for p in a.spmv_shape.split("/")]
+        sh64 = fix_shape(parts[0])
     else:
         sh64 = autotune.tune_spmv(W, W.values, xs, ys)
     t_s64 = time_spmv(W.values, xs, ys, reps)
-    if not a.spmv_shape:
-        sh32 = autotune.tune_spmv(W, v32, xs32, ys32)
+    sh32 = fix_shape(parts[-1]) if a.spmv_shape else autotune.tune_spmv(W, v32, xs32, ys32)
     t_s32 = time_spmv(v32, xs32, ys32, reps)  # the FP32 form and shape stay set for the solver's inner SpMV
     n_ent = N // 3
 
