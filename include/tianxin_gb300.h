@@ -362,6 +362,34 @@ int tx_graph_capture_end(tx_handle h, int32_t* graph_id);
 int tx_graph_launch(tx_handle h, int32_t graph_id);
 int tx_graph_destroy(tx_handle h, int32_t graph_id);
 
+/* ------------------------------------------------------------ blocked layout
+ * BlockedDOFManager + BlockedTpetraLinearObjFactory
+ * (disc-fe/src/lof/Panzer_BlockedTpetraLinearObjFactory_impl.hpp): the
+ * equation set's fields are grouped into n_blocks field blocks
+ * (field_block[f] = block of field f, fields in field order, every block
+ * non-empty).  Block i with b_i fields numbers its DOFs b_i * entity + k (k =
+ * the field's place in the block, entities in the interleaved numbering's LID
+ * order), block vectors are the product vector's pieces, and block (i, j) of
+ * the operator is a Tpetra-layout CRS whose row (entity r, k) holds the b_j
+ * columns b_j * m + l of every neighbour entity m of r, ascending.  Host
+ * calls; the data calls (graph, split, merge, spmv) are launch-only on the
+ * handle's stream.  Pointer arrays (xb, yb, blk_vals) are HOST arrays of
+ * DEVICE pointers; blk_vals has n_blocks^2 entries, row-major, NULL for an
+ * excluded pair (BlockedTpetraLinearObjFactory::addExcludedPair). */
+int tx_blocked_layout(tx_handle h, int32_t n_blocks, const int32_t* field_block);
+int tx_blocked_sizes(tx_handle h, int32_t i, int32_t j, int64_t* n_rows, int64_t* n_cols, int64_t* nnz);
+/* rowptr [n_rows + 1] int64, colind [nnz] int32 of block (i, j) (getGraph(i, j)) */
+int tx_blocked_graph_build(tx_handle h, int32_t i, int32_t j, int64_t* rowptr, int32_t* colind);
+/* interleaved vector x [N] -> block vectors xb[k] [n_rows(k)], and back */
+int tx_blocked_split_vector(tx_handle h, const double* x, double* const* xb);
+int tx_blocked_merge_vector(tx_handle h, const double* const* xb, double* x);
+/* interleaved CRS values (tx_graph_build's graph) -> block CRS values */
+int tx_blocked_split_matrix(tx_handle h, const double* crs_vals, double* const* blk_vals);
+/* y_i = alpha sum_j A_ij x_j + beta y_i over the blocks not excluded (the
+ * blocked Thyra operator's apply), FP64 */
+int tx_blocked_spmv(tx_handle h, const double* const* blk_vals, const double* const* xb, double* const* yb,
+                    double alpha, double beta);
+
 /* Parameter sensitivity of the residual (the dfdp vectors that
  * ScatterResidual_Tpetra<Tangent> fills for an active scalar parameter,
  * Panzer_ScatterResidual_Tpetra_impl.hpp:218-270): dfdp += df/dparams[param]

@@ -54,6 +54,13 @@ SIGNATURES = {
     "tx_batch_last_error": (C.c_char_p, [P]),
     "tx_batch_destroy": (None, [P]),
     "tx_eval_noalloc": (C.c_int, [P, C.POINTER(_abi.EvalArgs)]),
+    "tx_blocked_layout": (C.c_int, [P, I32, P]),
+    "tx_blocked_sizes": (C.c_int, [P, I32, I32, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)]),
+    "tx_blocked_graph_build": (C.c_int, [P, I32, I32, P, P]),
+    "tx_blocked_split_vector": (C.c_int, [P, P, P]),
+    "tx_blocked_merge_vector": (C.c_int, [P, P, P]),
+    "tx_blocked_split_matrix": (C.c_int, [P, P, P]),
+    "tx_blocked_spmv": (C.c_int, [P, P, P, P, D, D]),
     "tx_set_stream": (C.c_int, [P, P]),
     "tx_synchronize": (C.c_int, [P]),
 }

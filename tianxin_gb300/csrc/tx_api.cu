@@ -126,6 +126,16 @@ struct tx_handle_s {
   int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
+  // blocked layout (tx_blocked_layout) and the device graphs of its blocks,
+  // one per (fields in row block, fields in column block)
+  tx::BlockedMap blocked;
+  struct BlockGraph { int64_t* rp = nullptr; int32_t* col = nullptr; };
+  BlockGraph block_graphs[tx::kMaxFieldBlocks + 1][tx::kMaxFieldBlocks + 1];
+
+  void free_block_graphs() {
+    for (auto& row : block_graphs)
+      for (auto& g : row) { cudaFree(g.rp); cudaFree(g.col); g = BlockGraph(); }
+  }
 
   void free_dofs() {
     for (auto& ns : neumann) { cudaFree(ns.sides); cudaFree(ns.tables); }
@@ -147,6 +157,8 @@ struct tx_handle_s {
     cudaFree(d_erowptr); cudaFree(d_ecol); cudaFree(d_rowptr);
     d_erowptr = nullptr; d_ecol = nullptr; d_rowptr = nullptr;
     tx::solver_free(solver);
+    free_block_graphs();
+    blocked = tx::BlockedMap();
     have_dofs = false;
     have_host_dofs = false;
   }
@@ -913,6 +925,159 @@ int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll) {
   if (!tx::spmv_shape_valid(sh))
     return fail(h, TX_EINVAL, "tx_set_spmv_shape: lanes 4/8/16/32 and unroll 1/2/4, or both 0");
   h->spmv = sh;
+  return TX_OK;
+}
+
+// ---------------------------------------------------------------- blocked layout
+
+int tx_blocked_layout(tx_handle h, int32_t n_blocks, const int32_t* field_block) {
+  if (!h || !field_block) return TX_EINVAL;
+  if (!h->have_host_dofs) return fail(h, TX_ESTATE, "tx_blocked_layout before tx_dof_build");
+  const int nf = h->dofs.nf;
+  if (n_blocks < 1 || n_blocks > nf || nf > tx::kMaxFieldBlocks)
+    return fail(h, TX_EINVAL, "tx_blocked_layout: 1 <= n_blocks <= number of fields");
+  tx::BlockedMap M;
+  M.nf = nf;
+  M.nb = n_blocks;
+  for (int f = 0; f < nf; ++f) {
+    const int b = field_block[f];
+    if (b < 0 || b >= n_blocks) return fail(h, TX_EINVAL, "tx_blocked_layout: field block out of range");
+    M.fblock[f] = b;
+    M.fpos[f] = M.bnf[b]++;
+  }
+  for (int b = 0; b < n_blocks; ++b)
+    if (M.bnf[b] == 0) return fail(h, TX_EINVAL, "tx_blocked_layout: empty field block");
+  h->blocked = M;
+  return TX_OK;
+}
+
+int tx_blocked_sizes(tx_handle h, int32_t i, int32_t j, int64_t* n_rows, int64_t* n_cols, int64_t* nnz) {
+  if (!h) return TX_EINVAL;
+  const tx::BlockedMap& M = h->blocked;
+  if (M.nb == 0) return fail(h, TX_ESTATE, "tx_blocked_sizes before tx_blocked_layout");
+  if (i < 0 || i >= M.nb || j < 0 || j >= M.nb) return fail(h, TX_ERANGE, "tx_blocked_sizes: block out of range");
+  const int64_t ne = h->dofs.n_entities;
+  if (n_rows) *n_rows = (int64_t)M.bnf[i] * ne;
+  if (n_cols) *n_cols = (int64_t)M.bnf[j] * ne;
+  if (nnz) *nnz = (int64_t)M.bnf[i] * M.bnf[j] * h->dofs.erowptr[ne];
+  return TX_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// The device graph of blocks with bi x bj fields, built on first use.
+int block_graph(tx_handle h, int bi, int bj, tx_handle_s::BlockGraph*& out) {
+  tx_handle_s::BlockGraph& g = h->block_graphs[bi][bj];
+  if (!g.rp) {
+    const int64_t ne = h->dofs.n_entities, nnz = (int64_t)bi * bj * h->dofs.erowptr[ne];
+    if (cudaMalloc((void**)&g.rp, sizeof(int64_t) * (bi * ne + 1)) != cudaSuccess ||
+        cudaMalloc((void**)&g.col, sizeof(int32_t) * (nnz > 0 ? nnz : 1)) != cudaSuccess) {
+      cudaFree(g.rp); cudaFree(g.col); g = tx_handle_s::BlockGraph();
+      return fail(h, TX_ENOMEM, "blocked graph: out of device memory");
+    }
+    if (tx::launch_block_graph(h->d_erowptr, h->d_ecol, ne, bi, bj, g.rp, g.col, h->stream) != cudaSuccess)
+      return fail(h, TX_ECUDA, "blocked graph: launch failed");
+  }
+  out = &g;
+  return TX_OK;
+}
+
+int blocked_ready(tx_handle h, const char* who) {
+  if (!h->have_dofs) return fail(h, TX_ESTATE, std::string(who) + " before tx_dof_build");
+  if (h->blocked.nb == 0) return fail(h, TX_ESTATE, std::string(who) + " before tx_blocked_layout");
+  return TX_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int tx_blocked_graph_build(tx_handle h, int32_t i, int32_t j, int64_t* rowptr, int32_t* colind) {
+  if (!h || !rowptr || !colind) return TX_EINVAL;
+  int rc = blocked_ready(h, "tx_blocked_graph_build");
+  if (rc) return rc;
+  const tx::BlockedMap& M = h->blocked;
+  if (i < 0 || i >= M.nb || j < 0 || j >= M.nb) return fail(h, TX_ERANGE, "tx_blocked_graph_build: block out of range");
+  tx_handle_s::BlockGraph* g = nullptr;
+  if ((rc = block_graph(h, M.bnf[i], M.bnf[j], g))) return rc;
+  const int64_t ne = h->dofs.n_entities, nnz = (int64_t)M.bnf[i] * M.bnf[j] * h->dofs.erowptr[ne];
+  cudaError_t e = cudaMemcpyAsync(rowptr, g->rp, sizeof(int64_t) * (M.bnf[i] * ne + 1), cudaMemcpyDeviceToDevice,
+                                  h->stream);
+  if (e == cudaSuccess && nnz > 0)
+    e = cudaMemcpyAsync(colind, g->col, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_blocked_graph_build: ") + cudaGetErrorString(e));
+  return TX_OK;
+}
+
+int tx_blocked_split_vector(tx_handle h, const double* x, double* const* xb) {
+  if (!h || !x || !xb) return TX_EINVAL;
+  int rc = blocked_ready(h, "tx_blocked_split_vector");
+  if (rc) return rc;
+  tx::BlockPtrs P{};
+  for (int k = 0; k < h->blocked.nb; ++k) {
+    if (!xb[k]) return fail(h, TX_EINVAL, "tx_blocked_split_vector: null block vector");
+    P.p[k] = xb[k];
+  }
+  if (tx::launch_block_vector(h->dofs.n_entities, h->blocked, x, P, nullptr, true, h->stream) != cudaSuccess)
+    return fail(h, TX_ECUDA, "tx_blocked_split_vector: launch failed");
+  return TX_OK;
+}
+
+int tx_blocked_merge_vector(tx_handle h, const double* const* xb, double* x) {
+  if (!h || !x || !xb) return TX_EINVAL;
+  int rc = blocked_ready(h, "tx_blocked_merge_vector");
+  if (rc) return rc;
+  tx::BlockPtrs P{};
+  for (int k = 0; k < h->blocked.nb; ++k) {
+    if (!xb[k]) return fail(h, TX_EINVAL, "tx_blocked_merge_vector: null block vector");
+    P.p[k] = const_cast<double*>(xb[k]);
+  }
+  if (tx::launch_block_vector(h->dofs.n_entities, h->blocked, nullptr, P, x, false, h->stream) != cudaSuccess)
+    return fail(h, TX_ECUDA, "tx_blocked_merge_vector: launch failed");
+  return TX_OK;
+}
+
+int tx_blocked_split_matrix(tx_handle h, const double* crs_vals, double* const* blk_vals) {
+  if (!h || !crs_vals || !blk_vals) return TX_EINVAL;
+  int rc = blocked_ready(h, "tx_blocked_split_matrix");
+  if (rc) return rc;
+  tx::BlockPtrs P{};
+  const int nb = h->blocked.nb;
+  for (int k = 0; k < nb * nb; ++k) P.p[k] = blk_vals[k];
+  if (tx::launch_block_split_matrix(h->d_erowptr, h->dofs.n_entities, h->blocked, crs_vals, P, h->stream) !=
+      cudaSuccess)
+    return fail(h, TX_ECUDA, "tx_blocked_split_matrix: launch failed");
+  return TX_OK;
+}
+
+int tx_blocked_spmv(tx_handle h, const double* const* blk_vals, const double* const* xb, double* const* yb,
+                    double alpha, double beta) {
+  if (!h || !blk_vals || !xb || !yb) return TX_EINVAL;
+  int rc = blocked_ready(h, "tx_blocked_spmv");
+  if (rc) return rc;
+  const tx::BlockedMap& M = h->blocked;
+  const int64_t ne = h->dofs.n_entities;
+  for (int i = 0; i < M.nb; ++i) {
+    if (!yb[i] || !xb[i]) return fail(h, TX_EINVAL, "tx_blocked_spmv: null block vector");
+    const int64_t rows = (int64_t)M.bnf[i] * ne;
+    bool first = true;
+    for (int j = 0; j < M.nb; ++j) {
+      const double* v = blk_vals[i * M.nb + j];
+      if (!v) continue;  // excluded pair
+      tx_handle_s::BlockGraph* g = nullptr;
+      if ((rc = block_graph(h, M.bnf[i], M.bnf[j], g))) return rc;
+      const int64_t nnz = (int64_t)M.bnf[i] * M.bnf[j] * h->dofs.erowptr[ne];
+      if (tx::launch_spmv_f64(rows, g->rp, g->col, v, xb[j], yb[i], alpha, first ? beta : 1.0, nnz, h->stream,
+                              h->spmv) != cudaSuccess)
+        return fail(h, TX_ECUDA, "tx_blocked_spmv: launch failed");
+      first = false;
+    }
+    if (first) {  // a block row with every pair excluded: y_i = beta y_i
+      cudaError_t e = beta == 0.0 ? tx::launch_fill(yb[i], 0.0, rows, h->stream)
+                                  : tx::launch_axpby(yb[i], yb[i], 0.0, beta, rows, h->stream);
+      if (e != cudaSuccess) return fail(h, TX_ECUDA, "tx_blocked_spmv: launch failed");
+    }
+  }
   return TX_OK;
 }
 

@@ -110,6 +110,28 @@ cudaError_t launch_spmv_f32(int64_t n, const int64_t* rowptr, const int32_t* col
                             const float* x, float* y, float alpha, float beta, int64_t nnz_hint, cudaStream_t s,
                             SpmvShape shape = SpmvShape());
 
+// Blocked layout (BlockedTpetraLinearObjFactory): field f lives in block
+// fblock[f] at place fpos[f]; block k has bnf[k] fields.
+constexpr int kMaxFieldBlocks = 8;
+struct BlockedMap {
+  int nf = 0, nb = 0;
+  int fblock[kMaxFieldBlocks] = {}, fpos[kMaxFieldBlocks] = {}, bnf[kMaxFieldBlocks] = {};
+};
+// Block vectors (nb pointers) or block matrices (nb * nb, row-major; null =
+// excluded pair), passed to kernels by value.
+struct BlockPtrs {
+  double* p[kMaxFieldBlocks * kMaxFieldBlocks];
+};
+// CRS graph of block (i, j) with bi and bj fields: the entity graph expanded by bi x bj.
+cudaError_t launch_block_graph(const int64_t* erp, const int32_t* ecol, int64_t n_ent, int bi, int bj, int64_t* rp,
+                               int32_t* col, cudaStream_t s);
+// split: blocks.p[k] <- x (interleaved); else dst (interleaved) <- blocks.p[k].
+cudaError_t launch_block_vector(int64_t n_ent, const BlockedMap& M, const double* src, BlockPtrs blocks, double* dst,
+                                bool split, cudaStream_t s);
+// block CRS values blk.p[i * nb + j] <- interleaved CRS values.
+cudaError_t launch_block_split_matrix(const int64_t* erp, int64_t n_ent, const BlockedMap& M, const double* vals,
+                                      BlockPtrs blk, cudaStream_t s);
+
 // Work space of the iterative-refinement solver (owned by the handle).
 struct SolverWork {
   int64_t n = 0, nnz = 0;

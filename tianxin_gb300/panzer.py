@@ -212,6 +212,174 @@ class TpetraLinearObjFactory:
         return torch.zeros(self.dof.n_dofs, dtype=torch.float64, device=self.device)
 
 
+def _ptr_array(tensors):
+    """Host array of device pointers (NULL for None), kept alive by the caller."""
+    arr = (C.c_void_p * len(tensors))(*[None if t is None else t.data_ptr() for t in tensors])
+    return arr
+
+
+class BlockedDOFManager:
+    """BlockedDOFManager: the fields of one equation set grouped into field blocks.
+
+    blocks lists the field names of each block, e.g. [["UX"], ["UY"], ["UZ"]]
+    (every field in exactly one block; inside a block the fields take the
+    equation set's field order).  Block i numbers its DOFs
+    b_i * entity + k (k = the field's place in the block) over the entities
+    of the interleaved DOFManager in its LID order, as a DOFManager built on
+    the block's fields alone numbers them.
+    """
+
+    def __init__(self, dof, blocks):
+        self.dof, self.lib, self.h = dof, dof.lib, dof.h
+        # within a block the fields keep the equation set's field order
+        self.blocks = [sorted(b, key=dof.getFieldNum) for b in blocks]
+        fb = np.full(dof.n_fields, -1, np.int32)
+        for i, names in enumerate(self.blocks):
+            for name in names:
+                f = dof.getFieldNum(name)
+                if fb[f] >= 0:
+                    raise ValueError(f"field {name} in two blocks")
+                fb[f] = i
+        if (fb < 0).any():
+            raise ValueError("every field must be in a block")
+        self._fb = fb
+        check(self.h, self.lib.tx_blocked_layout(self.h, len(self.blocks), _np_ptr(fb)), "tx_blocked_layout")
+        self.n_entities = dof.n_dofs // dof.n_fields
+
+    def getNumFieldBlocks(self):
+        return len(self.blocks)
+
+    def getFieldBlocks(self):
+        return self.blocks
+
+    def getFieldBlock(self, name):
+        return int(self._fb[self.dof.getFieldNum(name)])
+
+    def getBlockSize(self, i):
+        return len(self.blocks[i]) * self.n_entities
+
+    def getFieldDOFs(self, i, name):
+        """Block-i LIDs of field name (entity order)."""
+        k = self.blocks[i].index(name)
+        return np.arange(self.n_entities, dtype=np.int64) * len(self.blocks[i]) + k
+
+    def getOwnedIndices(self, i):
+        """Block-i GIDs in block-LID order: ascending entity GID, the block's fields interleaved."""
+        g = self.dof.getOwnedIndices()
+        nf = self.dof.n_fields
+        ent_rank, f = g // nf, g % nf
+        keep = self._fb[f] == i
+        pos = np.array([self.blocks[i].index(self.dof.getFieldString(k)) if self._fb[k] == i else -1
+                        for k in range(nf)])
+        return ent_rank[keep] * len(self.blocks[i]) + pos[f[keep]]
+
+
+class BlockedCrsMatrix:
+    """The blocked operator [A_ij] (Thyra blocked linear op of Tpetra CRS blocks; None = excluded pair)."""
+
+    def __init__(self, blof, blocks):
+        self.blof, self.blocks = blof, blocks
+
+    def getBlock(self, i, j):
+        return self.blocks[i][j]
+
+    def initializeMatrix(self, v=0.0):
+        for row in self.blocks:
+            for m in row:
+                if m is not None:
+                    m.initializeMatrix(v)
+
+    def apply(self, xb, yb=None, alpha=1.0, beta=0.0):
+        """y_i = alpha sum_j A_ij x_j + beta y_i over the blocks not excluded."""
+        bd = self.blof.bdof
+        if yb is None:
+            yb = [torch.zeros(bd.getBlockSize(i), dtype=torch.float64, device=xb[0].device)
+                  for i in range(bd.getNumFieldBlocks())]
+        vals = [m.values if m is not None else None for row in self.blocks for m in row]
+        lib = bd.lib
+        lib.tx_set_stream(bd.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        pv, px, py = _ptr_array(vals), _ptr_array(xb), _ptr_array(yb)
+        check(bd.h, lib.tx_blocked_spmv(bd.h, pv, px, py, alpha, beta), "tx_blocked_spmv")
+        return yb
+
+
+class BlockedTpetraLinearObjFactory:
+    """BlockedTpetraLinearObjFactory: block graphs, block vectors and the blocked operator of a BlockedDOFManager."""
+
+    def __init__(self, bdof, device="cuda"):
+        self.bdof, self.device = bdof, device
+        self.excluded = set()
+        self._graphs = {}
+
+    def getBlockRowCount(self):
+        return self.bdof.getNumFieldBlocks()
+
+    def getBlockColCount(self):
+        return self.bdof.getNumFieldBlocks()
+
+    def addExcludedPair(self, i, j):
+        self.excluded.add((i, j))
+
+    def addExcludedPairs(self, pairs):
+        for i, j in pairs:
+            self.addExcludedPair(i, j)
+
+    def getGraph(self, i, j):
+        if (i, j) not in self._graphs:
+            bd = self.bdof
+            rows, cols, nnz = C.c_int64(), C.c_int64(), C.c_int64()
+            check(bd.h, bd.lib.tx_blocked_sizes(bd.h, i, j, C.byref(rows), C.byref(cols), C.byref(nnz)),
+                  "tx_blocked_sizes")
+            rp = torch.empty(rows.value + 1, dtype=torch.int64, device=self.device)
+            ci = torch.empty(nnz.value, dtype=torch.int32, device=self.device)
+            bd.lib.tx_set_stream(bd.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+            check(bd.h, bd.lib.tx_blocked_graph_build(bd.h, i, j, _ptr(rp), _ptr(ci)), "tx_blocked_graph_build")
+            self._graphs[(i, j)] = (rp, ci)
+        return self._graphs[(i, j)]
+
+    def getTpetraMatrix(self, i, j):
+        rp, ci = self.getGraph(i, j)
+        return CrsMatrix(self.bdof.dof, rp, ci)
+
+    def getTpetraDomainVector(self, i):
+        return torch.zeros(self.bdof.getBlockSize(i), dtype=torch.float64, device=self.device)
+
+    getTpetraRangeVector = getTpetraDomainVector
+
+    def getBlockedVector(self):
+        return [self.getTpetraDomainVector(i) for i in range(self.getBlockRowCount())]
+
+    def getBlockedMatrix(self):
+        n = self.getBlockRowCount()
+        return BlockedCrsMatrix(self, [[None if (i, j) in self.excluded else self.getTpetraMatrix(i, j)
+                                        for j in range(n)] for i in range(n)])
+
+    def splitVector(self, x, xb=None):
+        """Interleaved vector -> block vectors."""
+        xb = self.getBlockedVector() if xb is None else xb
+        bd = self.bdof
+        bd.lib.tx_set_stream(bd.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(bd.h, bd.lib.tx_blocked_split_vector(bd.h, _ptr(x), _ptr_array(xb)), "tx_blocked_split_vector")
+        return xb
+
+    def mergeVector(self, xb, x=None):
+        """Block vectors -> interleaved vector."""
+        x = torch.zeros(self.bdof.dof.n_dofs, dtype=torch.float64, device=self.device) if x is None else x
+        bd = self.bdof
+        bd.lib.tx_set_stream(bd.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(bd.h, bd.lib.tx_blocked_merge_vector(bd.h, _ptr_array(xb), _ptr(x)), "tx_blocked_merge_vector")
+        return x
+
+    def splitMatrix(self, W, Wb):
+        """Interleaved CRS values (the DOFManager's graph) -> the blocks of Wb (excluded blocks skipped)."""
+        bd = self.bdof
+        vals = [m.values if m is not None else None for row in Wb.blocks for m in row]
+        bd.lib.tx_set_stream(bd.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        check(bd.h, bd.lib.tx_blocked_split_matrix(bd.h, _ptr(W.values), _ptr_array(vals)),
+              "tx_blocked_split_matrix")
+        return Wb
+
+
 class DirichletBC:
     """Dirichlet parameter list: DOF Names on the box sides (a side mask), value g."""
 
@@ -424,6 +592,42 @@ class ModelEvaluator:
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_solve_cg_ir(self.dof.h, C.byref(a)), "tx_solve_cg_ir")
         return {"outer": int(a.stats[0]), "inner": int(a.stats[1]), "relres": a.stats[2], "r0": a.stats[3]}
+
+
+class BlockedModelEvaluator:
+    """evalModel on blocked containers: x, x_dot and f as lists of block vectors, W a BlockedCrsMatrix.
+
+    The gather from the product vector, the volume fill with its scatter, the
+    Neumann fluxes and the Dirichlet rows run as in ModelEvaluator on the
+    interleaved layout (the blocked numbering is a permutation of it), and
+    the results are split into the blocks; excluded blocks are not written.
+    """
+
+    def __init__(self, me, blof):
+        self.me, self.blof = me, blof
+        lof = me.lof
+        self._x, self._xd, self._f = lof.getTpetraVector(), lof.getTpetraVector(), lof.getTpetraVector()
+        self._W = None
+
+    def create_W_op(self):
+        return self.blof.getBlockedMatrix()
+
+    def evalModel(self, xb, x_dot=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False, **kw):
+        blof = self.blof
+        x = blof.mergeVector(xb, self._x)
+        xd = blof.mergeVector(x_dot, self._xd) if x_dot is not None else None
+        Wi = None
+        if W is not None:
+            if self._W is None:
+                self._W = self.me.create_W_op()
+            Wi = self._W
+        self.me.evalModel(x, x_dot=xd, alpha=alpha, beta=beta, t=t, f=self._f if f is not None else None, W=Wi,
+                          mixed=mixed, **kw)
+        if f is not None:
+            blof.splitVector(self._f, f)
+        if W is not None:
+            blof.splitMatrix(Wi, W)
+        return f, W
 
 
 _INTEGRANDS = {"Field": _abi.TX_INTEGRAND_FIELD, "L2 Error": _abi.TX_INTEGRAND_L2_ERROR,
