@@ -246,6 +246,8 @@ typedef struct tx_neumann_desc {
   int32_t n_table;         /* TIME_TABLE points                                         */
   const double* table_t;   /* "Time Values" (HOST, ascending, copied at creation)       */
   const double* table_v;   /* "BC Values" (HOST)                                        */
+  int32_t side_set;        /* explicit meshes: side set index + 1 ("SideSet Name" of a  */
+                           /* file); 0 = the box sides of side_mask (lattice meshes)    */
 } tx_neumann_desc;
 /* The functor value at time t (host only, no handle). */
 int tx_neumann_value(const tx_neumann_desc* d, double t, double* value);
@@ -361,6 +363,70 @@ int tx_graph_capture_begin(tx_handle h);
 int tx_graph_capture_end(tx_handle h, int32_t* graph_id);
 int tx_graph_launch(tx_handle h, int32_t graph_id);
 int tx_graph_destroy(tx_handle h, int32_t graph_id);
+
+/* ------------------------------------------------------------ explicit meshes
+ * Unstructured meshes for nodal (TX_HGRAD_C1) fields on hex8 and tet4 blocks,
+ * from arrays or from an Exodus II file (STK_ExodusReaderFactory,
+ * adapters-stk/src/Panzer_STK_ExodusReaderFactory.cpp).  Node numbers are
+ * 0-based and are the vertex GIDs of the numbering: DOF GIDs ascend in node
+ * number, fields interleaved, LIDs by first touch as on lattice meshes.
+ * Element vertices follow the Exodus/shards order.  Elements are numbered
+ * over the whole mesh, blocks in order.  Side sets list (element, side)
+ * pairs with the 0-based shards side ordinal (Exodus side - 1: hex faces
+ * {0,1,5,4} {1,2,6,5} {2,3,7,6} {0,4,7,3} {0,3,2,1} {4,5,6,7}; tet faces
+ * {0,1,3} {1,2,3} {0,3,2} {0,2,1}).  Dirichlet DOFs come from node sets
+ * (tx_dirichlet_dofs_node_set) and Neumann sides from side sets
+ * (tx_neumann_desc.side_set); the box-side forms give TX_EINVAL here. */
+typedef struct tx_explicit_block {
+  int32_t topology;        /* TX_TOPO_HEX (8 vertices) or TX_TOPO_TET (4)          */
+  int64_t n_elem;
+  const int64_t* conn;     /* [n_elem][8 or 4] node numbers (HOST)                 */
+  int64_t id;              /* element block id                                     */
+  const char* name;        /* block name or NULL                                   */
+} tx_explicit_block;
+typedef struct tx_explicit_set {
+  int64_t n;               /* side sets: n (element, side) pairs; node sets: n nodes */
+  const int64_t* entries;  /* HOST                                                   */
+  int64_t id;
+  const char* name;        /* or NULL                                                */
+} tx_explicit_set;
+typedef struct tx_mesh_explicit_desc {
+  int64_t n_nodes;
+  const double* coords;    /* [n_nodes][3] (HOST)                                  */
+  int32_t n_blocks;        /* 1..TX_MAX_BLOCKS                                      */
+  const tx_explicit_block* blocks;
+  int32_t n_side_sets;
+  const tx_explicit_set* side_sets;
+  int32_t n_node_sets;
+  const tx_explicit_set* node_sets;
+} tx_mesh_explicit_desc;
+/* err (may be NULL) receives the reason of a failure. */
+/* Vertex node numbers [n_elem][*nv] of a block's elements in shards vertex
+ * order (lattice and explicit meshes; vertices may be NULL to get *nv). */
+int tx_mesh_element_vertices(tx_handle h, int32_t block, int32_t* nv, int64_t* vertices);
+int tx_mesh_create_explicit(const tx_mesh_explicit_desc* d, tx_handle* out, char* err, int32_t err_len);
+/* A 3-D Exodus II file in the NetCDF classic container (CDF-1/2/5; NetCDF-4
+ * files: TX_EINVAL).  Blocks are HEX* or TET*; linear != 0 keeps the vertex
+ * nodes of quadratic elements (Panzer_STK_QuadraticToLinearMeshFactory's
+ * conversion), otherwise HEX20/HEX27/TETRA10 give TX_EINVAL.  Nodes are
+ * renumbered in ascending node_num_map order when the file has one. */
+int tx_mesh_create_exodus(const char* path, int32_t linear, tx_handle* out, char* err, int32_t err_len);
+typedef struct tx_exodus_summary {
+  int32_t version;         /* NetCDF container version 1, 2 or 5                   */
+  int64_t dim, n_nodes, n_elem, n_blocks, n_side_sets, n_node_sets;
+} tx_exodus_summary;
+/* Sizes of an Exodus file of any dimension, without building a mesh. */
+int tx_exodus_inspect(const char* path, tx_exodus_summary* s, char* err, int32_t err_len);
+/* Sets of an explicit mesh: kind 0 element blocks, 1 side sets, 2 node sets.
+ * tx_mesh_set_info: count of sets of that kind in *n when k < 0, else the
+ * set's id, name (NUL-terminated, truncated to name_len) and entry count
+ * (elements, pairs or nodes); tx_mesh_set_entries copies the entries
+ * (side sets: 2n values).  Lattice meshes have no sets (TX_ESTATE). */
+int tx_mesh_set_info(tx_handle h, int32_t kind, int32_t k, int64_t* id, char* name, int32_t name_len, int64_t* n);
+int tx_mesh_set_entries(tx_handle h, int32_t kind, int32_t k, int64_t* entries);
+/* Dirichlet DOF LIDs of the fields in field_mask at the nodes of a node set
+ * (ascending; the explicit-mesh form of tx_dirichlet_dofs). */
+int tx_dirichlet_dofs_node_set(tx_handle h, int32_t node_set, uint32_t field_mask, int64_t* n, int32_t* lids);
 
 /* ------------------------------------------------------------ blocked layout
  * BlockedDOFManager + BlockedTpetraLinearObjFactory

@@ -1,0 +1,149 @@
+"""Explicit meshes and Exodus II input on the host (no device calls).
+
+* The reader against the reference's own mesh files (skipped where those are
+  absent): sizes the reference's tests assert
+  (adapters-stk/test/stk_interface_test/tExodusReaderFactory.cpp:124-151,
+  742-750) and the geometry the meshes' Cubit journals define (hex20.jou,
+  tet10.jou: a 0.29 x 0.2 x 0.2 box minus a 0.25 x 0.14 x 0.1 cavity,
+  volume 0.0081, outer area 0.312, cavity area 0.148; hex20.gen's inner side
+  set lists 9 of the 10 cavity surfaces left by the webcut at z = 0, leaving
+  out one 0.14 x 0.05 half wall: 0.141).  Volumes and areas are summed from
+  the element vertices and side ordinals read, so they check coordinates,
+  connectivity and the side numbering.
+* Write -> read round trips of lattice meshes, and the explicit numbering
+  against the lattice numbering of the same mesh (bit-exact).
+* Errors: missing file, HDF5 container, unsupported element types.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import tianxin_gb300 as tx
+from tianxin_gb300 import _abi as A
+from tianxin_gb300.exodus import write_exodus
+
+import exodus_cases as X
+
+REF_MESHES = os.path.join(os.environ.get("TIANXIN_REFERENCE", "/root/reference"),
+                          "adapters-stk/test/stk_interface_test/meshes")
+needs_ref = pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference meshes not present")
+T6 = [[0, 1, 2, 6], [0, 2, 3, 6], [0, 3, 7, 6], [0, 7, 4, 6], [0, 4, 5, 6], [0, 5, 1, 6]]
+
+
+def _tetvol(p):
+    return np.einsum("ij,ij->i", p[:, 1] - p[:, 0], np.cross(p[:, 2] - p[:, 0], p[:, 3] - p[:, 0])) / 6
+
+
+def _geometry(m):
+    c = m.coordinates()
+    vols, conn = [], []
+    for b in range(m.numElementBlocks()):
+        cn = m.getElementVertices(b)
+        X_ = c[cn]
+        vols.append(_tetvol(X_) if cn.shape[1] == 4 else sum(_tetvol(X_[:, t]) for t in T6))
+        conn += list(cn)
+    areas = {}
+    for k, name in enumerate(m.getSidesetNames()):
+        a = 0.0
+        for e, s in m.getSideset(k):
+            cn = conn[e]
+            v = c[cn[(X.HEX_FACES if len(cn) == 8 else X.TET_FACES)[s]]]
+            n = np.cross(v[1] - v[0], v[2] - v[0]) if len(v) == 3 else np.cross(v[2] - v[0], v[3] - v[1])
+            a += 0.5 * np.linalg.norm(n)
+        areas[name] = a
+    return np.concatenate(vols), areas
+
+
+@needs_ref
+def test_reference_file_sizes():
+    s = tx.exodus_summary(os.path.join(REF_MESHES, "basic.gen"))
+    assert (s["dim"], s["n_elem"], s["n_blocks"], s["n_side_sets"], s["n_node_sets"]) == (2, 8, 2, 7, 2)
+    m = tx.ExodusReaderFactory(os.path.join(REF_MESHES, "2block_cylinders_30deg.g")).buildMesh()
+    assert m.n_elements == 12 and len(m.getSidesetNames()) == 5 and len(m.getNodesetNames()) == 3
+    with pytest.raises(tx.TxError) as e:  # 2-D meshes are inspected, not built
+        tx.ExodusReaderFactory(os.path.join(REF_MESHES, "basic.gen")).buildMesh()
+    assert e.value.code == A.TX_EINVAL
+
+
+@needs_ref
+@pytest.mark.parametrize("name,inner", [("hex20.gen", 0.148 - 0.14 * 0.05), ("tet10.gen", 0.148)])
+def test_reference_quadratic_meshes_as_linear(name, inner):
+    with pytest.raises(tx.TxError):
+        tx.ExodusReaderFactory(os.path.join(REF_MESHES, name)).buildMesh()  # quadratic needs linear=True
+    m = tx.ExodusReaderFactory(os.path.join(REF_MESHES, name), linear=True).buildMesh()
+    vols, areas = _geometry(m)
+    assert vols.min() > 0
+    assert abs(vols.sum() - 0.0081) <= 1e-12
+    assert abs(areas["outer_box"] - 0.312) <= 1e-12 and abs(areas["inner_box"] - inner) <= 1e-12
+
+
+@needs_ref
+def test_reference_unit_cube():
+    m = tx.ExodusReaderFactory(os.path.join(REF_MESHES, "basic3d.gen")).buildMesh()
+    vols, areas = _geometry(m)
+    assert vols.min() > 0 and abs(vols.sum() - 1.0) <= 1e-12
+    assert sorted(areas) == sorted(["left", "right", "top", "bottom", "front", "back"])
+    assert all(abs(a - 1.0) <= 1e-12 for a in areas.values())
+    assert m.getNodesetNames() == ["nodes", "origin"]
+
+
+@pytest.mark.parametrize("topo,version", [(A.TX_TOPO_HEX, 2), (A.TX_TOPO_TET, 1)])
+def test_round_trip_and_numbering_equal_the_lattice(tmp_path, topo, version):
+    conn, (coords, blocks, ss, ns) = X.box(n=(3, 2, 2), blocks=(1, 2, 1), topo=topo)
+    path = write_exodus(tmp_path / "box.exo", coords, blocks, ss, ns, version=version)
+    m = tx.ExodusReaderFactory(path).buildMesh()
+    assert np.array_equal(m.coordinates(), coords)
+    for b in range(len(blocks)):
+        assert np.array_equal(m.getElementVertices(b), blocks[b][1])
+    assert m.getSidesetNames() == X.SIDE_NAMES and m.getNodesetNames() == X.SIDE_NAMES
+    for k in range(6):
+        assert np.array_equal(m.getSideset(k), np.array(ss[k][2]).reshape(-1, 2))
+        assert np.array_equal(m.getNodeset(k), ns[k][2])
+    phys = A.TX_PHYS_ELASTICITY if topo == A.TX_TOPO_HEX else A.TX_PHYS_POISSON
+    q = A.equation_set(phys, params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.0) if phys == A.TX_PHYS_ELASTICITY else (1, 0, 0, 1))
+    d_lat = tx.DOFManager(conn, q, require_device=False)
+    d_exp = tx.DOFManager(m, q, require_device=False)
+    assert np.array_equal(d_lat.getOwnedIndices(), d_exp.getOwnedIndices())
+    for b in range(len(blocks)):
+        assert np.array_equal(d_lat.getElementLIDs(b), d_exp.getElementLIDs(b))
+        assert np.array_equal(d_lat.getElementGIDs(b), d_exp.getElementGIDs(b))
+    # node sets give the box-side Dirichlet DOFs
+    assert np.array_equal(d_exp.dirichletDofsNodeSet("zmin"), d_lat.dirichletDofs(A.SIDE_ZMIN))
+
+
+def test_node_num_map_orders_the_nodes(tmp_path):
+    conn, (coords, blocks, ss, ns) = X.box(n=(2, 2, 2))
+    rng = np.random.default_rng(3)
+    gid = rng.permutation(len(coords)) * 7 + 11  # global ids, any order
+    path = write_exodus(tmp_path / "perm.exo", coords, blocks, ss, ns, node_num_map=gid)
+    m = tx.ExodusReaderFactory(path).buildMesh()
+    rank = np.argsort(np.argsort(gid))  # file node i becomes node rank[i]
+    assert np.array_equal(m.coordinates()[rank], coords)
+    assert np.array_equal(m.getElementVertices(0), rank[blocks[0][1]])
+    assert np.array_equal(np.sort(m.getNodeset("xmax")), np.sort(rank[ns[1][2]]))
+
+
+def test_explicit_arrays_and_errors(tmp_path):
+    conn, (coords, blocks, ss, ns) = X.box(n=(2, 1, 1))
+    m = tx.ExplicitConnManager.from_arrays(coords, blocks, ss, ns)
+    assert m.n_elements == 2 and m.getElementBlockIds() == ["block_1"]
+    bad = [(A.TX_TOPO_HEX, blocks[0][1] + len(coords), 1, "b")]
+    with pytest.raises(tx.TxError):
+        tx.ExplicitConnManager.from_arrays(coords, bad)
+    with pytest.raises(tx.TxError):  # side ordinal 6 of a hex
+        tx.ExplicitConnManager.from_arrays(coords, blocks, [("s", 1, [(0, 6)])])
+    with pytest.raises(tx.TxError) as e:
+        tx.ExodusReaderFactory(tmp_path / "missing.exo").buildMesh()
+    assert "cannot open" in str(e.value)
+    h5 = tmp_path / "netcdf4.exo"
+    h5.write_bytes(b"\x89HDF\r\n\x1a\n" + b"\0" * 64)
+    with pytest.raises(tx.TxError) as e:
+        tx.exodus_summary(h5)
+    assert "HDF5" in str(e.value)
+    # explicit meshes carry nodal fields only; box-side queries are refused
+    with pytest.raises(tx.TxError):
+        tx.DOFManager(m, A.equation_set(A.TX_PHYS_HEAT, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0)), require_device=False)
+    d = tx.DOFManager(m, A.equation_set(A.TX_PHYS_POISSON, params=(1, 0, 0, 1)), require_device=False)
+    with pytest.raises(tx.TxError):
+        d.dirichletDofs(A.SIDE_ZMIN)

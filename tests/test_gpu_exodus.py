@@ -1,0 +1,88 @@
+"""Evaluation on explicit meshes (Exodus files and arrays) on the GPU.
+
+The explicit path must reproduce the lattice path on the same mesh: a
+lattice mesh written to an Exodus file (lattice node order, box sides as side
+sets and node sets) and read back gives the same numbering, so the
+deterministic (coloured) evaluation gives the same bits in f and W, with
+Dirichlet rows from node sets and Neumann fluxes from side sets in place of
+box sides (f to 1e-15: the flux sums with atomics).  With the nodes renumbered
+(node_num_map), the first-touch LIDs and so f and W in LID order are
+unchanged.  The lattice path is pinned to the oracle elsewhere.
+"""
+import numpy as np
+import pytest
+import torch
+
+import tianxin_gb300 as tx
+from tianxin_gb300 import _abi as A
+from tianxin_gb300.exodus import write_exodus
+
+import exodus_cases as X
+
+pytestmark = pytest.mark.gpu
+ELAST = (1.0, 0.3, 0.1, -0.2, -1.0, 0.7)
+
+
+def _evaluate(conn, q, explicit, x_np, nblocks):
+    dof = tx.DOFManager(conn, q)
+    lof = tx.TpetraLinearObjFactory(dof)
+    if explicit:
+        dbc = [tx.DirichletBC(dof, node_set="zmin")]
+        nbc = [tx.NeumannBC(dof, dof_name=dof.field_names[-1], value=-0.3, block=b, side_set="zmax")
+               for b in range(nblocks)]
+    else:
+        dbc = [tx.DirichletBC(dof, A.SIDE_ZMIN)]
+        nbc = [tx.NeumannBC(dof, A.SIDE_ZMAX, dof.field_names[-1], value=-0.3, block=b) for b in range(nblocks)]
+    me = tx.ModelEvaluator(lof, dbc, nbc)
+    x, f, W = torch.from_numpy(x_np).cuda(), lof.getTpetraVector(), me.create_W_op()
+    me.evalModel(x, x_dot=0.5 * x, alpha=0.5, beta=1.0, f=f, W=W, deterministic=True)
+    return dof, f.cpu().numpy(), W.values.cpu().numpy(), (me, lof)
+
+
+@pytest.mark.parametrize("topo,phys", [(A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY), (A.TX_TOPO_TET, A.TX_PHYS_POISSON)])
+def test_exodus_mesh_reproduces_the_lattice_path(cuda, tmp_path, topo, phys):
+    conn, (coords, blocks, ss, ns) = X.box(n=(3, 2, 2), blocks=(1, 2, 1), topo=topo)
+    path = write_exodus(tmp_path / "box.exo", coords, blocks, ss, ns)
+    mesh = tx.ExodusReaderFactory(path).buildMesh()
+    q = A.equation_set(phys, params=ELAST if phys == A.TX_PHYS_ELASTICITY else (1.0, 0.5, 1.0, 2.0))
+    nf = 3 if phys == A.TX_PHYS_ELASTICITY else 1
+    x_np = np.random.default_rng(2).uniform(-1, 1, nf * len(coords))
+    d0, f0, v0, _ = _evaluate(conn, q, False, x_np, len(blocks))
+    d1, f1, v1, _ = _evaluate(mesh, q, True, x_np, len(blocks))
+    assert np.array_equal(v0, v1)
+    assert np.abs(f0 - f1).max() <= 1e-15 * np.abs(f0).max()
+
+
+def test_renumbered_nodes_keep_lid_order_results(cuda, tmp_path):
+    conn, (coords, blocks, ss, ns) = X.box(n=(3, 3, 2))
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=ELAST)
+    gid = np.random.default_rng(7).permutation(len(coords)) + 1
+    m0 = tx.ExodusReaderFactory(write_exodus(tmp_path / "a.exo", coords, blocks, ss, ns)).buildMesh()
+    m1 = tx.ExodusReaderFactory(write_exodus(tmp_path / "b.exo", coords, blocks, ss, ns, node_num_map=gid)).buildMesh()
+    x_np = np.random.default_rng(8).uniform(-1, 1, 3 * len(coords))
+    d0, f0, v0, _ = _evaluate(m0, q, True, x_np, 1)
+    d1, f1, v1, _ = _evaluate(m1, q, True, x_np, 1)
+    assert np.array_equal(v0, v1)
+    assert np.abs(f0 - f1).max() <= 1e-15 * np.abs(f0).max()
+    rank = np.argsort(np.argsort(gid))
+    # owned GIDs follow the renumbered nodes: node n's DOFs are 3 rank[n] + field
+    g0, g1 = d0.getOwnedIndices(), d1.getOwnedIndices()
+    assert np.array_equal(g1, 3 * rank[g0 // 3] + g0 % 3)
+
+
+def test_solve_on_an_exodus_mesh(cuda, tmp_path):
+    conn, (coords, blocks, ss, ns) = X.box(n=(6, 5, 4), jitter=0.05)
+    mesh = tx.ExodusReaderFactory(write_exodus(tmp_path / "c.exo", coords, blocks, ss, ns)).buildMesh()
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0))
+    sols = []
+    for c, explicit in ((conn, False), (mesh, True)):
+        dof = tx.DOFManager(c, q)
+        lof = tx.TpetraLinearObjFactory(dof)
+        bc = tx.DirichletBC(dof, node_set="zmin") if explicit else tx.DirichletBC(dof, A.SIDE_ZMIN)
+        me = tx.ModelEvaluator(lof, [bc])
+        x, f, W = lof.getTpetraVector(), lof.getTpetraVector(), me.create_W_op()
+        me.evalModel(x, f=f, W=W, mixed=True)
+        st = me.solve(W, x, rtol=1e-11, matrix_free=True)
+        assert st["relres"] <= 1e-11
+        sols.append(x.cpu().numpy())
+    assert np.abs(sols[0] - sols[1]).max() <= 1e-10 * np.abs(sols[0]).max()

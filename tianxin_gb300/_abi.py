@@ -116,7 +116,29 @@ class NeumannDesc(C.Structure):
         ("block", C.c_int32), ("side_mask", C.c_uint32), ("field", C.c_int32), ("value_type", C.c_int32),
         ("value", C.c_double),
         ("n_table", C.c_int32), ("table_t", C.c_void_p), ("table_v", C.c_void_p),
+        ("side_set", C.c_int32),
     ]
+
+
+class ExplicitBlock(C.Structure):
+    _fields_ = [("topology", C.c_int32), ("n_elem", C.c_int64), ("conn", C.c_void_p), ("id", C.c_int64),
+                ("name", C.c_char_p)]
+
+
+class ExplicitSet(C.Structure):
+    _fields_ = [("n", C.c_int64), ("entries", C.c_void_p), ("id", C.c_int64), ("name", C.c_char_p)]
+
+
+class MeshExplicitDesc(C.Structure):
+    _fields_ = [("n_nodes", C.c_int64), ("coords", C.c_void_p),
+                ("n_blocks", C.c_int32), ("blocks", C.POINTER(ExplicitBlock)),
+                ("n_side_sets", C.c_int32), ("side_sets", C.POINTER(ExplicitSet)),
+                ("n_node_sets", C.c_int32), ("node_sets", C.POINTER(ExplicitSet))]
+
+
+class ExodusSummary(C.Structure):
+    _fields_ = [("version", C.c_int32), ("dim", C.c_int64), ("n_nodes", C.c_int64), ("n_elem", C.c_int64),
+                ("n_blocks", C.c_int64), ("n_side_sets", C.c_int64), ("n_node_sets", C.c_int64)]
 
 
 def mesh_desc(n, blocks=(1, 1, 1), topology=TX_TOPO_HEX, lengths=(1.0, 1.0, 1.0), jitter=0.0, seed=0):

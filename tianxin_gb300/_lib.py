@@ -61,6 +61,13 @@ SIGNATURES = {
     "tx_blocked_merge_vector": (C.c_int, [P, P, P]),
     "tx_blocked_split_matrix": (C.c_int, [P, P, P]),
     "tx_blocked_spmv": (C.c_int, [P, P, P, P, D, D]),
+    "tx_mesh_element_vertices": (C.c_int, [P, I32, C.POINTER(I32), P]),
+    "tx_mesh_create_explicit": (C.c_int, [C.POINTER(_abi.MeshExplicitDesc), C.POINTER(P), C.c_char_p, I32]),
+    "tx_mesh_create_exodus": (C.c_int, [C.c_char_p, I32, C.POINTER(P), C.c_char_p, I32]),
+    "tx_exodus_inspect": (C.c_int, [C.c_char_p, C.POINTER(_abi.ExodusSummary), C.c_char_p, I32]),
+    "tx_mesh_set_info": (C.c_int, [P, I32, I32, C.POINTER(I64), C.c_char_p, I32, C.POINTER(I64)]),
+    "tx_mesh_set_entries": (C.c_int, [P, I32, I32, P]),
+    "tx_dirichlet_dofs_node_set": (C.c_int, [P, I32, U32, C.POINTER(I64), P]),
     "tx_set_stream": (C.c_int, [P, P]),
     "tx_synchronize": (C.c_int, [P]),
 }

@@ -3,6 +3,7 @@
 // tx_assemble.cu and tx_linalg.cu.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -492,6 +493,136 @@ int tx_mesh_create(const tx_mesh_desc* desc, tx_handle* out) {
   return TX_OK;
 }
 
+}  // extern "C"
+
+namespace {
+void copy_err(char* err, int32_t len, const std::string& msg) {
+  if (!err || len <= 0) return;
+  const size_t n = std::min<size_t>(msg.size(), (size_t)len - 1);
+  std::memcpy(err, msg.data(), n);
+  err[n] = 0;
+}
+
+// Builds a handle around an explicit mesh made by make(); failures go to err.
+template <typename F>
+int create_explicit(tx_handle* out, char* err, int32_t err_len, F make) {
+  if (!out) return TX_EINVAL;
+  *out = nullptr;
+  copy_err(err, err_len, "");
+  std::unique_ptr<tx_handle_s> h(new (std::nothrow) tx_handle_s);
+  if (!h) return TX_ENOMEM;
+  try {
+    tx::build_mesh_explicit(h->mesh, make());
+  } catch (const std::invalid_argument& e) {
+    copy_err(err, err_len, e.what());
+    return TX_EINVAL;
+  } catch (const std::exception& e) {
+    copy_err(err, err_len, e.what());
+    return TX_EINVAL;
+  }
+  *out = h.release();
+  return TX_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int tx_mesh_create_explicit(const tx_mesh_explicit_desc* d, tx_handle* out, char* err, int32_t err_len) {
+  if (!d || !out) return TX_EINVAL;
+  return create_explicit(out, err, err_len, [&]() {
+    tx::ExplicitMesh M;
+    if (d->n_nodes < 1 || !d->coords) throw std::invalid_argument("explicit mesh: nodes and coordinates");
+    if (d->n_blocks < 1 || !d->blocks) throw std::invalid_argument("explicit mesh: element blocks");
+    M.n_nodes = d->n_nodes;
+    M.coords.assign(d->coords, d->coords + 3 * d->n_nodes);
+    for (int32_t b = 0; b < d->n_blocks; ++b) {
+      const tx_explicit_block& B = d->blocks[b];
+      tx::ExplicitBlock E;
+      E.topology = B.topology; E.n_elem = B.n_elem; E.id = B.id;
+      E.name = B.name ? B.name : "block_" + std::to_string(B.id);
+      const int nv = B.topology == TX_TOPO_TET ? 4 : 8;
+      if (B.n_elem < 0 || (B.n_elem > 0 && !B.conn)) throw std::invalid_argument("explicit mesh: connectivity");
+      if (B.n_elem > 0) E.conn.assign(B.conn, B.conn + B.n_elem * nv);
+      M.blocks.push_back(std::move(E));
+    }
+    auto sets = [](int32_t n, const tx_explicit_set* in, int per, std::vector<tx::ExplicitSet>& dst) {
+      if (n > 0 && !in) throw std::invalid_argument("explicit mesh: sets");
+      for (int32_t k = 0; k < n; ++k) {
+        tx::ExplicitSet S;
+        S.id = in[k].id;
+        S.name = in[k].name ? in[k].name : std::to_string(in[k].id);
+        if (in[k].n < 0 || (in[k].n > 0 && !in[k].entries)) throw std::invalid_argument("explicit mesh: set entries");
+        if (in[k].n > 0) S.entries.assign(in[k].entries, in[k].entries + in[k].n * per);
+        dst.push_back(std::move(S));
+      }
+    };
+    sets(d->n_side_sets, d->side_sets, 2, M.side_sets);
+    sets(d->n_node_sets, d->node_sets, 1, M.node_sets);
+    return M;
+  });
+}
+
+int tx_mesh_create_exodus(const char* path, int32_t linear, tx_handle* out, char* err, int32_t err_len) {
+  if (!path || !out) return TX_EINVAL;
+  return create_explicit(out, err, err_len, [&]() { return tx::read_exodus(path, linear != 0); });
+}
+
+int tx_exodus_inspect(const char* path, tx_exodus_summary* s, char* err, int32_t err_len) {
+  if (!path || !s) return TX_EINVAL;
+  copy_err(err, err_len, "");
+  try {
+    const tx::ExodusSummary x = tx::exodus_summary(path);
+    s->version = x.version; s->dim = x.dim; s->n_nodes = x.n_nodes; s->n_elem = x.n_elem;
+    s->n_blocks = x.n_blocks; s->n_side_sets = x.n_side_sets; s->n_node_sets = x.n_node_sets;
+  } catch (const std::exception& e) {
+    copy_err(err, err_len, e.what());
+    return TX_EINVAL;
+  }
+  return TX_OK;
+}
+
+int tx_mesh_set_info(tx_handle h, int32_t kind, int32_t k, int64_t* id, char* name, int32_t name_len, int64_t* n) {
+  if (!h || kind < 0 || kind > 2) return TX_EINVAL;
+  if (!h->mesh.is_explicit) return fail(h, TX_ESTATE, "tx_mesh_set_info: lattice meshes have no sets");
+  const tx::ExplicitMesh& M = h->mesh.ex;
+  const int64_t count = kind == 0 ? (int64_t)M.blocks.size() : kind == 1 ? (int64_t)M.side_sets.size()
+                                                                         : (int64_t)M.node_sets.size();
+  if (k < 0) {
+    if (n) *n = count;
+    return TX_OK;
+  }
+  if (k >= count) return fail(h, TX_ERANGE, "tx_mesh_set_info: set out of range");
+  const std::string* nm;
+  if (kind == 0) {
+    if (id) *id = M.blocks[k].id;
+    if (n) *n = M.blocks[k].n_elem;
+    nm = &M.blocks[k].name;
+  } else {
+    const tx::ExplicitSet& S = kind == 1 ? M.side_sets[k] : M.node_sets[k];
+    if (id) *id = S.id;
+    if (n) *n = (int64_t)S.entries.size() / (kind == 1 ? 2 : 1);
+    nm = &S.name;
+  }
+  copy_err(name, name_len, *nm);
+  return TX_OK;
+}
+
+int tx_mesh_set_entries(tx_handle h, int32_t kind, int32_t k, int64_t* entries) {
+  if (!h || !entries || kind < 0 || kind > 2) return TX_EINVAL;
+  if (!h->mesh.is_explicit) return fail(h, TX_ESTATE, "tx_mesh_set_entries: lattice meshes have no sets");
+  const tx::ExplicitMesh& M = h->mesh.ex;
+  if (kind == 0) {
+    if (k < 0 || k >= (int32_t)M.blocks.size()) return fail(h, TX_ERANGE, "tx_mesh_set_entries: block out of range");
+    const int64_t first = h->mesh.block_first[k];
+    for (int64_t i = 0; i < M.blocks[k].n_elem; ++i) entries[i] = first + i;
+    return TX_OK;
+  }
+  const std::vector<tx::ExplicitSet>& sets = kind == 1 ? M.side_sets : M.node_sets;
+  if (k < 0 || k >= (int32_t)sets.size()) return fail(h, TX_ERANGE, "tx_mesh_set_entries: set out of range");
+  std::copy(sets[k].entries.begin(), sets[k].entries.end(), entries);
+  return TX_OK;
+}
+
 void tx_destroy(tx_handle h) { delete h; }
 
 const char* tx_last_error(tx_handle h) { return h ? h->err.c_str() : "null handle"; }
@@ -516,6 +647,14 @@ int tx_mesh_block_elements(tx_handle h, int32_t block, int64_t* n, int64_t* elem
   const auto& v = h->mesh.block_elems[block];
   *n = (int64_t)v.size();
   if (elems) std::memcpy(elems, v.data(), sizeof(int64_t) * v.size());
+  return TX_OK;
+}
+
+int tx_mesh_element_vertices(tx_handle h, int32_t block, int32_t* nv, int64_t* vertices) {
+  if (!h || !nv) return TX_EINVAL;
+  if (block < 0 || block >= h->mesh.nblocks) return fail(h, TX_ERANGE, "block out of range");
+  *nv = h->mesh.desc.block_topology[block] == TX_TOPO_HEX ? 8 : 4;
+  if (vertices) tx::element_vertices(h->mesh, block, vertices);
   return TX_OK;
 }
 
@@ -613,6 +752,20 @@ int tx_dirichlet_dofs(tx_handle h, uint32_t side_mask, uint32_t field_mask, int6
   if (!h->have_host_dofs) return fail(h, TX_ESTATE, "before tx_dof_build");
   return guarded(h, [&]() {
     std::vector<int32_t> v = tx::dirichlet_dofs(h->dofs, h->mesh, side_mask, field_mask);
+    *n = (int64_t)v.size();
+    if (lids) std::memcpy(lids, v.data(), sizeof(int32_t) * v.size());
+    return TX_OK;
+  });
+}
+
+int tx_dirichlet_dofs_node_set(tx_handle h, int32_t node_set, uint32_t field_mask, int64_t* n, int32_t* lids) {
+  if (!h || !n) return TX_EINVAL;
+  if (!h->have_host_dofs) return fail(h, TX_ESTATE, "before tx_dof_build");
+  if (!h->mesh.is_explicit) return fail(h, TX_EINVAL, "tx_dirichlet_dofs_node_set: lattice meshes use side masks");
+  if (node_set < 0 || node_set >= (int32_t)h->mesh.ex.node_sets.size())
+    return fail(h, TX_ERANGE, "tx_dirichlet_dofs_node_set: node set out of range");
+  return guarded(h, [&]() {
+    std::vector<int32_t> v = tx::node_set_dofs(h->dofs, h->mesh, node_set, field_mask);
     *n = (int64_t)v.size();
     if (lids) std::memcpy(lids, v.data(), sizeof(int32_t) * v.size());
     return TX_OK;
@@ -739,7 +892,14 @@ int tx_neumann_create(tx_handle h, const tx_neumann_desc* d, int32_t* id, int64_
   if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_neumann_create before tx_dof_build");
   if (d->block < 0 || d->block >= h->mesh.nblocks) return fail(h, TX_ERANGE, "tx_neumann_create: block out of range");
   if (d->field < 0 || d->field >= h->dofs.nf) return fail(h, TX_ERANGE, "tx_neumann_create: field out of range");
-  if (d->side_mask == 0 || (d->side_mask & ~0x3fu)) return fail(h, TX_EINVAL, "tx_neumann_create: side_mask");
+  if (h->mesh.is_explicit) {
+    if (d->side_set < 1 || d->side_set > (int32_t)h->mesh.ex.side_sets.size())
+      return fail(h, TX_EINVAL, "tx_neumann_create: explicit meshes name a side set (side_set = index + 1)");
+  } else if (d->side_set != 0) {
+    return fail(h, TX_EINVAL, "tx_neumann_create: lattice meshes use side_mask (side_set = 0)");
+  } else if (d->side_mask == 0 || (d->side_mask & ~0x3fu)) {
+    return fail(h, TX_EINVAL, "tx_neumann_create: side_mask");
+  }
   if (h->blocks[d->block].basis == TX_HCURL_I1)
     return fail(h, TX_EINVAL, "tx_neumann_create: the flux integrates a scalar (HGRAD) basis");
   double v0;
@@ -761,7 +921,8 @@ int tx_neumann_create(tx_handle h, const tx_neumann_desc* d, int32_t* id, int64_
     ns.desc.table_t = nullptr;
     ns.desc.table_v = nullptr;
     const tx::BlockDofs& B = h->dofs.blocks[d->block];
-    std::vector<int64_t> sides = tx::side_workset(h->mesh, d->block, d->side_mask);
+    std::vector<int64_t> sides = d->side_set > 0 ? tx::side_set_workset(h->mesh, d->block, d->side_set - 1)
+                                                 : tx::side_workset(h->mesh, d->block, d->side_mask);
     tx::SideTables S = tx::make_side_tables(B.topo, B.basis, B.degree);
     ns.n_sides = (int64_t)sides.size();
     ns.stride = S.stride;

@@ -53,6 +53,35 @@ struct BlockView {
 struct Handle;  // defined in tx_api.cu
 
 // ----------------------------------------------------------------- setup
+// An explicit (unstructured) mesh: nodes, hex8 / tet4 blocks of node
+// connectivity (0-based node numbers, Exodus/shards vertex order), side sets
+// of (element, side) pairs (element numbered over the whole mesh, blocks in
+// order; 0-based shards side ordinal) and node sets.
+struct ExplicitBlock {
+  int topology = 0;
+  int64_t n_elem = 0, id = 0;
+  std::string name;
+  std::vector<int64_t> conn;  // [n_elem][nv]
+};
+struct ExplicitSet {
+  int64_t id = 0;
+  std::string name;
+  std::vector<int64_t> entries;  // side sets: (element, side) pairs; node sets: nodes
+};
+struct ExplicitMesh {
+  int64_t n_nodes = 0;
+  std::vector<double> coords;  // [n_nodes][3]
+  std::vector<ExplicitBlock> blocks;
+  std::vector<ExplicitSet> side_sets, node_sets;
+};
+struct ExodusSummary {
+  int version = 0;
+  int64_t dim = 0, n_nodes = 0, n_elem = 0, n_blocks = 0, n_side_sets = 0, n_node_sets = 0;
+};
+// tx_exodus.cpp
+ExodusSummary exodus_summary(const std::string& path);
+ExplicitMesh read_exodus(const std::string& path, bool linear);
+
 // Host-side mesh + numbering state (built by tx_setup.cpp).
 struct Mesh {
   tx_mesh_desc desc{};
@@ -64,6 +93,10 @@ struct Mesh {
   std::vector<int8_t> elem_sub;           // element -> sub-element (tet)
   std::vector<std::vector<int64_t>> block_elems;
   std::vector<double> coords;             // node GID order, xyz
+  // explicit meshes: node numbers are the vertex GIDs; no lattice
+  bool is_explicit = false;
+  ExplicitMesh ex;
+  std::vector<int64_t> block_first;       // first mesh element of each block
 };
 
 struct BlockDofs {
@@ -95,6 +128,9 @@ struct Dofs {
 };
 
 void build_mesh(Mesh& m, const tx_mesh_desc& d);
+void build_mesh_explicit(Mesh& m, ExplicitMesh&& x);
+// Vertex node numbers of a block's elements [E][nv] (shards order); returns nv.
+int element_vertices(const Mesh& m, int block, int64_t* out);
 void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q);
 // owned GIDs (LID order), element GIDs/LIDs of a block (reference geometric order)
 void dof_owned_gids(const Dofs& D, int64_t* out);
@@ -107,6 +143,12 @@ std::vector<int32_t> dirichlet_dofs(const Dofs& D, const Mesh& m, uint32_t side_
 // | local side ordinal) for every local side lying on one of the sides, in
 // block element order, then side ordinal.
 std::vector<int64_t> side_workset(const Mesh& m, int block, uint32_t side_mask);
+// Side workset of a block from side set k of an explicit mesh (same encoding,
+// ascending).
+std::vector<int64_t> side_set_workset(const Mesh& m, int block, int side_set);
+// DOF LIDs of the fields in field_mask at the nodes of node set k of an
+// explicit mesh (ascending; nodes without DOFs are skipped).
+std::vector<int32_t> node_set_dofs(const Dofs& D, const Mesh& m, int node_set, uint32_t field_mask);
 // Worksets of a block: consecutive element ranges with sizes drawn uniformly
 // in [min_size, max_size] from a seeded generator (min == max: even split).
 std::vector<int64_t> workset_bounds(int64_t n_elem, int64_t min_size, int64_t max_size, uint64_t seed);

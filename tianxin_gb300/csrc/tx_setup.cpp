@@ -286,6 +286,7 @@ SideTables make_side_tables(int topo, int basis, int degree) {
 }
 
 std::vector<int64_t> side_workset(const Mesh& m, int block, uint32_t side_mask) {
+  if (m.is_explicit) throw std::invalid_argument("box sides are not defined on an explicit mesh; use a side set");
   std::vector<int64_t> out;
   const int topo = m.desc.block_topology[block];
   const int nsides = topo == TX_TOPO_HEX ? 6 : 4;
@@ -474,6 +475,102 @@ void build_mesh(Mesh& m, const tx_mesh_desc& d) {
   }
 }
 
+void build_mesh_explicit(Mesh& m, ExplicitMesh&& x) {
+  const int nb = (int)x.blocks.size();
+  if (nb < 1 || nb > TX_MAX_BLOCKS) throw std::invalid_argument("explicit mesh: 1 to 8 element blocks");
+  if (x.n_nodes < 1 || x.n_nodes >= (int64_t)INT32_MAX) throw std::invalid_argument("explicit mesh: node count");
+  if ((int64_t)x.coords.size() != 3 * x.n_nodes) throw std::invalid_argument("explicit mesh: coordinates");
+  m = Mesh();
+  m.is_explicit = true;
+  m.nblocks = nb;
+  m.n_nodes = x.n_nodes;
+  m.block_elems.assign(nb, {});
+  m.block_first.assign(nb, 0);
+  int64_t ne = 0;
+  for (int b = 0; b < nb; ++b) {
+    const ExplicitBlock& B = x.blocks[b];
+    if (B.topology != TX_TOPO_HEX && B.topology != TX_TOPO_TET)
+      throw std::invalid_argument("explicit mesh: blocks are hex8 or tet4");
+    const int nv = B.topology == TX_TOPO_HEX ? 8 : 4;
+    if (B.n_elem < 0 || (int64_t)B.conn.size() != B.n_elem * nv)
+      throw std::invalid_argument("explicit mesh: connectivity size");
+    for (int64_t v : B.conn)
+      if (v < 0 || v >= x.n_nodes) throw std::invalid_argument("explicit mesh: node number out of range");
+    m.desc.block_topology[b] = B.topology;
+    m.block_first[b] = ne;
+    for (int64_t i = 0; i < B.n_elem; ++i) m.block_elems[b].push_back(ne + i);
+    ne += B.n_elem;
+  }
+  m.n_elements = ne;
+  for (const ExplicitSet& S : x.side_sets) {
+    if (S.entries.size() % 2) throw std::invalid_argument("explicit mesh: side set entries come in pairs");
+    for (size_t i = 0; i < S.entries.size(); i += 2) {
+      const int64_t e = S.entries[i], s = S.entries[i + 1];
+      if (e < 0 || e >= ne) throw std::invalid_argument("explicit mesh: side set element out of range");
+      int b = nb - 1;
+      while (b > 0 && m.block_first[b] > e) --b;
+      if (s < 0 || s >= (x.blocks[b].topology == TX_TOPO_HEX ? 6 : 4))
+        throw std::invalid_argument("explicit mesh: side ordinal out of range");
+    }
+  }
+  for (const ExplicitSet& S : x.node_sets)
+    for (int64_t v : S.entries)
+      if (v < 0 || v >= x.n_nodes) throw std::invalid_argument("explicit mesh: node set node out of range");
+  m.coords = x.coords;
+  m.ex = std::move(x);
+}
+
+std::vector<int64_t> side_set_workset(const Mesh& m, int block, int side_set) {
+  if (!m.is_explicit || side_set < 0 || side_set >= (int)m.ex.side_sets.size())
+    throw std::out_of_range("side set out of range");
+  const int64_t lo = m.block_first[block], hi = lo + (int64_t)m.block_elems[block].size();
+  const std::vector<int64_t>& en = m.ex.side_sets[side_set].entries;
+  std::vector<int64_t> out;
+  for (size_t i = 0; i < en.size(); i += 2)
+    if (en[i] >= lo && en[i] < hi) out.push_back((en[i] - lo) * 8 + en[i + 1]);
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+  return out;
+}
+
+std::vector<int32_t> node_set_dofs(const Dofs& D, const Mesh& m, int node_set, uint32_t field_mask) {
+  if (!m.is_explicit || node_set < 0 || node_set >= (int)m.ex.node_sets.size())
+    throw std::out_of_range("node set out of range");
+  std::vector<int32_t> lid(m.n_nodes, -1);
+  for (int64_t e = 0; e < D.n_entities; ++e) lid[D.ent_gid[e]] = (int32_t)e;
+  std::vector<int32_t> out;
+  for (int64_t v : m.ex.node_sets[node_set].entries) {
+    if (lid[v] < 0) continue;
+    for (int f = 0; f < D.nf; ++f)
+      if (field_mask & (1u << f)) out.push_back(lid[v] * D.nf + f);
+  }
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+  return out;
+}
+
+int element_vertices(const Mesh& m, int block, int64_t* out) {
+  const int topo = m.desc.block_topology[block];
+  const int nv = topo == TX_TOPO_HEX ? 8 : 4;
+  const std::vector<int64_t>& el = m.block_elems[block];
+  if (m.is_explicit) {
+    const std::vector<int64_t>& cn = m.ex.blocks[block].conn;
+    std::copy(cn.begin(), cn.end(), out);
+    return nv;
+  }
+  Lattice L;
+  L.init(m.NX, m.NY, m.NZ);
+  for (size_t i = 0; i < el.size(); ++i) {
+    const int64_t br = m.elem_brick[el[i]];
+    const int64_t I = br % m.NX, J = (br / m.NX) % m.NY, K = br / (m.NX * m.NY);
+    for (int v = 0; v < nv; ++v) {
+      const int bv = topo == TX_TOPO_HEX ? v : kTets[m.elem_sub[el[i]]][v];
+      out[i * nv + v] = L.gid(2 * (I + kVtx[bv][0]), 2 * (J + kVtx[bv][1]), 2 * (K + kVtx[bv][2]));
+    }
+  }
+  return nv;
+}
+
 // ------------------------------------------------------------------ dofs
 static void color_block(BlockDofs& B, int64_t E, int64_t n_entities);
 
@@ -484,9 +581,10 @@ void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q) {
       q.physics != TX_PHYS_MAXWELL)
     throw std::invalid_argument("tx_dof_build: unknown physics");
   const int nf = D.nf;
+  const bool ex = m.is_explicit;
   Lattice L;
-  L.init(m.NX, m.NY, m.NZ);
-  const int64_t gid_space = L.nodes + L.hexEdges + L.hexFaces + m.n_bricks;
+  if (!ex) L.init(m.NX, m.NY, m.NZ);
+  const int64_t gid_space = ex ? m.n_nodes : L.nodes + L.hexEdges + L.hexFaces + m.n_bricks;
   bool orient = false;
   D.blocks.assign(m.nblocks, BlockDofs());
   for (int b = 0; b < m.nblocks; ++b) {
@@ -497,6 +595,8 @@ void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q) {
       throw std::invalid_argument("tx_dof_build: HCURL basis goes with MAXWELL physics only");
     if (B.basis == TX_HCURL_I1 && B.topo != TX_TOPO_HEX)
       throw std::invalid_argument("tx_dof_build: HCURL is provided on hexahedra only");
+    if (ex && B.basis != TX_HGRAD_C1)
+      throw std::invalid_argument("tx_dof_build: explicit meshes carry nodal (HGRAD_C1) fields only");
     B.degree = q.integration_order[b] > 0 ? q.integration_order[b] : default_degree(B.topo, B.basis);
     B.ref = make_ref_tables(B.topo, B.basis, B.degree);
     B.nb = B.ref.nb; B.nv = B.ref.nv;
@@ -529,6 +629,18 @@ void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q) {
     egid[b].assign(E * B.nb, -1);
     epos3[b].assign(E * B.nb * 3, 0);
     B.vconn.assign(E * B.nv, 0);
+    if (ex) {  // node numbers are the vertex GIDs; one DOF entity per vertex
+      const std::vector<int64_t>& cn = m.ex.blocks[b].conn;
+      for (int64_t i = 0; i < E; ++i) {
+        for (int v = 0; v < B.nv; ++v) B.vconn[i * B.nv + v] = (int32_t)cn[i * B.nv + v];
+        for (size_t g = 0; g < B.geom_dim.size(); ++g) {
+          const int bi = B.geom_basis[g];
+          if (bi >= 0) egid[b][i * B.nb + bi] = cn[i * B.nv + B.geom_sub[g]];  // vertex sub-cells only
+        }
+      }
+      for (int64_t k = 0; k < E * B.nb; ++k) has[egid[b][k]] = 1;
+      continue;
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < E; ++i) {
       int64_t e = el[i];
@@ -744,6 +856,7 @@ int dof_field_offsets(const Dofs& D, int block, int field, int32_t* out) {
 }
 
 std::vector<int32_t> dirichlet_dofs(const Dofs& D, const Mesh& m, uint32_t side_mask, uint32_t field_mask) {
+  if (m.is_explicit) throw std::invalid_argument("box sides are not defined on an explicit mesh; use a node set");
   std::vector<int32_t> out;
   const int64_t lim[3] = {2 * m.NX, 2 * m.NY, 2 * m.NZ};
   for (int64_t e = 0; e < D.n_entities; ++e) {

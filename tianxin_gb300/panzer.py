@@ -35,6 +35,14 @@ def _np_ptr(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
+def _element_vertices(conn, block):
+    nv, n = C.c_int32(), len(conn.getElementBlock(block))
+    check(conn.h, conn.lib.tx_mesh_element_vertices(conn.h, block, C.byref(nv), None))
+    out = np.zeros((n, nv.value), np.int64)
+    check(conn.h, conn.lib.tx_mesh_element_vertices(conn.h, block, C.byref(nv), _np_ptr(out)))
+    return out
+
+
 class CartesianConnManager:
     """Brick lattice on one rank; blocks named eblock-i_j_k (i slowest)."""
 
@@ -73,6 +81,149 @@ class CartesianConnManager:
         out = np.zeros((self.n_vertices, 3))
         check(self.h, self.lib.tx_mesh_coordinates(self.h, _np_ptr(out)))
         return out
+
+    def getElementVertices(self, block):
+        """Vertex node numbers [E][nv] of a block's elements (shards order)."""
+        return _element_vertices(self, block)
+
+
+class ExplicitConnManager:
+    """An unstructured hex8/tet4 mesh (nodal fields) from arrays or an Exodus II file.
+
+    Node numbers are 0-based and are the vertex GIDs of the numbering.  Side
+    sets hold (element, side) pairs (element over the whole mesh, 0-based
+    shards side); node sets hold node numbers.  Blocks, side sets and node
+    sets are addressed by index or name.
+    """
+
+    def __init__(self, h, lib):
+        self.h, self.lib = h, lib
+        ne, nv, nb = C.c_int64(), C.c_int64(), C.c_int32()
+        self.lib.tx_mesh_sizes(self.h, C.byref(ne), C.byref(nv), C.byref(nb))
+        self.n_elements, self.n_vertices, self.n_blocks = ne.value, nv.value, nb.value
+
+    @classmethod
+    def from_arrays(cls, coords, blocks, side_sets=(), node_sets=()):
+        """blocks: [(topology, conn[E][nv], id, name)]; side_sets: [(name, id, [(elem, side), ...])];
+        node_sets: [(name, id, nodes)]."""
+        lib = load()
+        xyz = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
+        keep = [xyz]
+        bl = (_abi.ExplicitBlock * len(blocks))()
+        for k, (topo, conn, bid, name) in enumerate(blocks):
+            c = np.ascontiguousarray(conn, dtype=np.int64)
+            keep.append(c)
+            bl[k].topology, bl[k].n_elem, bl[k].conn, bl[k].id = topo, c.shape[0], _np_ptr(c), bid
+            bl[k].name = name.encode() if name else None
+
+        def sets(items, per):
+            arr = (_abi.ExplicitSet * max(len(items), 1))()
+            for k, (name, sid, entries) in enumerate(items):
+                e = np.ascontiguousarray(entries, dtype=np.int64).reshape(-1)
+                keep.append(e)
+                arr[k].n, arr[k].entries, arr[k].id = len(e) // per, _np_ptr(e), sid
+                arr[k].name = name.encode() if name else None
+            return arr
+
+        d = _abi.MeshExplicitDesc()
+        d.n_nodes, d.coords, d.n_blocks, d.blocks = len(xyz), _np_ptr(xyz), len(blocks), bl
+        d.n_side_sets, d.side_sets = len(side_sets), sets(side_sets, 2)
+        d.n_node_sets, d.node_sets = len(node_sets), sets(node_sets, 1)
+        h, err = C.c_void_p(), C.create_string_buffer(512)
+        rc = lib.tx_mesh_create_explicit(C.byref(d), C.byref(h), err, 512)
+        if rc != 0:
+            raise TxError(rc, "tx_mesh_create_explicit: " + err.value.decode())
+        return cls(h, lib)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.tx_destroy(self.h)
+            self.h = None
+
+    def _names(self, kind):
+        n = C.c_int64()
+        check(self.h, self.lib.tx_mesh_set_info(self.h, kind, -1, None, None, 0, C.byref(n)))
+        out = []
+        for k in range(n.value):
+            buf = C.create_string_buffer(256)
+            check(self.h, self.lib.tx_mesh_set_info(self.h, kind, k, None, buf, 256, None))
+            out.append(buf.value.decode())
+        return out
+
+    def _entries(self, kind, k):
+        n = C.c_int64()
+        check(self.h, self.lib.tx_mesh_set_info(self.h, kind, k, None, None, 0, C.byref(n)))
+        out = np.zeros(n.value * (2 if kind == 1 else 1), np.int64)
+        if len(out):
+            check(self.h, self.lib.tx_mesh_set_entries(self.h, kind, k, _np_ptr(out)))
+        return out.reshape(-1, 2) if kind == 1 else out
+
+    def _index(self, kind, key):
+        return key if isinstance(key, (int, np.integer)) else self._names(kind).index(key)
+
+    def numElementBlocks(self):
+        return self.n_blocks
+
+    def getElementBlockIds(self):
+        return self._names(0)
+
+    def getSidesetNames(self):
+        return self._names(1)
+
+    def getNodesetNames(self):
+        return self._names(2)
+
+    def getElementBlock(self, block):
+        return self._entries(0, self._index(0, block))
+
+    def getSideset(self, key):
+        """(element, side) pairs of a side set."""
+        return self._entries(1, self._index(1, key))
+
+    def getNodeset(self, key):
+        return self._entries(2, self._index(2, key))
+
+    def sideSetIndex(self, key):
+        return self._index(1, key)
+
+    def nodeSetIndex(self, key):
+        return self._index(2, key)
+
+    def coordinates(self):
+        out = np.zeros((self.n_vertices, 3))
+        check(self.h, self.lib.tx_mesh_coordinates(self.h, _np_ptr(out)))
+        return out
+
+    def getElementVertices(self, block):
+        """Vertex node numbers [E][nv] of a block's elements (shards order)."""
+        return _element_vertices(self, block)
+
+
+class ExodusReaderFactory:
+    """STK_ExodusReaderFactory: "File Name" of a 3-D Exodus II mesh (NetCDF classic).
+
+    linear=True keeps the vertex nodes of quadratic elements (the
+    QuadraticToLinearMeshFactory conversion)."""
+
+    def __init__(self, file_name, linear=False):
+        self.file_name, self.linear = str(file_name), linear
+
+    def buildMesh(self):
+        lib = load()
+        h, err = C.c_void_p(), C.create_string_buffer(512)
+        rc = lib.tx_mesh_create_exodus(self.file_name.encode(), int(self.linear), C.byref(h), err, 512)
+        if rc != 0:
+            raise TxError(rc, "tx_mesh_create_exodus: " + err.value.decode())
+        return ExplicitConnManager(h, lib)
+
+
+def exodus_summary(file_name):
+    """Sizes of an Exodus file of any dimension: version, dim, n_nodes, n_elem, n_blocks, n_side_sets, n_node_sets."""
+    s, err = _abi.ExodusSummary(), C.create_string_buffer(512)
+    rc = load().tx_exodus_inspect(str(file_name).encode(), C.byref(s), err, 512)
+    if rc != 0:
+        raise TxError(rc, "tx_exodus_inspect: " + err.value.decode())
+    return {k: getattr(s, k) for k, _ in _abi.ExodusSummary._fields_}
 
 
 class DOFManager:
@@ -126,6 +277,15 @@ class DOFManager:
         check(self.h, self.lib.tx_dof_field_offsets(self.h, block, field, C.byref(n), None))
         out = np.zeros(n.value, np.int32)
         check(self.h, self.lib.tx_dof_field_offsets(self.h, block, field, C.byref(n), _np_ptr(out)))
+        return out
+
+    def dirichletDofsNodeSet(self, node_set, field_mask=0x7):
+        """Sorted local DOF ids of the fields in field_mask at the nodes of a node set (explicit meshes)."""
+        k = self.conn.nodeSetIndex(node_set)
+        n = C.c_int64()
+        check(self.h, self.lib.tx_dirichlet_dofs_node_set(self.h, k, field_mask, C.byref(n), None))
+        out = np.zeros(n.value, np.int32)
+        check(self.h, self.lib.tx_dirichlet_dofs_node_set(self.h, k, field_mask, C.byref(n), _np_ptr(out)))
         return out
 
     def dirichletDofs(self, side_mask, field_mask=0x7):
@@ -381,14 +541,18 @@ class BlockedTpetraLinearObjFactory:
 
 
 class DirichletBC:
-    """Dirichlet parameter list: DOF Names on the box sides (a side mask), value g."""
+    """Dirichlet parameter list: DOF Names on the box sides (a side mask) or, on an explicit
+    mesh, on a node set (name or index), value g."""
 
-    def __init__(self, dof, side_mask, fields=None, value=0.0):
+    def __init__(self, dof, side_mask=None, fields=None, value=0.0, node_set=None):
         names = fields if fields is not None else dof.field_names
         mask = 0
         for n in names:
             mask |= 1 << dof.getFieldNum(n)
-        self.lids_host = dof.dirichletDofs(side_mask, mask)
+        if node_set is not None:
+            self.lids_host = dof.dirichletDofsNodeSet(node_set, mask)
+        else:
+            self.lids_host = dof.dirichletDofs(side_mask, mask)
         self.lids = torch.from_numpy(self.lids_host).to("cuda")
         if np.isscalar(value):
             self.g = None if value == 0.0 else torch.full((len(self.lids_host),), float(value), dtype=torch.float64,
@@ -401,10 +565,12 @@ _VALUE_TYPES = {"Constant": _abi.TX_VALUE_CONSTANT, "Linear": _abi.TX_VALUE_LINE
                 "TimeTable": _abi.TX_VALUE_TIME_TABLE}
 
 
-def neumann_desc(block, side_mask, field, value_type="Constant", value=0.0, times=None, values=None):
-    """tx_neumann_desc from the reference's parameter names; the table arrays stay referenced by the result."""
+def neumann_desc(block, side_mask, field, value_type="Constant", value=0.0, times=None, values=None, side_set=-1):
+    """tx_neumann_desc from the reference's parameter names; the table arrays stay referenced by the result.
+    side_set >= 0 names a side set of an explicit mesh by index (then side_mask is unused)."""
     d = _abi.NeumannDesc()
     d.block, d.side_mask, d.field = block, side_mask, field
+    d.side_set = side_set + 1
     d.value_type = _VALUE_TYPES[value_type] if isinstance(value_type, str) else int(value_type)
     d.value = float(value)
     if times is not None:
@@ -434,11 +600,12 @@ class NeumannBC:
     Creating it builds the side workset and side tables on the device; evaluate(f, t) adds the flux to f.
     """
 
-    def __init__(self, dof, side_mask, dof_name=None, value_type="Constant", value=0.0, times=None, values=None,
-                 block=0):
+    def __init__(self, dof, side_mask=0, dof_name=None, value_type="Constant", value=0.0, times=None, values=None,
+                 block=0, side_set=None):
         field = dof.getFieldNum(dof_name) if dof_name is not None else 0
         self.dof = dof
-        self.desc = neumann_desc(block, side_mask, field, value_type, value, times, values)
+        ss = dof.conn.sideSetIndex(side_set) if side_set is not None else -1
+        self.desc = neumann_desc(block, side_mask, field, value_type, value, times, values, side_set=ss)
         sid, ns = C.c_int32(), C.c_int64()
         check(dof.h, dof.lib.tx_neumann_create(dof.h, C.byref(self.desc), C.byref(sid), C.byref(ns)),
               "tx_neumann_create")
