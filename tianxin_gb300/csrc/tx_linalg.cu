@@ -126,20 +126,21 @@ __device__ __forceinline__ T row_dot(int64_t b, int64_t e, int sub, const int32_
       for (int t = 0; t < N; ++t) s += CH::at(v, t) * __ldg(x + CH::at(c, t));
     }
     return s;
-  }
-  for (int64_t k = b + sub; k < e; k += LANES * U) {
-    T v[U];
-    int32_t c[U];
+  } else {
+    for (int64_t k = b + sub; k < e; k += LANES * U) {
+      T v[U];
+      int32_t c[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int64_t kk = k + u * LANES;
-      v[u] = kk < e ? __ldcs(vals + kk) : T(0);
-      c[u] = kk < e ? __ldcs(col + kk) : 0;
+      for (int u = 0; u < U; ++u) {
+        const int64_t kk = k + u * LANES;
+        v[u] = kk < e ? __ldcs(vals + kk) : T(0);
+        c[u] = kk < e ? __ldcs(col + kk) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) s += v[u] * __ldg(x + c[u]);
     }
-#pragma unroll
-    for (int u = 0; u < U; ++u) s += v[u] * __ldg(x + c[u]);
+    return s;
   }
-  return s;
 }
 
 // Vector CSR: LANES threads per row, strided over the row, shuffle reduction.
@@ -368,11 +369,13 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return v;
 }
 
-__global__ void k_finalize(const double* __restrict__ red, int nslots, double* __restrict__ out) {
+// Sums the first nparts partials of each of nslots slots.
+__global__ void k_finalize(const double* __restrict__ red, int nslots, double* __restrict__ out,
+                           int nparts = kRedBlocks) {
   __shared__ double sh[32];
   for (int s = 0; s < nslots; ++s) {
     double v = 0.0;
-    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) v += red[s * kRedBlocks + i];
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += red[s * kRedBlocks + i];
     v = block_sum(v, sh);
     if (threadIdx.x == 0) out[s] = v;
     __syncthreads();
@@ -685,6 +688,22 @@ struct DotLaunch {
   }
 };
 
+// resident CTAs an SM of the SpMV+dot kernel of a shape
+struct DotOccupancy {
+  int* per;
+  template <int L, int U>
+  cudaError_t run() const {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, k_spmv_dot<L, U>, kThreads, 0);
+  }
+};
+struct DotEntityOccupancy {
+  int* per;
+  template <int L, int U>
+  cudaError_t run() const {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, k_spmv_dot_eb<kEntityNf, L, U>, kThreads, 0);
+  }
+};
+
 // the same in the entity-block form
 struct DotEntityLaunch {
   EntityGraph eg; const SolverWork* w; unsigned gb; cudaStream_t s;
@@ -716,13 +735,25 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
   SpmvShape shape = resolve_shape(w.spmv, n, w.nnz, true);
   if (shape.unroll == kSpmvVector && !chunk_aligned<float>(w.vals32, col)) shape.unroll = 1;
   const SpmvShape eshape = resolve_entity_shape(w.spmv_eb, true);
+  // The SpMV+dot grid is one full wave of resident CTAs (at most kRedBlocks
+  // partials): with 1024 CTAs and six resident an SM, a second wave of 112
+  // CTAs ran on 12 % of the GPU and nearly doubled the product's time.
+  unsigned gd = gb;
+  {
+    int per = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (eg) with_entity_shape(eshape, DotEntityOccupancy{&per});
+    else with_shape(shape, DotOccupancy{&per});
+    if (per > 0 && sms > 0 && per * sms < (int)gb) gd = (unsigned)(per * sms);
+  }
   auto spmv_dot = [&]() {
-    if (eg) with_entity_shape(eshape, DotEntityLaunch{*eg, &w, gb, s});
-    else with_shape(shape, DotLaunch{n, rp, col, &w, gb, s});
+    if (eg) with_entity_shape(eshape, DotEntityLaunch{*eg, &w, gd, s});
+    else with_shape(shape, DotLaunch{n, rp, col, &w, gd, s});
   };
   auto cg_iteration = [&]() {
     spmv_dot();
-    k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2);  // pq
+    k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2, (int)gd);  // pq
     k_cg_update<<<gb, kThreads, 0, s>>>(n, w.scal, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
     k_cg_finish<<<1, 1024, 0, s>>>(w.scal, w.red);
     k_cg_pupdate<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, w.scal, w.z, w.p);
