@@ -274,20 +274,43 @@ int tx_neumann_eval(tx_handle h, int32_t id, double t, double* f);
 enum tx_integrand {
   TX_INTEGRAND_FIELD = 1,     /* u_field(q)                                          */
   TX_INTEGRAND_L2_ERROR = 2,  /* (u(q) - u*(q))^2                                    */
-  TX_INTEGRAND_H1_ERROR = 3   /* (u(q) - u*(q))^2 + |grad u(q) - grad u*(q)|^2        */
+  TX_INTEGRAND_H1_ERROR = 3,  /* (u(q) - u*(q))^2 + |grad u(q) - grad u*(q)|^2        */
+  /* ExtremeValue ("Use Max" true / false; ResponseScatterEvaluator_ExtremeValue,
+   * disc-fe/src/responses/Panzer_ResponseScatterEvaluator_ExtremeValue_impl.hpp:136-146):
+   * the max / min of u at the cubature points of the covered cells; among
+   * equal values the lowest (block, cell, point) wins; d/dx = N_b(q*) at the
+   * winning cell's DOFs. */
+  TX_INTEGRAND_MAX = 4,
+  TX_INTEGRAND_MIN = 5,
+  /* Probe (Panzer_ResponseScatterEvaluator_Probe): u at point, in the first
+   * cell (blocks in order, cells in order) holding it; d/dx = N_b(xi). */
+  TX_INTEGRAND_PROBE = 6
 };
 typedef struct tx_response_desc {
   int32_t block;           /* element block, -1: every block                          */
   int32_t field;           /* DOF field number (HGRAD blocks)                         */
   int32_t integrand;       /* tx_integrand                                            */
   int32_t cubature_degree; /* <= 0: each block's integration order; hex up to 7, tet 2 */
+  /* FIELD over sides instead of cells (a sideset response): the block's sides
+   * on these box sides (lattice meshes) or in side set side_set - 1
+   * (explicit meshes); the side rule is the block's integration order, as for
+   * the Neumann flux.  0 / 0: the cells. */
+  uint32_t side_mask;
+  int32_t side_set;
+  double point[3];         /* PROBE: the point (HOST copy at creation)                */
 } tx_response_desc;
-/* Build the response (per-block cubature tables; allocates). */
+/* Build the response (per-block cubature tables; allocates).  PROBE locates
+ * the point here: TX_ERANGE when no cell holds it. */
 int tx_response_create(tx_handle h, const tx_response_desc* d, int32_t* id);
 /* *value (DEVICE double) = the integral at x, summed in a fixed order (the
  * same bits on every call); dvalue_dx (DEVICE [N], may be NULL) += its
  * gradient.  Launch only. */
 int tx_response_eval(tx_handle h, int32_t id, const double* x, double* value, double* dvalue_dx);
+/* IPCoordinates (Panzer_ResponseEvaluatorFactory_IPCoordinates): the physical
+ * cubature points of a block at cubature_degree (<= 0: its integration
+ * order), [n_elem][*nq][3] into xyz (DEVICE; NULL: sizes only).  The tables
+ * are cached on the handle, so later calls are launch-only. */
+int tx_ip_coordinates(tx_handle h, int32_t block, int32_t cubature_degree, int32_t* nq, double* xyz);
 
 /* y = alpha*A*x + beta*y over a Tpetra-layout CRS (CrsMatrix::apply).
  * vals/x/y are FP64 (TX_SPMV_F64) or FP32 (TX_SPMV_F32). */

@@ -61,6 +61,10 @@ def lib():
         L.orc_dirichlet_apply.argtypes = [P, I64, P, P, P, P, P]
         L.orc_response.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P]
         L.orc_neumann.restype = I64
+        L.orc_response_extreme.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P]
+        L.orc_response_side.argtypes = [P, C.c_int, C.c_uint32, C.c_int, P, P, P]
+        L.orc_response_probe.restype = I64
+        L.orc_response_probe.argtypes = [P, P, C.c_int, P, P, P]
         L.orc_neumann.argtypes = [P, C.c_int, C.c_uint32, C.c_int, D, P]
         L.orc_spmv.argtypes = [I64, P, P, P, P, P, D, D]
         L.orc_cg.argtypes = [I64, P, P, P, P, P, D, C.c_int, C.POINTER(D)]
@@ -203,6 +207,41 @@ def _response_impl(self, integrand, field=0, block=-1, degree=0, x=None, gradien
 
 
 Oracle.response = _response_impl
+
+
+def _extreme_impl(self, use_max=True, field=0, block=-1, degree=0, x=None, gradient=False):
+    """ExtremeValue response at x: max (or min) of the field at the cubature points; optional gradient."""
+    x = np.ascontiguousarray(x, np.float64)
+    val = C.c_double()
+    g = np.zeros(self.n_dofs) if gradient else None
+    if lib().orc_response_extreme(self.h, block, field, int(use_max), degree, _p(x), C.byref(val), _p(g)):
+        raise RuntimeError("oracle extreme value failed")
+    return (val.value, g) if gradient else val.value
+
+
+def _side_impl(self, side_mask, field=0, block=-1, x=None, gradient=False):
+    """Integral of the field over the block sides on the box sides of side_mask; optional gradient."""
+    x = np.ascontiguousarray(x, np.float64)
+    val = C.c_double()
+    g = np.zeros(self.n_dofs) if gradient else None
+    if lib().orc_response_side(self.h, block, side_mask, field, _p(x), C.byref(val), _p(g)):
+        raise RuntimeError("oracle side response failed")
+    return (val.value, g) if gradient else val.value
+
+
+def _probe_impl(self, point, field=0, x=None, gradient=False):
+    """Probe response: (value, element) of the field at point (element -1: outside); optional gradient."""
+    x = np.ascontiguousarray(x, np.float64)
+    pt = np.ascontiguousarray(point, np.float64)
+    val = C.c_double(np.nan)
+    g = np.zeros(self.n_dofs) if gradient else None
+    e = lib().orc_response_probe(self.h, _p(pt), field, _p(x), C.byref(val), _p(g))
+    return (val.value, int(e), g) if gradient else (val.value, int(e))
+
+
+Oracle.extreme = _extreme_impl
+Oracle.side_response = _side_impl
+Oracle.probe = _probe_impl
 
 
 def workset_functor(value_type, value=0.0, times=None, values=None, t=0.0):

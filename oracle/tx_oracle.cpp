@@ -1180,6 +1180,167 @@ static void response_integral(const Problem& P, int blk_sel, int field, int inte
   *value = total;
 }
 
+// ExtremeValue (disc-fe/src/responses/Panzer_ResponseScatterEvaluator_ExtremeValue_impl.hpp:136-146 over
+// CellExtreme's per-cell extreme of the field at the cubature points): the max (use_max) or min of u(q) over
+// the cells of the selected blocks (block order, cell order, point order); the first point reaching the
+// extreme wins.  dgdx += d value / d x = N_b(q*) at the winning cell's field DOFs.
+static void response_extreme(const Problem& P, int blk_sel, int field, bool use_max, int degree, const double* x,
+                             double* value, double* dgdx) {
+  const Topology& T = P.T;
+  const DofManager& D = P.D;
+  bool have = false;
+  double best = 0.0;
+  int best_blk = -1, best_q = -1;
+  LO best_e = -1;
+  for (int blk = 0; blk < T.nblocks; ++blk) {
+    if (blk_sel >= 0 && blk != blk_sel) continue;
+    const BasisDef& B = D.block_basis[blk];
+    if (B.hcurl) throw std::runtime_error("response: scalar basis only");
+    const Cubature C = make_cubature(T.block_topo[blk], degree > 0 ? degree : D.block_degree[blk]);
+    std::vector<double> N(B.nb), dN(3 * B.nb);
+    for (LO e : T.block_elems[blk])
+      for (int q = 0; q < C.np; ++q) {
+        eval_hgrad(B, &C.xi[3 * q], N.data(), (double(*)[3])dN.data());
+        double u = 0.0;
+        for (int b = 0; b < B.nb; ++b) u += N[b] * x[D.elementLIDs[e][D.offsets[blk][field][b]]];
+        if (!have || (use_max ? u > best : u < best)) {
+          have = true; best = u; best_blk = blk; best_e = e; best_q = q;
+        }
+      }
+  }
+  *value = best;
+  if (dgdx && have) {
+    const BasisDef& B = D.block_basis[best_blk];
+    const Cubature C = make_cubature(T.block_topo[best_blk], degree > 0 ? degree : D.block_degree[best_blk]);
+    std::vector<double> N(B.nb), dN(3 * B.nb);
+    eval_hgrad(B, &C.xi[3 * best_q], N.data(), (double(*)[3])dN.data());
+    for (int b = 0; b < B.nb; ++b) dgdx[D.elementLIDs[best_e][D.offsets[best_blk][field][b]]] += N[b];
+  }
+}
+
+// Integral of the field over the sides of the selected blocks on the box sides of side_mask: sum over
+// (cell, side) of sum_q w_q |J t_u x J t_v| u(xi_q) (the side rule of neumann_flux); dgdx += N_b w |.|.
+static void response_side(const Problem& P, int blk_sel, uint32_t side_mask, int field, const double* x,
+                          double* value, double* dgdx) {
+  const Topology& T = P.T;
+  const DofManager& D = P.D;
+  double total = 0.0;
+  for (int blk = 0; blk < T.nblocks; ++blk) {
+    if (blk_sel >= 0 && blk != blk_sel) continue;
+    const BasisDef& B = D.block_basis[blk];
+    if (B.hcurl) throw std::runtime_error("response: scalar basis only");
+    const int topo = T.block_topo[blk];
+    const int nsides = topo == TX_TOPO_HEX ? 6 : 4, nvs = topo == TX_TOPO_HEX ? 4 : 3;
+    BasisDef G;
+    geom_basis(topo, G);
+    const int nv = G.nb;
+    std::vector<double> xi, w, X(3 * nv), N(B.nb), dN(3 * B.nb), Ng(nv), dNg(3 * nv);
+    for (LO e : T.block_elems[blk]) {
+      GO I, J, K;
+      T.brick_ijk(T.elem_brick[e], I, J, K);
+      const int sub = T.elem_sub[e];
+      for (int s = 0; s < nsides; ++s) {
+        int bv[4];
+        for (int k = 0; k < nvs; ++k)
+          bv[k] = topo == TX_TOPO_HEX ? kHexFace[s][k] : kTetInHex[sub][kTetSideNodes[s][k]];
+        if (!on_sides(T, I, J, K, bv, nvs, side_mask)) continue;
+        double tu[3], tv[3];
+        side_rule(topo, D.block_degree[blk], s, xi, w, tu, tv);
+        T.elem_vertices(e, nv, X.data());
+        for (size_t q = 0; q < w.size(); ++q) {
+          eval_hgrad(G, &xi[3 * q], Ng.data(), (double(*)[3])dNg.data());
+          double Jm[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+          for (int n = 0; n < nv; ++n)
+            for (int i = 0; i < 3; ++i)
+              for (int j = 0; j < 3; ++j) Jm[3 * i + j] += X[3 * n + i] * dNg[3 * n + j];
+          double a[3], bb[3];
+          for (int i = 0; i < 3; ++i) {
+            a[i] = Jm[3 * i] * tu[0] + Jm[3 * i + 1] * tu[1] + Jm[3 * i + 2] * tu[2];
+            bb[i] = Jm[3 * i] * tv[0] + Jm[3 * i + 1] * tv[1] + Jm[3 * i + 2] * tv[2];
+          }
+          const double c[3] = {a[1] * bb[2] - a[2] * bb[1], a[2] * bb[0] - a[0] * bb[2], a[0] * bb[1] - a[1] * bb[0]};
+          const double wm = w[q] * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+          eval_hgrad(B, &xi[3 * q], N.data(), (double(*)[3])dN.data());
+          double u = 0.0;
+          for (int b = 0; b < B.nb; ++b) u += N[b] * x[D.elementLIDs[e][D.offsets[blk][field][b]]];
+          total += u * wm;
+          if (dgdx)
+            for (int b = 0; b < B.nb; ++b) dgdx[D.elementLIDs[e][D.offsets[blk][field][b]]] += N[b] * wm;
+        }
+      }
+    }
+  }
+  *value = total;
+}
+
+// Probe (disc-fe/src/responses/Panzer_ResponseScatterEvaluator_Probe_impl.hpp: the cell holding the point,
+// its reference coordinates by CellTools::mapToReferenceFrame, the basis there): the first cell (block
+// order, cell order) whose inverse geometry map puts the point inside the reference cell (tolerance 1e-10);
+// value = sum_b N_b(xi) u_b, dgdx += N_b(xi).  Returns the mesh element, or -1 when no cell holds it.
+static LO response_probe(const Problem& P, const double pt[3], int field, const double* x, double* value,
+                         double* dgdx) {
+  const Topology& T = P.T;
+  const DofManager& D = P.D;
+  for (int blk = 0; blk < T.nblocks; ++blk) {
+    const BasisDef& B = D.block_basis[blk];
+    const int topo = T.block_topo[blk];
+    BasisDef G;
+    geom_basis(topo, G);
+    const int nv = G.nb;
+    std::vector<double> X(3 * nv), Ng(nv), dNg(3 * nv), N(B.nb), dN(3 * B.nb);
+    for (LO e : T.block_elems[blk]) {
+      T.elem_vertices(e, nv, X.data());
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int n = 0; n < nv; ++n)
+        for (int d = 0; d < 3; ++d) { lo[d] = std::min(lo[d], X[3 * n + d]); hi[d] = std::max(hi[d], X[3 * n + d]); }
+      bool box = true;
+      for (int d = 0; d < 3; ++d) box = box && pt[d] >= lo[d] - 1e-12 && pt[d] <= hi[d] + 1e-12;
+      if (!box) continue;
+      double xi[3] = {0.0, 0.0, 0.0};
+      if (topo == TX_TOPO_TET) xi[0] = xi[1] = xi[2] = 0.25;
+      for (int it = 0; it < 50; ++it) {  // Newton on x(xi) = pt
+        eval_hgrad(G, xi, Ng.data(), (double(*)[3])dNg.data());
+        double r[3] = {-pt[0], -pt[1], -pt[2]}, Jm[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int n = 0; n < nv; ++n)
+          for (int i = 0; i < 3; ++i) {
+            r[i] += Ng[n] * X[3 * n + i];
+            for (int j = 0; j < 3; ++j) Jm[3 * i + j] += X[3 * n + i] * dNg[3 * n + j];
+          }
+        const double c00 = Jm[4] * Jm[8] - Jm[5] * Jm[7], c01 = Jm[5] * Jm[6] - Jm[3] * Jm[8];
+        const double c02 = Jm[3] * Jm[7] - Jm[4] * Jm[6];
+        const double det = Jm[0] * c00 + Jm[1] * c01 + Jm[2] * c02;
+        const double Ji[9] = {c00 / det, (Jm[2] * Jm[7] - Jm[1] * Jm[8]) / det, (Jm[1] * Jm[5] - Jm[2] * Jm[4]) / det,
+                              c01 / det, (Jm[0] * Jm[8] - Jm[2] * Jm[6]) / det, (Jm[2] * Jm[3] - Jm[0] * Jm[5]) / det,
+                              c02 / det, (Jm[1] * Jm[6] - Jm[0] * Jm[7]) / det, (Jm[0] * Jm[4] - Jm[1] * Jm[3]) / det};
+        double step = 0.0;
+        for (int i = 0; i < 3; ++i) {
+          const double d = Ji[3 * i] * r[0] + Ji[3 * i + 1] * r[1] + Ji[3 * i + 2] * r[2];
+          xi[i] -= d;
+          step = std::max(step, std::fabs(d));
+        }
+        if (step < 1e-15) break;
+      }
+      const double tol = 1e-10;
+      bool inside;
+      if (topo == TX_TOPO_HEX)
+        inside = std::fabs(xi[0]) <= 1 + tol && std::fabs(xi[1]) <= 1 + tol && std::fabs(xi[2]) <= 1 + tol;
+      else
+        inside = xi[0] >= -tol && xi[1] >= -tol && xi[2] >= -tol && xi[0] + xi[1] + xi[2] <= 1 + tol;
+      if (!inside) continue;
+      eval_hgrad(B, xi, N.data(), (double(*)[3])dN.data());
+      double u = 0.0;
+      for (int b = 0; b < B.nb; ++b) {
+        const LO lid = D.elementLIDs[e][D.offsets[blk][field][b]];
+        u += N[b] * x[lid];
+        if (dgdx) dgdx[lid] += N[b];
+      }
+      *value = u;
+      return e;
+    }
+  }
+  return -1;
+}
+
 }  // namespace orc
 
 // ====================================================================== C API
@@ -1443,6 +1604,33 @@ int orc_response(void* h, int blk, int field, int integrand, int degree, const d
   try {
     response_integral(*(Problem*)h, blk, field, integrand, degree, x, value, dgdx);
     return 0;
+  } catch (std::exception&) {
+    return -1;
+  }
+}
+
+// ExtremeValue (use_max 1: max, 0: min), side-set integral over box sides, probe: 0 (probe: the element
+// holding the point) or -1.
+int orc_response_extreme(void* h, int blk, int field, int use_max, int degree, const double* x, double* value,
+                         double* dgdx) {
+  try {
+    response_extreme(*(Problem*)h, blk, field, use_max != 0, degree, x, value, dgdx);
+    return 0;
+  } catch (std::exception&) {
+    return -1;
+  }
+}
+int orc_response_side(void* h, int blk, uint32_t side_mask, int field, const double* x, double* value, double* dgdx) {
+  try {
+    response_side(*(Problem*)h, blk, side_mask, field, x, value, dgdx);
+    return 0;
+  } catch (std::exception&) {
+    return -1;
+  }
+}
+int64_t orc_response_probe(void* h, const double* pt, int field, const double* x, double* value, double* dgdx) {
+  try {
+    return (int64_t)response_probe(*(Problem*)h, pt, field, x, value, dgdx);
   } catch (std::exception&) {
     return -1;
   }

@@ -86,3 +86,17 @@ def test_solve_on_an_exodus_mesh(cuda, tmp_path):
         assert st["relres"] <= 1e-11
         sols.append(x.cpu().numpy())
     assert np.abs(sols[0] - sols[1]).max() <= 1e-10 * np.abs(sols[0]).max()
+
+
+def test_side_set_and_probe_responses_on_an_exodus_mesh(cuda, tmp_path):
+    conn, (coords, blocks, ss, ns) = X.box(n=(3, 2, 2), blocks=(1, 2, 1))
+    mesh = tx.ExodusReaderFactory(write_exodus(tmp_path / "r.exo", coords, blocks, ss, ns)).buildMesh()
+    q = A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 1.0))
+    d_lat, d_exp = tx.DOFManager(conn, q), tx.DOFManager(mesh, q)
+    x = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, d_lat.n_dofs)).cuda()
+    for b in range(len(blocks)):
+        v0 = tx.Response(d_lat, "Field", block=b, side_mask=A.SIDE_ZMAX).value(x)
+        v1 = tx.Response(d_exp, "Field", block=b, side_set="zmax").value(x)
+        assert abs(v0 - v1) <= 1e-14 * max(1.0, abs(v0))
+    p = (0.4, 0.7, 0.3)
+    assert tx.Response(d_lat, "Probe", point=p).value(x) == tx.Response(d_exp, "Probe", point=p).value(x)

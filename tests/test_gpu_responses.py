@@ -102,3 +102,83 @@ def test_response_errors(cuda):
     dof = tx.DOFManager(conn, A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 1.0)))
     with pytest.raises(tx.TxError):
         tx.Response(dof, "Field", cubature_degree=4)  # tet rules: degree 2
+
+
+# ExtremeValue, side-set integrals, probes and integration-point coordinates against the oracle.
+# u(q) sums the same basis terms in the same order on both sides; the bars allow the GPU's fused
+# multiply-adds: 1e-14 relative for values, exact winner locations (random data has no ties).
+@pytest.mark.parametrize("name", ["poisson_hex8", "heat_hex27_tet10", "elasticity_uy_hex8"])
+@pytest.mark.parametrize("kind", ["Max", "Min"])
+def test_extreme_value_matches_oracle(cuda, name, kind):
+    c = CASES[name]
+    o, dof = _setup(c)
+    field = dof.getFieldNum(c["field"])
+    x = np.random.default_rng(11).uniform(-1, 1, o.n_dofs)
+    v_ref, g_ref = o.extreme(kind == "Max", field=field, degree=2, x=x, gradient=True)
+    r = tx.Response(dof, kind, c["field"], cubature_degree=2)
+    g = torch.zeros(o.n_dofs, dtype=torch.float64, device="cuda")
+    v = float(r.evaluate(torch.from_numpy(x).cuda(), g).item())
+    assert abs(v - v_ref) <= 1e-14 * abs(v_ref)
+    gn = g.cpu().numpy()
+    assert np.array_equal(np.flatnonzero(gn), np.flatnonzero(g_ref))  # the same winning cell and point
+    assert np.abs(gn - g_ref).max() <= 1e-14
+
+
+@pytest.mark.parametrize("name", ["poisson_hex8", "heat_hex27_tet10", "poisson_tet4", "elasticity_uy_hex8"])
+def test_side_integral_matches_oracle(cuda, name):
+    c = CASES[name]
+    o, dof = _setup(c)
+    field = dof.getFieldNum(c["field"])
+    x = np.random.default_rng(12).uniform(-1, 1, o.n_dofs)
+    for block in ((0, 1) if name == "heat_hex27_tet10" else (-1,)):
+        mask = A.SIDE_XMIN | A.SIDE_YMAX | A.SIDE_ZMAX
+        v_ref, g_ref = o.side_response(mask, field=field, block=block, x=x, gradient=True)
+        r = tx.Response(dof, "Field", c["field"], block=block, side_mask=mask)
+        g = torch.zeros(o.n_dofs, dtype=torch.float64, device="cuda")
+        v = float(r.evaluate(torch.from_numpy(x).cuda(), g).item())
+        assert abs(v - v_ref) <= 1e-13 * np.abs(g_ref).sum()
+        assert np.abs(g.cpu().numpy() - g_ref).max() <= 1e-14 * np.abs(g_ref).max()
+
+
+@pytest.mark.parametrize("name", ["poisson_hex8", "heat_hex27_tet10", "poisson_tet4"])
+def test_probe_matches_oracle(cuda, name):
+    c = CASES[name]
+    o, dof = _setup(c)
+    field = dof.getFieldNum(c["field"])
+    x = np.random.default_rng(13).uniform(-1, 1, o.n_dofs)
+    rng = np.random.default_rng(14)
+    for _ in range(4):
+        p = rng.uniform(0.05, 0.95, 3)  # the lattice spans the unit cube
+        v_ref, e, g_ref = o.probe(p, field=field, x=x, gradient=True)
+        assert e >= 0
+        r = tx.Response(dof, "Probe", c["field"], point=p)
+        g = torch.zeros(o.n_dofs, dtype=torch.float64, device="cuda")
+        v = float(r.evaluate(torch.from_numpy(x).cuda(), g).item())
+        assert abs(v - v_ref) <= 1e-12 * max(1.0, abs(v_ref))
+        assert np.abs(g.cpu().numpy() - g_ref).max() <= 1e-12
+    with pytest.raises(tx.TxError) as err:
+        tx.Response(dof, "Probe", c["field"], point=(5.0, 0.5, 0.5))
+    assert err.value.code == A.TX_ERANGE
+
+
+def test_ip_coordinates_match_oracle(cuda):
+    c = CASES["heat_hex27_tet10"]
+    o, dof = _setup(c)
+    xyz = o.coordinates()
+    for b, topo in ((0, A.TX_TOPO_HEX), (1, A.TX_TOPO_TET)):
+        pts = tx.ip_coordinates(dof, b, cubature_degree=2).cpu().numpy()
+        conn = dof.conn.getElementVertices(b)
+        assert pts.shape[0] == len(conn)
+        for e in (0, len(conn) // 2, len(conn) - 1):
+            ip = np.zeros((pts.shape[1], 3))
+            n = O.lib().orc_cell_values(topo, 2, O._p(np.ascontiguousarray(xyz[conn[e]])), None, O._p(ip))
+            assert n == pts.shape[1]
+            assert np.abs(pts[e] - ip).max() <= 1e-14
+
+
+def test_response_kind_errors(cuda):
+    o, dof = _setup(CASES["poisson_hex8"])
+    with pytest.raises(tx.TxError):
+        tx.Response(dof, "L2 Error", side_mask=A.SIDE_ZMAX)  # side responses integrate the field
+    with pytest.raises(tx.TxError):
+        tx.Response(dof, "Max", side_mask=A.SIDE_ZMAX)

@@ -238,3 +238,36 @@ def test_response_closed_forms_and_gradient(topo, basis):
             xm[i] -= h
             fd = (o.response(kind, x=xp) - o.response(kind, x=xm)) / (2 * h)
             assert abs(fd - g[i]) <= 1e-8 * max(1.0, abs(g[i])), (kind, i)
+
+
+@pytest.mark.parametrize("topo,basis", [(A.TX_TOPO_HEX, A.TX_HGRAD_C1), (A.TX_TOPO_HEX, A.TX_HGRAD_C2),
+                                        (A.TX_TOPO_TET, A.TX_HGRAD_C1)])
+def test_extreme_side_and_probe_closed_forms(topo, basis):
+    # u = x + 2y + 3z lies in every basis here, so: the integral of u over the
+    # z = 1 face is 0.5 + 1 + 3 = 4.5 and the face area 1 (ExtremeValue, side
+    # and probe responses of the restatement); the probe returns u exactly at
+    # any point, even on jittered cells, with a gradient that sums to 1
+    # (partition of unity); on the unjittered hex lattice the max over the
+    # Gauss points sits at the point nearest (1,1,1): each coordinate
+    # 1 - h/2 + h/(2 sqrt 3) for the 2-point rule.
+    n = 4
+    h = 1.0 / n
+    o = O.Oracle(A.mesh_desc(n, topology=topo), A.equation_set(A.TX_PHYS_POISSON, basis, params=(1.0, 0.0, 0.0, 0.0)))
+    X = o.dof_coordinates()
+    u = X[:, 0] + 2 * X[:, 1] + 3 * X[:, 2]
+    assert abs(o.side_response(A.SIDE_ZMAX, x=u) - 4.5) <= 1e-13
+    v, g = o.side_response(A.SIDE_ZMAX, x=np.ones(o.n_dofs), gradient=True)
+    assert abs(v - 1.0) <= 1e-14 and abs(g.sum() - 1.0) <= 1e-13
+    if topo == A.TX_TOPO_HEX and basis == A.TX_HGRAD_C1:
+        c = 1 - h / 2 + h / (2 * np.sqrt(3))
+        vmax, gmax = o.extreme(True, x=u, degree=2, gradient=True)
+        assert abs(vmax - 6 * c) <= 1e-13 and abs(gmax.sum() - 1.0) <= 1e-14
+        assert abs(o.extreme(False, x=u, degree=2) - 6 * (1 - c)) <= 1e-13
+    oj = O.Oracle(A.mesh_desc(n, topology=topo, jitter=0.2, seed=9),
+                  A.equation_set(A.TX_PHYS_POISSON, basis, params=(1.0, 0.0, 0.0, 0.0)))
+    Xj = oj.dof_coordinates()
+    uj = Xj[:, 0] + 2 * Xj[:, 1] + 3 * Xj[:, 2]
+    for p in ((0.31, 0.47, 0.52), (0.9, 0.05, 0.66)):
+        val, e, gp = oj.probe(p, x=uj, gradient=True)
+        assert e >= 0 and abs(val - (p[0] + 2 * p[1] + 3 * p[2])) <= 1e-12 and abs(gp.sum() - 1.0) <= 1e-12
+    assert oj.probe((1.5, 0.5, 0.5), x=uj)[1] == -1

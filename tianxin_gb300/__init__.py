@@ -9,11 +9,11 @@ from ._abi import (ALL_SIDES, SIDE_XMAX, SIDE_XMIN, SIDE_YMAX, SIDE_YMIN, SIDE_Z
                    TX_SOURCE_AFFINE, TX_SOURCE_CONST, TX_SOURCE_SINE, TX_TOPO_HEX, TX_TOPO_TET, equation_set,
                    mesh_desc)
 from ._lib import TxError, load
-from .panzer import (HEX, TET, AssemblyEngine, Batch, ExodusReaderFactory, ExplicitConnManager, exodus_summary, BlockedCrsMatrix, BlockedDOFManager, BlockedModelEvaluator,
+from .panzer import (HEX, TET, AssemblyEngine, Batch, ip_coordinates, ExodusReaderFactory, ExplicitConnManager, exodus_summary, BlockedCrsMatrix, BlockedDOFManager, BlockedModelEvaluator,
                      BlockedTpetraLinearObjFactory, CapturedGraph, CartesianConnManager, CrsMatrix, DirichletBC, DOFManager,
                      HostEvaluator, ModelEvaluator, NeumannBC, Response, TpetraLinearObjFactory, neumann_value,
                      synchronize)
 
 __all__ = ["CartesianConnManager", "DOFManager", "TpetraLinearObjFactory", "CrsMatrix", "DirichletBC",
-           "NeumannBC", "neumann_value", "Response", "CapturedGraph", "HostEvaluator", "AssemblyEngine", "ModelEvaluator", "ExodusReaderFactory", "ExplicitConnManager", "exodus_summary", "BlockedDOFManager", "BlockedTpetraLinearObjFactory", "BlockedCrsMatrix",
+           "NeumannBC", "neumann_value", "Response", "ip_coordinates", "CapturedGraph", "HostEvaluator", "AssemblyEngine", "ModelEvaluator", "ExodusReaderFactory", "ExplicitConnManager", "exodus_summary", "BlockedDOFManager", "BlockedTpetraLinearObjFactory", "BlockedCrsMatrix",
            "BlockedModelEvaluator", "TxError", "load", "equation_set", "mesh_desc", "synchronize"]

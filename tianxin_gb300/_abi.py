@@ -47,6 +47,9 @@ TX_SOLVE_ENTITY_BLOCKS = 0x8
 TX_INTEGRAND_FIELD = 1
 TX_INTEGRAND_L2_ERROR = 2
 TX_INTEGRAND_H1_ERROR = 3
+TX_INTEGRAND_MAX = 4
+TX_INTEGRAND_MIN = 5
+TX_INTEGRAND_PROBE = 6
 
 TX_VALUE_CONSTANT = 1
 TX_VALUE_LINEAR = 2
@@ -108,7 +111,8 @@ class SolveArgs(C.Structure):
 
 
 class ResponseDesc(C.Structure):
-    _fields_ = [("block", C.c_int32), ("field", C.c_int32), ("integrand", C.c_int32), ("cubature_degree", C.c_int32)]
+    _fields_ = [("block", C.c_int32), ("field", C.c_int32), ("integrand", C.c_int32), ("cubature_degree", C.c_int32),
+                ("side_mask", C.c_uint32), ("side_set", C.c_int32), ("point", C.c_double * 3)]
 
 
 class NeumannDesc(C.Structure):

@@ -39,6 +39,7 @@ SIGNATURES = {
     "tx_eval_dfdp": (C.c_int, [P, C.POINTER(_abi.EvalArgs), I32, P]),
     "tx_response_create": (C.c_int, [P, C.POINTER(_abi.ResponseDesc), C.POINTER(I32)]),
     "tx_response_eval": (C.c_int, [P, I32, P, P, P]),
+    "tx_ip_coordinates": (C.c_int, [P, I32, I32, C.POINTER(I32), P]),
     "tx_set_worksets": (C.c_int, [P, I64, I64, C.c_uint64]),
     "tx_set_grid_cap": (C.c_int, [P, I32]),
     "tx_set_spmv_shape": (C.c_int, [P, I32, I32]),

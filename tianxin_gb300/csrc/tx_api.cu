@@ -97,6 +97,15 @@ struct ResponseSet {
   std::vector<int64_t> offset;     // first partial of each covered block
   double* partial = nullptr;
   int64_t n_partial = 0;
+  int64_t* pidx = nullptr;          // ExtremeValue: per-partial winner keys
+  int64_t* winner = nullptr;        // ExtremeValue: the final winner key
+  bool side = false;                // FIELD over a side workset per covered block
+  std::vector<int64_t*> sides;
+  std::vector<int64_t> n_sides;
+  std::vector<int> stride, nqf;
+  int32_t* probe_lids = nullptr;    // PROBE: the cell's field DOFs and N_b(xi)
+  double* probe_n = nullptr;
+  int probe_nb = 0;
 };
 
 struct tx_handle_s {
@@ -127,6 +136,9 @@ struct tx_handle_s {
   int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
+  // cubature tables of tx_ip_coordinates per (block, degree)
+  struct IpTables { int block, degree, nq; double* tables; };
+  std::vector<IpTables> ip_tables;
   // blocked layout (tx_blocked_layout) and the device graphs of its blocks,
   // one per (fields in row block, fields in column block)
   tx::BlockedMap blocked;
@@ -143,9 +155,13 @@ struct tx_handle_s {
     neumann.clear();
     for (auto& rs : responses) {
       for (double* t : rs.tables) cudaFree(t);
-      cudaFree(rs.partial);
+      for (int64_t* sd : rs.sides) cudaFree(sd);
+      cudaFree(rs.partial); cudaFree(rs.pidx); cudaFree(rs.winner);
+      cudaFree(rs.probe_lids); cudaFree(rs.probe_n);
     }
     responses.clear();
+    for (auto& t : ip_tables) cudaFree(t.tables);
+    ip_tables.clear();
     for (auto& b : blocks) {
       cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
       cudaFree(b.color_perm);
@@ -186,6 +202,8 @@ int guarded(tx_handle h, F&& body) {
     return fail(h, TX_ECUDA, e.what());
   } catch (std::invalid_argument& e) {
     return fail(h, TX_EINVAL, e.what());
+  } catch (std::out_of_range& e) {
+    return fail(h, TX_ERANGE, e.what());
   } catch (std::bad_alloc&) {
     return fail(h, TX_ENOMEM, "host allocation failed");
   } catch (std::exception& e) {
@@ -975,32 +993,91 @@ int tx_response_create(tx_handle h, const tx_response_desc* d, int32_t* id) {
   if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_response_create before tx_dof_build");
   if (d->block < -1 || d->block >= h->mesh.nblocks) return fail(h, TX_ERANGE, "tx_response_create: block");
   if (d->field < 0 || d->field >= h->dofs.nf) return fail(h, TX_ERANGE, "tx_response_create: field");
-  if (d->integrand < TX_INTEGRAND_FIELD || d->integrand > TX_INTEGRAND_H1_ERROR)
+  if (d->integrand < TX_INTEGRAND_FIELD || d->integrand > TX_INTEGRAND_PROBE)
     return fail(h, TX_EINVAL, "tx_response_create: integrand");
+  const bool side = d->side_mask != 0 || d->side_set != 0;
+  if (side) {
+    if (d->integrand != TX_INTEGRAND_FIELD)
+      return fail(h, TX_EINVAL, "tx_response_create: side responses integrate the field (TX_INTEGRAND_FIELD)");
+    if (h->mesh.is_explicit ? (d->side_set < 1 || d->side_set > (int32_t)h->mesh.ex.side_sets.size())
+                            : (d->side_set != 0 || (d->side_mask & ~0x3fu)))
+      return fail(h, TX_EINVAL, "tx_response_create: side_mask (lattice meshes) or side_set (explicit meshes)");
+  }
+  const bool extreme = d->integrand == TX_INTEGRAND_MAX || d->integrand == TX_INTEGRAND_MIN;
   return guarded(h, [&]() {
     ResponseSet rs;
     rs.desc = *d;
+    rs.side = side;
+    auto release = [&]() {
+      for (double* t : rs.tables) cudaFree(t);
+      for (int64_t* sd : rs.sides) cudaFree(sd);
+      cudaFree(rs.partial); cudaFree(rs.pidx); cudaFree(rs.winner);
+      cudaFree(rs.probe_lids); cudaFree(rs.probe_n);
+    };
     try {
-      for (int b = 0; b < h->mesh.nblocks; ++b) {
-        if (d->block >= 0 && b != d->block) continue;
+      if (d->integrand == TX_INTEGRAND_PROBE) {
+        int b = -1;
+        int64_t i = -1;
+        double xi[3];
+        if (!tx::locate_point(h->mesh, h->dofs, d->point, b, i, xi))
+          throw std::out_of_range("tx_response_create: no cell holds the probe point");
         const tx::BlockDofs& B = h->dofs.blocks[b];
         if (B.basis == TX_HCURL_I1) throw std::invalid_argument("tx_response_create: HGRAD blocks only");
-        const int deg = d->cubature_degree > 0 ? d->cubature_degree : B.degree;
-        tx::RefTables R = tx::make_ref_tables(B.topo, B.basis, deg);
-        if (R.nq > 64) throw std::invalid_argument("tx_response_create: at most 64 cubature points");
-        double* t = nullptr;
-        ck(upload(t, R.packed()), "upload response tables");
-        rs.tables.push_back(t);
-        rs.blocks.push_back(b);
-        rs.nq.push_back(R.nq);
-        rs.offset.push_back(rs.n_partial);
-        rs.n_partial += tx::response_grid((int64_t)h->mesh.block_elems[b].size());
+        const tx::RefTables R = tx::tables_at(B.topo, B.basis, xi, 1);
+        std::vector<int32_t> lids(B.nb);
+        std::vector<double> n(B.nb);
+        for (int k = 0; k < B.nb; ++k) {
+          lids[k] = h->dofs.nf * B.dconn[i * B.nb + k] + d->field;
+          n[k] = R.val[k];
+        }
+        ck(upload(rs.probe_lids, lids), "upload probe DOFs");
+        ck(upload(rs.probe_n, n), "upload probe basis values");
+        rs.probe_nb = B.nb;
+      } else {
+        for (int b = 0; b < h->mesh.nblocks; ++b) {
+          if (d->block >= 0 && b != d->block) continue;
+          const tx::BlockDofs& B = h->dofs.blocks[b];
+          if (B.basis == TX_HCURL_I1) throw std::invalid_argument("tx_response_create: HGRAD blocks only");
+          double* t = nullptr;
+          if (side) {
+            std::vector<int64_t> sd = d->side_set > 0 ? tx::side_set_workset(h->mesh, b, d->side_set - 1)
+                                                      : tx::side_workset(h->mesh, b, d->side_mask);
+            const tx::SideTables S = tx::make_side_tables(B.topo, B.basis, B.degree);
+            if (S.nqf > 32) throw std::invalid_argument("tx_response_create: at most 32 side points");
+            int64_t* dsd = nullptr;
+            ck(upload(dsd, sd), "upload side workset");
+            rs.sides.push_back(dsd);
+            rs.n_sides.push_back((int64_t)sd.size());
+            rs.stride.push_back(S.stride);
+            rs.nqf.push_back(S.nqf);
+            ck(upload(t, S.packed), "upload side tables");
+            rs.tables.push_back(t);
+            rs.nq.push_back(S.nqf);
+            rs.offset.push_back(rs.n_partial);
+            rs.n_partial += tx::response_grid((int64_t)sd.size());
+          } else {
+            const int deg = d->cubature_degree > 0 ? d->cubature_degree : B.degree;
+            tx::RefTables R = tx::make_ref_tables(B.topo, B.basis, deg);
+            if (R.nq > 64) throw std::invalid_argument("tx_response_create: at most 64 cubature points");
+            ck(upload(t, R.packed()), "upload response tables");
+            rs.tables.push_back(t);
+            rs.nq.push_back(R.nq);
+            rs.offset.push_back(rs.n_partial);
+            rs.n_partial += tx::response_grid((int64_t)h->mesh.block_elems[b].size());
+          }
+          rs.blocks.push_back(b);
+        }
+        const size_t np = (size_t)(rs.n_partial > 0 ? rs.n_partial : 1);
+        ck(cudaMalloc((void**)&rs.partial, sizeof(double) * np), "alloc partials");
+        ck(cudaMemset(rs.partial, 0, sizeof(double) * np), "zero partials");
+        if (extreme) {
+          ck(cudaMalloc((void**)&rs.pidx, sizeof(int64_t) * np), "alloc partial keys");
+          ck(cudaMemset(rs.pidx, 0xff, sizeof(int64_t) * np), "clear partial keys");
+          ck(cudaMalloc((void**)&rs.winner, sizeof(int64_t)), "alloc winner");
+        }
       }
-      ck(cudaMalloc((void**)&rs.partial, sizeof(double) * (rs.n_partial > 0 ? rs.n_partial : 1)), "alloc partials");
-      ck(cudaMemset(rs.partial, 0, sizeof(double) * (rs.n_partial > 0 ? rs.n_partial : 1)), "zero partials");
     } catch (...) {
-      for (double* t : rs.tables) cudaFree(t);
-      cudaFree(rs.partial);
+      release();
       throw;
     }
     h->responses.push_back(rs);
@@ -1014,16 +1091,65 @@ int tx_response_eval(tx_handle h, int32_t id, const double* x, double* value, do
   if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_response_eval before tx_dof_build");
   if (id < 0 || id >= (int32_t)h->responses.size()) return fail(h, TX_ERANGE, "tx_response_eval: unknown response");
   const ResponseSet& rs = h->responses[id];
+  const int nf = h->dofs.nf, field = rs.desc.field, kind = rs.desc.integrand;
   cudaError_t e = cudaSuccess;
-  for (size_t k = 0; k < rs.blocks.size() && e == cudaSuccess; ++k) {
-    tx::BlockView v = h->blocks[rs.blocks[k]].view();
-    v.ref = rs.tables[k];
-    e = tx::launch_response(v, rs.nq[k], h->d_coords, x, h->dofs.nf, rs.desc.field, rs.desc.integrand,
-                            rs.partial + rs.offset[k], dvalue_dx, h->stream);
+  if (kind == TX_INTEGRAND_PROBE) {
+    e = tx::launch_response_probe(rs.probe_lids, rs.probe_n, rs.probe_nb, x, value, dvalue_dx, h->stream);
+  } else if (kind == TX_INTEGRAND_MAX || kind == TX_INTEGRAND_MIN) {
+    const bool use_max = kind == TX_INTEGRAND_MAX;
+    for (size_t k = 0; k < rs.blocks.size() && e == cudaSuccess; ++k) {
+      tx::BlockView v = h->blocks[rs.blocks[k]].view();
+      v.ref = rs.tables[k];
+      e = tx::launch_response_extreme(v, rs.nq[k], x, nf, field, use_max, (int)k, rs.partial + rs.offset[k],
+                                      rs.pidx + rs.offset[k], h->stream);
+    }
+    if (e == cudaSuccess)
+      e = tx::launch_response_extreme_final(rs.partial, rs.pidx, rs.n_partial, use_max, value, rs.winner, h->stream);
+    for (size_t k = 0; dvalue_dx && k < rs.blocks.size() && e == cudaSuccess; ++k) {
+      tx::BlockView v = h->blocks[rs.blocks[k]].view();
+      v.ref = rs.tables[k];
+      e = tx::launch_response_extreme_grad(v, rs.nq[k], (int)k, rs.winner, nf, field, dvalue_dx, h->stream);
+    }
+  } else {
+    for (size_t k = 0; k < rs.blocks.size() && e == cudaSuccess; ++k) {
+      tx::BlockView v = h->blocks[rs.blocks[k]].view();
+      v.ref = rs.tables[k];
+      e = rs.side ? tx::launch_response_side(v, h->d_coords, rs.sides[k], rs.n_sides[k], rs.tables[k], rs.stride[k],
+                                             rs.nqf[k], x, nf, field, rs.partial + rs.offset[k], dvalue_dx, h->stream)
+                  : tx::launch_response(v, rs.nq[k], h->d_coords, x, nf, field, kind, rs.partial + rs.offset[k],
+                                        dvalue_dx, h->stream);
+    }
+    if (e == cudaSuccess) e = tx::launch_response_sum(rs.partial, rs.n_partial, value, h->stream);
   }
-  if (e == cudaSuccess) e = tx::launch_response_sum(rs.partial, rs.n_partial, value, h->stream);
   if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_response_eval: ") + cudaGetErrorString(e));
   return TX_OK;
+}
+
+int tx_ip_coordinates(tx_handle h, int32_t block, int32_t cubature_degree, int32_t* nq, double* xyz) {
+  if (!h || !nq) return TX_EINVAL;
+  if (!h->have_dofs) return fail(h, TX_ESTATE, "tx_ip_coordinates before tx_dof_build");
+  if (block < 0 || block >= h->mesh.nblocks) return fail(h, TX_ERANGE, "tx_ip_coordinates: block");
+  return guarded(h, [&]() {
+    const tx::BlockDofs& B = h->dofs.blocks[block];
+    const int deg = cubature_degree > 0 ? cubature_degree : B.degree;
+    tx_handle_s::IpTables* t = nullptr;
+    for (auto& c : h->ip_tables)
+      if (c.block == block && c.degree == deg) t = &c;
+    if (!t) {
+      const tx::RefTables R = tx::make_ref_tables(B.topo, TX_HGRAD_C1, deg);
+      tx_handle_s::IpTables c{block, deg, R.nq, nullptr};
+      ck(upload(c.tables, R.packed()), "upload cubature tables");
+      h->ip_tables.push_back(c);
+      t = &h->ip_tables.back();
+    }
+    *nq = t->nq;
+    if (xyz) {
+      tx::BlockView v = h->blocks[block].view();
+      v.ref = t->tables;
+      ck(tx::launch_ip_coordinates(v, t->nq, h->d_coords, xyz, h->stream), "ip coordinates");
+    }
+    return TX_OK;
+  });
 }
 
 int tx_graph_capture_begin(tx_handle h) {

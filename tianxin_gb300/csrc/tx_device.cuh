@@ -103,6 +103,23 @@ int response_grid(int64_t n_elem);
 cudaError_t launch_response(const BlockView& B, int nq, const double* coords, const double* x, int nf, int field,
                             int integrand, double* partial, double* dgdx, cudaStream_t s);
 cudaError_t launch_response_sum(const double* partial, int64_t n, double* value, cudaStream_t s);
+// ExtremeValue: per-CTA best (value, key = block << 48 | cell << 6 | point);
+// the final pass picks the winner in index order; the gradient pass adds the
+// winner's basis values when it lies in the given block.
+cudaError_t launch_response_extreme(const BlockView& B, int nq, const double* x, int nf, int field, bool use_max,
+                                    int blk_key, double* pval, int64_t* pidx, cudaStream_t s);
+cudaError_t launch_response_extreme_final(const double* pval, const int64_t* pidx, int64_t n, bool use_max,
+                                          double* value, int64_t* winner, cudaStream_t s);
+cudaError_t launch_response_extreme_grad(const BlockView& B, int nq, int blk_key, const int64_t* winner, int nf,
+                                         int field, double* dgdx, cudaStream_t s);
+// Integral of a field over a side workset (response_grid(n) partials).
+cudaError_t launch_response_side(const BlockView& B, const double* coords, const int64_t* sides, int64_t n,
+                                 const double* tables, int stride, int nqf, const double* x, int nf, int field,
+                                 double* partial, double* dgdx, cudaStream_t s);
+cudaError_t launch_response_probe(const int32_t* lids, const double* N, int nb, const double* x, double* value,
+                                  double* dgdx, cudaStream_t s);
+// Physical cubature points [E][nq][3] of a block (ref = packed RefTables).
+cudaError_t launch_ip_coordinates(const BlockView& B, int nq, const double* coords, double* xyz, cudaStream_t s);
 cudaError_t launch_spmv_f64(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* vals,
                             const double* x, double* y, double alpha, double beta, int64_t nnz_hint, cudaStream_t s,
                             SpmvShape shape = SpmvShape());

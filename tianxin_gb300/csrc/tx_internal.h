@@ -26,6 +26,8 @@ struct RefTables {
 };
 
 RefTables make_ref_tables(int topo, int basis, int degree);
+// Basis and geometry tables at n given reference points (weights zero).
+RefTables tables_at(int topo, int basis, const double* xi, int n);
 int default_degree(int topo, int basis);
 
 // Side cubature tables of a block's reference element, one group per local
@@ -143,6 +145,10 @@ std::vector<int32_t> dirichlet_dofs(const Dofs& D, const Mesh& m, uint32_t side_
 // | local side ordinal) for every local side lying on one of the sides, in
 // block element order, then side ordinal.
 std::vector<int64_t> side_workset(const Mesh& m, int block, uint32_t side_mask);
+// The first element (blocks in order, block elements in order) whose inverse
+// geometry map puts p inside the reference cell (tolerance 1e-10): its block,
+// block-local index and reference coordinates.
+bool locate_point(const Mesh& m, const Dofs& D, const double p[3], int& block, int64_t& elem, double xi[3]);
 // Side workset of a block from side set k of an explicit mesh (same encoding,
 // ascending).
 std::vector<int64_t> side_set_workset(const Mesh& m, int block, int side_set);

@@ -219,6 +219,69 @@ RefTables make_ref_tables(int topo, int basis, int degree) {
   return R;
 }
 
+RefTables tables_at(int topo, int basis, const double* xi, int n) {
+  RefTables R = blank_tables(topo, basis, 0);
+  R.xi.assign(xi, xi + 3 * n);
+  R.w.assign(n, 0.0);
+  eval_tables(R);
+  return R;
+}
+
+bool locate_point(const Mesh& m, const Dofs& D, const double p[3], int& block, int64_t& elem, double xi[3]) {
+  for (int b = 0; b < m.nblocks; ++b) {
+    const BlockDofs& B = D.blocks[b];
+    const int nv = B.nv, topo = B.topo;
+    const int64_t E = (int64_t)m.block_elems[b].size();
+    for (int64_t i = 0; i < E; ++i) {
+      const int32_t* vc = &B.vconn[i * nv];
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int v = 0; v < nv; ++v)
+        for (int d = 0; d < 3; ++d) {
+          lo[d] = std::min(lo[d], m.coords[3 * vc[v] + d]);
+          hi[d] = std::max(hi[d], m.coords[3 * vc[v] + d]);
+        }
+      bool box = true;
+      for (int d = 0; d < 3; ++d) box = box && p[d] >= lo[d] - 1e-12 && p[d] <= hi[d] + 1e-12;
+      if (!box) continue;
+      // Newton on x(xi) = p with the geometry basis (trilinear hex, linear tet)
+      double z[3] = {0.0, 0.0, 0.0};
+      if (topo == TX_TOPO_TET) z[0] = z[1] = z[2] = 0.25;
+      for (int it = 0; it < 50; ++it) {
+        const RefTables G = tables_at(topo, TX_HGRAD_C1, z, 1);
+        double r[3] = {-p[0], -p[1], -p[2]}, J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int v = 0; v < nv; ++v)
+          for (int a = 0; a < 3; ++a) {
+            const double xa = m.coords[3 * vc[v] + a];
+            r[a] += G.geo_val[v] * xa;
+            for (int c = 0; c < 3; ++c) J[3 * a + c] += xa * G.geo_grad[3 * v + c];
+          }
+        const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[5] * J[6] - J[3] * J[8], c02 = J[3] * J[7] - J[4] * J[6];
+        const double det = J[0] * c00 + J[1] * c01 + J[2] * c02;
+        if (det == 0.0) break;
+        const double Ji[9] = {c00 / det, (J[2] * J[7] - J[1] * J[8]) / det, (J[1] * J[5] - J[2] * J[4]) / det,
+                              c01 / det, (J[0] * J[8] - J[2] * J[6]) / det, (J[2] * J[3] - J[0] * J[5]) / det,
+                              c02 / det, (J[1] * J[6] - J[0] * J[7]) / det, (J[0] * J[4] - J[1] * J[3]) / det};
+        double step = 0.0;
+        for (int a = 0; a < 3; ++a) {
+          const double d = Ji[3 * a] * r[0] + Ji[3 * a + 1] * r[1] + Ji[3 * a + 2] * r[2];
+          z[a] -= d;
+          step = std::max(step, std::fabs(d));
+        }
+        if (step < 1e-15) break;
+      }
+      const double tol = 1e-10;
+      const bool inside = topo == TX_TOPO_HEX
+                              ? std::fabs(z[0]) <= 1 + tol && std::fabs(z[1]) <= 1 + tol && std::fabs(z[2]) <= 1 + tol
+                              : z[0] >= -tol && z[1] >= -tol && z[2] >= -tol && z[0] + z[1] + z[2] <= 1 + tol;
+      if (!inside) continue;
+      block = b; elem = i;
+      xi[0] = z[0]; xi[1] = z[1]; xi[2] = z[2];
+      return true;
+    }
+  }
+  return false;
+}
+
 // shards Tetrahedron<4> side (face) node order
 static const int kTetSideVtx[4][3] = {{0, 1, 3}, {1, 2, 3}, {0, 3, 2}, {0, 2, 1}};
 

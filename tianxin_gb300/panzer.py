@@ -798,22 +798,32 @@ class BlockedModelEvaluator:
 
 
 _INTEGRANDS = {"Field": _abi.TX_INTEGRAND_FIELD, "L2 Error": _abi.TX_INTEGRAND_L2_ERROR,
-               "H1 Error": _abi.TX_INTEGRAND_H1_ERROR}
+               "H1 Error": _abi.TX_INTEGRAND_H1_ERROR, "Max": _abi.TX_INTEGRAND_MAX, "Min": _abi.TX_INTEGRAND_MIN,
+               "Probe": _abi.TX_INTEGRAND_PROBE}
 
 
 class Response:
-    """An integral response (TianXin Response_Integral / panzer Functional): "Field" integrates a DOF
-    field, "L2 Error" and "H1 Error" the Poisson example's error integrands against the manufactured
-    solution of TX_SOURCE_SINE.  evaluate() leaves the value in a device scalar and can add the
-    gradient (the Jacobian evaluation type); value() returns it on the host."""
+    """A response (TianXin Response_Integral / panzer Functional, ExtremeValue, Probe).
 
-    def __init__(self, dof, integrand="Field", dof_name=None, block=-1, cubature_degree=0):
+    "Field" integrates a DOF field over the cells, or over sides with side_mask (box sides) or side_set
+    (explicit meshes, name or index); "L2 Error" and "H1 Error" integrate the Poisson example's error
+    integrands against the manufactured solution of TX_SOURCE_SINE; "Max" / "Min" are the ExtremeValue
+    response of the field at the cubature points; "Probe" is the field's value at point.  evaluate()
+    leaves the value in a device scalar and can add the gradient (the Jacobian evaluation type);
+    value() returns it on the host."""
+
+    def __init__(self, dof, integrand="Field", dof_name=None, block=-1, cubature_degree=0, side_mask=0,
+                 side_set=None, point=None):
         self.dof = dof
         d = _abi.ResponseDesc()
         d.block = block
         d.field = dof.getFieldNum(dof_name) if dof_name is not None else 0
         d.integrand = _INTEGRANDS[integrand] if isinstance(integrand, str) else int(integrand)
         d.cubature_degree = cubature_degree
+        d.side_mask = side_mask
+        d.side_set = dof.conn.sideSetIndex(side_set) + 1 if side_set is not None else 0
+        if point is not None:
+            d.point[0], d.point[1], d.point[2] = (float(v) for v in point)
         rid = C.c_int32()
         check(dof.h, dof.lib.tx_response_create(dof.h, C.byref(d), C.byref(rid)), "tx_response_create")
         self.id = rid.value
@@ -828,6 +838,17 @@ class Response:
 
     def value(self, x):
         return float(self.evaluate(x).item())
+
+
+def ip_coordinates(dof, block, cubature_degree=0):
+    """IPCoordinates response: the physical cubature points [E][nq][3] of a block (device tensor)."""
+    nq = C.c_int32()
+    check(dof.h, dof.lib.tx_ip_coordinates(dof.h, block, cubature_degree, C.byref(nq), None), "tx_ip_coordinates")
+    ne = len(dof.conn.getElementBlock(block))
+    out = torch.empty((ne, nq.value, 3), dtype=torch.float64, device="cuda")
+    dof.lib.tx_set_stream(dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    check(dof.h, dof.lib.tx_ip_coordinates(dof.h, block, cubature_degree, C.byref(nq), _ptr(out)), "tx_ip_coordinates")
+    return out
 
 
 class HostEvaluator:
