@@ -134,6 +134,16 @@ enum tx_source {
  * dx/dp tangents; beta = 0, alpha = 1 those of x_dot.  FP64; f and crs_vals
  * are not touched (pass NULL); not with PERSISTENT or MIXED. */
 #define TX_EVAL_TANGENT 0x10u
+/* Two-phase evaluation: the element kernels write every element residual and
+ * Jacobian to scratch (held by the handle, about E * NE^2 values), then one
+ * warp per entity row sums its elements' rows in a fixed order and writes
+ * the row once.  f and crs_vals are OVERWRITTEN (no zeroing needed, no
+ * atomics, bitwise reproducible).  Needs crs_vals; whole-handle evaluations
+ * only (block = -1, all elements); not with TANGENT, PERSISTENT or
+ * DETERMINISTIC.  TX_EINVAL when an entity row is too long for the gather
+ * (nf^2 x row length > TX_GATHER_ROW_MAX). */
+#define TX_EVAL_GATHER 0x20u
+#define TX_GATHER_ROW_MAX 512
 #define TX_MAX_TANGENTS 4
 
 typedef struct tx_eval_args {

@@ -134,3 +134,54 @@ def test_warp_variant_falls_back_where_no_warp_kernel(cuda):
     assert rel(v2, v1) <= 1e-6 and rel(f2, f1) <= 1e-6
     with pytest.raises(tx.TxError):
         ae.setVariant(3)
+
+
+# ------------------------------------------------------------ two-phase (gather) evaluation
+@pytest.mark.parametrize("topo,phys,basis,blocks", [
+    (A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1, (1, 1, 1)),
+    (A.TX_TOPO_TET, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1, (1, 1, 1)),
+    ([A.TX_TOPO_HEX, A.TX_TOPO_TET], A.TX_PHYS_HEAT, A.TX_HGRAD_C2, (2, 1, 1)),
+    (A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_HGRAD_C1, (1, 1, 2)),
+    (A.TX_TOPO_HEX, A.TX_PHYS_MAXWELL, A.TX_HCURL_I1, (1, 1, 1)),
+])
+def test_gather_overwrites_and_matches_oracle(cuda, topo, phys, basis, blocks):
+    # f and W start as NaN: the two-phase form writes every entry; the sums have a fixed order, so
+    # two evaluations give the same bits
+    o, dof, lof = build((3, 3, 2), blocks, topo, phys, basis)
+    rng = np.random.default_rng(5)
+    x, xd, aux = rng.uniform(-1, 1, o.n_dofs), rng.uniform(-1, 1, o.n_dofs), rng.standard_normal(o.n_dofs)
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=0.5, beta=1.0)
+    dev = lambda a: torch.from_numpy(a).cuda()
+    for mixed, tol in ((False, FP64_TOL), (True, MIXED_TOL)):
+        outs = []
+        for _ in range(2):
+            f = torch.full((o.n_dofs,), float("nan"), dtype=torch.float64, device="cuda")
+            W = lof.getTpetraMatrix()
+            W.values.fill_(float("nan"))
+            tx.AssemblyEngine(lof).evaluate(dev(x), dev(xd), dev(aux), 0.5, 1.0, 0.0, f, W, mixed, gather=True)
+            outs.append((f.cpu().numpy(), W.values.cpu().numpy()))
+        (f1, v1), (f2, v2) = outs
+        assert np.array_equal(f1, f2) and np.array_equal(v1, v2)
+        assert rel(f1, f_ref) <= tol and rel(v1, v_ref) <= tol, (mixed, rel(f1, f_ref), rel(v1, v_ref))
+
+
+def test_gather_in_the_model_evaluator_and_its_limits(cuda):
+    o, dof, lof = build((4, 3, 3), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1)
+    me = tx.ModelEvaluator(lof, [tx.DirichletBC(dof, A.SIDE_ZMIN)])
+    x = torch.from_numpy(np.random.default_rng(2).uniform(-1, 1, o.n_dofs)).cuda()
+    res = []
+    for gather in (False, True):
+        me.ae.gather = gather
+        f, W = lof.getTpetraVector(), me.create_W_op()
+        f.fill_(7.0)
+        W.values.fill_(7.0)
+        me.evalModel(x, f=f, W=W)  # zeroes first only in the atomic form
+        res.append((f.cpu().numpy(), W.values.cpu().numpy()))
+    assert rel(res[1][0], res[0][0]) <= 1e-13 and rel(res[1][1], res[0][1]) <= 1e-13
+    ae = tx.AssemblyEngine(lof)
+    f, W = lof.getTpetraVector(), lof.getTpetraMatrix()
+    for kw in (dict(block=0), dict(deterministic=True)):
+        with pytest.raises(tx.TxError):
+            ae.evaluate(x, f=f, W=W, gather=True, **kw)
+    with pytest.raises(tx.TxError):
+        ae.evaluate(x, f=f, W=None, gather=True)

@@ -33,6 +33,7 @@ TX_EVAL_DETERMINISTIC = 0x2
 TX_EVAL_PERSISTENT = 0x4
 TX_EVAL_SCATTER_DIRECT = 0x8
 TX_EVAL_TANGENT = 0x10
+TX_EVAL_GATHER = 0x20
 TX_MAX_TANGENTS = 4
 
 TX_SPMV_F64 = 0

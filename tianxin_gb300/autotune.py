@@ -6,6 +6,10 @@ The knobs play the role of Panzer's HierarchicParallelism team/vector sizes
   * scatter   staged CTA-wide scatter vs per-thread row reductions
   * grid_cap  CTAs of the per-block launch (0 = occupancy x SMs x 4)
   * workset   elements per work item of the persistent / batched launch
+  * gather    two-phase evaluation (element rows to scratch, rows gathered and
+              written once) against the atomic scatter; atomic candidates are
+              timed with the zeroing of f and W they need, the two-phase form
+              overwrites them
 
 Each candidate is timed with CUDA events on the real evaluation (outputs in
 scratch vectors), the fastest is kept, and results are cached in
@@ -76,14 +80,29 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                                                   scatter_direct=direct), reps)
                     results.append(({"workset": ws, "grid_cap": 0, "scatter_direct": direct}, t))
         else:
-            # kernel variant (warp per element / CTA-staged / CTA direct scatter) x CTA cap
-            kernels = [(2, False), (1, False), (1, True)] if mixed else [(1, False), (1, True)]
-            for variant, direct in kernels:
+            # kernel variant (warp per element / CTA-staged / CTA direct scatter / two-phase) x CTA cap
+            kernels = [(2, False, False), (1, False, False), (1, True, False)] if mixed else \
+                [(1, False, False), (1, True, False)]
+            if W is not None:
+                kernels.append((1, False, True))
+
+            def step(direct, gather):
+                if not gather:  # the atomic forms sum into f and W, which a step zeroes first
+                    W.initializeMatrix(0.0)
+                    if f is not None:
+                        f.zero_()
+                ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, scatter_direct=direct, gather=gather)
+
+            for variant, direct, gather in kernels:
                 ae.setVariant(variant)
                 for cap in (0, sms * 2, sms * 4, sms * 8):
                     ae.setGridCap(cap)
-                    t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, scatter_direct=direct), reps)
-                    results.append(({"variant": variant, "scatter_direct": direct, "grid_cap": cap}, t))
+                    try:
+                        t = _time(lambda: step(direct, gather), reps)
+                    except Exception:  # the two-phase form refuses meshes with overlong rows
+                        continue
+                    results.append(({"variant": variant, "scatter_direct": direct, "gather": gather,
+                                     "grid_cap": cap}, t))
         best = min(results, key=lambda r: r[1])
         cfg = dict(best[0], ms=best[1], candidates=[dict(c, ms=t) for c, t in results])
         cache[key] = cfg
@@ -93,6 +112,7 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                 print(f"  {c}: {t:.3f} ms")
     ae.setGridCap(cfg.get("grid_cap", 0))
     ae.setVariant(cfg.get("variant", 0))
+    ae.gather = bool(cfg.get("gather", False))
     ae.scatter_direct = bool(cfg.get("scatter_direct", False))
     if "workset" in cfg:
         ae.setWorksetSize(cfg["workset"], cfg["workset"])

@@ -136,6 +136,13 @@ struct tx_handle_s {
   int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
+  // two-phase evaluation: entity -> (block, element, local basis) incidence
+  // (CSR, device) and the element scratch of the first phase
+  int64_t* d_inc_ptr = nullptr;
+  int64_t* d_inc = nullptr;
+  int gather_row_max = 0;             // nf^2 x longest entity row
+  unsigned char* gather_scratch = nullptr;
+  size_t gather_bytes = 0;
   // cubature tables of tx_ip_coordinates per (block, degree)
   struct IpTables { int block, degree, nq; double* tables; };
   std::vector<IpTables> ip_tables;
@@ -162,6 +169,8 @@ struct tx_handle_s {
     responses.clear();
     for (auto& t : ip_tables) cudaFree(t.tables);
     ip_tables.clear();
+    cudaFree(d_inc_ptr); cudaFree(d_inc); cudaFree(gather_scratch);
+    d_inc_ptr = nullptr; d_inc = nullptr; gather_scratch = nullptr; gather_bytes = 0; gather_row_max = 0;
     for (auto& b : blocks) {
       cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
       cudaFree(b.color_perm);
@@ -345,8 +354,83 @@ int eval_persistent(tx_handle h, const tx_eval_args& a) {
 }
 
 // Evaluate every requested block/range (volume fill).
+// Two-phase evaluation (TX_EVAL_GATHER): incidence lists built on first use,
+// element scratch grown to the precision's need, then per block the first
+// phase and one gather launch over every entity row.
+int eval_gather(tx_handle h, const tx_eval_args& a, const tx::EvalParams& P0) {
+  const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
+  if (!a.crs_vals) return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_GATHER needs crs_vals");
+  if (a.block >= 0) return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_GATHER evaluates every block (block = -1)");
+  if (a.flags & (TX_EVAL_TANGENT | TX_EVAL_PERSISTENT | TX_EVAL_DETERMINISTIC))
+    return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_GATHER is not combined with TANGENT, PERSISTENT or DETERMINISTIC");
+  const tx::Dofs& D = h->dofs;
+  const int nf = D.nf;
+  int rc = guarded(h, [&]() {
+    if (!h->d_inc_ptr) {
+      const int64_t ne = D.n_entities;
+      std::vector<int64_t> ptr(ne + 1, 0);
+      for (const tx::BlockDofs& B : D.blocks)
+        for (int32_t ent : B.dconn) ++ptr[ent + 1];
+      for (int64_t i = 0; i < ne; ++i) ptr[i + 1] += ptr[i];
+      std::vector<int64_t> inc(ptr[ne]), fill(ptr.begin(), ptr.end() - 1);
+      for (size_t b = 0; b < D.blocks.size(); ++b) {
+        const tx::BlockDofs& B = D.blocks[b];
+        const int64_t E = (int64_t)B.dconn.size() / B.nb;
+        for (int64_t e = 0; e < E; ++e)
+          for (int k = 0; k < B.nb; ++k)
+            inc[fill[B.dconn[e * B.nb + k]]++] = ((int64_t)b << 56) | (e << 8) | k;
+      }
+      int64_t maxdeg = 0;
+      for (int64_t r = 0; r < ne; ++r) maxdeg = std::max(maxdeg, D.erowptr[r + 1] - D.erowptr[r]);
+      h->gather_row_max = (int)(maxdeg * nf * nf);
+      ck(upload(h->d_inc_ptr, ptr), "upload incidence");
+      ck(upload(h->d_inc, inc), "upload incidence");
+    }
+    if (h->gather_row_max > tx::kGatherRowMax)
+      throw std::invalid_argument("tx_eval: an entity row is too long for TX_EVAL_GATHER");
+    for (const DevBlock& db : h->blocks)
+      if (nf * nf * db.nb > tx::kGatherElemRowMax)
+        throw std::invalid_argument("tx_eval: element rows too long for TX_EVAL_GATHER");
+    size_t need = 0;
+    for (const DevBlock& db : h->blocks) {
+      const size_t E = (size_t)db.n_elem, NE = (size_t)nf * db.nb, w = mixed ? 4 : 8;
+      need += ((E * NE * NE * w + 255) & ~size_t(255)) + ((E * NE * w + 255) & ~size_t(255));
+    }
+    if (need > h->gather_bytes) {
+      cudaFree(h->gather_scratch);
+      h->gather_scratch = nullptr;
+      h->gather_bytes = 0;
+      ck(cudaMalloc((void**)&h->gather_scratch, need), "alloc two-phase scratch");
+      h->gather_bytes = need;
+    }
+    return TX_OK;
+  });
+  if (rc) return rc;
+  tx::GatherBlocks G{};
+  size_t off = 0;
+  cudaError_t e = cudaSuccess;
+  for (size_t b = 0; b < h->blocks.size() && e == cudaSuccess; ++b) {
+    const DevBlock& db = h->blocks[b];
+    const size_t E = (size_t)db.n_elem, NE = (size_t)nf * db.nb, w = mixed ? 4 : 8;
+    tx::EvalParams P = P0;
+    P.kscr = h->gather_scratch + off;
+    off += (E * NE * NE * w + 255) & ~size_t(255);
+    P.rscr = h->gather_scratch + off;
+    off += (E * NE * w + 255) & ~size_t(255);
+    G.b[b] = tx::GatherBlock{P.kscr, P.rscr, db.epos, db.nb};
+    e = tx::launch_assemble(db.view(), P, mixed, nullptr, 0, db.n_elem, true, true, h->stream, h->grid_cap);
+  }
+  if (e == cudaSuccess)
+    e = tx::launch_gather_rows(D.n_entities, nf, h->d_inc_ptr, h->d_inc, G, mixed, h->d_erowptr, h->d_rowptr,
+                               a.crs_vals, a.f, h->stream);
+  if (e == cudaErrorInvalidValue) return fail(h, TX_EINVAL, "tx_eval: no kernel for this element family / cubature");
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: ") + cudaGetErrorString(e));
+  return TX_OK;
+}
+
 int eval_blocks(tx_handle h, const tx_eval_args& a, const CoefOverride* ov = nullptr) {
   tx::EvalParams P = make_params(h, a, ov);
+  if (a.flags & TX_EVAL_GATHER) return eval_gather(h, a, P);
   const bool mixed = (a.flags & TX_EVAL_MIXED) != 0;
   const bool det = (a.flags & TX_EVAL_DETERMINISTIC) != 0;
   const bool stage = (a.flags & TX_EVAL_SCATTER_DIRECT) == 0;
@@ -1564,6 +1648,7 @@ extern "C" int tx_eval_noalloc(tx_handle h, const tx_eval_args* a) {
   if (a->block != -1) return fail(h, TX_EINVAL, "tx_eval_noalloc evaluates every block (block = -1)");
   if (a->flags & TX_EVAL_DETERMINISTIC) return fail(h, TX_EINVAL, "tx_eval_noalloc: no deterministic form");
   if (a->flags & TX_EVAL_TANGENT) return fail(h, TX_EINVAL, "tx_eval_noalloc: no tangent form");
+  if (a->flags & TX_EVAL_GATHER) return fail(h, TX_EINVAL, "tx_eval_noalloc: the two-phase form allocates scratch");
   if (h->dofs.eq.physics == TX_PHYS_MAXWELL && !a->aux && a->f)
     return fail(h, TX_EINVAL, "tx_eval_noalloc: MAXWELL needs the current density J in aux");
   const int nb = (int)h->blocks.size();

@@ -9,21 +9,24 @@
 namespace tx {
 namespace {
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false>
+// SCR: the first phase of the two-phase evaluation (element rows to scratch).
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false,
+          bool SCR = false>
 __global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>(), min_blocks<Real, STAGE>())
 k_assemble(const BlockView B, const EvalParams P, const int32_t* perm, int64_t e_lo, int64_t e_hi) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
-  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, T, STAGE, TAN>(B, P, perm, e_lo, e_hi, blockIdx.x,
-                                                                         gridDim.x, smem);
+  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, T, STAGE, TAN, SCR>(B, P, perm, e_lo, e_hi, blockIdx.x,
+                                                                              gridDim.x, smem);
 }
 
-template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false>
+template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false,
+          bool SCR = false>
 cudaError_t launch_one(const BlockView& B, const EvalParams& P, const int32_t* perm, int64_t e_lo, int64_t e_hi,
                        cudaStream_t s, int grid_cap) {
   constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
   using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, T, STAGE>;
-  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, STAGE, TAN>;
+  auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, STAGE, TAN, SCR>;
   static int max_blocks_per_sm = -1;
   static int num_sms = 0;
   if (max_blocks_per_sm < 0) {
@@ -52,6 +55,12 @@ cudaError_t launch_prec(const BlockView& B, const EvalParams& P, bool mixed, con
   const bool jac = P.vals != nullptr;
   const bool st = stage && jac;
 #define TX_L(R, J, A, S) launch_one<TOPO, BASIS, NQ, PHYS, R, J, A, S>(B, P, perm, e_lo, e_hi, s, cap)
+  if (P.kscr) {  // two-phase, first phase: element rows to scratch (staged kernels' register rows)
+    if (!jac) return cudaErrorInvalidValue;
+    return mixed ? launch_one<TOPO, BASIS, NQ, PHYS, float, true, true, true, false, true>(B, P, perm, e_lo, e_hi, s, cap)
+                 : launch_one<TOPO, BASIS, NQ, PHYS, double, true, true, true, false, true>(B, P, perm, e_lo, e_hi, s,
+                                                                                           cap);
+  }
   if (P.tan) {  // Tangent: FP64 rows, atomic dfdp sums
     if (atomic) return launch_one<TOPO, BASIS, NQ, PHYS, double, true, true, false, true>(B, P, perm, e_lo, e_hi, s, cap);
     return launch_one<TOPO, BASIS, NQ, PHYS, double, true, false, false, true>(B, P, perm, e_lo, e_hi, s, cap);

@@ -127,7 +127,7 @@ __device__ __forceinline__ Real source_at(int kind, double c, double s0, const d
 // the coloured (deterministic) scatter: no two elements processed by one
 // launch share a row, so plain read-modify-write is race free.
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, int THREADS,
-          bool STAGE = false, bool TAN = false>
+          bool STAGE = false, bool TAN = false, bool SCR = false>
 __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalParams& P, const int32_t* perm,
                                               int64_t e_lo, int64_t e_hi, int64_t grp0, int64_t grp_stride,
                                               unsigned char* smem) {
@@ -412,8 +412,13 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           }
         }
         if constexpr (STAGE) {
+          if constexpr (SCR) {  // two-phase: the element residual to scratch
 #pragma unroll
-          for (int c = 0; c < NF; ++c) sR[a * NF + c] = r[c];
+            for (int c = 0; c < NF; ++c) reinterpret_cast<Real*>(P.rscr)[e * NE + a * NF + c] = r[c];
+          } else {
+#pragma unroll
+            for (int c = 0; c < NF; ++c) sR[a * NF + c] = r[c];
+          }
         } else if (P.f) {
 #pragma unroll
           for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.f + NF * la + c, widen(r[c]));
@@ -515,6 +520,30 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               for (int c = 0; c < NF; ++c) accumulate<ATOMIC>(P.dfdp + (int64_t)i * P.n + NF * la + c, rt[i][c]);
           }
         }
+      }
+    }
+    if constexpr (SCR && STAGE && JAC) {
+      {
+        // ---------------------------------------------------- 5 two-phase: rows to scratch
+        // the thread's NF consecutive element rows (a * NF .. a * NF + NF - 1), NF * NE values
+        if (my_a >= 0) {
+          Real* dst = reinterpret_cast<Real*>(P.kscr) + (e * NE + my_a * NF) * NE;
+          if constexpr (sizeof(Real) == 4 && (NE * NE) % 4 == 0 && (NF * NE) % 4 == 0) {
+            float4* d4 = reinterpret_cast<float4*>(dst);  // 16-byte aligned: rows start at multiples of 4 values
+#pragma unroll
+            for (int k = 0; k < NF * NE / 4; ++k)
+              d4[k] = make_float4(kreg[4 * k], kreg[4 * k + 1], kreg[4 * k + 2], kreg[4 * k + 3]);
+          } else if constexpr (sizeof(Real) == 8 && (NE * NE) % 2 == 0 && (NF * NE) % 2 == 0) {
+            double2* d2 = reinterpret_cast<double2*>(dst);
+#pragma unroll
+            for (int k = 0; k < NF * NE / 2; ++k) d2[k] = make_double2(kreg[2 * k], kreg[2 * k + 1]);
+          } else {
+#pragma unroll
+            for (int k = 0; k < NF * NE; ++k) dst[k] = kreg[k];
+          }
+        }
+        __syncthreads();
+        continue;
       }
     }
     if constexpr (STAGE) {

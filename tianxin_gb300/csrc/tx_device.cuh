@@ -27,6 +27,12 @@ struct EvalParams {
   double* dfdp;              // [ntan][n]
   int ntan;
   int64_t n;                 // DOF count (the stride of tan and dfdp)
+  // Two-phase (gather) evaluation, staged Jacobian kernels only: the element
+  // residual and matrix go to scratch (element arithmetic's type) instead of
+  // the scatter: kscr[(e * NE + row) * NE + col], rscr[e * NE + row], e the
+  // block-local element; launch_gather_rows then writes every row once.
+  void* kscr;
+  void* rscr;
 };
 constexpr int kMaxTangents = 4;
 
@@ -36,6 +42,26 @@ constexpr int kMaxTangents = 4;
 // cudaErrorInvalidValue for element families without a kernel.
 cudaError_t launch_assemble(const BlockView& B, const EvalParams& P, bool mixed, const int32_t* perm, int64_t e_lo,
                             int64_t e_hi, bool atomic, bool stage, cudaStream_t s, int grid_cap);
+
+// Two-phase (gather) evaluation: the scratch of each mesh block (element
+// matrices and residuals of the first phase) and its element-to-row map.
+constexpr int kGatherRowMax = TX_GATHER_ROW_MAX;  // nf * nf * (entity row length) the gather kernel holds
+constexpr int kGatherElemRowMax = 128;  // nf * (element DOFs): the values of one entity's element rows
+struct GatherBlock {
+  const void* k;        // [E][NE][NE] element Jacobians (Real)
+  const void* r;        // [E][NE] element residuals (Real)
+  const uint8_t* epos;  // [E][nb][nb]
+  int nb;
+};
+struct GatherBlocks {
+  GatherBlock b[TX_MAX_BLOCKS];
+};
+// One warp per entity: f[nf*a + c] and the CRS rows of entity a written
+// once from the element rows listed in inc (block << 56 | element << 8 |
+// local basis, entity-major, CSR by inc_ptr).
+cudaError_t launch_gather_rows(int64_t n_ent, int nf, const int64_t* inc_ptr, const int64_t* inc,
+                               const GatherBlocks& G, bool mixed, const int64_t* erp, const int64_t* rowptr,
+                               double* vals, double* f, cudaStream_t s);
 
 // One chunk of elements of one block view (views[view], params[view]).
 struct WorkItem {

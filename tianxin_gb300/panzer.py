@@ -644,6 +644,7 @@ class AssemblyEngine:
     def __init__(self, lof):
         self.lof, self.dof = lof, lof.dof
         self.scatter_direct = False  # set by the autotuner
+        self.gather = False          # two-phase evaluation (TX_EVAL_GATHER), set by the autotuner
 
     def setWorksetSize(self, min_size, max_size=None, seed=0):
         """Worksets of the persistent evaluation: sizes uniform in [min_size, max_size]."""
@@ -657,12 +658,23 @@ class AssemblyEngine:
         """Assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element (hex8 elasticity, mixed)."""
         check(self.dof.h, self.dof.lib.tx_set_assembly_variant(self.dof.h, variant), "tx_set_assembly_variant")
 
+    def gather_applies(self, W, block=-1, workset=(0, -1), deterministic=False, persistent=False):
+        """Whether evaluate() with these arguments takes the two-phase form (f and W overwritten)."""
+        return (self.gather and W is not None and block < 0 and tuple(workset) == (0, -1) and not deterministic
+                and not persistent)
+
     def evaluate(self, x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False,
-                 block=-1, workset=(0, -1), deterministic=False, persistent=False, scatter_direct=None):
+                 block=-1, workset=(0, -1), deterministic=False, persistent=False, scatter_direct=None, gather=None):
+        """Volume fill.  Summed into f and W, except in the two-phase form (gather=True, or the tuned
+        default for whole-handle Jacobian evaluations), which overwrites them."""
         if scatter_direct is None:
             scatter_direct = self.scatter_direct
+        if gather is None:
+            gather = self.gather_applies(W, block, workset, deterministic, persistent)
         a = eval_args(x, x_dot, aux, alpha, beta, t, f, W, mixed, block, workset, deterministic, persistent,
                       scatter_direct)
+        if gather:
+            a.flags |= _abi.TX_EVAL_GATHER
         lib = self.dof.lib
         lib.tx_set_stream(self.dof.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
         check(self.dof.h, lib.tx_eval(self.dof.h, C.byref(a)), "tx_eval")
@@ -702,13 +714,17 @@ class ModelEvaluator:
 
     def evalModel(self, x, x_dot=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, aux=None, mixed=False,
                   zero=True, deterministic=False, persistent=False):
-        if zero:
+        # A Jacobian evaluation from zero may take the two-phase form, which overwrites f and W (no zeroing):
+        # when the autotuner chose it, and for deterministic evaluations, where its fixed-order row sums
+        # are faster than the coloured launches.  zero=False sums into f and W: the atomic forms.
+        gather = zero and W is not None and not persistent and (self.ae.gather or deterministic)
+        if zero and not gather:
             if f is not None:
                 f.zero_()
             if W is not None:
                 W.initializeMatrix(0.0)
-        self.ae.evaluate(x, x_dot, aux, alpha, beta, t, f, W, mixed, deterministic=deterministic,
-                         persistent=persistent)
+        self.ae.evaluate(x, x_dot, aux, alpha, beta, t, f, W, mixed, deterministic=deterministic and not gather,
+                         persistent=persistent, gather=gather)
         if f is not None:  # Neumann sums into equations before Dirichlet overwrites rows
             for bc in self.neumann:
                 bc.evaluate(f, t)
