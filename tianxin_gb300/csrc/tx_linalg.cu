@@ -206,14 +206,13 @@ __device__ __forceinline__ void entity_dot(int64_t b, int64_t deg, int sub, cons
     for (int u = 0; u < U; ++u) {
       T xm[NF];
 #pragma unroll
-      for (int d = 0; d < NF; ++d) {
-        const T xv = __ldg(x + NF * m[u] + d);
-        xm[d] = in[u] ? xv : T(0);
+      for (int d = 0; d < NF; ++d) xm[d] = __ldg(x + NF * m[u] + d);
+      if (in[u]) {  // a pass slot past the row end issues no FMAs
+#pragma unroll
+        for (int c = 0; c < NF; ++c)
+#pragma unroll
+          for (int d = 0; d < NF; ++d) s[c] += v[u][c][d] * xm[d];
       }
-#pragma unroll
-      for (int c = 0; c < NF; ++c)
-#pragma unroll
-        for (int d = 0; d < NF; ++d) s[c] += v[u][c][d] * xm[d];
     }
   }
 }
@@ -226,7 +225,20 @@ __device__ __forceinline__ void entity_dot(int64_t b, int64_t deg, int sub, cons
 // returns row sub.  G >= 4.
 template <typename T, int NF, int G>
 __device__ __forceinline__ T entity_reduce(const T (&s)[NF], int sub) {
-  static_assert(NF == 3 && G >= 4, "reduce-scatter of three rows over at least four lanes");
+  static_assert(NF == 3 && (G == 3 || G >= 4), "reduce-scatter of three rows over three or at least four lanes");
+  if constexpr (G == 3) {
+    // three lanes, three rows: lane sub keeps row sub and takes it from the two
+    // other lanes of its group, each of which sends the row its receiver keeps
+    const int base = (threadIdx.x & 31) - sub;
+    T k = sub == 0 ? s[0] : sub == 1 ? s[1] : s[2];
+#pragma unroll
+    for (int o = 1; o < 3; ++o) {
+      const int want = sub >= o ? sub - o : sub + 3 - o;  // the row of the lane this one sends to
+      const T send = want == 0 ? s[0] : want == 1 ? s[1] : s[2];
+      k += __shfl_sync(0xffffffffu, send, base + (sub + o < 3 ? sub + o : sub + o - 3));
+    }
+    return k;
+  }
   const bool hi = (sub & 2) != 0, lo = (sub & 1) != 0;
   T a0 = hi ? s[2] : s[0];
   T a1 = hi ? T(0) : s[1];
@@ -241,23 +253,25 @@ __device__ __forceinline__ T entity_reduce(const T (&s)[NF], int sub) {
   return k;
 }
 
-// Six resident CTAs an SM (40 registers) for up to 16 lanes an entity, four
-// (64 registers) for 32 lanes, whose FP64 form would spill at 40.
-constexpr int entity_min_blocks(int G) { return G >= 32 ? 4 : 6; }
+// Six resident CTAs an SM (40 registers) for up to 16 lanes an entity; four
+// (64 registers) for 32 lanes and for three lanes with three blocks a pass,
+// whose FP64 forms would spill at 40.
+constexpr int entity_min_blocks(int G, int U) { return G >= 32 || (G < 4 && U >= 3) ? 4 : 6; }
 
 // y = alpha A x + beta y in the entity-block form; entity loop per warp as in
 // k_spmv (warp-uniform trip count for the full-mask shuffles).
 template <typename T, int NF, int G, int U>
-__global__ void __launch_bounds__(kThreads, entity_min_blocks(G)) k_spmv_eb(int64_t n_ent, const int64_t* __restrict__ erp,
+__global__ void __launch_bounds__(kThreads, entity_min_blocks(G, U)) k_spmv_eb(int64_t n_ent, const int64_t* __restrict__ erp,
                                                       const int32_t* __restrict__ ecol, const T* __restrict__ vals,
                                                       const T* __restrict__ x, T* __restrict__ y, T alpha, T beta) {
-  constexpr int GPW = 32 / G;  // entities per warp
-  const int sub = threadIdx.x % G;
-  const int g = (threadIdx.x & 31) / G;
+  constexpr int GPW = 32 / G;  // entities per warp (G = 3: ten, lanes 30 and 31 idle)
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G < GPW ? lane / G : GPW;  // GPW: an idle lane
+  const int sub = lane - (lane / G) * G;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t base = warp * GPW; base < n_ent; base += nwarps * GPW) {
-    const int64_t r = base + g;
+    const int64_t r = g < GPW ? base + g : n_ent;  // idle lanes take no entity
     T s[NF];
 #pragma unroll
     for (int c = 0; c < NF; ++c) s[c] = T(0);
@@ -336,6 +350,7 @@ template <typename F>
 cudaError_t with_entity_shape(SpmvShape sh, F&& f) {
 #define TX_ESHAPE(L, U) \
   if (sh.lanes == L && sh.unroll == U) return f.template run<L, U>();
+  TX_ESHAPE(3, 1) TX_ESHAPE(3, 2) TX_ESHAPE(3, 3)
   TX_ESHAPE(4, 1) TX_ESHAPE(4, 2) TX_ESHAPE(8, 1) TX_ESHAPE(8, 2)
   TX_ESHAPE(16, 1) TX_ESHAPE(16, 2) TX_ESHAPE(32, 1) TX_ESHAPE(32, 2)
 #undef TX_ESHAPE
@@ -347,7 +362,7 @@ struct EntitySpmvLaunch {
   EntityGraph eg; const T* vals; const T* x; T* y; T a, b; cudaStream_t s;
   template <int L, int U>
   cudaError_t run() const {
-    k_spmv_eb<T, kEntityNf, L, U><<<grid_for(eg.n_ent, kThreads / L, 152 * 64), kThreads, 0, s>>>(
+    k_spmv_eb<T, kEntityNf, L, U><<<grid_for(eg.n_ent, (kThreads / 32) * (32 / L), 152 * 64), kThreads, 0, s>>>(
         eg.n_ent, eg.erp, eg.ecol, vals, x, y, a, b);
     return cudaGetLastError();
   }
@@ -482,19 +497,20 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(int64_t n, const int64_t*
 
 // q = A p and partial dot(p, q) in the entity-block form
 template <int NF, int G, int U>
-__global__ void __launch_bounds__(kThreads, entity_min_blocks(G)) k_spmv_dot_eb(int64_t n_ent, const int64_t* __restrict__ erp,
+__global__ void __launch_bounds__(kThreads, entity_min_blocks(G, U)) k_spmv_dot_eb(int64_t n_ent, const int64_t* __restrict__ erp,
                                                           const int32_t* __restrict__ ecol,
                                                           const float* __restrict__ vals, const float* __restrict__ p,
                                                           float* __restrict__ q, double* __restrict__ red) {
   __shared__ double sh[32];
   constexpr int GPW = 32 / G;
-  const int sub = threadIdx.x % G;
-  const int g = (threadIdx.x & 31) / G;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G < GPW ? lane / G : GPW;  // GPW: an idle lane
+  const int sub = lane - (lane / G) * G;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   double pq = 0.0;
   for (int64_t base = warp * GPW; base < n_ent; base += nwarps * GPW) {  // warp-uniform trip count
-    const int64_t r = base + g;
+    const int64_t r = g < GPW ? base + g : n_ent;  // idle lanes take no entity
     float s[NF];
 #pragma unroll
     for (int c = 0; c < NF; ++c) s[c] = 0.0f;
@@ -596,6 +612,7 @@ bool spmv_shape_valid(SpmvShape sh) {
 }
 bool entity_shape_valid(SpmvShape sh) {
   if (sh.lanes == 0 && sh.unroll == 0) return true;
+  if (sh.lanes == 3) return sh.unroll >= 1 && sh.unroll <= 3;
   const bool l = sh.lanes == 4 || sh.lanes == 8 || sh.lanes == 16 || sh.lanes == 32;
   return l && (sh.unroll == 1 || sh.unroll == 2);
 }
