@@ -108,18 +108,6 @@ static void brick_entity_offset(int dim, int id, int o[3]) {
   }
 }
 
-// Geometric vertices of sub-cell c (dim) of an element, as brick vertices.
-static int subcell_vertices(int topo, int sub, int dim, int c, int v[4]) {
-  if (dim == 0) { v[0] = topo == TX_TOPO_HEX ? c : kTets[sub][c]; return 1; }
-  if (dim == 1) {
-    if (topo == TX_TOPO_HEX) { v[0] = kEdgeVtx[c][0]; v[1] = kEdgeVtx[c][1]; return 2; }
-    v[0] = kTets[sub][kTetEdgeVtx[c][0]]; v[1] = kTets[sub][kTetEdgeVtx[c][1]];
-    return 2;
-  }
-  if (dim == 2 && topo == TX_TOPO_HEX) { for (int k = 0; k < 4; ++k) v[k] = kFaceVtx[c][k]; return 4; }
-  return 0;
-}
-
 // ------------------------------------------------------------ reference
 int default_degree(int topo, int basis) { return (topo == TX_TOPO_HEX && basis == TX_HGRAD_C2) ? 4 : 2; }
 
