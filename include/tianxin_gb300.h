@@ -213,11 +213,14 @@ int tx_graph_build(tx_handle h, int64_t* rowptr, int32_t* colind);
  * graph (rowptr/colind of tx_graph_build). */
 int tx_eval(tx_handle h, const tx_eval_args* args);
 
-/* DirichletEvalautor<Jacobian>/<Residual>: f[d] = x[d] - g[i];
- * Jacobian rows d -> unit rows (columns untouched, pivot 1.0;
- * TianXin_Dirichlet_impl.hpp:75-81, Tpetra
- * applyDirichletBoundaryConditionToLocalMatrixRows).  lids/g are DEVICE
- * arrays of n entries; g may be NULL (g = 0).  f or crs_vals may be NULL. */
+/* DirichletEvalautor<Jacobian>/<Residual> through the container's
+ * applyDirichletBoundaryCondition (TianXin_Dirichlet_impl.hpp:75-81,
+ * lof/Panzer_TpetraLinearObjContainer.hpp:228-238): with a residual f,
+ * f[d] = x[d] - g[i] and the Jacobian rows d become unit rows (columns
+ * untouched, pivot 1.0: applyDirichletBoundaryConditionToLocalMatrixRows);
+ * with f == NULL the columns d are cleared as well, the diagonal kept at 1
+ * (applyDirichletBoundaryConditionToLocalMatrixRowsAndColumns).  lids/g are
+ * DEVICE arrays of n entries; g may be NULL (g = 0); crs_vals may be NULL. */
 int tx_dirichlet_apply(tx_handle h, int64_t n, const int32_t* lids, const double* g,
                        const double* x, double* f, double* crs_vals);
 

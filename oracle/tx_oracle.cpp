@@ -1483,7 +1483,10 @@ int64_t orc_dirichlet_dofs(void* h, uint32_t side_mask, uint32_t field_mask, int
   return (int64_t)v.size();
 }
 
-// f[d] = x[d] - g; Jacobian rows -> unit rows (applyDirichletBoundaryConditionToLocalMatrixRows)
+// TpetraLinearObjContainer::applyDirichletBoundaryCondition (disc-fe/src/lof/Panzer_TpetraLinearObjContainer.hpp:
+// 228-238): with a residual, f[d] = x[d] - g and the Jacobian rows become unit rows
+// (applyDirichletBoundaryConditionToLocalMatrixRows); without one (f == NULL), rows and columns are cleared with
+// 1 on the diagonal (applyDirichletBoundaryConditionToLocalMatrixRowsAndColumns).
 void orc_dirichlet_apply(void* h, int64_t n, const int32_t* lids, const double* g, const double* x, double* f,
                          double* vals) {
   Problem* P = (Problem*)h;
@@ -1492,6 +1495,14 @@ void orc_dirichlet_apply(void* h, int64_t n, const int32_t* lids, const double* 
     if (f) f[d] = x[d] - (g ? g[i] : 0.0);
     if (vals)
       for (int64_t k = P->D.rowptr[d]; k < P->D.rowptr[d + 1]; ++k) vals[k] = P->D.colind[k] == d ? 1.0 : 0.0;
+  }
+  if (vals && !f) {
+    const int64_t N = (int64_t)P->D.rowptr.size() - 1;
+    std::vector<char> on(N, 0);
+    for (int64_t i = 0; i < n; ++i) on[lids[i]] = 1;
+    for (int64_t r = 0; r < N; ++r)
+      for (int64_t k = P->D.rowptr[r]; k < P->D.rowptr[r + 1]; ++k)
+        if (on[P->D.colind[k]] && P->D.colind[k] != r) vals[k] = 0.0;
   }
 }
 

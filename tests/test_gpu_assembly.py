@@ -170,3 +170,30 @@ def test_direct_scatter_matches(cuda, name, n, blocks, topo, phys, basis, source
     tx.AssemblyEngine(lof).evaluate(dev(x), dev(xd), dev(aux), 0.5, 1.0, 0.0, f, W, mixed, scatter_direct=True)
     tol = MIXED_TOL if mixed else FP64_TOL
     assert rel(f.cpu().numpy(), f_ref) <= tol and rel(W.values.cpu().numpy(), v_ref) <= tol
+
+
+def test_dirichlet_rows_and_columns_without_a_residual(cuda):
+    # the reference container clears rows and columns when the evaluation has no residual
+    # (applyDirichletBoundaryConditionToLocalMatrixRowsAndColumns), rows only otherwise
+    m = A.mesh_desc((3, 2, 2), jitter=0.1, seed=3)
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.5))
+    o = O.Oracle(m, q)
+    conn = tx.CartesianConnManager(3, 2, 2, jitter=0.1, seed=3)
+    dof = tx.DOFManager(conn, q)
+    lof = tx.TpetraLinearObjFactory(dof)
+    bc = tx.DirichletBC(dof, A.SIDE_XMIN | A.SIDE_ZMAX)
+    x = np.random.default_rng(4).uniform(-1, 1, o.n_dofs)
+    _, v_ref = o.evaluate(x, None, None, alpha=0.0, beta=1.0)
+    o.dirichlet_apply(bc.lids_host, None, x, None, v_ref)
+    me = tx.ModelEvaluator(lof, [bc])
+    W = me.create_W_op()
+    me.evalModel(torch.from_numpy(x).cuda(), W=W)
+    v = W.values.cpu().numpy()
+    assert np.abs(v - v_ref).max() <= 1e-12 * np.abs(v_ref).max()
+    rp, ci = W.rowptr.cpu().numpy(), W.colind.cpu().numpy()
+    on = np.zeros(o.n_dofs, bool)
+    on[bc.lids_host] = True
+    rows = np.repeat(np.arange(o.n_dofs), np.diff(rp))
+    cleared = on[ci] & (rows != ci)
+    assert cleared.any() and np.all(v[cleared] == 0.0)           # the columns
+    assert np.all(v[on[rows] & (rows == ci)] == 1.0)               # unit diagonal

@@ -271,3 +271,20 @@ def test_extreme_side_and_probe_closed_forms(topo, basis):
         val, e, gp = oj.probe(p, x=uj, gradient=True)
         assert e >= 0 and abs(val - (p[0] + 2 * p[1] + 3 * p[2])) <= 1e-12 and abs(gp.sum() - 1.0) <= 1e-12
     assert oj.probe((1.5, 0.5, 0.5), x=uj)[1] == -1
+
+
+def test_dirichlet_rows_and_columns_keep_symmetry():
+    # RowsAndColumns (no residual) keeps a symmetric Jacobian symmetric; rows only does not
+    import scipy.sparse as sp
+    o = O.Oracle(A.mesh_desc(3, jitter=0.1, seed=2), A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0)))
+    x = np.random.default_rng(1).uniform(-1, 1, o.n_dofs)
+    _, v = o.evaluate(x, None, None)
+    rp, ci = o.graph()
+    lids = np.flatnonzero(o.dof_coordinates()[:, 2] == 0.0).astype(np.int32)
+    for with_f, symmetric in ((False, True), (True, False)):
+        vv = v.copy()
+        f = np.zeros(o.n_dofs) if with_f else None
+        o.dirichlet_apply(lids, None, x, f, vv)
+        K = sp.csr_matrix((vv, ci, rp), shape=(o.n_dofs, o.n_dofs))
+        assert (abs(K - K.T).max() <= 1e-14 * abs(K).max()) == symmetric
+        assert np.all(K.diagonal()[lids] == 1.0)

@@ -57,9 +57,25 @@ __global__ void k_expand_colind(const int64_t* __restrict__ erp, const int32_t* 
   }
 }
 
+// position of entity r in the sorted entity row of m (the pattern is
+// symmetric: r is in m's row when m is in r's)
+__device__ __forceinline__ int64_t entity_pos(const int64_t* __restrict__ erp, const int32_t* __restrict__ ecol,
+                                              int64_t m, int32_t r) {
+  int64_t lo = erp[m], hi = erp[m + 1];
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (ecol[mid] < r) lo = mid + 1; else hi = mid;
+  }
+  return lo - erp[m];
+}
+
 // one warp per Dirichlet DOF d = nf*r + c: zero row d, put 1 on the
 // diagonal, whose block position is that of entity r in its own sorted
-// entity row
+// entity row.  Without a residual (f == NULL) the columns go too, as the
+// reference container's applyDirichletBoundaryConditionToLocalMatrixRowsAndColumns
+// does: entry (j, d) of every row j = nf*m + c' of a neighbour entity m,
+// j != d, is set to zero.  Two Dirichlet DOFs may both write an entry (j, d)
+// with j and d Dirichlet: both write zero; diagonals only their own row writes.
 __global__ void k_dirichlet(int64_t n, const int32_t* __restrict__ lids, const double* __restrict__ g,
                             const double* __restrict__ x, double* __restrict__ f, const int64_t* __restrict__ rp,
                             const int64_t* __restrict__ erp, const int32_t* __restrict__ ecol, int nf,
@@ -79,6 +95,15 @@ __global__ void k_dirichlet(int64_t n, const int32_t* __restrict__ lids, const d
       }
       const int64_t diag = rp[d] + (int64_t)nf * (lo - erp[r]) + c;
       for (int64_t k = rp[d] + lane; k < rp[d + 1]; k += 32) vals[k] = k == diag ? 1.0 : 0.0;
+      if (!f) {  // rows and columns
+        const int64_t b0 = erp[r], deg = erp[r + 1] - b0;
+        for (int64_t t = lane; t < deg * nf; t += 32) {
+          const int64_t m = ecol[b0 + t / nf];
+          const int cc = (int)(t - (t / nf) * nf);
+          const int64_t j = (int64_t)nf * m + cc;
+          if (j != d) vals[rp[j] + (int64_t)nf * entity_pos(erp, ecol, m, r) + c] = 0.0;
+        }
+      }
     }
   }
 }
