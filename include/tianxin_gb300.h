@@ -295,8 +295,11 @@ enum tx_integrand {
    * winning cell's DOFs. */
   TX_INTEGRAND_MAX = 4,
   TX_INTEGRAND_MIN = 5,
-  /* Probe (Panzer_ResponseScatterEvaluator_Probe): u at point, in the first
-   * cell (blocks in order, cells in order) holding it; d/dx = N_b(xi). */
+  /* Probe (disc-fe/src/responses/Panzer_ResponseScatterEvaluator_Probe_impl.hpp:
+   * the containing cell by checkPointwiseInclusion :144 and the reference
+   * point by mapToReferenceFrame :187, evaluateFields :262): u at point, in
+   * the first cell (blocks in order, cells in order) holding it;
+   * d/dx = N_b(xi). */
   TX_INTEGRAND_PROBE = 6
 };
 typedef struct tx_response_desc {
@@ -319,7 +322,8 @@ int tx_response_create(tx_handle h, const tx_response_desc* d, int32_t* id);
  * same bits on every call); dvalue_dx (DEVICE [N], may be NULL) += its
  * gradient.  Launch only. */
 int tx_response_eval(tx_handle h, int32_t id, const double* x, double* value, double* dvalue_dx);
-/* IPCoordinates (Panzer_ResponseEvaluatorFactory_IPCoordinates): the physical
+/* IPCoordinates (disc-fe/src/responses/Panzer_ResponseEvaluatorFactory_IPCoordinates_impl.hpp:79,
+ * Panzer_ResponseScatterEvaluator_IPCoordinates_impl.hpp:105): the physical
  * cubature points of a block at cubature_degree (<= 0: its integration
  * order), [n_elem][*nq][3] into xyz (DEVICE; NULL: sizes only).  The tables
  * are cached on the handle, so later calls are launch-only. */
@@ -402,8 +406,9 @@ int tx_graph_destroy(tx_handle h, int32_t graph_id);
 
 /* ------------------------------------------------------------ explicit meshes
  * Unstructured meshes for nodal (TX_HGRAD_C1) fields on hex8 and tet4 blocks,
- * from arrays or from an Exodus II file (STK_ExodusReaderFactory,
- * adapters-stk/src/Panzer_STK_ExodusReaderFactory.cpp).  Node numbers are
+ * from arrays or from an Exodus II file (STK_ExodusReaderFactory::buildMesh,
+ * adapters-stk/src/stk_interface/Panzer_STK_ExodusReaderFactory.cpp:111-197,
+ * with its element block, side set and node set registration at :178-180).  Node numbers are
  * 0-based and are the vertex GIDs of the numbering: DOF GIDs ascend in node
  * number, fields interleaved, LIDs by first touch as on lattice meshes.
  * Element vertices follow the Exodus/shards order.  Elements are numbered
@@ -466,7 +471,10 @@ int tx_dirichlet_dofs_node_set(tx_handle h, int32_t node_set, uint32_t field_mas
 
 /* ------------------------------------------------------------ blocked layout
  * BlockedDOFManager + BlockedTpetraLinearObjFactory
- * (disc-fe/src/lof/Panzer_BlockedTpetraLinearObjFactory_impl.hpp): the
+ * (dof-mgr/src/Panzer_BlockedDOFManager.hpp:68; disc-fe/src/lof/
+ * Panzer_BlockedTpetraLinearObjFactory_impl.hpp: getGraph :709,
+ * buildTpetraGraph :799, getTpetraMatrix :903, getTpetraDomainVector :933,
+ * getBlockRowCount :969, addExcludedPair :295): the
  * equation set's fields are grouped into n_blocks field blocks
  * (field_block[f] = block of field f, fields in field order, every block
  * non-empty).  Block i with b_i fields numbers its DOFs b_i * entity + k (k =
