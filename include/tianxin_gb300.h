@@ -140,8 +140,10 @@ enum tx_source {
  * the row once.  f and crs_vals are OVERWRITTEN (no zeroing needed, no
  * atomics, bitwise reproducible).  Needs crs_vals; whole-handle evaluations
  * only (block = -1, all elements); not with TANGENT, PERSISTENT or
- * DETERMINISTIC.  TX_EINVAL when an entity row is too long for the gather
- * (nf^2 x row length > TX_GATHER_ROW_MAX). */
+ * DETERMINISTIC.  TX_EINVAL when the rows do not fit the gather: an entity
+ * row (nf^2 x row length > TX_GATHER_ROW_MAX) or an element's rows
+ * (nf^2 x basis count > 128), e.g. quadratic elasticity; see
+ * tx_eval_gather_supported. */
 #define TX_EVAL_GATHER 0x20u
 #define TX_GATHER_ROW_MAX 512
 #define TX_MAX_TANGENTS 4
@@ -212,6 +214,10 @@ int tx_graph_build(tx_handle h, int64_t* rowptr, int32_t* colind);
  * crs_vals == NULL gives the Residual evaluation type.  Uses the handle's
  * graph (rowptr/colind of tx_graph_build). */
 int tx_eval(tx_handle h, const tx_eval_args* args);
+
+/* *supported = 1 when TX_EVAL_GATHER holds this handle's rows (after
+ * tx_dof_build), else 0; a host query, no device work. */
+int tx_eval_gather_supported(tx_handle h, int32_t* supported);
 
 /* DirichletEvalautor<Jacobian>/<Residual> through the container's
  * applyDirichletBoundaryCondition (TianXin_Dirichlet_impl.hpp:75-81,
@@ -405,7 +411,9 @@ int tx_graph_launch(tx_handle h, int32_t graph_id);
 int tx_graph_destroy(tx_handle h, int32_t graph_id);
 
 /* ------------------------------------------------------------ explicit meshes
- * Unstructured meshes for nodal (TX_HGRAD_C1) fields on hex8 and tet4 blocks,
+ * Unstructured meshes for nodal fields: TX_HGRAD_C1 on hex8 / tet4 blocks, and
+ * TX_HGRAD_C2 on hex27 / tet10 blocks (the quadratic nodes carry the DOFs; the
+ * geometry is the vertices' trilinear / linear map),
  * from arrays or from an Exodus II file (STK_ExodusReaderFactory::buildMesh,
  * adapters-stk/src/stk_interface/Panzer_STK_ExodusReaderFactory.cpp:111-197,
  * with its element block, side set and node set registration at :178-180).  Node numbers are
@@ -421,9 +429,12 @@ int tx_graph_destroy(tx_handle h, int32_t graph_id);
 typedef struct tx_explicit_block {
   int32_t topology;        /* TX_TOPO_HEX (8 vertices) or TX_TOPO_TET (4)          */
   int64_t n_elem;
-  const int64_t* conn;     /* [n_elem][8 or 4] node numbers (HOST)                 */
+  const int64_t* conn;     /* [n_elem][nodes_per_elem] node numbers (HOST)         */
   int64_t id;              /* element block id                                     */
   const char* name;        /* block name or NULL                                   */
+  int32_t nodes_per_elem;  /* 0 or 8 / 4: the vertices; 27 (HEX27) / 10 (TETRA10):  */
+                           /* quadratic nodes in shards order, which carry the      */
+                           /* TX_HGRAD_C2 DOFs (basis b <-> node b)                 */
 } tx_explicit_block;
 typedef struct tx_explicit_set {
   int64_t n;               /* side sets: n (element, side) pairs; node sets: n nodes */
@@ -447,9 +458,10 @@ typedef struct tx_mesh_explicit_desc {
 int tx_mesh_element_vertices(tx_handle h, int32_t block, int32_t* nv, int64_t* vertices);
 int tx_mesh_create_explicit(const tx_mesh_explicit_desc* d, tx_handle* out, char* err, int32_t err_len);
 /* A 3-D Exodus II file in the NetCDF classic container (CDF-1/2/5; NetCDF-4
- * files: TX_EINVAL).  Blocks are HEX* or TET*; linear != 0 keeps the vertex
- * nodes of quadratic elements (Panzer_STK_QuadraticToLinearMeshFactory's
- * conversion), otherwise HEX20/HEX27/TETRA10 give TX_EINVAL.  Nodes are
+ * files: TX_EINVAL).  Blocks are HEX* or TET*; HEX27 and TETRA10 keep their
+ * quadratic nodes (for TX_HGRAD_C2 fields), or with linear != 0 only their
+ * vertices (Panzer_STK_QuadraticToLinearMeshFactory's conversion, also the
+ * only form of HEX20).  Nodes are
  * renumbered in ascending node_num_map order when the file has one. */
 int tx_mesh_create_exodus(const char* path, int32_t linear, tx_handle* out, char* err, int32_t err_len);
 typedef struct tx_exodus_summary {

@@ -39,3 +39,54 @@ def box(n=(3, 2, 2), blocks=(1, 1, 1), topo=A.TX_TOPO_HEX, jitter=0.1, seed=5):
     bricks = tuple(a * b for a, b in zip(n, blocks))
     conn = tx.CartesianConnManager(*n, *blocks, topology=topo, jitter=jitter, seed=seed)
     return conn, lattice_as_explicit(conn, bricks)
+
+
+# quadratic nodes in shards order (Hexahedron<27>, Tetrahedron<10>), which are
+# also Exodus II's HEX27 / TETRA10 orders: the mid-edge node of edge c, the
+# mid-face node of face c, the centre
+HEX_EDGES = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7)]
+HEX_EDGE_NODE = [8, 9, 10, 11, 16, 17, 18, 19, 12, 13, 14, 15]
+HEX_FACE_NODE = [25, 24, 26, 23, 21, 22]
+TET_EDGES = [(0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)]
+
+
+def side_nodes(topo, s):
+    """Quadratic node ordinals on side s."""
+    if topo == A.TX_TOPO_HEX:
+        fv = HEX_FACES[s]
+        return fv + [HEX_EDGE_NODE[c] for c, (a, b) in enumerate(HEX_EDGES) if a in fv and b in fv] + \
+            [HEX_FACE_NODE[s]]
+    fv = TET_FACES[s]
+    return fv + [4 + c for c, (a, b) in enumerate(TET_EDGES) if a in fv and b in fv]
+
+
+def quadratic_lattice_as_explicit(conn, n, q):
+    """A lattice mesh with a TX_HGRAD_C2 field as hex27 / tet10 blocks whose node k
+    is the lattice's DOF entity k (GID // fields), so that the explicit numbering
+    equals the lattice numbering; mid-edge / mid-face / centre nodes sit at the
+    means of their vertices.  Returns (coords, blocks, side_sets, node_sets)."""
+    dof = tx.DOFManager(conn, q, require_device=False)
+    nf = dof.n_fields
+    coords_v, blocks_v, ss, _ = lattice_as_explicit(conn, n)
+    coords = np.zeros((dof.n_dofs // nf, 3))
+    blocks, conns = [], []
+    for b, (topo, cv, bid, name) in enumerate(blocks_v):
+        g = dof.getElementGIDs(b)[:, dof.getGIDFieldOffsets(b, 0)] // nf  # [E][nodes] in basis order
+        pv = coords_v[cv]
+        coords[g[:, :cv.shape[1]]] = pv
+        if topo == A.TX_TOPO_HEX:
+            for c, (a, e) in enumerate(HEX_EDGES):
+                coords[g[:, HEX_EDGE_NODE[c]]] = 0.5 * (pv[:, a] + pv[:, e])
+            for s, fv in enumerate(HEX_FACES):
+                coords[g[:, HEX_FACE_NODE[s]]] = pv[:, fv].mean(axis=1)
+            coords[g[:, 20]] = pv.mean(axis=1)
+        else:
+            for c, (a, e) in enumerate(TET_EDGES):
+                coords[g[:, 4 + c]] = 0.5 * (pv[:, a] + pv[:, e])
+        blocks.append((topo, g, bid, name))
+        conns += [(topo, row) for row in g]
+    node_sets = []
+    for name, sid, pairs in ss:
+        nodes = {int(conns[e][1][k]) for e, s in pairs for k in side_nodes(conns[e][0], s)}
+        node_sets.append((name, sid, np.array(sorted(nodes), dtype=np.int64)))
+    return coords, blocks, ss, node_sets

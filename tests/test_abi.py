@@ -78,3 +78,21 @@ def test_spmv_shape_validation_needs_no_device():
     assert lib.tx_set_spmv_entity_shape(conn.h, 3, 3) == 0
     assert lib.tx_set_spmv_entity_shape(conn.h, 3, 4) == A.TX_EINVAL
     assert lib.tx_set_spmv_entity_shape(conn.h, 2, 1) == A.TX_EINVAL
+
+
+def test_two_phase_fit_is_a_host_query():
+    """TX_EVAL_GATHER holds linear elasticity's rows, not quadratic elasticity's
+    (81 element DOFs, 125-entity rows): the query answers without a device."""
+    import ctypes as C
+    import tianxin_gb300 as tx
+    from tianxin_gb300 import _abi as A
+    lib = _lib.load()
+    conn = tx.CartesianConnManager(2, 2, 2)
+    ok = C.c_int32(-1)
+    assert lib.tx_eval_gather_supported(conn.h, C.byref(ok)) == A.TX_ESTATE
+    params = (1.0, 0.3, 0.0, 0.0, -1.0, 0.0)
+    for basis, fits in ((A.TX_HGRAD_C1, 1), (A.TX_HGRAD_C2, 0)):
+        tx.DOFManager(conn, A.equation_set(A.TX_PHYS_ELASTICITY, basis, params=params), require_device=False)
+        assert lib.tx_eval_gather_supported(conn.h, C.byref(ok)) == 0 and ok.value == fits
+    tx.DOFManager(conn, A.equation_set(A.TX_PHYS_HEAT, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0)), require_device=False)
+    assert lib.tx_eval_gather_supported(conn.h, C.byref(ok)) == 0 and ok.value == 1

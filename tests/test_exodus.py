@@ -10,8 +10,10 @@
   out one 0.14 x 0.05 half wall: 0.141).  Volumes and areas are summed from
   the element vertices and side ordinals read, so they check coordinates,
   connectivity and the side numbering.
-* Write -> read round trips of lattice meshes, and the explicit numbering
-  against the lattice numbering of the same mesh (bit-exact).
+* Write -> read round trips of lattice meshes (hex8 / tet4, and hex27 / tet10
+  carrying quadratic fields), and the explicit numbering against the lattice
+  numbering of the same mesh (bit-exact); the reference's tet10 file read with
+  its quadratic nodes (mid-edge nodes at the edge midpoints, shards order).
 * Errors: missing file, HDF5 container, unsupported element types.
 """
 import os
@@ -69,13 +71,37 @@ def test_reference_file_sizes():
 @needs_ref
 @pytest.mark.parametrize("name,inner", [("hex20.gen", 0.148 - 0.14 * 0.05), ("tet10.gen", 0.148)])
 def test_reference_quadratic_meshes_as_linear(name, inner):
-    with pytest.raises(tx.TxError):
-        tx.ExodusReaderFactory(os.path.join(REF_MESHES, name)).buildMesh()  # quadratic needs linear=True
+    if name == "hex20.gen":
+        with pytest.raises(tx.TxError):
+            tx.ExodusReaderFactory(os.path.join(REF_MESHES, name)).buildMesh()  # HEX20 needs linear=True
     m = tx.ExodusReaderFactory(os.path.join(REF_MESHES, name), linear=True).buildMesh()
     vols, areas = _geometry(m)
     assert vols.min() > 0
     assert abs(vols.sum() - 0.0081) <= 1e-12
     assert abs(areas["outer_box"] - 0.312) <= 1e-12 and abs(areas["inner_box"] - inner) <= 1e-12
+
+
+@needs_ref
+def test_reference_tet10_quadratic_nodes():
+    """TETRA10 read with its quadratic nodes: the vertices and side sets equal the
+    linear read, and the TX_HGRAD_C2 DOF of basis 4 + c sits at the midpoint of
+    shards edge c (Cubit's straight-sided tet10), which pins the node order."""
+    path = os.path.join(REF_MESHES, "tet10.gen")
+    mq = tx.ExodusReaderFactory(path).buildMesh()
+    ml = tx.ExodusReaderFactory(path, linear=True).buildMesh()
+    assert mq.n_elements == ml.n_elements
+    for b in range(mq.numElementBlocks()):
+        assert np.array_equal(mq.getElementVertices(b), ml.getElementVertices(b))
+    for k in range(len(mq.getSidesetNames())):
+        assert np.array_equal(mq.getSideset(k), ml.getSideset(k))
+    d = tx.DOFManager(mq, A.equation_set(A.TX_PHYS_HEAT, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0)), require_device=False)
+    c = mq.coordinates()
+    assert d.n_dofs == len(c)  # every node carries a DOF; GIDs are node numbers
+    for b in range(mq.numElementBlocks()):
+        g = d.getElementGIDs(b)[:, d.getGIDFieldOffsets(b, 0)]
+        assert np.array_equal(g[:, :4], mq.getElementVertices(b))
+        for e, (i, j) in enumerate(X.TET_EDGES):
+            assert np.abs(c[g[:, 4 + e]] - 0.5 * (c[g[:, i]] + c[g[:, j]])).max() <= 1e-12
 
 
 @needs_ref
@@ -112,6 +138,41 @@ def test_round_trip_and_numbering_equal_the_lattice(tmp_path, topo, version):
     assert np.array_equal(d_exp.dirichletDofsNodeSet("zmin"), d_lat.dirichletDofs(A.SIDE_ZMIN))
 
 
+@pytest.mark.parametrize("topo,phys", [(A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY), (A.TX_TOPO_TET, A.TX_PHYS_POISSON)])
+def test_quadratic_round_trip_and_numbering_equal_the_lattice(tmp_path, topo, phys):
+    """HEX27 / TETRA10 blocks carry TX_HGRAD_C2 fields: written and read back, the
+    explicit numbering equals the lattice's quadratic numbering, and the node
+    sets (vertices and mid-side nodes) give its box-side Dirichlet DOFs."""
+    n, nb = (2, 2, 1), (1, 1, 2)
+    conn = tx.CartesianConnManager(*n, *nb, topology=topo, jitter=0.1, seed=5)
+    bricks = tuple(a * b for a, b in zip(n, nb))
+    q = A.equation_set(phys, A.TX_HGRAD_C2,
+                       params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.0) if phys == A.TX_PHYS_ELASTICITY else (1, 0, 0, 1))
+    coords, blocks, ss, ns = X.quadratic_lattice_as_explicit(conn, bricks, q)
+    path = write_exodus(tmp_path / "quad.exo", coords, blocks, ss, ns)
+    assert tx.exodus_summary(path)["n_nodes"] == len(coords)
+    m = tx.ExodusReaderFactory(path).buildMesh()
+    ml = tx.ExodusReaderFactory(path, linear=True).buildMesh()
+    nv = 8 if topo == A.TX_TOPO_HEX else 4
+    for b in range(len(blocks)):
+        assert np.array_equal(m.getElementVertices(b), blocks[b][1][:, :nv])
+        assert np.array_equal(ml.getElementVertices(b), blocks[b][1][:, :nv])
+    d_lat = tx.DOFManager(conn, q, require_device=False)
+    d_exp = tx.DOFManager(m, q, require_device=False)
+    assert np.array_equal(d_lat.getOwnedIndices(), d_exp.getOwnedIndices())
+    for b in range(len(blocks)):
+        assert np.array_equal(d_lat.getElementLIDs(b), d_exp.getElementLIDs(b))
+        assert np.array_equal(d_lat.getElementGIDs(b), d_exp.getElementGIDs(b))
+    assert np.array_equal(d_exp.dirichletDofsNodeSet("zmin"), d_lat.dirichletDofs(A.SIDE_ZMIN))
+    assert np.array_equal(d_exp.dirichletDofsNodeSet("xmax"), d_lat.dirichletDofs(A.SIDE_XMAX))
+    # a linear field on quadratic connectivity lives on the vertices: as on the linear read
+    q1 = A.equation_set(phys, A.TX_HGRAD_C1, params=q.params[:6])
+    d1, d1l = tx.DOFManager(m, q1, require_device=False), tx.DOFManager(ml, q1, require_device=False)
+    assert np.array_equal(d1.getOwnedIndices(), d1l.getOwnedIndices())
+    for b in range(len(blocks)):
+        assert np.array_equal(d1.getElementLIDs(b), d1l.getElementLIDs(b))
+
+
 def test_node_num_map_orders_the_nodes(tmp_path):
     conn, (coords, blocks, ss, ns) = X.box(n=(2, 2, 2))
     rng = np.random.default_rng(3)
@@ -141,7 +202,7 @@ def test_explicit_arrays_and_errors(tmp_path):
     with pytest.raises(tx.TxError) as e:
         tx.exodus_summary(h5)
     assert "HDF5" in str(e.value)
-    # explicit meshes carry nodal fields only; box-side queries are refused
+    # quadratic fields need quadratic connectivity; box-side queries are refused
     with pytest.raises(tx.TxError):
         tx.DOFManager(m, A.equation_set(A.TX_PHYS_HEAT, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0)), require_device=False)
     d = tx.DOFManager(m, A.equation_set(A.TX_PHYS_POISSON, params=(1, 0, 0, 1)), require_device=False)

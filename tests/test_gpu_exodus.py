@@ -3,7 +3,8 @@
 The explicit path must reproduce the lattice path on the same mesh: a
 lattice mesh written to an Exodus file (lattice node order, box sides as side
 sets and node sets) and read back gives the same numbering, so the
-deterministic (coloured) evaluation gives the same bits in f and W, with
+deterministic (coloured) evaluation gives the same bits in f and W (linear
+fields on hex8 / tet4, quadratic fields on hex27 / tet10), with
 Dirichlet rows from node sets and Neumann fluxes from side sets in place of
 box sides (f to 1e-15: the flux sums with atomics).  With the nodes renumbered
 (node_num_map), the first-touch LIDs and so f and W in LID order are
@@ -49,6 +50,24 @@ def test_exodus_mesh_reproduces_the_lattice_path(cuda, tmp_path, topo, phys):
     x_np = np.random.default_rng(2).uniform(-1, 1, nf * len(coords))
     d0, f0, v0, _ = _evaluate(conn, q, False, x_np, len(blocks))
     d1, f1, v1, _ = _evaluate(mesh, q, True, x_np, len(blocks))
+    assert np.array_equal(v0, v1)
+    assert np.abs(f0 - f1).max() <= 1e-15 * np.abs(f0).max()
+
+
+@pytest.mark.parametrize("topo,phys", [(A.TX_TOPO_HEX, A.TX_PHYS_HEAT), (A.TX_TOPO_TET, A.TX_PHYS_POISSON)])
+def test_quadratic_exodus_mesh_reproduces_the_lattice_path(cuda, tmp_path, topo, phys):
+    """TX_HGRAD_C2 fields on HEX27 / TETRA10 blocks read from an Exodus file: the
+    same bits as the lattice's quadratic path (node sets with the mid-side nodes
+    for Dirichlet, side sets for Neumann)."""
+    n, nb = (2, 2, 1), (1, 1, 2)
+    conn = tx.CartesianConnManager(*n, *nb, topology=topo, jitter=0.1, seed=5)
+    q = A.equation_set(phys, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0) if phys == A.TX_PHYS_HEAT else (1.0, 0.5, 1.0, 2.0))
+    coords, blocks, ss, ns = X.quadratic_lattice_as_explicit(conn, tuple(a * b for a, b in zip(n, nb)), q)
+    mesh = tx.ExodusReaderFactory(write_exodus(tmp_path / "quad.exo", coords, blocks, ss, ns)).buildMesh()
+    x_np = np.random.default_rng(3).uniform(-1, 1, len(coords))
+    d0, f0, v0, _ = _evaluate(conn, q, False, x_np, len(blocks))
+    d1, f1, v1, _ = _evaluate(mesh, q, True, x_np, len(blocks))
+    assert np.array_equal(d0.getOwnedIndices(), d1.getOwnedIndices())
     assert np.array_equal(v0, v1)
     assert np.abs(f0 - f1).max() <= 1e-15 * np.abs(f0).max()
 

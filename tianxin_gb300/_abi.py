@@ -127,7 +127,7 @@ class NeumannDesc(C.Structure):
 
 class ExplicitBlock(C.Structure):
     _fields_ = [("topology", C.c_int32), ("n_elem", C.c_int64), ("conn", C.c_void_p), ("id", C.c_int64),
-                ("name", C.c_char_p)]
+                ("name", C.c_char_p), ("nodes_per_elem", C.c_int32)]
 
 
 class ExplicitSet(C.Structure):

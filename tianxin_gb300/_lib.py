@@ -30,6 +30,7 @@ SIGNATURES = {
     "tx_dirichlet_dofs": (C.c_int, [P, U32, U32, C.POINTER(I64), P]),
     "tx_graph_build": (C.c_int, [P, P, P]),
     "tx_eval": (C.c_int, [P, C.POINTER(_abi.EvalArgs)]),
+    "tx_eval_gather_supported": (C.c_int, [P, C.POINTER(C.c_int32)]),
     "tx_dirichlet_apply": (C.c_int, [P, I64, P, P, P, P, P]),
     "tx_spmv": (C.c_int, [P, I32, I64, P, P, P, P, P, D, D]),
     "tx_solve_cg_ir": (C.c_int, [P, C.POINTER(_abi.SolveArgs)]),

@@ -22,6 +22,7 @@ import os
 import torch
 
 from . import _abi as A
+from ._lib import TxError as tx_error
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
@@ -83,7 +84,7 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
             # kernel variant (warp per element / CTA-staged / CTA direct scatter / two-phase) x CTA cap
             kernels = [(2, False, False), (1, False, False), (1, True, False)] if mixed else \
                 [(1, False, False), (1, True, False)]
-            if W is not None:
+            if W is not None and ae.gather_supported():
                 kernels.append((1, False, True))
 
             def step(direct, gather):
@@ -99,7 +100,7 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                     ae.setGridCap(cap)
                     try:
                         t = _time(lambda: step(direct, gather), reps)
-                    except Exception:  # the two-phase form refuses meshes with overlong rows
+                    except tx_error:  # a configuration the handle refuses
                         continue
                     results.append(({"variant": variant, "scatter_direct": direct, "gather": gather,
                                      "grid_cap": cap}, t))

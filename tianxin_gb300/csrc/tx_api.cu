@@ -140,7 +140,6 @@ struct tx_handle_s {
   // (CSR, device) and the element scratch of the first phase
   int64_t* d_inc_ptr = nullptr;
   int64_t* d_inc = nullptr;
-  int gather_row_max = 0;             // nf^2 x longest entity row
   unsigned char* gather_scratch = nullptr;
   size_t gather_bytes = 0;
   // cubature tables of tx_ip_coordinates per (block, degree)
@@ -170,7 +169,7 @@ struct tx_handle_s {
     for (auto& t : ip_tables) cudaFree(t.tables);
     ip_tables.clear();
     cudaFree(d_inc_ptr); cudaFree(d_inc); cudaFree(gather_scratch);
-    d_inc_ptr = nullptr; d_inc = nullptr; gather_scratch = nullptr; gather_bytes = 0; gather_row_max = 0;
+    d_inc_ptr = nullptr; d_inc = nullptr; gather_scratch = nullptr; gather_bytes = 0;
     for (auto& b : blocks) {
       cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
       cudaFree(b.color_perm);
@@ -353,6 +352,18 @@ int eval_persistent(tx_handle h, const tx_eval_args& a) {
   return TX_OK;
 }
 
+// Whether the two-phase form holds this handle's rows: nf^2 x the longest
+// entity row in the gather kernel's shared row, nf^2 x an element's basis
+// count in its per-entity element-row window.
+const char* gather_misfit(const tx::Dofs& D) {
+  int64_t maxdeg = 0;
+  for (int64_t r = 0; r < D.n_entities; ++r) maxdeg = std::max(maxdeg, D.erowptr[r + 1] - D.erowptr[r]);
+  if (maxdeg * D.nf * D.nf > tx::kGatherRowMax) return "tx_eval: an entity row is too long for TX_EVAL_GATHER";
+  for (const tx::BlockDofs& B : D.blocks)
+    if (D.nf * D.nf * B.nb > tx::kGatherElemRowMax) return "tx_eval: element rows too long for TX_EVAL_GATHER";
+  return nullptr;
+}
+
 // Evaluate every requested block/range (volume fill).
 // Two-phase evaluation (TX_EVAL_GATHER): incidence lists built on first use,
 // element scratch grown to the precision's need, then per block the first
@@ -365,6 +376,7 @@ int eval_gather(tx_handle h, const tx_eval_args& a, const tx::EvalParams& P0) {
     return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_GATHER is not combined with TANGENT, PERSISTENT or DETERMINISTIC");
   const tx::Dofs& D = h->dofs;
   const int nf = D.nf;
+  if (const char* why = gather_misfit(D)) return fail(h, TX_EINVAL, why);
   int rc = guarded(h, [&]() {
     if (!h->d_inc_ptr) {
       const int64_t ne = D.n_entities;
@@ -380,17 +392,9 @@ int eval_gather(tx_handle h, const tx_eval_args& a, const tx::EvalParams& P0) {
           for (int k = 0; k < B.nb; ++k)
             inc[fill[B.dconn[e * B.nb + k]]++] = ((int64_t)b << 56) | (e << 8) | k;
       }
-      int64_t maxdeg = 0;
-      for (int64_t r = 0; r < ne; ++r) maxdeg = std::max(maxdeg, D.erowptr[r + 1] - D.erowptr[r]);
-      h->gather_row_max = (int)(maxdeg * nf * nf);
       ck(upload(h->d_inc_ptr, ptr), "upload incidence");
       ck(upload(h->d_inc, inc), "upload incidence");
     }
-    if (h->gather_row_max > tx::kGatherRowMax)
-      throw std::invalid_argument("tx_eval: an entity row is too long for TX_EVAL_GATHER");
-    for (const DevBlock& db : h->blocks)
-      if (nf * nf * db.nb > tx::kGatherElemRowMax)
-        throw std::invalid_argument("tx_eval: element rows too long for TX_EVAL_GATHER");
     size_t need = 0;
     for (const DevBlock& db : h->blocks) {
       const size_t E = (size_t)db.n_elem, NE = (size_t)nf * db.nb, w = mixed ? 4 : 8;
@@ -642,9 +646,11 @@ int tx_mesh_create_explicit(const tx_mesh_explicit_desc* d, tx_handle* out, char
       tx::ExplicitBlock E;
       E.topology = B.topology; E.n_elem = B.n_elem; E.id = B.id;
       E.name = B.name ? B.name : "block_" + std::to_string(B.id);
-      const int nv = B.topology == TX_TOPO_TET ? 4 : 8;
+      E.npe = B.nodes_per_elem > 0 ? B.nodes_per_elem : (B.topology == TX_TOPO_TET ? 4 : 8);
+      if (E.npe != 4 && E.npe != 8 && E.npe != 10 && E.npe != 27)
+        throw std::invalid_argument("explicit mesh: nodes per element");
       if (B.n_elem < 0 || (B.n_elem > 0 && !B.conn)) throw std::invalid_argument("explicit mesh: connectivity");
-      if (B.n_elem > 0) E.conn.assign(B.conn, B.conn + B.n_elem * nv);
+      if (B.n_elem > 0) E.conn.assign(B.conn, B.conn + B.n_elem * E.npe);
       M.blocks.push_back(std::move(E));
     }
     auto sets = [](int32_t n, const tx_explicit_set* in, int per, std::vector<tx::ExplicitSet>& dst) {
@@ -893,6 +899,13 @@ int tx_eval(tx_handle h, const tx_eval_args* args) {
   if (h->dofs.eq.physics == TX_PHYS_MAXWELL && !args->aux && args->f)
     return fail(h, TX_EINVAL, "tx_eval: MAXWELL needs the current density J in aux");
   return eval_blocks(h, *args);
+}
+
+int tx_eval_gather_supported(tx_handle h, int32_t* supported) {
+  if (!h || !supported) return TX_EINVAL;
+  if (!h->have_host_dofs) return fail(h, TX_ESTATE, "tx_eval_gather_supported before tx_dof_build");
+  *supported = gather_misfit(h->dofs) ? 0 : 1;
+  return TX_OK;
 }
 
 int tx_dirichlet_apply(tx_handle h, int64_t n, const int32_t* lids, const double* g, const double* x, double* f,

@@ -290,14 +290,21 @@ ExplicitMesh read_exodus(const std::string& path, bool linear) {
     else if (et.rfind("TET", 0) == 0) { B.topology = TX_TOPO_TET; nv = 4; }
     else if (ne > 0) throw std::invalid_argument("Exodus: element type '" + et + "' is not provided (hex or tet)");
     else { B.topology = TX_TOPO_HEX; nv = 8; }
-    if (ne > 0 && npe != nv && !linear)
-      throw std::invalid_argument("Exodus: " + et + " elements need linear=true (their vertex nodes are kept)");
     if (ne > 0 && npe < nv) throw std::invalid_argument("Exodus: too few nodes per element for " + et);
-    B.conn.reserve((size_t)(ne * nv));
+    // kept nodes: the vertices (linear elements, or linear=true), or every node of HEX27 / TETRA10
+    const int quad = B.topology == TX_TOPO_HEX ? 27 : 10;
+    int keep = nv;
+    if (ne > 0 && npe != nv) {
+      if (!linear && npe != quad)
+        throw std::invalid_argument("Exodus: " + et + " elements are read with linear=true (their vertex nodes)");
+      keep = linear ? nv : quad;
+    }
+    B.npe = keep;
+    B.conn.reserve((size_t)(ne * keep));
     if (ne > 0) {
       std::vector<int64_t> c = f.read<int64_t>(cv);
       for (int64_t e = 0; e < ne; ++e)
-        for (int a = 0; a < nv; ++a) {
+        for (int a = 0; a < keep; ++a) {
           const int64_t node = c[e * npe + a] - 1;
           if (node < 0 || node >= nn) throw std::invalid_argument("Exodus: node number out of range in " + cv);
           B.conn.push_back(rank[node]);

@@ -61,9 +61,10 @@ struct Handle;  // defined in tx_api.cu
 // order; 0-based shards side ordinal) and node sets.
 struct ExplicitBlock {
   int topology = 0;
+  int npe = 0;                // nodes an element: the vertices (8 / 4) or quadratic (27 / 10)
   int64_t n_elem = 0, id = 0;
   std::string name;
-  std::vector<int64_t> conn;  // [n_elem][nv]
+  std::vector<int64_t> conn;  // [n_elem][npe], shards node order
 };
 struct ExplicitSet {
   int64_t id = 0;

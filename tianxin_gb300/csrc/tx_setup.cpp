@@ -542,8 +542,11 @@ void build_mesh_explicit(Mesh& m, ExplicitMesh&& x) {
     const ExplicitBlock& B = x.blocks[b];
     if (B.topology != TX_TOPO_HEX && B.topology != TX_TOPO_TET)
       throw std::invalid_argument("explicit mesh: blocks are hex8 or tet4");
-    const int nv = B.topology == TX_TOPO_HEX ? 8 : 4;
-    if (B.n_elem < 0 || (int64_t)B.conn.size() != B.n_elem * nv)
+    const int nv = B.topology == TX_TOPO_HEX ? 8 : 4, nq = B.topology == TX_TOPO_HEX ? 27 : 10;
+    if (B.npe == 0) x.blocks[b].npe = nv;
+    const int npe = x.blocks[b].npe;
+    if (npe != nv && npe != nq) throw std::invalid_argument("explicit mesh: nodes per element (vertices or quadratic)");
+    if (B.n_elem < 0 || (int64_t)B.conn.size() != B.n_elem * npe)
       throw std::invalid_argument("explicit mesh: connectivity size");
     for (int64_t v : B.conn)
       if (v < 0 || v >= x.n_nodes) throw std::invalid_argument("explicit mesh: node number out of range");
@@ -605,8 +608,9 @@ int element_vertices(const Mesh& m, int block, int64_t* out) {
   const int nv = topo == TX_TOPO_HEX ? 8 : 4;
   const std::vector<int64_t>& el = m.block_elems[block];
   if (m.is_explicit) {
-    const std::vector<int64_t>& cn = m.ex.blocks[block].conn;
-    std::copy(cn.begin(), cn.end(), out);
+    const ExplicitBlock& B = m.ex.blocks[block];
+    for (int64_t i = 0; i < B.n_elem; ++i)
+      for (int v = 0; v < nv; ++v) out[i * nv + v] = B.conn[i * B.npe + v];
     return nv;
   }
   Lattice L;
@@ -646,8 +650,10 @@ void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q) {
       throw std::invalid_argument("tx_dof_build: HCURL basis goes with MAXWELL physics only");
     if (B.basis == TX_HCURL_I1 && B.topo != TX_TOPO_HEX)
       throw std::invalid_argument("tx_dof_build: HCURL is provided on hexahedra only");
-    if (ex && B.basis != TX_HGRAD_C1)
-      throw std::invalid_argument("tx_dof_build: explicit meshes carry nodal (HGRAD_C1) fields only");
+    if (ex && B.basis != TX_HGRAD_C1 && B.basis != TX_HGRAD_C2)
+      throw std::invalid_argument("tx_dof_build: explicit meshes carry nodal (HGRAD) fields only");
+    if (ex && B.basis == TX_HGRAD_C2 && m.ex.blocks[b].npe != n_basis(B.topo, B.basis))
+      throw std::invalid_argument("tx_dof_build: quadratic fields need quadratic (hex27 / tet10) connectivity");
     B.degree = q.integration_order[b] > 0 ? q.integration_order[b] : default_degree(B.topo, B.basis);
     B.ref = make_ref_tables(B.topo, B.basis, B.degree);
     B.nb = B.ref.nb; B.nv = B.ref.nv;
@@ -680,14 +686,12 @@ void build_dofs(const Mesh& m, Dofs& D, const tx_equation_set_desc& q) {
     egid[b].assign(E * B.nb, -1);
     epos3[b].assign(E * B.nb * 3, 0);
     B.vconn.assign(E * B.nv, 0);
-    if (ex) {  // node numbers are the vertex GIDs; one DOF entity per vertex
+    if (ex) {  // node numbers are the GIDs; basis b lives on the element's node b (shards order)
       const std::vector<int64_t>& cn = m.ex.blocks[b].conn;
+      const int npe = m.ex.blocks[b].npe;
       for (int64_t i = 0; i < E; ++i) {
-        for (int v = 0; v < B.nv; ++v) B.vconn[i * B.nv + v] = (int32_t)cn[i * B.nv + v];
-        for (size_t g = 0; g < B.geom_dim.size(); ++g) {
-          const int bi = B.geom_basis[g];
-          if (bi >= 0) egid[b][i * B.nb + bi] = cn[i * B.nv + B.geom_sub[g]];  // vertex sub-cells only
-        }
+        for (int v = 0; v < B.nv; ++v) B.vconn[i * B.nv + v] = (int32_t)cn[i * npe + v];
+        for (int bi = 0; bi < B.nb; ++bi) egid[b][i * B.nb + bi] = cn[i * npe + bi];
       }
       for (int64_t k = 0; k < E * B.nb; ++k) has[egid[b][k]] = 1;
       continue;

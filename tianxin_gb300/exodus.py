@@ -1,7 +1,7 @@
 """Exodus II mesh output in the NetCDF classic container (STK_Interface::writeToExodus's
 role for the mesh itself: adapters-stk/src/Panzer_STK_Interface.cpp).
 
-Writes coordinates, hex8/tet4 element blocks, side sets and node sets with
+Writes coordinates, hex8/tet4/hex27/tet10 element blocks, side sets and node sets with
 the Exodus II variable names (1-based element and node numbers, 1-based side
 ordinals) in CDF-1 or CDF-2; no results variables.  Host-side utility: the
 file is what the library's reader (tx_mesh_create_exodus) and other Exodus
@@ -15,7 +15,7 @@ _NC_DIMENSION, _NC_VARIABLE, _NC_ATTRIBUTE = 0x0A, 0x0B, 0x0C
 _NC_CHAR, _NC_INT, _NC_FLOAT, _NC_DOUBLE = 2, 4, 5, 6
 _SIZE = {_NC_CHAR: 1, _NC_INT: 4, _NC_FLOAT: 4, _NC_DOUBLE: 8}
 _FMT = {_NC_INT: ">i4", _NC_FLOAT: ">f4", _NC_DOUBLE: ">f8"}
-_ELEM_TYPE = {0: "HEX8", 1: "TETRA4"}  # TX_TOPO_HEX, TX_TOPO_TET
+_ELEM_TYPE = {(0, 8): "HEX8", (1, 4): "TETRA4", (0, 27): "HEX27", (1, 10): "TETRA10"}  # (topology, nodes)
 _LEN_NAME = 33
 
 
@@ -49,7 +49,8 @@ def _names_array(names):
 def write_exodus(path, coords, blocks, side_sets=(), node_sets=(), node_num_map=None, version=2, title="tianxin"):
     """Write a 3-D mesh.
 
-    coords [n][3]; blocks [(topology, conn[E][nv] 0-based nodes, id, name)];
+    coords [n][3]; blocks [(topology, conn[E][nodes] 0-based, id, name)] with the vertices (hex8 / tet4) or
+    the quadratic nodes (hex27 / tet10, shards order);
     side_sets [(name, id, [(element, side), ...])] with 0-based elements over
     the whole mesh and 0-based shards sides; node_sets [(name, id, nodes)];
     node_num_map: optional global node ids (1-based, any order).
@@ -70,7 +71,7 @@ def write_exodus(path, coords, blocks, side_sets=(), node_sets=(), node_num_map=
     dim("four", 4)
     d_dim = dim("num_dim", 3)
     d_nodes = dim("num_nodes", len(coords))
-    dim("num_elem", sum(len(np.asarray(b[1]).reshape(-1, 8 if b[0] == 0 else 4)) for b in blocks))
+    dim("num_elem", sum(len(np.asarray(b[1])) for b in blocks))
     d_blk = dim("num_el_blk", len(blocks))
     side_sets = [s for s in side_sets if len(s[2])]
     node_sets = [s for s in node_sets if len(s[2])]
@@ -86,11 +87,11 @@ def write_exodus(path, coords, blocks, side_sets=(), node_sets=(), node_num_map=
     var("eb_status", [d_blk], _NC_INT, np.ones(len(blocks), np.int64))
     var("eb_prop1", [d_blk], _NC_INT, np.array([b[2] for b in blocks]), [("name", _NC_CHAR, "ID")])
     for k, (topo, conn, _, _) in enumerate(blocks, 1):
-        nv = 8 if topo == 0 else 4
-        c = np.asarray(conn, dtype=np.int64).reshape(-1, nv)
+        c = np.asarray(conn, dtype=np.int64)
+        c = c.reshape(len(c), -1)
         de = dim(f"num_el_in_blk{k}", len(c))
-        dn = dim(f"num_nod_per_el{k}", nv)
-        var(f"connect{k}", [de, dn], _NC_INT, c + 1, [("elem_type", _NC_CHAR, _ELEM_TYPE[topo])])
+        dn = dim(f"num_nod_per_el{k}", c.shape[1])
+        var(f"connect{k}", [de, dn], _NC_INT, c + 1, [("elem_type", _NC_CHAR, _ELEM_TYPE[(topo, c.shape[1])])])
     if side_sets:
         var("ss_names", [d_ss, d_name], _NC_CHAR, _names_array([s[0] for s in side_sets]))
         var("ss_status", [d_ss], _NC_INT, np.ones(len(side_sets), np.int64))

@@ -104,7 +104,8 @@ class ExplicitConnManager:
 
     @classmethod
     def from_arrays(cls, coords, blocks, side_sets=(), node_sets=()):
-        """blocks: [(topology, conn[E][nv], id, name)]; side_sets: [(name, id, [(elem, side), ...])];
+        """blocks: [(topology, conn[E][nodes], id, name)] with the vertices or the hex27 / tet10 nodes (shards order);
+        side_sets: [(name, id, [(elem, side), ...])];
         node_sets: [(name, id, nodes)]."""
         lib = load()
         xyz = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
@@ -114,6 +115,7 @@ class ExplicitConnManager:
             c = np.ascontiguousarray(conn, dtype=np.int64)
             keep.append(c)
             bl[k].topology, bl[k].n_elem, bl[k].conn, bl[k].id = topo, c.shape[0], _np_ptr(c), bid
+            bl[k].nodes_per_elem = c.shape[1] if c.ndim == 2 else 0  # vertices, or hex27 / tet10 nodes
             bl[k].name = name.encode() if name else None
 
         def sets(items, per):
@@ -645,6 +647,7 @@ class AssemblyEngine:
         self.lof, self.dof = lof, lof.dof
         self.scatter_direct = False  # set by the autotuner
         self.gather = False          # two-phase evaluation (TX_EVAL_GATHER), set by the autotuner
+        self._gather_fits = None     # whether TX_EVAL_GATHER holds the handle's rows (asked once)
 
     def setWorksetSize(self, min_size, max_size=None, seed=0):
         """Worksets of the persistent evaluation: sizes uniform in [min_size, max_size]."""
@@ -658,10 +661,18 @@ class AssemblyEngine:
         """Assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element (hex8 elasticity, mixed)."""
         check(self.dof.h, self.dof.lib.tx_set_assembly_variant(self.dof.h, variant), "tx_set_assembly_variant")
 
+    def gather_supported(self):
+        """Whether the two-phase form holds this handle's rows (not, e.g., quadratic elasticity's)."""
+        if self._gather_fits is None:
+            ok = C.c_int32()
+            check(self.dof.h, self.dof.lib.tx_eval_gather_supported(self.dof.h, C.byref(ok)), "tx_eval_gather_supported")
+            self._gather_fits = bool(ok.value)
+        return self._gather_fits
+
     def gather_applies(self, W, block=-1, workset=(0, -1), deterministic=False, persistent=False):
         """Whether evaluate() with these arguments takes the two-phase form (f and W overwritten)."""
         return (self.gather and W is not None and block < 0 and tuple(workset) == (0, -1) and not deterministic
-                and not persistent)
+                and not persistent and self.gather_supported())
 
     def evaluate(self, x, x_dot=None, aux=None, alpha=0.0, beta=1.0, t=0.0, f=None, W=None, mixed=False,
                  block=-1, workset=(0, -1), deterministic=False, persistent=False, scatter_direct=None, gather=None):
@@ -717,7 +728,8 @@ class ModelEvaluator:
         # A Jacobian evaluation from zero may take the two-phase form, which overwrites f and W (no zeroing):
         # when the autotuner chose it, and for deterministic evaluations, where its fixed-order row sums
         # are faster than the coloured launches.  zero=False sums into f and W: the atomic forms.
-        gather = zero and W is not None and not persistent and (self.ae.gather or deterministic)
+        gather = zero and W is not None and not persistent and (self.ae.gather or deterministic) and \
+            self.ae.gather_supported()
         if zero and not gather:
             if f is not None:
                 f.zero_()
