@@ -372,8 +372,18 @@ def run_ours(a):
         e.record(stream)
         barrier()
         te = maxall(s.elapsed_time(e) / 1e3)
+        # the host link alone: the same step's bytes copied back with nothing else running (its bound)
+        s.record(stream)
+        for k in range(2):
+            fh.copy_(f, non_blocking=True)
+            Wh.copy_(W.values, non_blocking=True)
+        e.record(stream)
+        e.synchronize()
+        link_s = s.elapsed_time(e) / 2e3
+        d2h = 8 * N + 8 * nnz
         e2e = {"value": ws * E * K2 / te, "unit": UNIT, "h2d_bytes_per_step": 8 * N,
-               "d2h_bytes_per_step": 8 * N + 8 * nnz, "steps": K2,
+               "d2h_bytes_per_step": d2h, "steps": K2,
+               "link_d2h_gbs": d2h / link_s / 1e9, "link_bound_frac": link_s / (te / K2),
                "path": "host x -> tx_eval(mixed) + Dirichlet -> host f and CRS values (HostEvaluator: copy-back "
                        "of step k overlapped with the assembly of step k+1)"}
         del Wh, hev
