@@ -539,8 +539,8 @@ int tx_set_grid_cap(tx_handle h, int32_t max_ctas);
 int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll);
 /* Launch shape of the entity-block form (TX_SPMV_ENTITY_BLOCKS,
  * TX_SOLVE_ENTITY_BLOCKS): lanes per entity 3 (blocks per pass 1/2/3; ten
- * entities a warp, two lanes idle) or 4/8/16/32 (1/2); (0, 0) = FP64 4
- * lanes, 1 block, FP32 16 lanes, 2. */
+ * entities a warp, two lanes idle), 4 or 8 (1/2/4) or 16/32 (1/2); (0, 0) =
+ * FP64 4 lanes, 4 blocks, FP32 16 lanes, 2. */
 int tx_set_spmv_entity_shape(tx_handle h, int32_t lanes, int32_t unroll);
 /* Assembly kernel of the per-block mixed evaluation: 0 automatic (the
  * warp-per-element kernel where the element family has one, hex8 elasticity;

@@ -74,7 +74,8 @@ def test_spmv_shape_validation_needs_no_device():
     assert lib.tx_set_spmv_shape(conn.h, 8, 16) == 0
     assert lib.tx_set_spmv_entity_shape(conn.h, 8, 2) == 0
     assert lib.tx_set_spmv_entity_shape(conn.h, 0, 0) == 0
-    assert lib.tx_set_spmv_entity_shape(conn.h, 8, 4) == A.TX_EINVAL
+    assert lib.tx_set_spmv_entity_shape(conn.h, 8, 4) == 0
+    assert lib.tx_set_spmv_entity_shape(conn.h, 16, 4) == A.TX_EINVAL
     assert lib.tx_set_spmv_entity_shape(conn.h, 3, 3) == 0
     assert lib.tx_set_spmv_entity_shape(conn.h, 3, 4) == A.TX_EINVAL
     assert lib.tx_set_spmv_entity_shape(conn.h, 2, 1) == A.TX_EINVAL

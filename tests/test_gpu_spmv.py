@@ -118,7 +118,8 @@ def test_spmv_every_launch_shape(cuda, name):
             assert np.abs(y32 - y_ref).max() <= 1e-5 * np.abs(y_ref).max(), (lanes, unroll)
     W.setApplyShape(0, 0)
     W.setApplyForm("entity")
-    for lanes, unroll in [(3, 1), (3, 2), (3, 3)] + [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2)]:
+    for lanes, unroll in [(3, 1), (3, 2), (3, 3), (4, 4), (8, 4)] + \
+            [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2)]:
         if True:
             W.setEntityApplyShape(lanes, unroll)
             y = W.apply(xd).cpu().numpy()

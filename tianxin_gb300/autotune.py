@@ -121,7 +121,8 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
 
 
 SPMV_SHAPES = [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2, 4, 16)]  # 16: 16-byte loads
-ENTITY_SHAPES = [(3, 1), (3, 2), (3, 3)] + [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2)]
+ENTITY_SHAPES = [(3, 1), (3, 2), (3, 3)] + [(lanes, unroll) for lanes in (4, 8, 16, 32) for unroll in (1, 2)] + \
+    [(4, 4), (8, 4)]
 
 
 def tune_spmv(W, vals, x, y, reps=5):

@@ -1469,7 +1469,7 @@ int tx_set_spmv_entity_shape(tx_handle h, int32_t lanes, int32_t unroll) {
   if (!h) return TX_EINVAL;
   const tx::SpmvShape sh{lanes, unroll};
   if (!tx::entity_shape_valid(sh))
-    return fail(h, TX_EINVAL, "tx_set_spmv_entity_shape: lanes 4/8/16/32 and unroll 1/2, or both 0");
+    return fail(h, TX_EINVAL, "tx_set_spmv_entity_shape: lanes 3 (unroll 1-3), 4/8 (1/2/4), 16/32 (1/2), or both 0");
   h->spmv_eb = sh;
   return TX_OK;
 }

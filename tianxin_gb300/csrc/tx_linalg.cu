@@ -282,12 +282,15 @@ __device__ __forceinline__ T entity_reduce(const T (&s)[NF], int sub) {
 // Six resident CTAs an SM (40 registers) for up to 16 lanes an entity; four
 // (64 registers) for 32 lanes and for three lanes with three blocks a pass,
 // whose FP64 forms would spill at 40.
-constexpr int entity_min_blocks(int G, int U) { return G >= 32 || (G < 4 && U >= 3) ? 4 : 6; }
+constexpr int entity_min_blocks(int G, int U, int bytes = 4) {
+  if (U >= 4) return bytes == 8 ? 3 : 4;  // four blocks in flight: 36 values a lane in registers
+  return G >= 32 || (G < 4 && U >= 3) ? 4 : 6;
+}
 
 // y = alpha A x + beta y in the entity-block form; entity loop per warp as in
 // k_spmv (warp-uniform trip count for the full-mask shuffles).
 template <typename T, int NF, int G, int U>
-__global__ void __launch_bounds__(kThreads, entity_min_blocks(G, U)) k_spmv_eb(int64_t n_ent, const int64_t* __restrict__ erp,
+__global__ void __launch_bounds__(kThreads, entity_min_blocks(G, U, sizeof(T))) k_spmv_eb(int64_t n_ent, const int64_t* __restrict__ erp,
                                                       const int32_t* __restrict__ ecol, const T* __restrict__ vals,
                                                       const T* __restrict__ x, T* __restrict__ y, T alpha, T beta) {
   constexpr int GPW = 32 / G;  // entities per warp (G = 3: ten, lanes 30 and 31 idle)
@@ -362,14 +365,16 @@ cudaError_t spmv_dispatch(int64_t n, const int64_t* rp, const int32_t* col, cons
   return with_shape(sh, SpmvLaunch<T>{n, rp, col, vals, x, y, a, b, s});
 }
 
-// Entity-block shapes: lanes per entity 4/8/16/32, blocks per lane pass 1/2.
-// {0, 0}: FP64 4 lanes, 1 block: GB300's FP64 pipe (about two FMAs a clock an
-// SM) bounds the FP64 product, and 4 lanes waste the fewest FMA slots on the
-// 27 blocks of an interior entity (28 slots) and on the row sums; FP32 16
-// lanes, 2 blocks, the fastest of the eight on the 128^3 elasticity operator.
+// Entity-block shapes: lanes per entity 3 (blocks per lane pass 1-3), 4/8
+// (1/2/4), 16/32 (1/2).  {0, 0}: FP64 4 lanes, 4 blocks: GB300's FP64 pipe
+// (about two FMAs a clock an SM) bounds the FP64 product, 4 lanes waste few
+// FMA slots on the 27 blocks of an interior entity (two passes of 16) and on
+// the row sums, and four blocks a lane keep 36 values in flight; FP32 16
+// lanes, 2 blocks.  Both the fastest of their precision on the 128^3
+// elasticity operator.
 SpmvShape resolve_entity_shape(SpmvShape sh, bool f32) {
   if (sh.lanes > 0 && sh.unroll > 0) return sh;
-  return f32 ? SpmvShape{16, 2} : SpmvShape{4, 1};
+  return f32 ? SpmvShape{16, 2} : SpmvShape{4, 4};
 }
 
 template <typename F>
@@ -377,7 +382,7 @@ cudaError_t with_entity_shape(SpmvShape sh, F&& f) {
 #define TX_ESHAPE(L, U) \
   if (sh.lanes == L && sh.unroll == U) return f.template run<L, U>();
   TX_ESHAPE(3, 1) TX_ESHAPE(3, 2) TX_ESHAPE(3, 3)
-  TX_ESHAPE(4, 1) TX_ESHAPE(4, 2) TX_ESHAPE(8, 1) TX_ESHAPE(8, 2)
+  TX_ESHAPE(4, 1) TX_ESHAPE(4, 2) TX_ESHAPE(4, 4) TX_ESHAPE(8, 1) TX_ESHAPE(8, 2) TX_ESHAPE(8, 4)
   TX_ESHAPE(16, 1) TX_ESHAPE(16, 2) TX_ESHAPE(32, 1) TX_ESHAPE(32, 2)
 #undef TX_ESHAPE
   return cudaErrorInvalidValue;
@@ -646,7 +651,7 @@ bool entity_shape_valid(SpmvShape sh) {
   if (sh.lanes == 0 && sh.unroll == 0) return true;
   if (sh.lanes == 3) return sh.unroll >= 1 && sh.unroll <= 3;
   const bool l = sh.lanes == 4 || sh.lanes == 8 || sh.lanes == 16 || sh.lanes == 32;
-  return l && (sh.unroll == 1 || sh.unroll == 2);
+  return l && (sh.unroll == 1 || sh.unroll == 2 || (sh.unroll == 4 && sh.lanes <= 8));
 }
 cudaError_t launch_spmv_entity_f64(const EntityGraph& eg, const double* vals, const double* x, double* y, double a,
                                    double b, cudaStream_t s, SpmvShape shape) {
