@@ -119,3 +119,49 @@ def test_side_set_and_probe_responses_on_an_exodus_mesh(cuda, tmp_path):
         assert abs(v0 - v1) <= 1e-14 * max(1.0, abs(v0))
     p = (0.4, 0.7, 0.3)
     assert tx.Response(d_lat, "Probe", point=p).value(x) == tx.Response(d_exp, "Probe", point=p).value(x)
+
+
+def test_empty_block_and_empty_sets_change_nothing(cuda):
+    """An element block with no elements, an empty side set and an empty node set (ragged inputs the
+    reference's meshes can hold): every evaluation form, Neumann, Dirichlet and the responses give what
+    the mesh without them gives."""
+    conn, (coords, blocks, ss, ns) = X.box(n=(3, 2, 2))
+    empty = (A.TX_TOPO_TET, np.zeros((0, 4), np.int64), 9, "empty")
+    m0 = tx.ExplicitConnManager.from_arrays(coords, blocks, ss, ns)
+    m1 = tx.ExplicitConnManager.from_arrays(coords, [empty] + list(blocks), ss + [("none", 7, [])],
+                                            ns + [("nonodes", 8, [])])
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=ELAST)
+    x_np = np.random.default_rng(9).uniform(-1, 1, 3 * len(coords))
+    outs = []
+    for m, nb in ((m0, 1), (m1, 2)):
+        dof = tx.DOFManager(m, q)
+        lof = tx.TpetraLinearObjFactory(dof)
+        dbc = [tx.DirichletBC(dof, node_set="zmin")] + ([tx.DirichletBC(dof, node_set="nonodes")] if nb == 2 else [])
+        nbc = [tx.NeumannBC(dof, dof_name="UZ", value=-0.3, block=b, side_set=s)
+               for b in range(nb) for s in (("zmax", "none") if nb == 2 else ("zmax",))]
+        me = tx.ModelEvaluator(lof, dbc, nbc)
+        x = torch.from_numpy(x_np).cuda()
+        res = []
+        for kw in (dict(deterministic=True), dict(mixed=True), dict(persistent=True)):
+            f, W = lof.getTpetraVector(), me.create_W_op()
+            me.evalModel(x, x_dot=0.5 * x, alpha=0.5, beta=1.0, f=f, W=W, **kw)
+            res.append((f.cpu().numpy(), W.values.cpu().numpy()))
+        me.ae.gather = True
+        f, W = lof.getTpetraVector(), me.create_W_op()
+        me.evalModel(x, f=f, W=W)
+        res.append((f.cpu().numpy(), W.values.cpu().numpy()))
+        last = nb - 1  # the non-empty block
+        resp = [tx.Response(dof, "Field", block=last).value(x),
+                tx.Response(dof, "Max", dof_name="UX").value(x),
+                tx.Response(dof, "Field", block=last, side_set="zmax").value(x)]
+        if nb == 2:
+            assert tx.Response(dof, "Field", block=0).value(x) == 0.0
+            assert tuple(tx.ip_coordinates(dof, 0).shape)[0] == 0
+        outs.append((dof.getOwnedIndices(), res, resp))
+    (g0, r0, p0), (g1, r1, p1) = outs
+    assert np.array_equal(g0, g1)
+    assert np.array_equal(r0[0][1], r1[0][1])  # deterministic: same bits
+    for (f0, v0), (f1, v1) in zip(r0, r1):
+        assert np.abs(f0 - f1).max() <= 1e-14 * np.abs(f0).max()
+        assert np.abs(v0 - v1).max() <= 1e-14 * np.abs(v0).max()
+    assert p0[1] == p1[1] and abs(p0[0] - p1[0]) <= 1e-14 * abs(p0[0]) and abs(p0[2] - p1[2]) <= 1e-14 * abs(p0[2])
