@@ -170,6 +170,8 @@ typedef struct tx_handle_s* tx_handle;
 /* CartesianConnManager::initialize (CartesianConnManager.cpp:159-294). */
 int tx_mesh_create(const tx_mesh_desc* desc, tx_handle* out);
 void tx_destroy(tx_handle h);
+/* The handle's last error message; tx_last_error(NULL): the calling thread's
+ * last failed tx_mesh_create (no handle was made), else "null handle". */
 const char* tx_last_error(tx_handle h);
 
 /* Mesh sizes: bricks, elements, vertices (global), blocks. */

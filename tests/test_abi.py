@@ -97,3 +97,22 @@ def test_two_phase_fit_is_a_host_query():
         assert lib.tx_eval_gather_supported(conn.h, C.byref(ok)) == 0 and ok.value == fits
     tx.DOFManager(conn, A.equation_set(A.TX_PHYS_HEAT, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0)), require_device=False)
     assert lib.tx_eval_gather_supported(conn.h, C.byref(ok)) == 0 and ok.value == 1
+
+
+def test_size_limits_are_refused_before_allocation():
+    """Index widths: vertex and DOF numbers are int32 on the device (CRS column indices), so a lattice with
+    2^31 or more vertices is refused at creation, from its sizes alone, and block counts above
+    TX_MAX_BLOCKS likewise."""
+    import time
+
+    import pytest
+    import tianxin_gb300 as tx
+    from tianxin_gb300 import _abi as A
+    t0 = time.perf_counter()
+    with pytest.raises(tx.TxError) as e:
+        tx.CartesianConnManager(1291, 1291, 1291)  # 1292^3 = 2.16e9 vertices
+    assert e.value.code == A.TX_EINVAL and "2^31" in str(e.value)
+    assert time.perf_counter() - t0 < 5.0
+    with pytest.raises(tx.TxError) as e:
+        tx.CartesianConnManager(2, 2, 2, 3, 3, 1)  # nine blocks
+    assert "too many blocks" in str(e.value)

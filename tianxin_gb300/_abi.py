@@ -155,7 +155,7 @@ def mesh_desc(n, blocks=(1, 1, 1), topology=TX_TOPO_HEX, lengths=(1.0, 1.0, 1.0)
     d.bx, d.by, d.bz = blocks
     nb = blocks[0] * blocks[1] * blocks[2]
     topo = [topology] * nb if isinstance(topology, int) else list(topology)
-    for i, t in enumerate(topo):
+    for i, t in enumerate(topo[:TX_MAX_BLOCKS]):  # more blocks: the library refuses the description
         d.block_topology[i] = t
     d.lx, d.ly, d.lz = lengths
     d.jitter = jitter

@@ -197,6 +197,12 @@ struct tx_handle_s {
 
 namespace {
 
+// The calling thread's last failed tx_mesh_create message.
+std::string& create_error() {
+  thread_local std::string e;
+  return e;
+}
+
 int fail(tx_handle h, int code, const std::string& msg) {
   if (h) h->err = msg;
   return code;
@@ -594,7 +600,10 @@ int tx_mesh_create(const tx_mesh_desc* desc, tx_handle* out) {
     tx::build_mesh(h->mesh, *desc);
     return TX_OK;
   });
-  if (rc) return rc;  // message is lost with the handle; sizes were invalid
+  if (rc) {  // no handle: the message stays with the calling thread (tx_last_error(NULL))
+    create_error() = h->err;
+    return rc;
+  }
   *out = h.release();
   return TX_OK;
 }
@@ -733,7 +742,10 @@ int tx_mesh_set_entries(tx_handle h, int32_t kind, int32_t k, int64_t* entries) 
 
 void tx_destroy(tx_handle h) { delete h; }
 
-const char* tx_last_error(tx_handle h) { return h ? h->err.c_str() : "null handle"; }
+const char* tx_last_error(tx_handle h) {
+  if (h) return h->err.c_str();
+  return create_error().empty() ? "null handle" : create_error().c_str();
+}
 
 int tx_mesh_sizes(tx_handle h, int64_t* n_elements, int64_t* n_vertices, int32_t* n_blocks) {
   if (!h) return TX_EINVAL;

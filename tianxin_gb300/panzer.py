@@ -52,7 +52,7 @@ class CartesianConnManager:
         h = C.c_void_p()
         rc = self.lib.tx_mesh_create(C.byref(self.desc), C.byref(h))
         if rc != 0:
-            raise TxError(rc, "tx_mesh_create: invalid mesh description")
+            raise TxError(rc, "tx_mesh_create: " + self.lib.tx_last_error(None).decode())
         self.h = h
         ne, nv, nb = C.c_int64(), C.c_int64(), C.c_int32()
         self.lib.tx_mesh_sizes(self.h, C.byref(ne), C.byref(nv), C.byref(nb))
