@@ -373,6 +373,12 @@ int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowpt
 /* The operator lies on the handle's graph: the solver's SpMVs take the
  * entity-block form of TX_SPMV_ENTITY_BLOCKS. */
 #define TX_SOLVE_ENTITY_BLOCKS 0x8u
+/* Inner preconditioner with TX_SOLVE_ENTITY_BLOCKS and three fields an
+ * entity: the inverses of the 3x3 entity diagonal blocks (block Jacobi,
+ * Dirichlet rows and columns eliminated, inverted in FP64, applied in FP32)
+ * instead of the diagonal; otherwise ignored.  Same solution, fewer inner
+ * iterations on vector problems such as elasticity. */
+#define TX_SOLVE_BLOCK_JACOBI 0x10u
 typedef struct tx_solve_args {
   const int64_t* rowptr; const int32_t* colind; const double* vals;
   const double* b;         /* right-hand side (ignored with MATRIX_FREE: b = -f(x0)) */

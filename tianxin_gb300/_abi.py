@@ -44,6 +44,7 @@ TX_SOLVE_MATRIX_FREE_RESIDUAL = 0x1
 TX_SOLVE_FIXED_ITERATIONS = 0x2
 TX_SOLVE_REUSE_OPERATOR = 0x4
 TX_SOLVE_ENTITY_BLOCKS = 0x8
+TX_SOLVE_BLOCK_JACOBI = 0x10
 
 TX_INTEGRAND_FIELD = 1
 TX_INTEGRAND_L2_ERROR = 2

@@ -1001,7 +1001,7 @@ int tx_solve_cg_ir(tx_handle h, tx_solve_args* a) {
                            a->inner_rtol > 0 ? a->inner_rtol : 1e-5, a->max_outer > 0 ? a->max_outer : 50,
                            a->max_inner > 0 ? a->max_inner : 100000, a->stats, h->stream, err,
                            (a->flags & TX_SOLVE_FIXED_ITERATIONS) != 0, (a->flags & TX_SOLVE_REUSE_OPERATOR) != 0,
-                           a->stats_device, eg);
+                           a->stats_device, eg, (a->flags & TX_SOLVE_BLOCK_JACOBI) != 0);
   if (rc == TX_ETIMEDOUT) return fail(h, rc, "tx_solve_cg_ir: did not reach rtol within max_outer iterations");
   if (rc) return fail(h, rc, err);
   return TX_OK;

@@ -180,6 +180,8 @@ struct SolverWork {
   int64_t n = 0, nnz = 0;
   float* vals32 = nullptr;     // FP32 Jacobian with symmetric Dirichlet elimination
   float* dinv = nullptr;       // Jacobi preconditioner
+  float* binv = nullptr;       // block Jacobi: inverses of the 3x3 entity diagonal blocks [n / 3][9]
+  bool binv_valid = false;     // binv belongs to the current FP32 operator
   float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *d = nullptr;
   double* r64 = nullptr;       // outer residual
   double* xdw = nullptr;       // x_dot work vector of implicit integration
@@ -204,7 +206,7 @@ int solve_cg_ir(SolverWork& w, const int64_t* rowptr, const int32_t* colind, con
                 int64_t n_dir, const int32_t* dir_lids, double* x, ResidualFn resid, void* ctx,
                 double rtol, double inner_rtol, int max_outer, int max_inner, double* stats,
                 cudaStream_t s, std::string& err, bool fixed, bool reuse_op, double* stats_dev,
-                const EntityGraph* eg = nullptr);
+                const EntityGraph* eg = nullptr, bool block_jacobi = false);
 
 // Vector helpers used by the API layer
 cudaError_t launch_fill(double* p, double v, int64_t n, cudaStream_t s);

@@ -473,6 +473,51 @@ __global__ void k_make_f32(int64_t n, const int64_t* __restrict__ rp, const int3
   }
 }
 
+// Block Jacobi: per entity the inverse of its 3x3 diagonal block (row (r, c),
+// neighbour r, field d at rp[3r + c] + 3 j0 + d, j0 = r's place in its own
+// row), with Dirichlet rows and columns made identity as in k_make_f32;
+// inverted in FP64 by cofactors, a singular block falls back to its diagonal.
+__global__ void k_make_binv(int64_t n_ent, const int64_t* __restrict__ erp, const int32_t* __restrict__ ecol,
+                            const int64_t* __restrict__ rp, const double* __restrict__ v64,
+                            const uint8_t* __restrict__ mask, float* __restrict__ binv) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_ent; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t j0 = -1;
+    for (int64_t k = erp[r]; k < erp[r + 1]; ++k)
+      if (ecol[k] == r) { j0 = k - erp[r]; break; }
+    double B[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        double v = j0 >= 0 ? v64[rp[3 * r + c] + 3 * j0 + d] : (c == d ? 1.0 : 0.0);
+        if (mask[3 * r + c] || mask[3 * r + d]) v = c == d ? 1.0 : 0.0;
+        B[c][d] = v;
+      }
+    const double c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1], c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2],
+                 c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+    const double det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
+    float* o = binv + 9 * r;
+    const double scale = fabs(B[0][0]) + fabs(B[1][1]) + fabs(B[2][2]);
+    if (det != 0.0 && isfinite(det) && fabs(det) > 1e-30 * scale * scale * scale) {
+      const double id = 1.0 / det;
+      o[0] = (float)(c00 * id);
+      o[1] = (float)((B[0][2] * B[2][1] - B[0][1] * B[2][2]) * id);
+      o[2] = (float)((B[0][1] * B[1][2] - B[0][2] * B[1][1]) * id);
+      o[3] = (float)(c01 * id);
+      o[4] = (float)((B[0][0] * B[2][2] - B[0][2] * B[2][0]) * id);
+      o[5] = (float)((B[0][2] * B[1][0] - B[0][0] * B[1][2]) * id);
+      o[6] = (float)(c02 * id);
+      o[7] = (float)((B[0][1] * B[2][0] - B[0][0] * B[2][1]) * id);
+      o[8] = (float)((B[0][0] * B[1][1] - B[0][1] * B[1][0]) * id);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) o[k] = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[4 * c] = B[c][c] != 0.0 ? (float)(1.0 / B[c][c]) : 1.0f;
+    }
+  }
+}
+
 __global__ void k_mask(int64_t n, const int32_t* lids, uint8_t* mask) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     mask[lids[i]] = 1;
@@ -497,6 +542,67 @@ __global__ void k_cg_init(int64_t n, const double* __restrict__ r64, const uint8
   }
   rz = block_sum(rz, sh);
   if (threadIdx.x == 0) red[0 * kRedBlocks + blockIdx.x] = rz;
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) red[1 * kRedBlocks + blockIdx.x] = rr;
+}
+
+// Block-Jacobi forms of k_cg_init / k_cg_update: one thread per entity, z = B^-1 r on its three DOFs.
+__device__ __forceinline__ void block_apply(const float* __restrict__ bi, const float (&r)[3], float (&z)[3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) z[c] = bi[3 * c] * r[0] + bi[3 * c + 1] * r[1] + bi[3 * c + 2] * r[2];
+}
+
+__global__ void k_cg_init_b(int64_t n_ent, const double* __restrict__ r64, const uint8_t* __restrict__ mask,
+                            const float* __restrict__ binv, float* r, float* z, float* p, float* d, double* red) {
+  __shared__ double sh[32];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_ent; e += (int64_t)gridDim.x * blockDim.x) {
+    float ri[3], zi[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) ri[c] = mask[3 * e + c] ? 0.0f : (float)r64[3 * e + c];
+    block_apply(binv + 9 * e, ri, zi);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t i = 3 * e + c;
+      r[i] = ri[c]; z[i] = zi[c]; p[i] = zi[c]; d[i] = 0.0f;
+      const double rd = widen(ri[c]);
+      rz += rd * widen(zi[c]);
+      rr += rd * rd;
+    }
+  }
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) red[0 * kRedBlocks + blockIdx.x] = rz;
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) red[1 * kRedBlocks + blockIdx.x] = rr;
+}
+
+__global__ void k_cg_update_b(int64_t n_ent, const double* __restrict__ scal, const float* __restrict__ binv,
+                              const float* __restrict__ p, const float* __restrict__ q, float* r, float* z, float* d,
+                              double* red) {
+  __shared__ double sh[32];
+  const double pq = scal[2];
+  const float a = pq != 0.0 ? (float)(scal[0] / pq) : 0.0f;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_ent; e += (int64_t)gridDim.x * blockDim.x) {
+    float ri[3], zi[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t i = 3 * e + c;
+      d[i] += a * p[i];
+      ri[c] = r[i] - a * q[i];
+    }
+    block_apply(binv + 9 * e, ri, zi);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t i = 3 * e + c;
+      r[i] = ri[c]; z[i] = zi[c];
+      const double rd = widen(ri[c]);
+      rz += rd * widen(zi[c]);
+      rr += rd * rd;
+    }
+  }
+  rz = block_sum(rz, sh);
+  if (threadIdx.x == 0) red[3 * kRedBlocks + blockIdx.x] = rz;
   rr = block_sum(rr, sh);
   if (threadIdx.x == 0) red[1 * kRedBlocks + blockIdx.x] = rr;
 }
@@ -700,6 +806,7 @@ cudaError_t solver_alloc(SolverWork& w, int64_t n, int64_t nnz) {
   cudaError_t e;
   if ((e = cmalloc(w.vals32, nnz)) != cudaSuccess) return e;
   if ((e = cmalloc(w.dinv, n)) != cudaSuccess) return e;
+  if ((e = cmalloc(w.binv, 3 * n)) != cudaSuccess) return e;
   if ((e = cmalloc(w.r, n)) != cudaSuccess) return e;
   if ((e = cmalloc(w.z, n)) != cudaSuccess) return e;
   if ((e = cmalloc(w.p, n)) != cudaSuccess) return e;
@@ -717,7 +824,7 @@ cudaError_t solver_alloc(SolverWork& w, int64_t n, int64_t nnz) {
 }
 
 void solver_free(SolverWork& w) {
-  cudaFree(w.vals32); cudaFree(w.dinv); cudaFree(w.r); cudaFree(w.z); cudaFree(w.p); cudaFree(w.q);
+  cudaFree(w.vals32); cudaFree(w.dinv); cudaFree(w.binv); cudaFree(w.r); cudaFree(w.z); cudaFree(w.p); cudaFree(w.q);
   cudaFree(w.d); cudaFree(w.r64); cudaFree(w.xdw); cudaFree(w.mask); cudaFree(w.red); cudaFree(w.scal);
   if (w.host_scal) cudaFreeHost(w.host_scal);
   w = SolverWork();
@@ -771,7 +878,7 @@ struct DotEntityLaunch {
 int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const double* vals, int64_t n_dir,
                 const int32_t* dir, double* x, ResidualFn resid, void* ctx, double rtol, double inner_rtol,
                 int max_outer, int max_inner, double* stats, cudaStream_t s, std::string& err, bool fixed,
-                bool reuse_op, double* stats_dev, const EntityGraph* eg) {
+                bool reuse_op, double* stats_dev, const EntityGraph* eg, bool block_jacobi) {
   const int64_t n = w.n;
   const unsigned gb = kRedBlocks;
   auto cuda_fail = [&](cudaError_t e, const char* where) {
@@ -785,7 +892,20 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     if (n_dir > 0) k_mask<<<grid_for(n_dir, kThreads), kThreads, 0, s>>>(n_dir, dir, w.mask);
     k_make_f32<<<grid_for(n, kThreads / 32), kThreads, 0, s>>>(n, rp, col, vals, w.mask, w.vals32, w.dinv);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: make_f32");
+    w.binv_valid = false;
   }
+  // block Jacobi: the entity-block form's three-field rows only
+  const bool blk = block_jacobi && eg && n == 3 * eg->n_ent;
+  if (blk && !w.binv_valid) {
+    k_make_binv<<<grid_for(eg->n_ent, kThreads), kThreads, 0, s>>>(eg->n_ent, eg->erp, eg->ecol, rp, vals, w.mask,
+                                                                   w.binv);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "cg: make_binv");
+    w.binv_valid = true;
+  }
+  auto cg_init = [&]() {
+    if (blk) k_cg_init_b<<<gb, kThreads, 0, s>>>(eg->n_ent, w.r64, w.mask, w.binv, w.r, w.z, w.p, w.d, w.red);
+    else k_cg_init<<<gb, kThreads, 0, s>>>(n, w.r64, w.mask, w.dinv, w.r, w.z, w.p, w.d, w.red);
+  };
   SpmvShape shape = resolve_shape(w.spmv, n, w.nnz, true);
   if (shape.unroll == kSpmvVector && !chunk_aligned<float>(w.vals32, col)) shape.unroll = 1;
   const SpmvShape eshape = resolve_entity_shape(w.spmv_eb, true);
@@ -808,7 +928,8 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
   auto cg_iteration = [&]() {
     spmv_dot();
     k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2, (int)gd);  // pq
-    k_cg_update<<<gb, kThreads, 0, s>>>(n, w.scal, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
+    if (blk) k_cg_update_b<<<gb, kThreads, 0, s>>>(eg->n_ent, w.scal, w.binv, w.p, w.q, w.r, w.z, w.d, w.red);
+    else k_cg_update<<<gb, kThreads, 0, s>>>(n, w.scal, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
     k_cg_finish<<<1, 1024, 0, s>>>(w.scal, w.red);
     k_cg_pupdate<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, w.scal, w.z, w.p);
   };
@@ -820,7 +941,7 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
       if (rc) { err = "cg: residual evaluation failed"; return rc; }
       if (outer == 0 && (e = launch_norm2sq(w.r64, n, w.red, w.scal + 5, s)) != cudaSuccess)
         return cuda_fail(e, "cg: norm");
-      k_cg_init<<<gb, kThreads, 0, s>>>(n, w.r64, w.mask, w.dinv, w.r, w.z, w.p, w.d, w.red);
+      cg_init();
       k_finalize<<<1, 1024, 0, s>>>(w.red, 2, w.scal);
       for (int it = 0; it < max_inner; ++it) cg_iteration();
       k_add_f32<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, x, w.d);
@@ -844,7 +965,7 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     if (r0 < 0.0) r0 = rn > 0.0 ? rn : 1.0;
     if (rn <= rtol * r0 || outer >= max_outer) break;
     // inner FP32 Jacobi-PCG on A32 d = r
-    k_cg_init<<<gb, kThreads, 0, s>>>(n, w.r64, w.mask, w.dinv, w.r, w.z, w.p, w.d, w.red);
+    cg_init();
     k_finalize<<<1, 1024, 0, s>>>(w.red, 2, w.scal);  // scal[0] = rz, scal[1] = rr
     cudaMemcpyAsync(w.host_scal, w.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cg: init");

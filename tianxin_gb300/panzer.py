@@ -760,8 +760,11 @@ class ModelEvaluator:
 
     def solve(self, W, x, b=None, rtol=1e-10, inner_rtol=1e-5, max_outer=50, max_inner=100000, matrix_free=False,
               x_dot=None, alpha=0.0, beta=1.0, t=0.0, fixed=False, reuse_operator=False, stats_device=None,
-              x_pred=None, x_dot_coef=0.0):
+              x_pred=None, x_dot_coef=0.0, block_jacobi=False):
         """FP64 iterative refinement around FP32 Jacobi-CG; x updated in place. Returns stats.
+
+        block_jacobi=True preconditions with the 3x3 entity diagonal blocks when W applies in the
+        entity-block form (three-field problems), the diagonal otherwise.
 
         fixed=True runs exactly max_outer x max_inner iterations without host
         reads (capturable); its statistics go to stats_device (device f64[4]).
@@ -777,7 +780,8 @@ class ModelEvaluator:
         a.flags = ((_abi.TX_SOLVE_MATRIX_FREE_RESIDUAL if matrix_free else 0) |
                    (_abi.TX_SOLVE_FIXED_ITERATIONS if fixed else 0) |
                    (_abi.TX_SOLVE_REUSE_OPERATOR if reuse_operator else 0) |
-                   (_abi.TX_SOLVE_ENTITY_BLOCKS if getattr(W, "apply_form", "crs") == "entity" else 0))
+                   (_abi.TX_SOLVE_ENTITY_BLOCKS if getattr(W, "apply_form", "crs") == "entity" else 0) |
+                   (_abi.TX_SOLVE_BLOCK_JACOBI if block_jacobi else 0))
         a.x_dot, a.alpha, a.beta, a.t = _ptr(x_dot), alpha, beta, t
         a.stats_device = _ptr(stats_device)
         a.x_pred, a.x_dot_coef = _ptr(x_pred), x_dot_coef
