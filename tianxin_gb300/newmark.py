@@ -10,7 +10,8 @@ the acceleration is passed in the x_dot slot and
 
 For a step with a = c (u - u_pred), c = 1/(beta_N dt^2), evalModel with
 alpha = c, beta = 1 gives the effective Jacobian K_eff = K + c M.  The step
-(predictor, FP64-refined FP32 Jacobi-CG on K_eff, corrector) has no host
+(predictor, FP64-refined FP32 CG on K_eff, block-Jacobi preconditioned on the
+entity-block form, corrector) has no host
 synchronisation and is captured once as a CUDA graph, then replayed.
 
 The refinement residual is FP64.  For a linear problem (linear=True, the
@@ -23,9 +24,10 @@ import torch
 
 
 class NewmarkElastodynamics:
-    def __init__(self, me, dt, beta=0.25, gamma=0.5, mixed=True, outer=3, inner=24, linear=True):
+    def __init__(self, me, dt, beta=0.25, gamma=0.5, mixed=True, outer=3, inner=24, linear=True, block_jacobi=True):
         self.me, self.dt, self.beta_n, self.gamma_n = me, dt, beta, gamma
         self.mixed, self.outer, self.inner, self.linear = mixed, outer, inner, linear
+        self.block_jacobi = block_jacobi  # 3x3 block-Jacobi inner CG on the entity-block form
         self.c = 1.0 / (beta * dt * dt)
         lof = me.lof
         z = lof.getTpetraVector
@@ -63,10 +65,10 @@ class NewmarkElastodynamics:
         self.x.copy_(self.u)
         if self.linear:
             self._rhs(self.u)
-            self.me.solve(self.W, self.x, b=self.b, fixed=True, max_outer=1, max_inner=1, stats_device=self.stats)
+            self.me.solve(self.W, self.x, b=self.b, fixed=True, max_outer=1, max_inner=1, stats_device=self.stats, block_jacobi=self.block_jacobi)
         else:
             self.me.solve(self.W, self.x, matrix_free=True, fixed=True, max_outer=1, max_inner=1,
-                          stats_device=self.stats, x_pred=self.u, x_dot_coef=self.c, alpha=self.c, beta=1.0)
+                          stats_device=self.stats, block_jacobi=self.block_jacobi, x_pred=self.u, x_dot_coef=self.c, alpha=self.c, beta=1.0)
 
     def _rhs(self, u_pred):
         """b = F + c M u_pred (FP64 SpMV)."""
@@ -82,10 +84,10 @@ class NewmarkElastodynamics:
         if self.linear:
             self._rhs(self.u_pred)
             self.me.solve(self.W, self.x, b=self.b, fixed=True, reuse_operator=True, max_outer=self.outer,
-                          max_inner=self.inner, stats_device=self.stats)
+                          max_inner=self.inner, stats_device=self.stats, block_jacobi=self.block_jacobi)
         else:
             self.me.solve(self.W, self.x, matrix_free=True, fixed=True, reuse_operator=True, max_outer=self.outer,
-                          max_inner=self.inner, stats_device=self.stats, x_pred=self.u_pred, x_dot_coef=self.c,
+                          max_inner=self.inner, stats_device=self.stats, block_jacobi=self.block_jacobi, x_pred=self.u_pred, x_dot_coef=self.c,
                           alpha=self.c, beta=1.0)
         torch.sub(self.x, self.u_pred, out=self.a)
         self.a.mul_(self.c)
