@@ -348,7 +348,18 @@ def run_ours(a):
                  "seconds": ts, "residual": "FP64 matrix-free (Residual evaluation)",
                  "inner": "FP32 CG, 3x3 block-Jacobi preconditioner (point Jacobi without the entity form)",
                  "max_u": float(xsol.abs().max())}
-        del xsol
+        # the mixed path against the FP64 path at full size: both Jacobians (FP32 element math with FP64
+        # sums, and FP64-plain) refined with the same FP64 residual to 1e-12; their solutions' difference
+        sols = []
+        for mixed in (True, False):
+            xs = lof.getTpetraVector()
+            me.evalModel(xs, f=f, W=W, mixed=mixed)
+            st2 = me.solve(W, xs, rtol=1e-12, inner_rtol=1e-5, matrix_free=True, max_outer=40, block_jacobi=True)
+            sols.append((xs, st2["relres"]))
+        (xm, rm), (xd, rd) = sols
+        solve["mixed_vs_fp64"] = {"rtol": 1e-12, "relres": [rm, rd],
+                                  "solution_maxrel": float((xm - xd).abs().max() / xd.abs().max())}
+        del xsol, xm, xd, sols
 
     # ---- e2e through the public API with host buffers
     e2e = None
