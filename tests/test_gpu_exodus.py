@@ -70,6 +70,16 @@ def test_quadratic_exodus_mesh_reproduces_the_lattice_path(cuda, tmp_path, topo,
     assert np.array_equal(d0.getOwnedIndices(), d1.getOwnedIndices())
     assert np.array_equal(v0, v1)
     assert np.abs(f0 - f1).max() <= 1e-15 * np.abs(f0).max()
+    # responses over the quadratic field: block integrals, a side-set integral, the extreme value
+    x = torch.from_numpy(x_np).cuda()
+    for b in range(len(blocks)):
+        r0 = tx.Response(d0, "Field", block=b).value(x)
+        r1 = tx.Response(d1, "Field", block=b).value(x)
+        assert abs(r0 - r1) <= 1e-14 * max(1.0, abs(r0))
+        s0 = tx.Response(d0, "Field", block=b, side_mask=A.SIDE_ZMAX).value(x)
+        s1 = tx.Response(d1, "Field", block=b, side_set="zmax").value(x)
+        assert abs(s0 - s1) <= 1e-14 * max(1.0, abs(s0))
+    assert tx.Response(d0, "Max").value(x) == tx.Response(d1, "Max").value(x)
 
 
 def test_renumbered_nodes_keep_lid_order_results(cuda, tmp_path):
