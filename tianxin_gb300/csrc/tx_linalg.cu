@@ -415,6 +415,23 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return v;
 }
 
+// block_sum with the total in every thread.
+__device__ __forceinline__ double block_sum_all(double v, double* sh) {
+  v = block_sum(v, sh);
+  __syncthreads();  // every read of sh in block_sum is done
+  if (threadIdx.x == 0) sh[0] = v;
+  __syncthreads();
+  return sh[0];
+}
+
+// The sum of nparts partials in every thread, in one fixed order: every CTA
+// that reduces the same partials gets the same bits.
+__device__ __forceinline__ double partials_sum(const double* __restrict__ part, int nparts, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += part[i];
+  return block_sum_all(v, sh);
+}
+
 // Sums the first nparts partials of each of nslots slots.
 __global__ void k_finalize(const double* __restrict__ red, int nslots, double* __restrict__ out,
                            int nparts = kRedBlocks) {
@@ -576,12 +593,12 @@ __global__ void k_cg_init_b(int64_t n_ent, const double* __restrict__ r64, const
   if (threadIdx.x == 0) red[1 * kRedBlocks + blockIdx.x] = rr;
 }
 
-__global__ void k_cg_update_b(int64_t n_ent, const double* __restrict__ scal, const float* __restrict__ binv,
-                              const float* __restrict__ p, const float* __restrict__ q, float* r, float* z, float* d,
-                              double* red) {
+__global__ void k_cg_update_b(int64_t n_ent, const double* __restrict__ rz_in, const double* __restrict__ pq_part,
+                              int pq_parts, const float* __restrict__ binv, const float* __restrict__ p,
+                              const float* __restrict__ q, float* r, float* z, float* d, double* red) {
   __shared__ double sh[32];
-  const double pq = scal[2];
-  const float a = pq != 0.0 ? (float)(scal[0] / pq) : 0.0f;
+  const double pq = partials_sum(pq_part, pq_parts, sh);
+  const float a = pq != 0.0 ? (float)(*rz_in / pq) : 0.0f;
   double rz = 0.0, rr = 0.0;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_ent; e += (int64_t)gridDim.x * blockDim.x) {
     float ri[3], zi[3];
@@ -670,13 +687,14 @@ __global__ void __launch_bounds__(kThreads, entity_min_blocks(G, U)) k_spmv_dot_
   if (threadIdx.x == 0) red[2 * kRedBlocks + blockIdx.x] = pq;
 }
 
-// scal: [0] rz, [1] rr, [2] pq.  d += a p, r -= a q, z = dinv r; partial rz', rr'
-__global__ void k_cg_update(int64_t n, const double* __restrict__ scal, const float* __restrict__ dinv,
-                            const float* __restrict__ p, const float* __restrict__ q, float* r, float* z, float* d,
-                            double* red) {
+// a = rz / pq (pq from the SpMV's partials, reduced by every CTA); d += a p,
+// r -= a q, z = dinv r; partials of rz' and rr'
+__global__ void k_cg_update(int64_t n, const double* __restrict__ rz_in, const double* __restrict__ pq_part,
+                            int pq_parts, const float* __restrict__ dinv, const float* __restrict__ p,
+                            const float* __restrict__ q, float* r, float* z, float* d, double* red) {
   __shared__ double sh[32];
-  const double pq = scal[2];
-  const float a = pq != 0.0 ? (float)(scal[0] / pq) : 0.0f;
+  const double pq = partials_sum(pq_part, pq_parts, sh);
+  const float a = pq != 0.0 ? (float)(*rz_in / pq) : 0.0f;
   double rz = 0.0, rr = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     d[i] += a * p[i];
@@ -693,26 +711,21 @@ __global__ void k_cg_update(int64_t n, const double* __restrict__ scal, const fl
   if (threadIdx.x == 0) red[1 * kRedBlocks + blockIdx.x] = rr;
 }
 
-// new scalars: rz' = sum slot 3, rr' = slot 1; beta = rz'/rz; p = z + beta p; scal[0] = rz'
-__global__ void k_cg_finish(double* scal, const double* __restrict__ red) {
+// rz' = sum of the update's slot-3 partials (reduced by every CTA), beta =
+// rz' / rz; p = z + beta p.  CTA 0 stores rz' in the other parity's slot
+// (rz_out; every CTA reads rz from rz_in, which nothing writes here) and rr'
+// for the host's convergence check.
+__global__ void k_cg_pupdate(int64_t n, const double* __restrict__ rz_in, const double* __restrict__ red,
+                             double* __restrict__ rz_out, double* __restrict__ rr_out, const float* __restrict__ z,
+                             float* p) {
   __shared__ double sh[32];
-  double rz = 0.0, rr = 0.0;
-  for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) {
-    rz += red[3 * kRedBlocks + i];
-    rr += red[1 * kRedBlocks + i];
+  const double rz = partials_sum(red + 3 * kRedBlocks, kRedBlocks, sh);
+  const double rzo = *rz_in;
+  const float be = rzo != 0.0 ? (float)(rz / rzo) : 0.0f;
+  if (blockIdx.x == 0) {
+    const double rr = partials_sum(red + 1 * kRedBlocks, kRedBlocks, sh);
+    if (threadIdx.x == 0) { *rz_out = rz; *rr_out = rr; }
   }
-  rz = block_sum(rz, sh);
-  __syncthreads();
-  rr = block_sum(rr, sh);
-  if (threadIdx.x == 0) {
-    scal[3] = scal[0] != 0.0 ? rz / scal[0] : 0.0;  // beta
-    scal[0] = rz;
-    scal[1] = rr;
-  }
-}
-
-__global__ void k_cg_pupdate(int64_t n, const double* __restrict__ scal, const float* __restrict__ z, float* p) {
-  const float be = (float)scal[3];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = z[i] + be * p[i];
 }
@@ -925,13 +938,23 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     if (eg) with_entity_shape(eshape, DotEntityLaunch{*eg, &w, gd, s});
     else with_shape(shape, DotLaunch{n, rp, col, &w, gd, s});
   };
+  // Three launches an iteration: SpMV + dot partials, the update (reducing the
+  // dot itself), the p update (reducing rz' itself).  rz alternates between
+  // scal[0] and scal[6] by iteration parity, so no CTA reads a slot another
+  // CTA of the same launch writes; an inner solve starts at parity 0 (the
+  // initialisation's rz in scal[0]); rr is in scal[1].
+  int par = 0;
+  auto rz_slot = [&](int q) { return w.scal + (q ? 6 : 0); };
   auto cg_iteration = [&]() {
     spmv_dot();
-    k_finalize<<<1, 1024, 0, s>>>(w.red + 2 * kRedBlocks, 1, w.scal + 2, (int)gd);  // pq
-    if (blk) k_cg_update_b<<<gb, kThreads, 0, s>>>(eg->n_ent, w.scal, w.binv, w.p, w.q, w.r, w.z, w.d, w.red);
-    else k_cg_update<<<gb, kThreads, 0, s>>>(n, w.scal, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
-    k_cg_finish<<<1, 1024, 0, s>>>(w.scal, w.red);
-    k_cg_pupdate<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, w.scal, w.z, w.p);
+    const double* pq_part = w.red + 2 * kRedBlocks;
+    if (blk)
+      k_cg_update_b<<<gb, kThreads, 0, s>>>(eg->n_ent, rz_slot(par), pq_part, (int)gd, w.binv, w.p, w.q, w.r, w.z,
+                                            w.d, w.red);
+    else
+      k_cg_update<<<gb, kThreads, 0, s>>>(n, rz_slot(par), pq_part, (int)gd, w.dinv, w.p, w.q, w.r, w.z, w.d, w.red);
+    k_cg_pupdate<<<gb, kThreads, 0, s>>>(n, rz_slot(par), w.red, rz_slot(par ^ 1), w.scal + 1, w.z, w.p);
+    par ^= 1;
   };
   if (fixed) {
     // Capturable form: exact iteration counts, no host reads; statistics
@@ -943,6 +966,7 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
         return cuda_fail(e, "cg: norm");
       cg_init();
       k_finalize<<<1, 1024, 0, s>>>(w.red, 2, w.scal);
+      par = 0;
       for (int it = 0; it < max_inner; ++it) cg_iteration();
       k_add_f32<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, x, w.d);
     }
@@ -967,6 +991,7 @@ int solve_cg_ir(SolverWork& w, const int64_t* rp, const int32_t* col, const doub
     // inner FP32 Jacobi-PCG on A32 d = r
     cg_init();
     k_finalize<<<1, 1024, 0, s>>>(w.red, 2, w.scal);  // scal[0] = rz, scal[1] = rr
+    par = 0;
     cudaMemcpyAsync(w.host_scal, w.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cg: init");
     const double rr0 = w.host_scal[1];
