@@ -228,8 +228,14 @@ static void eval_hgrad(const BasisDef& B, const double xi[3], double* N, double 
 }
 
 // Lowest-order Nedelec hex: values and reference curls at xi.  Function i
-// is tangential to shards edge i, oriented first->second vertex, with unit
-// tangential moment over the edge.
+// is tangential to shards edge i, oriented first->second vertex, dual to the
+// degrees of freedom L_j(u) = u(m_j) . t_j, m_j the midpoint of edge j and t_j
+// its reference tangent (half the edge vector, a unit vector on [-1,1]^3).
+// That is the quadrilateral convention the reference pins
+// (disc-fe/test/core_tests/basis_values2.cpp:404-406: value -0.5 (y - 1) and
+// curl 0.5 for quad edge 0), and it makes the tangential trace of every hex
+// function on a face the quadrilateral function of that face's edge:
+// function 0 = (1 - y)(1 - z)/4 e_x restricted to z = -1 is 0.5 (1 - y) e_x.
 static void eval_hcurl_hex(const double xi[3], double (*V)[3], double (*C)[3]) {
   const double x = xi[0], y = xi[1], z = xi[2];
   for (int i = 0; i < 12; ++i)
@@ -239,29 +245,29 @@ static void eval_hcurl_hex(const double xi[3], double (*V)[3], double (*C)[3]) {
   const int xs[4][3] = {{-1, -1, 1}, {1, -1, -1}, {-1, 1, 1}, {1, 1, -1}};  // sy, sz, direction
   for (int k = 0; k < 4; ++k) {
     double sy = xs[k][0], sz = xs[k][1], dir = xs[k][2];
-    V[xe[k]][0] = dir * (1 + sy * y) * (1 + sz * z) / 8.0;
+    V[xe[k]][0] = dir * (1 + sy * y) * (1 + sz * z) / 4.0;
     // curl of (f,0,0) = (0, df/dz, -df/dy)
-    C[xe[k]][1] = dir * (1 + sy * y) * sz / 8.0;
-    C[xe[k]][2] = -dir * sy * (1 + sz * z) / 8.0;
+    C[xe[k]][1] = dir * (1 + sy * y) * sz / 4.0;
+    C[xe[k]][2] = -dir * sy * (1 + sz * z) / 4.0;
   }
   // y-directed edges 1 (x+,z-,+y) 3 (x-,z-,-y) 5 (x+,z+,+y) 7 (x-,z+,-y)
   const int ye[4] = {1, 3, 5, 7};
   const int ys[4][3] = {{1, -1, 1}, {-1, -1, -1}, {1, 1, 1}, {-1, 1, -1}};  // sx, sz, direction
   for (int k = 0; k < 4; ++k) {
     double sx = ys[k][0], sz = ys[k][1], dir = ys[k][2];
-    V[ye[k]][1] = dir * (1 + sx * x) * (1 + sz * z) / 8.0;
+    V[ye[k]][1] = dir * (1 + sx * x) * (1 + sz * z) / 4.0;
     // curl of (0,g,0) = (-dg/dz, 0, dg/dx)
-    C[ye[k]][0] = -dir * (1 + sx * x) * sz / 8.0;
-    C[ye[k]][2] = dir * sx * (1 + sz * z) / 8.0;
+    C[ye[k]][0] = -dir * (1 + sx * x) * sz / 4.0;
+    C[ye[k]][2] = dir * sx * (1 + sz * z) / 4.0;
   }
   // z-directed edges 8..11 at (x,y) = (-,-), (+,-), (+,+), (-,+), all +z
   const int zs[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
   for (int k = 0; k < 4; ++k) {
     double sx = zs[k][0], sy = zs[k][1];
-    V[8 + k][2] = (1 + sx * x) * (1 + sy * y) / 8.0;
+    V[8 + k][2] = (1 + sx * x) * (1 + sy * y) / 4.0;
     // curl of (0,0,h) = (dh/dy, -dh/dx, 0)
-    C[8 + k][0] = (1 + sx * x) * sy / 8.0;
-    C[8 + k][1] = -sx * (1 + sy * y) / 8.0;
+    C[8 + k][0] = (1 + sx * x) * sy / 4.0;
+    C[8 + k][1] = -sx * (1 + sy * y) / 4.0;
   }
 }
 
@@ -499,7 +505,7 @@ struct DofManager {
   std::vector<std::vector<LO>> elementLIDs;
   std::vector<std::vector<std::vector<int>>> offsets;    // [block][field][basis]
   std::vector<GO> owned;                                  // LID -> GID
-  std::unordered_map<GO, LO> g2l;
+  std::vector<LO> g2l;                                    // GID -> LID (GIDs are 0..N-1 on one rank)
   // graph
   std::vector<int64_t> rowptr;
   std::vector<LO> colind;
@@ -549,19 +555,17 @@ static void build_dofs(const Topology& T, DofManager& D, const tx_equation_set_d
     for (LO e : T.block_elems[b])
       for (auto& dc : D.geom[b]) D.conn[e].push_back(T.entity_gid(e, dc.first, dc.second));
   // overlap map: sorted unique entity GIDs (buildOverlapMapFromElements)
-  std::set<GO> overlapset;
-  for (GO e = 0; e < nelem; ++e)
-    for (GO g : D.conn[e]) overlapset.insert(g);
-  std::vector<GO> overlap(overlapset.begin(), overlapset.end());
-  std::unordered_map<GO, size_t> ov_index;
-  ov_index.reserve(overlap.size() * 2);
-  for (size_t i = 0; i < overlap.size(); ++i) ov_index[overlap[i]] = i;
+  std::vector<GO> overlap;
+  for (GO e = 0; e < nelem; ++e) overlap.insert(overlap.end(), D.conn[e].begin(), D.conn[e].end());
+  std::sort(overlap.begin(), overlap.end());
+  overlap.erase(std::unique(overlap.begin(), overlap.end()), overlap.end());
+  auto ov_index = [&](GO g) { return (size_t)(std::lower_bound(overlap.begin(), overlap.end(), g) - overlap.begin()); };
   // tagged multivector: max over elements of DOFs per (entity, field)
   std::vector<GO> tagged(overlap.size() * nf, 0);
   for (int b = 0; b < T.nblocks; ++b)
     for (LO e : T.block_elems[b])
       for (size_t c = 0; c < D.conn[e].size(); ++c) {
-        size_t lid = ov_index[D.conn[e][c]];
+        size_t lid = ov_index(D.conn[e][c]);
         for (int f = 0; f < nf; ++f) {
           GO cnt = D.geom_ndof[b][c];
           if (cnt > tagged[lid * nf + f]) tagged[lid * nf + f] = cnt;
@@ -578,15 +582,19 @@ static void build_dofs(const Topology& T, DofManager& D, const tx_equation_set_d
       }
   // element GIDs (fillGIDsFromOverlappedMV)
   D.elementGIDs.assign(nelem, {});
-  for (int b = 0; b < T.nblocks; ++b)
-    for (LO e : T.block_elems[b]) {
+  for (int b = 0; b < T.nblocks; ++b) {
+    const std::vector<LO>& be = T.block_elems[b];
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < be.size(); ++i) {
+      const LO e = be[i];
       auto& g = D.elementGIDs[e];
       for (size_t c = 0; c < D.conn[e].size(); ++c) {
-        size_t lid = ov_index[D.conn[e][c]];
+        size_t lid = ov_index(D.conn[e][c]);
         for (int f = 0; f < nf; ++f)
           for (int k = 0; k < D.geom_ndof[b][c]; ++k) g.push_back(base[lid * nf + f] + k);
       }
     }
+  }
   // offsets per field (FieldAggPattern::localOffsets_build)
   D.offsets.assign(T.nblocks, std::vector<std::vector<int>>(nf));
   for (int b = 0; b < T.nblocks; ++b) {
@@ -600,18 +608,20 @@ static void build_dofs(const Topology& T, DofManager& D, const tx_equation_set_d
     }
   }
   // owned_: first touch in block order, element order, GID order
-  std::unordered_set<GO> seen;
-  seen.reserve((size_t)which * 2);
+  std::vector<unsigned char> seen((size_t)which, 0);
   D.owned.clear();
   for (int b = 0; b < T.nblocks; ++b)
     for (LO e : T.block_elems[b])
       for (GO g : D.elementGIDs[e])
-        if (seen.insert(g).second) D.owned.push_back(g);
+        if (!seen[g]) {
+          seen[g] = 1;
+          D.owned.push_back(g);
+        }
   if ((GO)D.owned.size() != which) throw std::runtime_error("numbering failure: owned count mismatch");
-  D.g2l.clear();
-  D.g2l.reserve(D.owned.size() * 2);
+  D.g2l.assign((size_t)which, -1);
   for (size_t i = 0; i < D.owned.size(); ++i) D.g2l[D.owned[i]] = (LO)i;
   D.elementLIDs.assign(nelem, {});
+#pragma omp parallel for schedule(static)
   for (GO e = 0; e < nelem; ++e)
     for (GO g : D.elementGIDs[e]) D.elementLIDs[e].push_back(D.g2l[g]);
   // edge orientations (lowest-order HCURL): +1 if the local edge direction
@@ -635,14 +645,18 @@ static void build_dofs(const Topology& T, DofManager& D, const tx_equation_set_d
       for (LO r : l) rows[r].insert(rows[r].end(), l.begin(), l.end());
     }
   D.rowptr.assign(N + 1, 0);
-  D.colind.clear();
+#pragma omp parallel for schedule(dynamic, 4096)
   for (GO r = 0; r < N; ++r) {
     auto& v = rows[r];
     std::sort(v.begin(), v.end());
     v.erase(std::unique(v.begin(), v.end()), v.end());
-    D.rowptr[r + 1] = D.rowptr[r] + (int64_t)v.size();
-    D.colind.insert(D.colind.end(), v.begin(), v.end());
-    std::vector<LO>().swap(v);
+  }
+  for (GO r = 0; r < N; ++r) D.rowptr[r + 1] = D.rowptr[r] + (int64_t)rows[r].size();
+  D.colind.assign((size_t)D.rowptr[N], 0);
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (GO r = 0; r < N; ++r) {
+    std::copy(rows[r].begin(), rows[r].end(), D.colind.begin() + D.rowptr[r]);
+    std::vector<LO>().swap(rows[r]);
   }
 }
 
@@ -1508,6 +1522,7 @@ void orc_dirichlet_apply(void* h, int64_t n, const int32_t* lids, const double* 
 
 void orc_spmv(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* x,
               double* y, double alpha, double beta) {
+#pragma omp parallel for schedule(static)
   for (int64_t r = 0; r < n; ++r) {
     double s = 0.0;
     for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) s += vals[k] * x[colind[k]];
@@ -1519,6 +1534,7 @@ void orc_spmv(int64_t n, const int64_t* rowptr, const int32_t* colind, const dou
 int orc_cg(int64_t n, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* b, double* x,
            double rtol, int maxit, double* relres) {
   std::vector<double> r(n), z(n), p(n), q(n), dinv(n);
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
     double d = 0.0;
     for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
@@ -1527,6 +1543,7 @@ int orc_cg(int64_t n, const int64_t* rowptr, const int32_t* colind, const double
   }
   orc_spmv(n, rowptr, colind, vals, x, q.data(), 1.0, 0.0);
   double bn = 0.0, rz = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : bn, rz)
   for (int64_t i = 0; i < n; ++i) {
     r[i] = b[i] - q[i];
     z[i] = dinv[i] * r[i];
@@ -1540,13 +1557,16 @@ int orc_cg(int64_t n, const int64_t* rowptr, const int32_t* colind, const double
   double rn = 0.0;
   for (; it < maxit; ++it) {
     rn = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rn)
     for (int64_t i = 0; i < n; ++i) rn += r[i] * r[i];
     if (std::sqrt(rn) <= rtol * bn) break;
     orc_spmv(n, rowptr, colind, vals, p.data(), q.data(), 1.0, 0.0);
     double pq = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : pq)
     for (int64_t i = 0; i < n; ++i) pq += p[i] * q[i];
     double a = rz / pq;
     double rz2 = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rz2)
     for (int64_t i = 0; i < n; ++i) {
       x[i] += a * p[i];
       r[i] -= a * q[i];
@@ -1555,10 +1575,12 @@ int orc_cg(int64_t n, const int64_t* rowptr, const int32_t* colind, const double
     }
     double be = rz2 / rz;
     rz = rz2;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) p[i] = z[i] + be * p[i];
   }
   rn = 0.0;
   orc_spmv(n, rowptr, colind, vals, x, q.data(), 1.0, 0.0);
+#pragma omp parallel for schedule(static) reduction(+ : rn)
   for (int64_t i = 0; i < n; ++i) rn += (b[i] - q[i]) * (b[i] - q[i]);
   if (relres) *relres = std::sqrt(rn) / bn;
   return it;
