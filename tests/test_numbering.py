@@ -4,7 +4,12 @@ Numbering facts checked: owned_ GIDs in LID order, element GID and LID
 vectors, per-field offsets (Panzer_DOFManager.cpp:449-716,1293-1372,
 Panzer_FieldAggPattern.cpp:369-413), Dirichlet DOF sets
 (TianXin_PointEvaluator_impl.hpp:104,196-202) and vertex coordinates.
+The numbering itself is pinned by the reference's one-rank CubeHex fixture
+(adapters-stk/test/stk_connmngr/tCubeHexMeshDOFManager.cpp:137-193).
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -96,3 +101,36 @@ def test_invalid_descriptions_raise():
     conn = tx.CartesianConnManager(1, 1, 1, topology=A.TX_TOPO_TET)
     with pytest.raises(tx.TxError):
         tx.DOFManager(conn, A.equation_set(A.TX_PHYS_MAXWELL, A.TX_HCURL_I1), require_device=False)
+
+
+def _cube_hex_fixture():
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_known_answers.json")) as fh:
+        return json.load(fh)["cube_hex_dof_numbering"]
+
+
+def _cube_hex_explicit(n):
+    """The CubeHex factory's mesh as an explicit mesh: nodes x-fastest, elements x-fastest, shards vertex order."""
+    nx, ny, nz = n
+    idx = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
+    coords = [(i / nx, j / ny, k / nz) for k in range(nz + 1) for j in range(ny + 1) for i in range(nx + 1)]
+    conn = [[idx(i, j, k), idx(i + 1, j, k), idx(i + 1, j + 1, k), idx(i, j + 1, k),
+             idx(i, j, k + 1), idx(i + 1, j, k + 1), idx(i + 1, j + 1, k + 1), idx(i, j + 1, k + 1)]
+            for k in range(nz) for j in range(ny) for i in range(nx)]
+    return tx.ExplicitConnManager.from_arrays(coords, [(A.TX_TOPO_HEX, conn, 1, "eblock-0_0_0")])
+
+
+def test_cube_hex_numbering_fixture_of_the_reference():
+    # tCubeHexMeshDOFManager's one-rank element GIDs (three nodal fields interleaved per node, GIDs ascending by
+    # node GID) on the oracle, the lattice numbering and the explicit-mesh numbering of the same mesh
+    g = _cube_hex_fixture()
+    n = tuple(g["mesh"])
+    q = A.equation_set(A.TX_PHYS_ELASTICITY)  # three HGRAD_C1 fields, like ux, uy, p
+    assert len(A.field_names(A.TX_PHYS_ELASTICITY)) == g["n_fields"]
+    o = O.Oracle(A.mesh_desc(n), q)
+    lattice = tx.DOFManager(tx.CartesianConnManager(*n), q, require_device=False)
+    explicit = tx.DOFManager(_cube_hex_explicit(n), q, require_device=False)
+    for source in (o.element_gids(0), lattice.getElementGIDs(0), explicit.getElementGIDs(0)):
+        for e, gids in g["element_gids"].items():
+            assert list(source[int(e)]) == gids, e
+    for e, nodes in g["element_nodes"].items():
+        assert list(o.element_conn(int(e))) == nodes, e

@@ -5,6 +5,7 @@ Each test restates one of the reference's unit tests on the oracle:
   two-hex integrals    disc-fe/test/evaluator_tests/integrator_scalar.cpp:393-410,500-501
   first IP coordinate  disc-fe/test/core_tests/integration_values2.cpp:103-110
   hex27 sub-cell map   dof-mgr/test/dofmngr_test/tIntrepidFieldPattern.cpp:527-573
+  HCurl quadrilateral  disc-fe/test/core_tests/basis_values2.cpp:289-426 (and the hex I1 functions' face traces)
   scatter pattern      adapters-stk/test/evaluator_tests/tpetra_scatter_residual.cpp:281-305
   reproduction         dof-mgr/test/fe_assembly/test_fe_assembly_HEX.hpp:672-677 (||b-Ax|| <= 1e-10)
 """
@@ -95,21 +96,114 @@ def test_partition_of_unity_and_gradients():
             assert np.allclose(g.sum(axis=0), 0.0, atol=1e-13)
 
 
-def test_nedelec_tangential_moments():
-    # each lowest-order edge function has unit tangential moment on its own edge, zero on the others
-    edges = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7)]
-    V = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]],
-                 float)
+HEX_V = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1],
+                  [-1, 1, 1]], float)
+HEX_EDGES = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7)]
+QUAD_V = np.array([[-1, -1], [1, -1], [1, 1], [-1, 1]], float)
+
+
+def quad_i1(x, y):
+    """Lowest-order Nedelec on [-1,1]^2, shards edges 0..3 (v0->v1, v1->v2, v2->v3, v3->v0): values (4, 2) and
+    scalar curls (4,), dual to u(edge midpoint) . (half edge vector)."""
+    val = np.array([[0.5 * (1 - y), 0.0], [0.0, 0.5 * (1 + x)], [-0.5 * (1 + y), 0.0], [0.0, -0.5 * (1 - x)]])
+    curl = np.full(4, 0.5)
+    return val, curl
+
+
+def test_hcurl_quad_fixture_of_the_reference():
+    # basis_values2.cpp's HCurl quadrilateral test, restated: reference values and curl of function 0, and the
+    # covariant transforms on its 0.5 x 0.5 cells (value J^-T v, curl c / det J, weights w det J)
+    g = json.load(open(os.path.join(GOLDEN, "reference_known_answers.json")))["hcurl_quad_i1"]
+    s, w1 = np.polynomial.legendre.leggauss(3)  # degree 4 rule: 3 x 3 Gauss points
+    h = g["cell_size"]
+    J = np.eye(2) * h / 2
+    det = np.linalg.det(J)
+    assert det == g["rel_cell_vol"]
+    for i, xq in enumerate(s):
+        for j, yq in enumerate(s):
+            val, curl = quad_i1(xq, yq)
+            assert val[0, 0] == -0.5 * (yq - 1.0) and val[0, 1] == 0.0
+            assert curl[0] == g["function0_curl"]
+            phys = val @ np.linalg.inv(J)  # rows: J^-T v
+            pcurl = curl / det
+            weight = w1[i] * w1[j]
+            assert np.allclose(val, g["value_scale"] * phys, rtol=0, atol=1e-15)
+            assert np.allclose(curl, g["rel_cell_vol"] * pcurl, rtol=0, atol=1e-15)
+            assert np.allclose(weight * det * phys, g["rel_cell_vol"] * weight * phys, rtol=0, atol=1e-15)
+    # the restated functions are dual to the midpoint tangential values
+    for k in range(4):
+        a, b = QUAD_V[k], QUAD_V[(k + 1) % 4]
+        val, _ = quad_i1(*((a + b) / 2))
+        assert np.allclose(val @ ((b - a) / 2), np.eye(4)[k], atol=1e-15)
+
+
+def test_nedelec_hex_dual_to_midpoint_tangential_values():
+    # the oracle's hex functions: u_i(m_j) . t_j = delta_ij (t_j half the edge vector), and the line integral
+    # of every function along its own edge is 2 (the edge length), along the others 0
     s, w = np.polynomial.legendre.leggauss(3)
-    for k, (a, b) in enumerate(edges):
-        t = V[b] - V[a]
-        mom = np.zeros(12)
+    for k, (a, b) in enumerate(HEX_EDGES):
+        t = (HEX_V[b] - HEX_V[a]) / 2
+        val, _ = O.basis_eval(A.TX_TOPO_HEX, A.TX_HCURL_I1, (HEX_V[a] + HEX_V[b]) / 2)
+        assert np.allclose(val @ t, np.eye(12)[k], atol=1e-15)
+        line = np.zeros(12)
         for sj, wj in zip(s, w):
-            val, _ = O.basis_eval(A.TX_TOPO_HEX, A.TX_HCURL_I1, V[a] + (sj + 1) / 2 * t)
-            mom += wj / 2 * val @ t
-        expect = np.zeros(12)
-        expect[k] = 1.0
-        assert np.allclose(mom, expect, atol=1e-14)
+            v, _ = O.basis_eval(A.TX_TOPO_HEX, A.TX_HCURL_I1, HEX_V[a] + (sj + 1) / 2 * (HEX_V[b] - HEX_V[a]))
+            line += wj * v @ t
+        assert np.allclose(line, 2.0 * np.eye(12)[k], atol=1e-14)
+
+
+def test_nedelec_hex_face_traces_are_the_pinned_quad_functions():
+    # on each face, the tangential trace of the hex edge functions is the quadrilateral I1 function of the face's
+    # edge (orientation included) and the trace of every other function vanishes: the hex normalisation follows
+    # from the reference's quadrilateral fixture
+    faces = [(0, 1, 5, 4), (1, 2, 6, 5), (2, 3, 7, 6), (0, 4, 7, 3), (0, 3, 2, 1), (4, 5, 6, 7)]  # shards
+    rng = np.random.default_rng(0)
+    for fv in faces:
+        P = HEX_V[list(fv)]
+        eu, ev = (P[1] - P[0]) / 2, (P[3] - P[0]) / 2  # local axes: face vertex 0 at (-1, -1)
+        centre = P.mean(axis=0)
+        quad_edge_of = {}
+        for q in range(4):
+            a, b = fv[q], fv[(q + 1) % 4]
+            k = [i for i, e in enumerate(HEX_EDGES) if set(e) == {a, b}][0]
+            quad_edge_of[k] = (q, 1.0 if HEX_EDGES[k] == (a, b) else -1.0)
+        for _ in range(4):
+            uv = rng.uniform(-1, 1, 2)
+            val, _ = O.basis_eval(A.TX_TOPO_HEX, A.TX_HCURL_I1, centre + uv[0] * eu + uv[1] * ev)
+            qv, _ = quad_i1(*uv)
+            for k in range(12):
+                trace = np.array([val[k] @ eu, val[k] @ ev])
+                expect = quad_edge_of[k][1] * qv[quad_edge_of[k][0]] if k in quad_edge_of else np.zeros(2)
+                assert np.allclose(trace, expect, atol=1e-15), (fv, k)
+
+
+@pytest.mark.parametrize("h", [1.0, 0.25])
+def test_nedelec_hex_physical_transforms(h):
+    # one hex of side h: the oracle's Maxwell Jacobian is (1/mu) int curl N . curl N + sigma int N . N with
+    # N = J^-T N_ref and curl N = J curl N_ref / det J (the transforms the quadrilateral fixture pins), J = h/2 I,
+    # and the edge signs of the lattice's vertex GIDs
+    inv_mu, sigma = 1.5, 0.75
+    o = O.Oracle(A.mesh_desc(1, lengths=(h, h, h)), A.equation_set(A.TX_PHYS_MAXWELL, A.TX_HCURL_I1,
+                                                                     params=(inv_mu, sigma)))
+    z = np.zeros(o.n_dofs)
+    _, v = o.evaluate(z, aux=z)
+    W = dense(o, v)
+    lids = o.element_lids(0)[0]
+    K = W[np.ix_(lids, lids)]
+    gid = lambda p: int((p[0] > 0) + 2 * (p[1] > 0) + 4 * (p[2] > 0))
+    sign = np.array([1.0 if gid(HEX_V[a]) < gid(HEX_V[b]) else -1.0 for a, b in HEX_EDGES])
+    s, w = np.polynomial.legendre.leggauss(2)
+    A_ref, B_ref = np.zeros((12, 12)), np.zeros((12, 12))
+    for i, xq in enumerate(s):
+        for j, yq in enumerate(s):
+            for k, zq in enumerate(s):
+                val, curl = O.basis_eval(A.TX_TOPO_HEX, A.TX_HCURL_I1, np.array([xq, yq, zq]))
+                wq = w[i] * w[j] * w[k]
+                A_ref += wq * curl @ curl.T
+                B_ref += wq * val @ val.T
+    det = (h / 2) ** 3
+    expect = np.outer(sign, sign) * (inv_mu * (h / 2) ** 2 / det ** 2 * det * A_ref + sigma * (2 / h) ** 2 * det * B_ref)
+    assert np.allclose(K, expect, rtol=0, atol=1e-14 * np.abs(expect).max())
 
 
 def test_scatter_pattern_counts():

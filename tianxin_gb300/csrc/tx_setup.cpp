@@ -397,7 +397,9 @@ static void eval_tables(RefTables& R) {
     }
     if (R.hcurl) {
       // lowest-order Nedelec: edge k along axis a, tangent sign s,
-      // phi = s * prod_{d != a} (1 + c_d x_d) / 8 * e_a,  curl_i = eps_{i j a} d_j phi_a
+      // phi = s * prod_{d != a} (1 + c_d x_d) / 4 * e_a,  curl_i = eps_{i j a} d_j phi_a;
+      // dual to u(edge midpoint) . (half edge vector), the quadrilateral I1
+      // convention extended so that face traces are the quadrilateral functions
       for (int e = 0; e < 12; ++e) {
         const int* v0 = kVtx[kEdgeVtx[e][0]];
         const int* v1 = kVtx[kEdgeVtx[e][1]];
@@ -406,11 +408,11 @@ static void eval_tables(RefTables& R) {
         double s = v1[a] > v0[a] ? 1.0 : -1.0;
         double c[3], fac[3];
         for (int d = 0; d < 3; ++d) { c[d] = v0[d] ? 1.0 : -1.0; fac[d] = d == a ? 1.0 : 1.0 + c[d] * x[d]; }
-        double phi = s * fac[0] * fac[1] * fac[2] / 8.0;
+        double phi = s * fac[0] * fac[1] * fac[2] / 4.0;
         double dphi[3];
         for (int j = 0; j < 3; ++j) {
           if (j == a) { dphi[j] = 0.0; continue; }
-          double prod = s / 8.0;
+          double prod = s / 4.0;
           for (int d = 0; d < 3; ++d) prod *= (d == j) ? c[d] : fac[d];
           dphi[j] = prod;
         }
