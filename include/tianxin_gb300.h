@@ -573,18 +573,21 @@ const char* tx_batch_last_error(tx_batch b);
 void tx_batch_destroy(tx_batch b);
 
 /* Volume fill that allocates no device memory.  It has no counterpart in the
- * reference; it exists for callers that may not allocate: code running
- * while a CUDA graph capture is open (cudaMalloc is not allowed then) and
- * applications that pre-reserve all device memory in their own pool.
- * Same result as tx_eval with TX_EVAL_PERSISTENT (every block, even
- * worksets of the size set by tx_set_worksets' min_size; TX_EVAL_MIXED
- * honoured, TX_EVAL_DETERMINISTIC refused, block must be -1).  Its scratch
- * (work counter, parameter tables, workset list) is one static device array
- * holding at most TX_NOALLOC_MAX_WORKSETS worksets (about 1.6 MB, kept by
- * every GPU that loads the library until exit); larger work lists are
- * rejected with TX_ERANGE.  The first call on a device looks the array up
- * (make it before any stream capture).  All calls share the array: calls
- * that overlap on the GPU race. */
+ * reference.  It exists for callers that may not allocate: applications that
+ * reserve all device memory up front in their own pool (a driver allocation
+ * outside the pool fails or starves a neighbour), and step loops that must not
+ * stall the device, which a cudaFree of grown scratch does.
+ * Same result as tx_eval with TX_EVAL_PERSISTENT (every block, even worksets
+ * of the size set by tx_set_worksets' min_size, each cut into the same work
+ * items; TX_EVAL_MIXED honoured, TX_EVAL_DETERMINISTIC refused, block must
+ * be -1), up to the order of the FP64 sums.  Its scratch (work counter,
+ * parameter tables, work list) is one static device array holding at most
+ * TX_NOALLOC_MAX_WORKSETS work items (about 1.6 MB, kept by every GPU that
+ * loads the library until exit); larger work lists are rejected with
+ * TX_ERANGE.  The parameter tables reach the device as kernel arguments, not
+ * host copies.  The first call on a device looks the array's address up
+ * (make that first call before any stream capture).  All calls share the
+ * array and each rewrites it: calls that overlap on the GPU race. */
 #define TX_NOALLOC_MAX_WORKSETS 65536
 int tx_eval_noalloc(tx_handle h, const tx_eval_args* args);
 

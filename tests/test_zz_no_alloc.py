@@ -1,14 +1,14 @@
 """tx_eval_noalloc: the volume fill for callers that may not allocate device memory.
 
-Code that runs while a CUDA graph capture is open (a time integrator
-capturing its step) cannot call cudaMalloc, and applications that pre-reserve
-all device memory in their own pool forbid further driver allocations.  For
-them the library offers tx_eval_noalloc, which keeps the persistent
-evaluation's scratch (work counter, parameter tables, workset list) in a
-fixed static device array instead of allocating it.  These tests call it
-through the C-ABI and check it against tx_eval with TX_EVAL_PERSISTENT, the
-existing entry point, on two calls in a row.  This file is collected last so
-that a failure here leaves every other test already run.
+Applications that reserve all device memory up front in their own pool
+cannot accept a driver allocation outside it, and step loops that must not
+stall the device cannot afford the cudaFree of grown scratch.  For them the
+library offers tx_eval_noalloc, which keeps the persistent evaluation's
+scratch (work counter, parameter tables, work list) in a fixed static device
+array instead of allocating it.  These tests call it through the C-ABI and
+check it against tx_eval with TX_EVAL_PERSISTENT, the existing entry point,
+on two calls in a row.  This file is collected last so that a failure here
+leaves every other test already run.
 """
 import ctypes as C
 
@@ -68,14 +68,14 @@ def test_noalloc_matches_persistent_twice(cuda, case, mixed):
 
 def test_noalloc_rejects_work_lists_beyond_the_limit(cuda):
     lib = _lib.load()
-    n = 41  # 68,921 elements: one-element worksets exceed the 65,536-workset limit
+    n = 41  # 68,921 elements: one-element worksets exceed the 65,536-item limit
     conn, dof, lof = _setup((n, n, n), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_HGRAD_C1,
                             (1.0, 0.0, 0.0, 1.0), ws=1)
     x, f = lof.getTpetraVector(), lof.getTpetraVector()
     rc = _call(lib, dof, eval_args(x, f=f))
     assert rc == A.TX_ERANGE
     assert b"65536" in lib.tx_last_error(dof.h)
-    tx.AssemblyEngine(lof).setWorksetSize(64, 64)  # 1,077 worksets: accepted
+    tx.AssemblyEngine(lof).setWorksetSize(64, 64)  # 1,077 worksets of one item each: accepted
     assert _call(lib, dof, eval_args(x, f=f)) == 0
     f_ref = lof.getTpetraVector()
     tx.AssemblyEngine(lof).evaluate(x, f=f_ref)

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -1619,48 +1620,71 @@ int tx_batch_eval(tx_batch b, const tx_eval_args* args) {
 // Volume fill for callers that cannot allocate device memory.
 //
 // tx_eval's persistent form keeps its scratch -- the work counter, the
-// per-block parameter tables and the workset list -- in device memory that
-// the handle allocates on first use.  Two kinds of caller cannot accept
-// that: code that runs inside CUDA graph stream capture (a time integrator
-// capturing its whole step; cudaMalloc is not a stream operation and may not
-// be called while a capture is open), and applications that reserve all
-// device memory up front in their own pool and forbid further driver
-// allocations (a solver embedded in a larger simulation with a fixed memory
-// budget).  tx_eval_noalloc runs the same kernel with that scratch in one
-// file-scope static device array of fixed size, so a call allocates nothing.
+// per-block parameter tables and the work list -- in device memory that the
+// handle allocates on first use.  Some callers cannot accept that:
+// applications that reserve all device memory up front in their own pool (a
+// solver embedded in a larger simulation with a fixed memory budget, where a
+// driver allocation outside the pool fails or pushes a neighbour out of
+// memory), and time-step loops that must not stall the device, which a
+// cudaFree of grown scratch does.  tx_eval_noalloc runs the same kernel with
+// that scratch in one file-scope static device array of fixed size, so a call
+// allocates nothing.
 namespace {
 
-constexpr int64_t kNoAllocMaxWorksets = TX_NOALLOC_MAX_WORKSETS;
+constexpr int64_t kNoAllocMaxItems = TX_NOALLOC_MAX_WORKSETS;
 constexpr size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kNaCounter = 0;
 constexpr size_t kNaViews = 256;
 constexpr size_t kNaParams = al256(kNaViews + sizeof(tx::BlockView) * TX_MAX_BLOCKS);
 constexpr size_t kNaItems = al256(kNaParams + sizeof(tx::EvalParams) * TX_MAX_BLOCKS);
-constexpr size_t kNaBytes = kNaItems + sizeof(tx::WorkItem) * kNoAllocMaxWorksets;
+constexpr size_t kNaBytes = kNaItems + sizeof(tx::WorkItem) * kNoAllocMaxItems;
 
-// The scratch: [counter | views | params | worksets].  Every call shares it
-// and it keeps the last call's contents; the counter is cleared per call.
+// The scratch: [counter | views | params | work items].  Every call shares it
+// and it keeps the last call's contents; each call rewrites the tables and
+// the work list and clears the counter before the persistent launch.
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
-// Device address of g_noalloc_scratch per device ordinal (the host-side name
-// of a __device__ array is only a stand-in, not a device address).
-unsigned char* g_noalloc_addr[256] = {};
+// Device address of g_noalloc_scratch per device ordinal, looked up once per
+// device by the first call (the host-side name of a __device__ array is only
+// a stand-in, not a device address).  Threads that race on the first call
+// look up the same address, so a relaxed atomic suffices.
+std::atomic<unsigned char*> g_noalloc_addr[256] = {};
 
-struct NaBlocks {
-  int64_t first[TX_MAX_BLOCKS + 1];  // first workset of each block
+// Everything the persistent launch reads, passed by value so that no host
+// buffer is copied: the block views, the evaluation parameters and the work
+// list's shape.  Items follow tx_eval's persistent work list: each block's
+// even worksets of `ws` elements, each cut into items of at most `cap[b]`
+// elements (a few CTA passes of the family).
+struct NaTables {
+  tx::BlockView views[TX_MAX_BLOCKS];
+  tx::EvalParams params;
+  int64_t first[TX_MAX_BLOCKS + 1];  // first item of each block
   int64_t n_elem[TX_MAX_BLOCKS];
+  int64_t cap[TX_MAX_BLOCKS];        // elements an item
+  int64_t per_ws[TX_MAX_BLOCKS];     // items of a full workset
   int32_t kind[TX_MAX_BLOCKS];
   int32_t nblocks;
+  int64_t ws;
 };
 
-// Even worksets of `ws` elements: workset i of block b = elements
-// [(i - first[b]) * ws, min(... + ws, n_elem[b])).
-__global__ void k_noalloc_worksets(tx::WorkItem* items, int64_t n_items, NaBlocks nb, int64_t ws) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_items; i += (int64_t)gridDim.x * blockDim.x) {
+// Writes the parameter tables and the work list into the scratch.  Item j of
+// block b lies in workset w = j / per_ws[b], as chunk c = j % per_ws[b]:
+// elements [w ws + c cap, min(w ws + (c + 1) cap, (w + 1) ws, n_elem)).
+__global__ void k_noalloc_setup(unsigned char* base, int64_t n_items, NaTables t) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (tid < t.nblocks) {
+    ((tx::BlockView*)(base + kNaViews))[tid] = t.views[tid];
+    ((tx::EvalParams*)(base + kNaParams))[tid] = t.params;
+  }
+  tx::WorkItem* items = (tx::WorkItem*)(base + kNaItems);
+  for (int64_t i = tid; i < n_items; i += (int64_t)gridDim.x * blockDim.x) {
     int b = 0;
-    while (b + 1 < nb.nblocks && i >= nb.first[b + 1]) ++b;
-    const int64_t e0 = (i - nb.first[b]) * ws;
-    const int64_t e1 = e0 + ws < nb.n_elem[b] ? e0 + ws : nb.n_elem[b];
-    items[i] = tx::WorkItem{nb.kind[b], b, e0, e1};
+    while (b + 1 < t.nblocks && i >= t.first[b + 1]) ++b;
+    const int64_t j = i - t.first[b];
+    const int64_t w = j / t.per_ws[b], c = j % t.per_ws[b];
+    const int64_t w1 = (w + 1) * t.ws < t.n_elem[b] ? (w + 1) * t.ws : t.n_elem[b];
+    const int64_t e0 = w * t.ws + c * t.cap[b];
+    const int64_t e1 = e0 + t.cap[b] < w1 ? e0 + t.cap[b] : w1;
+    items[i] = tx::WorkItem{t.kind[b], b, e0, e1};
   }
 }
 
@@ -1678,51 +1702,46 @@ extern "C" int tx_eval_noalloc(tx_handle h, const tx_eval_args* a) {
     return fail(h, TX_EINVAL, "tx_eval_noalloc: MAXWELL needs the current density J in aux");
   const int nb = (int)h->blocks.size();
   const int64_t ws = h->ws_min;
-  NaBlocks blk{};
-  blk.nblocks = nb;
+  const bool mixed = (a->flags & TX_EVAL_MIXED) != 0;
+  const bool stage = a->crs_vals != nullptr && (a->flags & TX_EVAL_SCATTER_DIRECT) == 0;
+  NaTables t{};
+  t.nblocks = nb;
+  t.ws = ws;
+  t.params = make_params(h, *a);
+  size_t smem = 0;
   for (int b = 0; b < nb; ++b) {
-    if (h->blocks[b].kind < 0) return fail(h, TX_EINVAL, "tx_eval_noalloc: no kernel for this element family");
-    blk.first[b + 1] = blk.first[b] + (h->blocks[b].n_elem + ws - 1) / ws;
-    blk.n_elem[b] = h->blocks[b].n_elem;
-    blk.kind[b] = h->blocks[b].kind;
+    const DevBlock& db = h->blocks[b];
+    if (db.kind < 0) return fail(h, TX_EINVAL, "tx_eval_noalloc: no kernel for this element family");
+    t.views[b] = db.view();
+    t.kind[b] = db.kind;
+    t.n_elem[b] = db.n_elem;
+    t.cap[b] = std::min<int64_t>(ws, (int64_t)tx::batched_elements_per_pass(db.kind) * kItemPasses);
+    t.per_ws[b] = (ws + t.cap[b] - 1) / t.cap[b];
+    const int64_t rem = db.n_elem % ws;
+    t.first[b + 1] = t.first[b] + (db.n_elem / ws) * t.per_ws[b] + (rem + t.cap[b] - 1) / t.cap[b];
+    smem = std::max(smem, tx::batched_smem_bytes(db.kind, mixed, stage));
   }
-  const int64_t n_items = blk.first[nb];
-  if (n_items > kNoAllocMaxWorksets)
+  const int64_t n_items = t.first[nb];
+  if (n_items > kNoAllocMaxItems)
     return fail(h, TX_ERANGE,
-                "tx_eval_noalloc: " + std::to_string(n_items) + " worksets exceed the static limit of " +
-                    std::to_string(kNoAllocMaxWorksets) + "; raise the workset size with tx_set_worksets");
+                "tx_eval_noalloc: " + std::to_string(n_items) + " work items exceed the static limit of " +
+                    std::to_string(kNoAllocMaxItems) + "; raise the workset size with tx_set_worksets");
   // set-up, once per device, with that device current
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 256) return fail(h, TX_ECUDA, "tx_eval_noalloc: no current device");
-  if (!g_noalloc_addr[dev]) {
+  unsigned char* base = g_noalloc_addr[dev].load(std::memory_order_relaxed);
+  if (!base) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval_noalloc: ") + cudaGetErrorString(e));
-    g_noalloc_addr[dev] = (unsigned char*)p;
+    base = (unsigned char*)p;
+    g_noalloc_addr[dev].store(base, std::memory_order_relaxed);
   }
-  unsigned char* base = g_noalloc_addr[dev];
-  // parameter tables from the stack (a pageable source is copied before the call returns)
-  unsigned char tab[(sizeof(tx::BlockView) + sizeof(tx::EvalParams)) * TX_MAX_BLOCKS];
-  const bool mixed = (a->flags & TX_EVAL_MIXED) != 0;
-  const bool stage = a->crs_vals != nullptr && (a->flags & TX_EVAL_SCATTER_DIRECT) == 0;
-  tx::EvalParams P = make_params(h, *a);
-  size_t smem = 0;
-  for (int b = 0; b < nb; ++b) {
-    tx::BlockView V = h->blocks[b].view();
-    std::memcpy(tab + b * sizeof(tx::BlockView), &V, sizeof V);
-    std::memcpy(tab + nb * sizeof(tx::BlockView) + b * sizeof(tx::EvalParams), &P, sizeof P);
-    smem = std::max(smem, tx::batched_smem_bytes(h->blocks[b].kind, mixed, stage));
-  }
-  e = cudaMemcpyAsync(base + kNaViews, tab, nb * sizeof(tx::BlockView), cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(base + kNaParams, tab + nb * sizeof(tx::BlockView), nb * sizeof(tx::EvalParams),
-                        cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess && n_items > 0) {
-    const int64_t blocks = std::min<int64_t>((n_items + 255) / 256, 1024);
-    k_noalloc_worksets<<<(unsigned)blocks, 256, 0, h->stream>>>((tx::WorkItem*)(base + kNaItems), n_items, blk, ws);
-    e = cudaGetLastError();
-  }
+  if (n_items == 0) return TX_OK;
+  const int64_t blocks = std::min<int64_t>((n_items + 255) / 256, 1024);
+  k_noalloc_setup<<<(unsigned)blocks, 256, 0, h->stream>>>(base, n_items, t);
+  e = cudaGetLastError();
   if (e == cudaSuccess)  // clears the counter, then one persistent launch
     e = tx::launch_assemble_batched((const tx::BlockView*)(base + kNaViews), (const tx::EvalParams*)(base + kNaParams),
                                     (const tx::WorkItem*)(base + kNaItems), (int)n_items, (int*)(base + kNaCounter),
