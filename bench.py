@@ -42,6 +42,7 @@ def args():
     p.add_argument("--n", type=int, default=128, help="bricks per direction (default: the 128^3 workload)")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-configs", action="store_true", help="skip the other named workloads")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--spmv-shape", default=None,
                    help="fixed SpMV launch shape instead of the autotuner: lanes,unroll (both precisions) "
@@ -149,6 +150,78 @@ def cpu_sample(budget_s, threads=None):
     return {"value": reps * n ** 3 / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"R+J of elasticity hex8 {n}^3 sub-lattice ({n ** 3} elements, same physics/jitter), "
                       f"{reps} evaluations in {dt:.1f} s, oracle CPU restatement, OpenMP"}
+
+
+def _oracle_rate(o, x, budget_s, threads, **kw):
+    """Elements/s of the oracle's R+J on one mesh, repeated for about budget_s."""
+    o.evaluate(x, threads=threads, **kw)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        o.evaluate(x, threads=threads, **kw)
+        reps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    return reps * o.n_elements / (time.perf_counter() - t0), reps
+
+
+def config_cpu_baselines(budget_s=3.0):
+    """The oracle (CPU restatement, AD Jacobians) on bounded samples of the other named workloads."""
+    import numpy as np
+
+    from oracle import oracle as O
+    from tianxin_gb300 import _abi as A
+    from tianxin_gb300 import workloads as WL
+    cores = os.cpu_count()
+    out = {}
+    # Poisson hex8 16^3: the whole mesh on one thread (the Kokkos Serial equivalent)
+    q = A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 0.0), source_kind=A.TX_SOURCE_SINE)
+    o = O.Oracle(A.mesh_desc(16, jitter=0.1, seed=1), q)
+    v, reps = _oracle_rate(o, np.random.default_rng(0).uniform(-1, 1, o.n_dofs), budget_s, 1)
+    out["poisson_hex8_16"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                              "sample": f"the whole 16^3 mesh (4096 elements), {reps} R+J evaluations, one thread"}
+    # heat: 8^3 hex27 + 8^3 tet10 bricks of the same two-block layout
+    q = A.equation_set(A.TX_PHYS_HEAT, A.TX_HGRAD_C2, params=(1.0, 0.5, 1.0), integration_order=[4, 2])
+    o = O.Oracle(A.mesh_desc((8, 8, 8), (2, 1, 1), [A.TX_TOPO_HEX, A.TX_TOPO_TET], (2.0, 1.0, 1.0), 0.0, 3), q)
+    v, reps = _oracle_rate(o, np.random.default_rng(0).uniform(0, 1, o.n_dofs), budget_s, cores)
+    out["heat_hex27_tet10_48"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                  "sample": f"8^3 hex27 + 8^3 bricks of tet10 ({o.n_elements} elements), {reps} R+J "
+                                            "evaluations, OpenMP"}
+    # elastodynamics: K + c M on a 16^3 sub-lattice (x_dot and alpha = 1 / (beta dt^2))
+    q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.25, 0.0, 0.0, 0.0, 1.0))
+    o = O.Oracle(A.mesh_desc(16, jitter=0.0, seed=4), q)
+    rng = np.random.default_rng(0)
+    x = rng.normal(0, 1e-3, o.n_dofs)
+    v, reps = _oracle_rate(o, x, budget_s, cores, x_dot=rng.normal(0, 1.0, o.n_dofs), alpha=4e6, beta=1.0)
+    out["elastodynamics_hex8_96"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                     "sample": f"K + M/(beta dt^2) of a 16^3 sub-lattice (4096 elements), {reps} "
+                                               "R+J evaluations, OpenMP"}
+    # batch: the first instances of the 256-mesh plan, each evaluated once, until the budget is spent
+    done, nel, t_eval = 0, 0, 0.0
+    for i, (kind, n) in enumerate(WL.batch_plan(256)):
+        if kind == "poisson_hex8":
+            q = A.equation_set(A.TX_PHYS_POISSON, params=(1.0, 0.0, 0.0, 0.0), source_kind=A.TX_SOURCE_SINE)
+            m, aux = A.mesh_desc(n, jitter=0.1, seed=5000 + i), None
+        elif kind == "elasticity_tet4":
+            q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.0))
+            m, aux = A.mesh_desc(n, topology=A.TX_TOPO_TET, jitter=0.1, seed=5000 + i), None
+        else:
+            q = A.equation_set(A.TX_PHYS_MAXWELL, A.TX_HCURL_I1, params=(1.0, 1.0))
+            m, aux = A.mesh_desc(n, jitter=0.1, seed=5000 + i), True
+        o = O.Oracle(m, q)
+        x = np.random.default_rng(i).uniform(0, 1, o.n_dofs)
+        kw = {"aux": np.random.default_rng(i + 1).normal(0, 1, o.n_dofs)} if aux else {}
+        t0 = time.perf_counter()
+        o.evaluate(x, threads=cores, **kw)
+        t_eval += time.perf_counter() - t0
+        done += 1
+        nel += o.n_elements
+        if t_eval >= budget_s:
+            break
+    out["mixed_batch_256"] = {"value": nel / t_eval, "unit": UNIT, "cores": cores, "kind": "port",
+                              "sample": f"the first {done} instances of the plan ({nel} elements), one R+J "
+                                        "evaluation each, OpenMP"}
+    return out
 
 
 def run_reference(a):
@@ -322,14 +395,18 @@ def run_ours(a):
     achieved = bytes_alg / k_mixed / 1e9
     traffic = None
     warp_kernel = tuned.get("variant") == 2
-    # the two-phase form is two kernels: element rows to scratch, then the row gather
-    kernel_name = ("k_assemble<hex8,elasticity,f32,jac,scratch> + k_gather_rows<float>" if gather
+    lattice = gather and me.ae.gather_form() == "lattice"
+    # the two-phase form is two kernels: element rows to scratch, then the row gather; the lattice
+    # form gathers x into node order, then owns and writes each node's rows once
+    kernel_name = ("k_lattice_gather_u + k_lattice_gather<hex8,elasticity,f32>" if lattice
+                   else "k_assemble<hex8,elasticity,f32,jac,scratch> + k_gather_rows<float>" if gather
                    else "k_assemble_wpe<hex8,elasticity,f32,jac>" if warp_kernel
                    else "k_assemble<hex8,elasticity,f32,jac>")
     tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf)).get(("gather" if gather else "assemble_wpe" if warp_kernel else "assemble")
+            traffic = json.load(open(tf)).get(("lattice" if lattice else "gather" if gather else
+                                               "assemble_wpe" if warp_kernel else "assemble")
                                               + "_elasticity_hex8_mixed_bytes_per_launch_128")
         except Exception:
             traffic = None
@@ -403,12 +480,24 @@ def run_ours(a):
                                   "solution_maxrel": float((xm - xd).abs().max() / xd.abs().max())}
         del xm, xd, sols
 
+    # the other named workloads at their stated sizes (after the headline legs)
+    configs = None
+    if not a.no_configs:
+        from tianxin_gb300 import workloads as WL
+        configs = WL.measure_configs(peak)
+
     cpu = None
     if rank == 0 and ws == 1:
         try:
             cpu = cpu_sample(a.cpu_seconds)
         except Exception as ex:  # the baseline is reported, not required
             cpu = {"value": None, "error": str(ex)}
+        if configs is not None:
+            try:
+                for k, v in config_cpu_baselines().items():
+                    configs[k]["cpu_baseline"] = v
+            except Exception as ex:
+                configs["cpu_baseline_error"] = str(ex)
 
     if rank == 0:
         line = {
@@ -445,6 +534,7 @@ def run_ours(a):
                                                  for c in tuned.get("candidates", [])],
                          "fp64": {k: v for k, v in tuned64.items() if k != "candidates"}},
             "clocks": clk,
+            "configs": configs,
         }
         print(json.dumps(line), flush=True)
     if dist:

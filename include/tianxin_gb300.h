@@ -221,6 +221,20 @@ int tx_eval(tx_handle h, const tx_eval_args* args);
  * tx_dof_build), else 0; a host query, no device work. */
 int tx_eval_gather_supported(tx_handle h, int32_t* supported);
 
+/* The form TX_EVAL_GATHER takes on this handle with TX_EVAL_MIXED:
+ * TX_GATHER_LATTICE for one hex8 elasticity block on the whole brick lattice
+ * (owner-computes: each CTA owns a column of nodes, sums the rows of its
+ * nodes from the eight elements around each in shared memory and registers,
+ * and writes every f entry and CRS value once; no element scratch), else
+ * TX_GATHER_TWO_PHASE (element rows to scratch, then the row gather), or 0
+ * when TX_EVAL_GATHER does not apply.  FP64 evaluations always take the
+ * two-phase form.  The replaced step is the atomic sumIntoValues scatter
+ * into a zeroed matrix (Panzer_ScatterResidual_Tpetra_impl.hpp:390-439,
+ * Panzer_ModelEvaluator_impl.hpp:1788-1789).  A host query. */
+#define TX_GATHER_TWO_PHASE 1
+#define TX_GATHER_LATTICE 2
+int tx_eval_gather_form(tx_handle h, int32_t* form);
+
 /* DirichletEvalautor<Jacobian>/<Residual> through the container's
  * applyDirichletBoundaryCondition (TianXin_Dirichlet_impl.hpp:75-81,
  * lof/Panzer_TpetraLinearObjContainer.hpp:228-238): with a residual f,
@@ -559,6 +573,16 @@ int tx_set_spmv_entity_shape(tx_handle h, int32_t lanes, int32_t unroll);
 #define TX_VARIANT_CTA 1
 #define TX_VARIANT_WARP 2
 int tx_set_assembly_variant(tx_handle h, int32_t variant);
+/* Tile shape of the CTA-staged Jacobian kernel: threads a CTA, 64, 128 (the
+ * default; 0 restores it) or 256.  Each element takes TPE threads (its basis
+ * count rounded up to a power of two), so a CTA assembles threads / TPE
+ * elements: hex8 8, 16 or 32, tet10 4, 8 or 16, hex27 2, 4 or 8.  Blocks of
+ * hex8 elasticity, hex27 heat and tet10 heat take the shape; other families
+ * keep 128 (TX_EINVAL when no block of the handle has it).  Replaces the
+ * team size of Panzer's HierarchicParallelism
+ * (disc-fe/src/Panzer_HierarchicParallelism.hpp:78-128); the autotuner's
+ * fourth knob. */
+int tx_set_cta_threads(tx_handle h, int32_t threads);
 
 /* Many independent meshes in one persistent launch: the volume fill of every
  * block of every handle, cut into worksets, is one work list.  args holds one

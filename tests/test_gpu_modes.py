@@ -185,3 +185,34 @@ def test_gather_in_the_model_evaluator_and_its_limits(cuda):
             ae.evaluate(x, f=f, W=W, gather=True, **kw)
     with pytest.raises(tx.TxError):
         ae.evaluate(x, f=f, W=None, gather=True)
+
+
+@pytest.mark.parametrize("topo,phys,basis,shapes", [(A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_HGRAD_C1, (64, 256)),
+                                                    (A.TX_TOPO_HEX, A.TX_PHYS_HEAT, A.TX_HGRAD_C2, (64,)),
+                                                    (A.TX_TOPO_TET, A.TX_PHYS_HEAT, A.TX_HGRAD_C2, (64, 256))])
+def test_cta_tile_shapes_against_oracle(cuda, topo, phys, basis, shapes):
+    # the staged kernel at 64 and 256 threads a CTA (half and twice the elements a CTA) gives the oracle's
+    # values in both precisions; shapes whose FP64 tables do not fit a CTA (hex27 at 256) and others are refused
+    o, dof, lof = build((5, 4, 3), (1, 1, 1), topo, phys, basis)
+    rng = np.random.default_rng(4)
+    x, xd, aux = rng.uniform(-1, 1, o.n_dofs), rng.uniform(-1, 1, o.n_dofs), rng.standard_normal(o.n_dofs)
+    f_ref, v_ref = o.evaluate(x, xd, aux, alpha=0.5, beta=1.0)
+    ae = tx.AssemblyEngine(lof)
+    for threads in (64, 256):
+        if threads not in shapes:
+            with pytest.raises(tx.TxError):
+                ae.setCtaThreads(threads)
+            continue
+        ae.setCtaThreads(threads)
+        for mixed, tol in ((False, FP64_TOL), (True, MIXED_TOL)):
+            f, v = run(dof, lof, x, xd, aux, mixed=mixed)
+            assert rel(f, f_ref) <= tol and rel(v, v_ref) <= tol, (threads, mixed)
+    ae.setCtaThreads(0)
+    with pytest.raises(tx.TxError):
+        ae.setCtaThreads(96)
+
+
+def test_cta_tile_shape_refused_without_a_family(cuda):
+    o, dof, lof = build((2, 2, 2), (1, 1, 1), A.TX_TOPO_TET, A.TX_PHYS_POISSON, A.TX_HGRAD_C1)
+    with pytest.raises(tx.TxError):
+        tx.AssemblyEngine(lof).setCtaThreads(64)

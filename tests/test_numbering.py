@@ -134,3 +134,18 @@ def test_cube_hex_numbering_fixture_of_the_reference():
             assert list(source[int(e)]) == gids, e
     for e, nodes in g["element_nodes"].items():
         assert list(o.element_conn(int(e))) == nodes, e
+
+
+def test_gather_form_query():
+    # the owner-computes lattice form applies to one hex8 elasticity block on the whole lattice only
+    import ctypes as C
+    form = C.c_int32()
+    cases = [((3, 2, 2), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_GATHER_LATTICE),
+             ((3, 2, 2), (1, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_POISSON, A.TX_GATHER_TWO_PHASE),
+             ((3, 2, 2), (1, 1, 1), A.TX_TOPO_TET, A.TX_PHYS_ELASTICITY, A.TX_GATHER_TWO_PHASE),
+             ((2, 1, 2), (2, 1, 1), A.TX_TOPO_HEX, A.TX_PHYS_ELASTICITY, A.TX_GATHER_TWO_PHASE)]
+    for n, blocks, topo, phys, expect in cases:
+        conn = tx.CartesianConnManager(*n, *blocks, topology=topo)
+        dof = tx.DOFManager(conn, A.equation_set(phys), require_device=False)
+        assert dof.lib.tx_eval_gather_form(dof.h, C.byref(form)) == 0
+        assert form.value == expect, (n, blocks, topo, phys)

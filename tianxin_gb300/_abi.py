@@ -34,6 +34,8 @@ TX_EVAL_PERSISTENT = 0x4
 TX_EVAL_SCATTER_DIRECT = 0x8
 TX_EVAL_TANGENT = 0x10
 TX_EVAL_GATHER = 0x20
+TX_GATHER_TWO_PHASE = 1
+TX_GATHER_LATTICE = 2
 TX_MAX_TANGENTS = 4
 
 TX_SPMV_F64 = 0

@@ -31,6 +31,7 @@ SIGNATURES = {
     "tx_graph_build": (C.c_int, [P, P, P]),
     "tx_eval": (C.c_int, [P, C.POINTER(_abi.EvalArgs)]),
     "tx_eval_gather_supported": (C.c_int, [P, C.POINTER(C.c_int32)]),
+    "tx_eval_gather_form": (C.c_int, [P, C.POINTER(C.c_int32)]),
     "tx_dirichlet_apply": (C.c_int, [P, I64, P, P, P, P, P]),
     "tx_spmv": (C.c_int, [P, I32, I64, P, P, P, P, P, D, D]),
     "tx_solve_cg_ir": (C.c_int, [P, C.POINTER(_abi.SolveArgs)]),
@@ -46,6 +47,7 @@ SIGNATURES = {
     "tx_set_spmv_shape": (C.c_int, [P, I32, I32]),
     "tx_set_spmv_entity_shape": (C.c_int, [P, I32, I32]),
     "tx_set_assembly_variant": (C.c_int, [P, I32]),
+    "tx_set_cta_threads": (C.c_int, [P, C.c_int32]),
     "tx_graph_capture_begin": (C.c_int, [P]),
     "tx_graph_capture_end": (C.c_int, [P, C.POINTER(I32)]),
     "tx_graph_launch": (C.c_int, [P, I32]),

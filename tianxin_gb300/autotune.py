@@ -7,9 +7,13 @@ The knobs play the role of Panzer's HierarchicParallelism team/vector sizes
   * grid_cap  CTAs of the per-block launch (0 = occupancy x SMs x 4)
   * workset   elements per work item of the persistent / batched launch
   * gather    two-phase evaluation (element rows to scratch, rows gathered and
-              written once) against the atomic scatter; atomic candidates are
-              timed with the zeroing of f and W they need, the two-phase form
-              overwrites them
+              written once; on a hex8 elasticity lattice the owner-computes
+              lattice kernel) against the atomic scatter; atomic candidates are
+              timed with the zeroing of f and W they need, the gather forms
+              overwrite them
+  * threads   threads a CTA of the staged kernel, 64 / 128 / 256: elements per
+              CTA (threads over the element's basis count rounded up to a
+              power of two), Panzer's team size
 
 Each candidate is timed with CUDA events on the real evaluation (outputs in
 scratch vectors), the fastest is kept, and results are cached in
@@ -81,11 +85,14 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                                                   scatter_direct=direct), reps)
                     results.append(({"workset": ws, "grid_cap": 0, "scatter_direct": direct}, t))
         else:
-            # kernel variant (warp per element / CTA-staged / CTA direct scatter / two-phase) x CTA cap
-            kernels = [(2, False, False), (1, False, False), (1, True, False)] if mixed else \
-                [(1, False, False), (1, True, False)]
+            # kernel variant (warp per element / CTA-staged / CTA direct scatter / two-phase) x CTA tile
+            # shape (threads a CTA of the staged kernel: elements per CTA) x CTA cap
+            kernels = [(2, False, False, 0), (1, False, False, 0), (1, True, False, 0)] if mixed else \
+                [(1, False, False, 0), (1, True, False, 0)]
+            if W is not None:
+                kernels += [(1, False, False, 64), (1, False, False, 256)]
             if W is not None and ae.gather_supported():
-                kernels.append((1, False, True))
+                kernels.append((1, False, True, 0))
 
             def step(direct, gather):
                 if not gather:  # the atomic forms sum into f and W, which a step zeroes first
@@ -94,8 +101,12 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                         f.zero_()
                 ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, scatter_direct=direct, gather=gather)
 
-            for variant, direct, gather in kernels:
+            for variant, direct, gather, threads in kernels:
                 ae.setVariant(variant)
+                try:
+                    ae.setCtaThreads(threads)
+                except tx_error:  # no block of this handle has the tile shape
+                    continue
                 for cap in (0, sms * 2, sms * 4, sms * 8):
                     ae.setGridCap(cap)
                     try:
@@ -103,7 +114,8 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                     except tx_error:  # a configuration the handle refuses
                         continue
                     results.append(({"variant": variant, "scatter_direct": direct, "gather": gather,
-                                     "grid_cap": cap}, t))
+                                     "cta_threads": threads, "grid_cap": cap}, t))
+            ae.setCtaThreads(0)
         best = min(results, key=lambda r: r[1])
         cfg = dict(best[0], ms=best[1], candidates=[dict(c, ms=t) for c, t in results])
         cache[key] = cfg
@@ -113,6 +125,7 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                 print(f"  {c}: {t:.3f} ms")
     ae.setGridCap(cfg.get("grid_cap", 0))
     ae.setVariant(cfg.get("variant", 0))
+    ae.setCtaThreads(cfg.get("cta_threads", 0))
     ae.gather = bool(cfg.get("gather", False))
     ae.scatter_direct = bool(cfg.get("scatter_direct", False))
     if "workset" in cfg:

@@ -135,6 +135,7 @@ struct tx_handle_s {
   tx::SpmvShape spmv;     // SpMV launch shape ({0, 0}: automatic)
   tx::SpmvShape spmv_eb;  // the same for the entity-block form
   int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element
+  int cta_threads = 0; // threads a CTA of the staged Jacobian kernel (0: 128); tx_set_cta_threads
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
   // two-phase evaluation: entity -> (block, element, local basis) incidence
@@ -143,6 +144,11 @@ struct tx_handle_s {
   int64_t* d_inc = nullptr;
   unsigned char* gather_scratch = nullptr;
   size_t gather_bytes = 0;
+  // owner-computes lattice assembly (single-block hex8 elasticity lattices):
+  // per-node records and the gathered x / x_dot of a call
+  tx::LatticeNode* d_lat = nullptr;
+  float4* d_lat_u = nullptr;
+  float4* d_lat_ud = nullptr;
   // cubature tables of tx_ip_coordinates per (block, degree)
   struct IpTables { int block, degree, nq; double* tables; };
   std::vector<IpTables> ip_tables;
@@ -171,6 +177,8 @@ struct tx_handle_s {
     ip_tables.clear();
     cudaFree(d_inc_ptr); cudaFree(d_inc); cudaFree(gather_scratch);
     d_inc_ptr = nullptr; d_inc = nullptr; gather_scratch = nullptr; gather_bytes = 0;
+    cudaFree(d_lat); cudaFree(d_lat_u); cudaFree(d_lat_ud);
+    d_lat = nullptr; d_lat_u = nullptr; d_lat_ud = nullptr;
     for (auto& b : blocks) {
       cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
       cudaFree(b.color_perm);
@@ -371,6 +379,103 @@ const char* gather_misfit(const tx::Dofs& D) {
   return nullptr;
 }
 
+// Whether the handle is one hex8 elasticity block on the whole brick lattice
+// (the owner-computes lattice assembly applies).
+bool lattice_gather_applies(tx_handle h) {
+  const tx::Mesh& m = h->mesh;
+  const tx::Dofs& D = h->dofs;
+  if (m.is_explicit || m.nblocks != 1 || D.blocks.size() != 1) return false;
+  const tx::BlockDofs& B = D.blocks[0];
+  return B.topo == TX_TOPO_HEX && B.basis == TX_HGRAD_C1 && B.ref.nq == 8 && D.eq.physics == TX_PHYS_ELASTICITY &&
+         D.nf == 3 && D.n_entities == m.n_nodes && (int64_t)B.dconn.size() == 8 * m.NX * m.NY * m.NZ &&
+         (int64_t)D.ent_lattice.size() == 3 * D.n_entities;
+}
+
+// Per-node records of the lattice assembly (node GID order): FP32 hi/lo
+// coordinates, entity LID, first CRS value of the node's rows and the
+// position of each lattice neighbour in the node's sorted entity row.
+void build_lattice_nodes(tx_handle h) {
+  const tx::Mesh& m = h->mesh;
+  const tx::Dofs& D = h->dofs;
+  const int64_t NX = m.NX, NY = m.NY, NZ = m.NZ, nn = (NX + 1) * (NY + 1) * (NZ + 1);
+  std::vector<int32_t> lid_of(nn, -1);
+  for (int64_t l = 0; l < D.n_entities; ++l) {
+    const int32_t* p = &D.ent_lattice[3 * l];
+    if ((p[0] | p[1] | p[2]) & 1) throw std::invalid_argument("lattice assembly: an entity is not a vertex");
+    lid_of[p[0] / 2 + (NX + 1) * (p[1] / 2 + (NY + 1) * (int64_t)(p[2] / 2))] = (int32_t)l;
+  }
+  std::vector<tx::LatticeNode> rec(nn);
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t g = 0; g < nn; ++g) {
+    tx::LatticeNode& r = rec[g];
+    std::memset(&r, 0, sizeof r);
+    std::memset(r.npos, 0xff, sizeof r.npos);
+    const int64_t i = g % (NX + 1), j = (g / (NX + 1)) % (NY + 1), k = g / ((NX + 1) * (NY + 1));
+    const int32_t l = lid_of[g];
+    if (l < 0) { bad = 1; continue; }
+    r.lid = l;
+    r.rowstart = 9 * D.erowptr[l];
+    for (int d = 0; d < 3; ++d) {
+      const double X = m.coords[3 * g + d];
+      const float hi = (float)X;
+      r.xh[d] = hi;
+      r.xl[d] = (float)(X - (double)hi);
+    }
+    const int32_t* row = D.ecol.data() + D.erowptr[l];
+    const int64_t len = D.erowptr[l + 1] - D.erowptr[l];
+    int64_t found = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int64_t a = i + dx, b = j + dy, c = k + dz;
+          if (a < 0 || a > NX || b < 0 || b > NY || c < 0 || c > NZ) continue;
+          const int32_t lm = lid_of[a + (NX + 1) * (b + (NY + 1) * c)];
+          const int32_t* pos = std::lower_bound(row, row + len, lm);
+          if (pos == row + len || *pos != lm) { bad = 1; continue; }
+          r.npos[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)] = (uint8_t)(pos - row);
+          ++found;
+        }
+    if (found != len) bad = 1;
+  }
+  if (bad) throw std::invalid_argument("lattice assembly: the entity graph is not the lattice's");
+  ck(upload(h->d_lat, rec), "upload lattice nodes");
+  ck(cudaMalloc((void**)&h->d_lat_u, sizeof(float4) * nn), "alloc lattice u");
+  ck(cudaMalloc((void**)&h->d_lat_ud, sizeof(float4) * nn), "alloc lattice u_dot");
+}
+
+// Owner-computes mixed R+J of a lattice hex8 elasticity block: f and the CRS
+// values overwritten, each once.
+int eval_lattice(tx_handle h, const tx_eval_args& a, const tx::EvalParams& P) {
+  int rc = guarded(h, [&]() {
+    if (!h->d_lat) build_lattice_nodes(h);
+    return TX_OK;
+  });
+  if (rc) return rc;
+  const tx::Mesh& m = h->mesh;
+  tx::LatticeArgs L;
+  L.nx = m.NX; L.ny = m.NY; L.nz = m.NZ;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // z chunks: about eight tasks per resident CTA (two per SM), so the last wave is short
+  const int64_t cols = ((m.NX + 4) / 4) * ((m.NY + 4) / 4);
+  const int64_t want = 8 * 2 * (int64_t)sms;
+  const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(m.NZ + 1, (want + cols - 1) / cols));
+  L.zchunk = (m.NZ + 1 + chunks - 1) / chunks;
+  L.grid = h->grid_cap;
+  L.nodes = h->d_lat;
+  L.ref = h->blocks[0].ref;
+  L.lam = (float)P.lam; L.mu = (float)P.mu; L.rho = (float)P.p[5];
+  L.alpha = (float)P.alpha; L.beta = (float)P.beta;
+  for (int d = 0; d < 3; ++d) L.body[d] = (float)P.p[2 + d];
+  L.f = a.f;
+  L.vals = a.crs_vals;
+  cudaError_t e = tx::launch_lattice_gather(L, h->d_lat_u, h->d_lat_ud, a.x, a.x_dot, h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_eval: ") + cudaGetErrorString(e));
+  return TX_OK;
+}
+
 // Evaluate every requested block/range (volume fill).
 // Two-phase evaluation (TX_EVAL_GATHER): incidence lists built on first use,
 // element scratch grown to the precision's need, then per block the first
@@ -381,6 +486,7 @@ int eval_gather(tx_handle h, const tx_eval_args& a, const tx::EvalParams& P0) {
   if (a.block >= 0) return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_GATHER evaluates every block (block = -1)");
   if (a.flags & (TX_EVAL_TANGENT | TX_EVAL_PERSISTENT | TX_EVAL_DETERMINISTIC))
     return fail(h, TX_EINVAL, "tx_eval: TX_EVAL_GATHER is not combined with TANGENT, PERSISTENT or DETERMINISTIC");
+  if (mixed && lattice_gather_applies(h)) return eval_lattice(h, a, P0);
   const tx::Dofs& D = h->dofs;
   const int nf = D.nf;
   if (const char* why = gather_misfit(D)) return fail(h, TX_EINVAL, why);
@@ -469,8 +575,13 @@ int eval_blocks(tx_handle h, const tx_eval_args& a, const CoefOverride* ov = nul
       if (e0 < 0 || e1 > db.n_elem || e0 > e1) return fail(h, TX_ERANGE, "tx_eval: element range outside the block");
     }
     cudaError_t e = cudaSuccess;
-    const bool wpe = !det && mixed && stage && h->variant != 1 && tx::wpe_supported(V, P);
-    if (wpe) {
+    const bool tiled = !det && stage && P.vals && !P.tan && h->cta_threads != 0 &&
+                       tx::tile_shape_supported(db.kind, h->cta_threads);
+    const bool wpe = !det && !tiled && mixed && stage && h->variant != 1 && h->cta_threads == 0 &&
+                     tx::wpe_supported(V, P);
+    if (tiled) {
+      e = tx::launch_assemble_tile(V, P, mixed, h->cta_threads, e0, e1, h->stream, h->grid_cap);
+    } else if (wpe) {
       e = tx::launch_assemble_wpe(V, P, e0, e1, h->stream, h->grid_cap);
     } else if (!det) {
       e = tx::launch_assemble(V, P, mixed, nullptr, e0, e1, true, stage, h->stream, h->grid_cap);
@@ -914,6 +1025,13 @@ int tx_eval(tx_handle h, const tx_eval_args* args) {
   return eval_blocks(h, *args);
 }
 
+int tx_eval_gather_form(tx_handle h, int32_t* form) {
+  if (!h || !form) return TX_EINVAL;
+  if (!h->have_host_dofs) return fail(h, TX_ESTATE, "tx_eval_gather_form before tx_dof_build");
+  *form = lattice_gather_applies(h) ? TX_GATHER_LATTICE : gather_misfit(h->dofs) ? 0 : TX_GATHER_TWO_PHASE;
+  return TX_OK;
+}
+
 int tx_eval_gather_supported(tx_handle h, int32_t* supported) {
   if (!h || !supported) return TX_EINVAL;
   if (!h->have_host_dofs) return fail(h, TX_ESTATE, "tx_eval_gather_supported before tx_dof_build");
@@ -1306,6 +1424,20 @@ int tx_graph_destroy(tx_handle h, int32_t graph_id) {
     return fail(h, TX_ERANGE, "tx_graph_destroy: unknown graph");
   cudaGraphExecDestroy(h->graphs[graph_id]);
   h->graphs[graph_id] = nullptr;
+  return TX_OK;
+}
+
+int tx_set_cta_threads(tx_handle h, int32_t threads) {
+  if (!h) return TX_EINVAL;
+  if (threads == 128) threads = 0;
+  if (threads != 0 && threads != 64 && threads != 256)
+    return fail(h, TX_EINVAL, "tx_set_cta_threads: 0 (or 128), 64 or 256");
+  if (threads != 0) {
+    bool any = false;
+    for (const DevBlock& db : h->blocks) any = any || tx::tile_shape_supported(db.kind, threads);
+    if (!any) return fail(h, TX_EINVAL, "tx_set_cta_threads: no block of this handle has that tile shape");
+  }
+  h->cta_threads = threads;
   return TX_OK;
 }
 

@@ -80,6 +80,46 @@ cudaError_t launch_assemble_batched(const BlockView* views, const EvalParams* pa
                                     int n_items, int* counter, size_t smem, bool mixed, bool jac, bool stage,
                                     int grid, cudaStream_t s);
 
+// The CTA-staged Jacobian kernel at 64 or 256 threads a CTA (tx_assemble_tiles.cu),
+// for the families tile_shape_supported lists (element family ids of assemble_kind).
+bool tile_shape_supported(int kind, int threads);
+cudaError_t launch_assemble_tile(const BlockView& B, const EvalParams& P, bool mixed, int threads, int64_t e_lo,
+                                 int64_t e_hi, cudaStream_t s, int grid_cap);
+
+// ---- owner-computes lattice assembly (tx_lattice.cu)
+// One node of a single-block hex8 brick lattice, in node GID order: FP32
+// hi/lo coordinates (x = hi + lo), its entity LID, the first CRS value of
+// its three rows (nf = 3) and the position of neighbour (dx, dy, dz) in its
+// sorted entity row at npos[(dx + 1) + 3 (dy + 1) + 9 (dz + 1)] (0xff: none).
+struct __align__(16) LatticeNode {
+  float xh[3];
+  int32_t lid;
+  float xl[3];
+  int32_t pad0;
+  int64_t rowstart;
+  int64_t pad1;
+  uint8_t npos[32];
+};
+static_assert(sizeof(LatticeNode) == 80, "LatticeNode layout");
+struct LatticeArgs {
+  int64_t nx = 0, ny = 0, nz = 0;   // bricks per direction
+  int64_t zchunk = 0;               // node layers per task
+  int grid = 0;                     // CTA cap (0: one wave of resident CTAs)
+  const LatticeNode* nodes = nullptr;
+  const float* u = nullptr;         // [nodes][4] FP32 (set by the launcher)
+  const float* ud = nullptr;
+  const double* ref = nullptr;      // packed RefTables of the block
+  float lam = 0, mu = 0, rho = 0, alpha = 0, beta = 0;
+  float body[3] = {0, 0, 0};
+  double* f = nullptr;              // overwritten (may be null)
+  double* vals = nullptr;           // overwritten
+};
+// Mixed R+J of elasticity on the lattice: f and vals written once.  u_work and
+// ud_work hold nodes x 4 floats each (the gathered x and x_dot).
+cudaError_t launch_lattice_gather(LatticeArgs A, float4* u_work, float4* ud_work, const double* x, const double* xdot,
+                                  cudaStream_t s);
+size_t lattice_gather_smem();
+
 // ---- linear algebra (tx_linalg.cu)
 cudaError_t launch_expand_rowptr(const int64_t* erowptr, int64_t n_ent, int nf, int64_t* rowptr, cudaStream_t s);
 cudaError_t launch_expand_colind(const int64_t* erowptr, const int32_t* ecol, int64_t n_ent, int nf,

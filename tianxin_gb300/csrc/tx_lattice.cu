@@ -1,0 +1,426 @@
+// tx_lattice.cu -- owner-computes ("gather") assembly of a brick-lattice hex8
+// block: every CRS row of a node is summed inside one CTA and written once.
+//
+// The reference scatters every element's rows into the Tpetra CRS with
+// atomic sumIntoValues (disc-fe/src/evaluators/Panzer_ScatterResidual_Tpetra_
+// impl.hpp:390-439) after zeroing f and the matrix (Panzer_ModelEvaluator_
+// impl.hpp:1788-1789).  On the brick lattice of a CartesianConnManager block
+// the elements around a node are known from its lattice position, so here
+// the rows are gathered instead: a CTA owns a 4 x 4 column of nodes and
+// walks it up the z axis one node layer at a time.  At layer k it
+//
+//   1. computes the geometry and point stresses of the 5 x 5 elements of
+//      element layer k (its own 4 x 4 and a one-element halo) into a ring of
+//      two element layers in shared memory;
+//   2. assembles the rows of its 16 nodes of layer k from the 8 elements
+//      around each node (element layers k - 1 and k): eight lanes per node,
+//      one element each; each lane forms its element's 3 x 24 block-row of
+//      the node (the closed form of the AD Jacobian, as in the per-element
+//      kernel) and the eight lanes sum the blocks that land on the same
+//      neighbour with three butterfly exchanges (x, y, z), a fixed order;
+//   3. stages the node's 3 rows (81 values each in the interior) in shared
+//      memory in CRS order and writes them with coalesced stores.
+//
+// f and the CRS values are written exactly once (no zeroing, no atomics, no
+// read-modify-write of the 4 GB matrix) and every run gives the same bits.
+// Halo elements are recomputed by the neighbouring columns (25 element
+// geometries per 16 nodes); the Jacobian rows themselves are formed once.
+//
+// Precision: the mixed evaluation type (TX_EVAL_MIXED): FP32 geometry,
+// stresses and contractions; the eight element contributions of an entry
+// are summed in FP32 (at most three roundings) and widened to FP64 exactly.
+// Vertex coordinates enter as FP32 hi/lo pairs split on the host, so the
+// element edge vectors keep their FP64 accuracy.
+#include <algorithm>
+#include <cstdint>
+
+#include "tx_device.cuh"
+#include "tx_numeric.cuh"
+
+namespace tx {
+namespace {
+
+constexpr int kTile = 4;                    // owned nodes per CTA along x and y
+constexpr int kPlane = kTile + 2;           // node plane of a step: owned nodes, halo on both sides
+constexpr int kElem = kTile + 1;            // element columns of a step along x and y
+constexpr int kElems = kElem * kElem;       // 25 elements per layer
+constexpr int kNodes = kTile * kTile;       // 16 owned nodes per layer
+constexpr int kThreads = kNodes * 8;        // eight lanes per node
+constexpr int kRowMax = 243;                // 3 rows x 81 entries (interior node)
+
+// Element record in shared memory, laid out so that the eight lanes of a
+// node (eight different elements, eight different vertices B of them) and
+// the eight points q of one element each hit eight different bank groups:
+//   G: grad N (physical) of the vertex with lattice bits B at point q, in
+//      float4 slot 8 q + (B ^ q);
+//   S: (s00 s11 s22 s01 | s02 s12 f0 f1 | f2 - - -) of point q in slots
+//      3 q + j + rot, rot = the element's lattice parity (x | y << 1 | z << 2),
+//      which differs between the eight elements around a node;
+//   W: w_q det J_q at float 4 rot + q.
+// The record size is a multiple of 128 B (whole bank rows).
+constexpr int kRecG = 0;
+constexpr int kRecS = 64 * 16;
+constexpr int kRecW = kRecS + 31 * 16;
+constexpr int kRecBytes = ((kRecW + 36 * 4) + 127) / 128 * 128;
+static_assert(kRecBytes == 1664, "element record");
+
+// Node record of a plane: coordinates (FP32 hi, lo), u, u_dot.
+struct __align__(16) PlaneNode {
+  float4 xh, xl, u, ud;
+};
+
+// shared memory layout
+constexpr int kSmRefGrad = 0;                                    // [q][v] float4 (dN^/dxi, N)
+constexpr int kSmRefW = kSmRefGrad + 64 * 16;                    // [q] w_q
+constexpr int kSmPlane = kSmRefW + 8 * 4;                        // 2 x 36 PlaneNode
+constexpr int kSmPlaneInfo = kSmPlane + 2 * kPlane * kPlane * 64;  // owned-node info of the 2 planes
+constexpr int kInfoBytes = 48;                                   // rowstart (8) lid (4) nnb (4) npos (32)
+constexpr int kSmElem = kSmPlaneInfo + 2 * kNodes * kInfoBytes;
+constexpr int kSmStage = kSmElem + 2 * kElems * kRecBytes;       // [node][243] float
+constexpr int kSmBytes = kSmStage + kNodes * kRowMax * 4;
+
+// shards Hexahedron<8> vertex v <-> lattice offset bits (x | y << 1 | z << 2);
+// the map is an involution on these eight codes
+__device__ __forceinline__ int vbits(int v) {
+  constexpr unsigned kTab = 0u | (1u << 3) | (3u << 6) | (2u << 9) | (4u << 12) | (5u << 15) | (7u << 18) | (6u << 21);
+  return (kTab >> (3 * v)) & 7;
+}
+
+__device__ __forceinline__ float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+
+// Loads plane node records of node layer kk for the task's 6 x 6 window and
+// the owned nodes' row information.
+__device__ __forceinline__ void load_plane(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t kk,
+                                           unsigned char* smem, int slot) {
+  PlaneNode* pl = reinterpret_cast<PlaneNode*>(smem + kSmPlane) + slot * kPlane * kPlane;
+  const int t = threadIdx.x;
+  if (t < kPlane * kPlane) {
+    const int64_t i = i0 - 1 + t % kPlane, j = j0 - 1 + t / kPlane;
+    PlaneNode p{f4(0, 0, 0, 0), f4(0, 0, 0, 0), f4(0, 0, 0, 0), f4(0, 0, 0, 0)};
+    if (i >= 0 && i <= A.nx && j >= 0 && j <= A.ny && kk >= 0 && kk <= A.nz) {
+      const int64_t g = i + (A.nx + 1) * (j + (A.ny + 1) * kk);
+      const LatticeNode& n = A.nodes[g];
+      p.xh = f4(n.xh[0], n.xh[1], n.xh[2], 0.f);
+      p.xl = f4(n.xl[0], n.xl[1], n.xl[2], 0.f);
+      p.u = reinterpret_cast<const float4*>(A.u)[g];
+      p.ud = A.ud ? reinterpret_cast<const float4*>(A.ud)[g] : f4(0, 0, 0, 0);
+    }
+    pl[t] = p;
+  } else if (t >= 64 && t < 64 + kNodes) {
+    const int ln = t - 64;
+    const int64_t i = i0 + (ln & 3), j = j0 + (ln >> 2);
+    unsigned char* info = smem + kSmPlaneInfo + (slot * kNodes + ln) * kInfoBytes;
+    if (i <= A.nx && j <= A.ny && kk >= 0 && kk <= A.nz) {
+      const int64_t g = i + (A.nx + 1) * (j + (A.ny + 1) * kk);
+      const LatticeNode& n = A.nodes[g];
+      *reinterpret_cast<int64_t*>(info) = n.rowstart;
+      reinterpret_cast<int32_t*>(info)[2] = n.lid;
+      const int nnb = (1 + (i > 0) + (i < A.nx)) * (1 + (j > 0) + (j < A.ny)) * (1 + (kk > 0) + (kk < A.nz));
+      reinterpret_cast<int32_t*>(info)[3] = nnb;
+      const uint4* src = reinterpret_cast<const uint4*>(n.npos);
+      reinterpret_cast<uint4*>(info + 16)[0] = src[0];
+      reinterpret_cast<uint4*>(info + 16)[1] = src[1];
+    } else {
+      reinterpret_cast<int32_t*>(info)[3] = 0;  // no node
+    }
+  }
+}
+
+// Geometry, physical gradients and point stresses of the 5 x 5 elements of
+// element layer ek (vertices in plane slots ek & 1 and (ek + 1) & 1).
+// Reference table rg: (dN^/dxi, N) of the vertex with lattice bits B at point
+// q in slot 8 q + (B ^ q).
+__device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t ek,
+                                              unsigned char* smem) {
+  if (ek < 0 || ek >= A.nz) return;
+  const float4* rg = reinterpret_cast<const float4*>(smem + kSmRefGrad);
+  const float* rw = reinterpret_cast<const float*>(smem + kSmRefW);
+  const PlaneNode* plo = reinterpret_cast<const PlaneNode*>(smem + kSmPlane) + (int)(ek & 1) * kPlane * kPlane;
+  const PlaneNode* phi = reinterpret_cast<const PlaneNode*>(smem + kSmPlane) + (int)((ek + 1) & 1) * kPlane * kPlane;
+  unsigned char* rec0 = smem + kSmElem + (int)(ek & 1) * kElems * kRecBytes;
+  for (int task = threadIdx.x; task < kElems * 8; task += blockDim.x) {
+    const int el = task >> 3, q = task & 7;
+    const int ex = el % kElem, ey = el / kElem;
+    const int64_t gx = i0 - 1 + ex, gy = j0 - 1 + ey;
+    if (gx < 0 || gx >= A.nx || gy < 0 || gy >= A.ny) continue;
+    const int rot = (int)(gx & 1) | ((int)(gy & 1) << 1) | ((int)(ek & 1) << 2);
+    unsigned char* rec = rec0 + el * kRecBytes;
+    // vertex with lattice bits B at plane (ex + Bx, ey + By), layer Bz
+    float dX[8][3], U[8][3], UD[8][3];
+    float x0h[3], x0l[3];
+#pragma unroll
+    for (int B = 0; B < 8; ++B) {
+      const PlaneNode& p = ((B >> 2) ? phi : plo)[(ex + (B & 1)) + kPlane * (ey + ((B >> 1) & 1))];
+      const float4 h = p.xh, l = p.xl, u = p.u, ud = p.ud;
+      if (B == 0) {
+        x0h[0] = h.x; x0h[1] = h.y; x0h[2] = h.z;
+        x0l[0] = l.x; x0l[1] = l.y; x0l[2] = l.z;
+      }
+      dX[B][0] = (h.x - x0h[0]) + (l.x - x0l[0]);
+      dX[B][1] = (h.y - x0h[1]) + (l.y - x0l[1]);
+      dX[B][2] = (h.z - x0h[2]) + (l.z - x0l[2]);
+      U[B][0] = u.x; U[B][1] = u.y; U[B][2] = u.z;
+      UD[B][0] = ud.x; UD[B][1] = ud.y; UD[B][2] = ud.z;
+    }
+    float J[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) J[k] = 0.f;
+#pragma unroll
+    for (int B = 1; B < 8; ++B) {
+      const float4 g = rg[q * 8 + (B ^ q)];
+      J[0] += dX[B][0] * g.x; J[1] += dX[B][0] * g.y; J[2] += dX[B][0] * g.z;
+      J[3] += dX[B][1] * g.x; J[4] += dX[B][1] * g.y; J[5] += dX[B][1] * g.z;
+      J[6] += dX[B][2] * g.x; J[7] += dX[B][2] * g.y; J[8] += dX[B][2] * g.z;
+    }
+    const float c00 = J[4] * J[8] - J[5] * J[7];
+    const float c01 = J[5] * J[6] - J[3] * J[8];
+    const float c02 = J[3] * J[7] - J[4] * J[6];
+    const float det = J[0] * c00 + J[1] * c01 + J[2] * c02;
+    const float id = 1.0f / det;
+    float Ji[9];
+    Ji[0] = c00 * id; Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+    Ji[3] = c01 * id; Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[5] = (J[2] * J[3] - J[0] * J[5]) * id;
+    Ji[6] = c02 * id; Ji[7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[8] = (J[0] * J[4] - J[1] * J[3]) * id;
+    float Gu[9], acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Gu[k] = 0.f;
+    float4* G = reinterpret_cast<float4*>(rec + kRecG) + q * 8;
+#pragma unroll
+    for (int B = 0; B < 8; ++B) {
+      const float4 g = rg[q * 8 + (B ^ q)];
+      // grad_i = sum_j Jinv(j, i) grad^_j
+      const float gx0 = Ji[0] * g.x + Ji[3] * g.y + Ji[6] * g.z;
+      const float gy0 = Ji[1] * g.x + Ji[4] * g.y + Ji[7] * g.z;
+      const float gz0 = Ji[2] * g.x + Ji[5] * g.y + Ji[8] * g.z;
+      G[B ^ q] = f4(gx0, gy0, gz0, 0.f);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Gu[3 * c + 0] += gx0 * U[B][c];
+        Gu[3 * c + 1] += gy0 * U[B][c];
+        Gu[3 * c + 2] += gz0 * U[B][c];
+        acc[c] += g.w * UD[B][c];
+      }
+    }
+    const float tr = Gu[0] + Gu[4] + Gu[8];
+    const float lam = A.lam, mu = A.mu;
+    float4* S = reinterpret_cast<float4*>(rec + kRecS) + 3 * q + rot;
+    S[0] = f4(mu * (Gu[0] + Gu[0]) + lam * tr, mu * (Gu[4] + Gu[4]) + lam * tr, mu * (Gu[8] + Gu[8]) + lam * tr,
+              mu * (Gu[1] + Gu[3]));
+    S[1] = f4(mu * (Gu[2] + Gu[6]), mu * (Gu[5] + Gu[7]), A.rho * acc[0] - A.body[0], A.rho * acc[1] - A.body[1]);
+    S[2] = f4(A.rho * acc[2] - A.body[2], 0.f, 0.f, 0.f);
+    reinterpret_cast<float*>(rec + kRecW)[4 * rot + q] = rw[q] * det;
+  }
+}
+
+// The rows of the 16 owned nodes of node layer k.
+__device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t k,
+                                           unsigned char* smem) {
+  const float4* rg = reinterpret_cast<const float4*>(smem + kSmRefGrad);
+  const int lane = threadIdx.x & 31;
+  const int ln = threadIdx.x >> 3;     // owned node of this lane
+  const int e = threadIdx.x & 7;       // element around it: offset bits (x | y << 1 | z << 2)
+  const int ex = e & 1, ey = (e >> 1) & 1, ez = e >> 2;
+  const int lx = ln & 3, ly = ln >> 2;
+  const unsigned char* info = smem + kSmPlaneInfo + ((int)(k & 1) * kNodes + ln) * kInfoBytes;
+  const int nnb = reinterpret_cast<const int32_t*>(info)[3];
+  const int64_t gx = i0 + lx - 1 + ex, gy = j0 + ly - 1 + ey, gz = k - 1 + ez;
+  const bool valid = nnb > 0 && gx >= 0 && gx < A.nx && gy >= 0 && gy < A.ny && gz >= 0 && gz < A.nz;
+  // the node's own vertex: lattice bits complement to the element's offset
+  const int lbits = 7 - e;
+  const int rot = (int)(gx & 1) | ((int)(gy & 1) << 1) | ((int)(gz & 1) << 2);
+  const unsigned char* rec =
+      smem + kSmElem + ((int)((k - 1 + ez) & 1) * kElems + (lx + ex) + kElem * (ly + ey)) * kRecBytes;
+  const float4* G = reinterpret_cast<const float4*>(rec + kRecG);
+  const float4* S = reinterpret_cast<const float4*>(rec + kRecS) + rot;
+  const float4* W4 = reinterpret_cast<const float4*>(rec + kRecW) + rot;
+
+  // the lane's own weighted gradients and values: W_q grad N_a(q), W_q N_a(q)
+  float wg[8][3], wn[8];
+  float r[3] = {0.f, 0.f, 0.f};
+  float blk[8][9];
+  if (valid) {
+    const float4 wa = W4[0], wb = W4[1];
+    const float Wq[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+    const float sgn = Wq[0] < 0.f ? -1.f : 1.f;  // computeCellMeasure: |.| by the first point's sign
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float w = Wq[q] * sgn;
+      const float4 g = G[q * 8 + (lbits ^ q)];
+      wg[q][0] = w * g.x; wg[q][1] = w * g.y; wg[q][2] = w * g.z;
+      wn[q] = w * rg[q * 8 + (lbits ^ q)].w;
+      const float4 s0 = S[q * 3], s1 = S[q * 3 + 1], s2 = S[q * 3 + 2];
+      // residual row a: grad N_a . sigma + N_a (rho acc - b)
+      r[0] += wg[q][0] * s0.x + wg[q][1] * s0.w + wg[q][2] * s1.x + wn[q] * s1.z;
+      r[1] += wg[q][0] * s0.w + wg[q][1] * s0.y + wg[q][2] * s1.y + wn[q] * s1.w;
+      r[2] += wg[q][0] * s1.x + wg[q][1] * s1.y + wg[q][2] * s0.z + wn[q] * s2.x;
+    }
+    const float lam = A.lam, mu = A.mu, beta = A.beta, am = A.alpha * A.rho;
+    // slot c holds the block of the element vertex with bits c ^ lbits (bit per
+    // axis: 0 = the node's own lattice line, 1 = this element's neighbour line)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int bb = c ^ lbits;
+      float P[9], M = 0.f;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) P[t] = 0.f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float4 g = G[q * 8 + (bb ^ q)];
+        P[0] += wg[q][0] * g.x; P[1] += wg[q][0] * g.y; P[2] += wg[q][0] * g.z;
+        P[3] += wg[q][1] * g.x; P[4] += wg[q][1] * g.y; P[5] += wg[q][1] * g.z;
+        P[6] += wg[q][2] * g.x; P[7] += wg[q][2] * g.y; P[8] += wg[q][2] * g.z;
+        M += wn[q] * rg[q * 8 + (bb ^ q)].w;
+      }
+      const float tp = P[0] + P[4] + P[8];
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          float kv = beta * (lam * P[3 * cc + d] + mu * P[3 * d + cc]);
+          if (cc == d) kv += beta * mu * tp + am * M;
+          blk[c][3 * cc + d] = kv;
+        }
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+#pragma unroll
+      for (int t = 0; t < 9; ++t) blk[c][t] = 0.f;
+  }
+  // butterflies: on each axis the slot with bit 0 (neighbour on the node's own
+  // line) is shared by the two elements on either side; both lanes end with
+  // the same sum (a + b == b + a in IEEE arithmetic)
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if (c & (1 << ax)) continue;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) blk[c][t] += __shfl_xor_sync(0xffffffffu, blk[c][t], 1 << ax);
+    }
+#pragma unroll
+    for (int t = 0; t < 3; ++t) r[t] += __shfl_xor_sync(0xffffffffu, r[t], 1 << ax);
+  }
+  // stage the node's rows: slot c of lane e is neighbour offset
+  // d_a = 0 (bit 0) or 2 e_a - 1 (bit 1); the lane with e_a = 0 on every
+  // shared axis writes it
+  float* stage = reinterpret_cast<float*>(smem + kSmStage) + ln * kRowMax;
+  if (nnb > 0) {
+    const uint8_t* npos = info + 16;
+    const int rl = 3 * nnb;  // entries of one row
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if ((e & ~c & 7) != 0) continue;
+      const int dx = (c & 1) ? 2 * ex - 1 : 0, dy = (c & 2) ? 2 * ey - 1 : 0, dz = (c & 4) ? 2 * ez - 1 : 0;
+      const int p = npos[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
+      if (p == 0xff) continue;
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) stage[cc * rl + 3 * p + d] = blk[c][3 * cc + d];
+    }
+    if (e == 0 && A.f) {
+      const int32_t lid = reinterpret_cast<const int32_t*>(info)[2];
+#pragma unroll
+      for (int t = 0; t < 3; ++t) A.f[3 * (int64_t)lid + t] = widen(r[t]);
+    }
+  }
+  __syncwarp();
+  // the warp's four nodes: coalesced FP64 stores of each node's 3 rows
+  const int wn0 = (threadIdx.x >> 5) * 4;
+#pragma unroll 1
+  for (int m = 0; m < 4; ++m) {
+    const unsigned char* inf = smem + kSmPlaneInfo + ((int)(k & 1) * kNodes + wn0 + m) * kInfoBytes;
+    const int nb = reinterpret_cast<const int32_t*>(inf)[3];
+    if (nb == 0) continue;
+    double* dst = A.vals + *reinterpret_cast<const int64_t*>(inf);
+    const float* src = reinterpret_cast<const float*>(smem + kSmStage) + (wn0 + m) * kRowMax;
+    for (int t = lane; t < 9 * nb; t += 32) __stcs(dst + t, widen(src[t]));
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 2) k_lattice_gather(LatticeArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  // reference tables (hex8, 2 x 2 x 2 Gauss): [q][v] (dN^/dxi, N), w_q
+  {
+    const double* ref = A.ref;  // [w | geo_val | geo_grad | val | grad]
+    float4* rg = reinterpret_cast<float4*>(smem + kSmRefGrad);
+    float* rw = reinterpret_cast<float*>(smem + kSmRefW);
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) {  // i = q * 8 + v (shards vertex v)
+      const int q = i >> 3, B = vbits(i & 7);
+      const double* gr = ref + 8 + 64 + 192 + 64 + 3 * i;
+      rg[q * 8 + (B ^ q)] = f4(narrow(gr[0]), narrow(gr[1]), narrow(gr[2]), narrow(ref[8 + 64 + 192 + i]));
+    }
+    for (int i = threadIdx.x; i < 8; i += blockDim.x) rw[i] = narrow(ref[i]);
+  }
+  const int64_t tx_n = (A.nx + kTile) / kTile, ty_n = (A.ny + kTile) / kTile;  // node tiles: nx + 1 nodes
+  const int64_t tz_n = (A.nz + A.zchunk) / A.zchunk;
+  const int64_t ntask = tx_n * ty_n * tz_n;
+  for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x) {
+    const int64_t tz = task / (tx_n * ty_n), rem = task - tz * tx_n * ty_n;
+    const int64_t i0 = (rem % tx_n) * kTile, j0 = (rem / tx_n) * kTile;
+    const int64_t k0 = tz * A.zchunk;
+    const int64_t k1 = k0 + A.zchunk < A.nz + 1 ? k0 + A.zchunk : A.nz + 1;
+    __syncthreads();  // the previous task's last reads of the rings are done
+    // prologue: planes k0 - 1 and k0, element layer k0 - 1
+    load_plane(A, i0, j0, k0 - 1, smem, (int)((k0 - 1) & 1));
+    load_plane(A, i0, j0, k0, smem, (int)(k0 & 1));
+    __syncthreads();
+    element_layer(A, i0, j0, k0 - 1, smem);
+    for (int64_t k = k0; k < k1; ++k) {
+      __syncthreads();  // node layer k - 1 done with plane slot (k + 1) & 1
+      load_plane(A, i0, j0, k + 1, smem, (int)((k + 1) & 1));
+      __syncthreads();
+      element_layer(A, i0, j0, k, smem);
+      __syncthreads();
+      node_layer(A, i0, j0, k, smem);
+    }
+  }
+}
+
+// u and u_dot of every lattice node, FP32, in node GID order (x, y, z, 0).
+__global__ void k_lattice_gather_u(const LatticeNode* nodes, int64_t n, const double* x, const double* xdot,
+                                   float4* u, float4* ud) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = 3 * (int64_t)nodes[g].lid;
+    u[g] = f4(narrow(x[l]), narrow(x[l + 1]), narrow(x[l + 2]), 0.f);
+    if (xdot) ud[g] = f4(narrow(xdot[l]), narrow(xdot[l + 1]), narrow(xdot[l + 2]), 0.f);
+  }
+}
+
+}  // namespace
+
+size_t lattice_gather_smem() { return kSmBytes; }
+
+cudaError_t launch_lattice_gather(LatticeArgs A, float4* u_work, float4* ud_work, const double* x, const double* xdot,
+                                  cudaStream_t s) {
+  const int64_t n_nodes = (A.nx + 1) * (A.ny + 1) * (A.nz + 1);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  {
+    const int64_t blocks = std::min<int64_t>((n_nodes + 255) / 256, (int64_t)sms * 8);
+    k_lattice_gather_u<<<(unsigned)blocks, 256, 0, s>>>(A.nodes, n_nodes, x, xdot, u_work, xdot ? ud_work : nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  A.u = reinterpret_cast<const float*>(u_work);
+  A.ud = xdot ? reinterpret_cast<const float*>(ud_work) : nullptr;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_lattice_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lattice_gather, kThreads, kSmBytes);
+  if (e != cudaSuccess) return e;
+  const int64_t ntask = ((A.nx + kTile) / kTile) * ((A.ny + kTile) / kTile) * ((A.nz + A.zchunk) / A.zchunk);
+  int64_t grid = (int64_t)(per_sm > 0 ? per_sm : 1) * sms;
+  if (A.grid > 0 && A.grid < grid) grid = A.grid;
+  if (grid > ntask) grid = ntask;
+  k_lattice_gather<<<(unsigned)grid, kThreads, kSmBytes, s>>>(A);
+  return cudaGetLastError();
+}
+
+}  // namespace tx

@@ -661,6 +661,11 @@ class AssemblyEngine:
         """Assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element (hex8 elasticity, mixed)."""
         check(self.dof.h, self.dof.lib.tx_set_assembly_variant(self.dof.h, variant), "tx_set_assembly_variant")
 
+    def setCtaThreads(self, threads):
+        """Threads a CTA of the staged Jacobian kernel (64, 128 or 256; elements per CTA = threads / the
+        element's basis count rounded up to a power of two); 0 restores 128."""
+        check(self.dof.h, self.dof.lib.tx_set_cta_threads(self.dof.h, threads), "tx_set_cta_threads")
+
     def gather_supported(self):
         """Whether the two-phase form holds this handle's rows (not, e.g., quadratic elasticity's)."""
         if self._gather_fits is None:
@@ -668,6 +673,13 @@ class AssemblyEngine:
             check(self.dof.h, self.dof.lib.tx_eval_gather_supported(self.dof.h, C.byref(ok)), "tx_eval_gather_supported")
             self._gather_fits = bool(ok.value)
         return self._gather_fits
+
+    def gather_form(self):
+        """The form of TX_EVAL_GATHER with mixed precision: "lattice" (owner-computes rows of a hex8 elasticity
+        lattice), "two-phase" (element rows to scratch, then the row gather) or None."""
+        form = C.c_int32()
+        check(self.dof.h, self.dof.lib.tx_eval_gather_form(self.dof.h, C.byref(form)), "tx_eval_gather_form")
+        return {_abi.TX_GATHER_LATTICE: "lattice", _abi.TX_GATHER_TWO_PHASE: "two-phase"}.get(form.value)
 
     def gather_applies(self, W, block=-1, workset=(0, -1), deterministic=False, persistent=False):
         """Whether evaluate() with these arguments takes the two-phase form (f and W overwritten)."""

@@ -112,6 +112,164 @@ def time_eval(ae, x, f, W, reps=5, **kw):
     return s.elapsed_time(e) / reps
 
 
+def assembly_bytes(n_vertices, n_dofs, nnz, conn_entries):
+    """Algorithmic bytes of one residual + Jacobian evaluation: vertex coordinates, x, element connectivity
+    (DOF entities of every element), f written, CRS values written, column indices and rowptr read."""
+    return 24 * n_vertices + 8 * n_dofs + 4 * conn_entries + 8 * n_dofs + 12 * nnz + 8 * (n_dofs + 1)
+
+
+def _lattice_vertices(w):
+    d = w.mesh_desc
+    return (d.nx * d.bx + 1) * (d.ny * d.by + 1) * (d.nz * d.bz + 1)
+
+
+def _conn_entries(w):
+    return sum(len(w.conn.getElementBlock(b)) * w.dof.getElementBlockGIDCount(b) // w.dof.n_fields
+               for b in range(w.conn.n_blocks))
+
+
+def _time_kernel(fn, prep, reps):
+    """Mean ms of fn() with CUDA events around each call only (prep() runs outside the events)."""
+    for _ in range(2):
+        prep()
+        fn()
+    torch.cuda.synchronize()
+    total = 0.0
+    for _ in range(reps):
+        prep()
+        s, e = _events()
+        s.record()
+        fn()
+        e.record()
+        e.synchronize()
+        total += s.elapsed_time(e)
+    return total / reps
+
+
+def _assembly_legs(w, ae, x, f, W, peak_gbs, reps, persistent=False, aux=None):
+    """FP64 and mixed R+J of one workload: each precision's tuned kernel, timed alone (zeroing outside)."""
+    from . import autotune
+    E, N = w.n_elements, w.dof.n_dofs
+    bytes_ = assembly_bytes(_lattice_vertices(w), N, w.dof.nnz, _conn_entries(w))
+    out = {"elements": E, "dofs": N, "nnz": w.dof.nnz, "algorithmic_bytes": bytes_}
+    for tag, mixed in (("fp64", False), ("mixed", True)):
+        # per-block launches: the tuned kernel; the persistent launch keeps the workload's worksets
+        cfg = {} if persistent else autotune.tune(ae, x, f, W, mixed=mixed, aux=aux, force=True, reps=2)
+        gather = ae.gather and not persistent
+
+        def prep():
+            if not gather:
+                f.zero_()
+                W.initializeMatrix(0.0)
+        ms = _time_kernel(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, persistent=persistent), prep, reps)
+        form = ("lattice" if gather and mixed and ae.gather_form() == "lattice" else "two-phase" if gather
+                else "persistent" if persistent else "staged" if cfg.get("variant") != 2 else "warp")
+        gbs = bytes_ / ms / 1e6
+        out[tag] = {"ms": ms, "elements_per_s": E / ms * 1e3, "form": form, "achieved_gbs": gbs,
+                    "frac": gbs / peak_gbs}
+    out["mixed_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    return out
+
+
+def newton_heat(w, mixed, tol=1e-10, max_it=12):
+    """Newton on the nonlinear heat workload with T = 0 on the box sides, from T = 0: iterations until
+    ||f|| <= tol ||f(T0)||.  The residual is always FP64; the Jacobian is FP64 or mixed (FP32 element
+    arithmetic), and each linear step J dT = -f is solved by the FP64-refined FP32 CG."""
+    from .panzer import DirichletBC, ModelEvaluator
+    me = ModelEvaluator(w.lof, [DirichletBC(w.dof, A.ALL_SIDES)])
+    T = w.lof.getTpetraVector()
+    f, W, dT = w.lof.getTpetraVector(), me.create_W_op(), w.lof.getTpetraVector()
+    norms = []
+    for _ in range(max_it + 1):
+        me.evalModel(T, f=f)  # FP64 residual
+        norms.append(float(f.norm()))
+        if norms[-1] <= tol * norms[0]:
+            break
+        me.evalModel(T, W=W, mixed=mixed)
+        dT.zero_()
+        me.solve(W, dT, b=-f, rtol=1e-12, inner_rtol=1e-5, max_outer=60)
+        T.add_(dT)
+    return {"iterations": len(norms) - 1, "residual_norms": norms}
+
+
+def measure_configs(peak_gbs, reps=5):
+    """The other named workloads at their stated sizes: FP64 and mixed (or batched) R+J elements/s with the
+    roofline fraction of each precision's tuned kernel (algorithmic bytes / kernel time / HBM peak), the
+    Newmark step of the elastodynamics workload and Newton iteration counts of the nonlinear heat workload."""
+    import gc
+    from .newmark import NewmarkElastodynamics
+    from .panzer import AssemblyEngine, Batch
+    out = {}
+    # C1: Poisson hex8 16^3 (launch-latency bound at this size)
+    w = poisson_hex8(16)
+    ae, x = AssemblyEngine(w.lof), w.lof.getTpetraVector()
+    x.uniform_(-1.0, 1.0)
+    f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
+    out["poisson_hex8_16"] = _assembly_legs(w, ae, x, f, W, peak_gbs, reps)
+    del w, ae, x, f, W
+    # C3: nonlinear heat, hex27 48^3 + tet10 48^3, uneven worksets in one persistent launch
+    w = heat_hex27_tet10(48)
+    ae = AssemblyEngine(w.lof)
+    ae.setWorksetSize(256, 1024, seed=11)
+    g = torch.Generator(device="cuda").manual_seed(2)
+    x = torch.rand(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g)
+    f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
+    r = _assembly_legs(w, ae, x, f, W, peak_gbs, reps, persistent=True)
+    ae.setWorksetSize(256, 1024, seed=11)
+    r["newton"] = {"mixed": newton_heat(w, True), "fp64": newton_heat(w, False)}
+    out["heat_hex27_tet10_48"] = r
+    del w, ae, x, f, W
+    gc.collect()
+    torch.cuda.empty_cache()
+    # C4: elastodynamics hex8 96^3: K_eff assembly and the graph-captured Newmark step
+    w = elastodynamics_hex8(96)
+    ae = AssemblyEngine(w.lof)
+    g = torch.Generator(device="cuda").manual_seed(4)
+    u0 = torch.randn(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g) * 1e-3
+    f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
+    r = _assembly_legs(w, ae, u0, f, W, peak_gbs, reps)
+    del f, W
+    nm = NewmarkElastodynamics(w.me, 1e-3, 0.25, 0.5, mixed=True, outer=3, inner=24)
+    nm.initialize(u0)
+    nm.capture()
+    nm.step()
+    torch.cuda.synchronize()
+    s, e = _events()
+    s.record()
+    rel = [nm.step()[2] for _ in range(10)]
+    e.record()
+    torch.cuda.synchronize()
+    r["newmark"] = {"steps": 10, "ms_per_step": s.elapsed_time(e) / 10,
+                    "max_step_relres": max(float(v) for v in rel)}
+    out["elastodynamics_hex8_96"] = r
+    del w, ae, u0, nm
+    gc.collect()
+    torch.cuda.empty_cache()
+    # C5: 256 independent meshes in one persistent launch
+    ws = mixed_batch(256)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    xs = [torch.rand(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g) for w in ws]
+    auxs = [w.extras.get("J") for w in ws]
+    fs = [w.lof.getTpetraVector() for w in ws]
+    Ws = [w.lof.getTpetraMatrix() for w in ws]
+    b = Batch([w.dof for w in ws], workset=(512, 512))
+    nel = sum(w.n_elements for w in ws)
+    bytes_ = sum(assembly_bytes(_lattice_vertices(w), w.dof.n_dofs, w.dof.nnz, _conn_entries(w)) for w in ws)
+    r = {"instances": len(ws), "elements": nel, "algorithmic_bytes": bytes_}
+    for tag, mixed in (("fp64", False), ("mixed", True)):
+        def prep():
+            for f_, W_ in zip(fs, Ws):
+                f_.zero_()
+                W_.initializeMatrix(0.0)
+        ms = _time_kernel(lambda: b.evaluate(xs, fs, Ws, auxs=auxs, mixed=mixed), prep, reps)
+        gbs = bytes_ / ms / 1e6
+        r[tag] = {"ms": ms, "elements_per_s": nel / ms * 1e3, "form": "batched persistent", "achieved_gbs": gbs,
+                  "frac": gbs / peak_gbs}
+    r["mixed_vs_fp64"] = r["fp64"]["ms"] / r["mixed"]["ms"]
+    out["mixed_batch_256"] = r
+    return out
+
+
 def report(names=("poisson_hex8", "heat_hex27_tet10", "elastodynamics_hex8", "mixed_batch")):
     """Elements/s of the non-headline workloads (one JSON object)."""
     import json
