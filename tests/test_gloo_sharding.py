@@ -1,9 +1,11 @@
 """Sharded assembly on 2 CPU ranks (gloo): partition + Export-ADD = global result.
 
-Each rank assembles the elements of its brick partition (the reference's
-CartesianConnManager split) with the oracle, then the sum-exchange combines
-the ghosted residuals and CRS values; the result must equal the one-rank
-assembly.  Runs without a GPU.
+Each rank takes its brick partition (the reference's CartesianConnManager
+split), reads its elements' LIDs from the product's host numbering
+(DOFManager without a device), builds the export plan of the interface rows,
+assembles its elements with the oracle (the kernels need a GPU) and sums the
+interface rows with the other rank; the result must equal the one-rank
+assembly, and only interface rows may travel.  Runs without a GPU.
 """
 import os
 import socket
@@ -37,22 +39,31 @@ def _worker(rank, world, port, out):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
+        import tianxin_gb300 as tx
         from oracle import oracle as O
         from tianxin_gb300 import _abi as A
         n = (4, 4, 6)
         q = A.equation_set(A.TX_PHYS_ELASTICITY, params=(1.0, 0.3, 0.0, 0.0, -1.0, 0.0))
         o = O.Oracle(A.mesh_desc(n, jitter=0.1, seed=8), q)
+        dof = tx.DOFManager(tx.CartesianConnManager(*n, jitter=0.1, seed=8), q, require_device=False)
         x = np.random.default_rng(0).uniform(-1, 1, o.n_dofs)
         mine = sharding.owned_bricks(n, (1, 1, world), rank)
         lo, hi = min(mine), max(mine) + 1
         assert hi - lo == len(mine)  # z-split: a contiguous element range
+        rowptr, _ = o.graph()
+        plan = sharding.ExportPlan([dof.getElementLIDs(0)[lo:hi]], dof.n_dofs, rowptr)
         f, v = o.evaluate(x, block=0, elem_range=(lo, hi))
         ft, vt = torch.from_numpy(f), torch.from_numpy(v)
-        sharding.export_add([ft, vt])
+        sharding.export_add(plan, ft, vt)
         if rank == 0:
             f_ref, v_ref = o.evaluate(x)
-            out.put((float(np.abs(ft.numpy() - f_ref).max() / np.abs(f_ref).max()),
-                     float(np.abs(vt.numpy() - v_ref).max() / np.abs(v_ref).max())))
+            # every row this rank holds is complete after the exchange
+            rows = plan.local_rows
+            ents = np.concatenate([np.arange(rowptr[r], rowptr[r + 1]) for r in rows])
+            # the interface is the node layer z = 3 (5 x 5 nodes, 3 DOFs each)
+            out.put((float(np.abs(ft.numpy()[rows] - f_ref[rows]).max() / np.abs(f_ref).max()),
+                     float(np.abs(vt.numpy()[ents] - v_ref[ents]).max() / np.abs(v_ref).max()),
+                     len(plan.all_rows), plan.volume(), o.n_dofs + o.nnz))
     finally:
         dist.destroy_process_group()
 
@@ -67,5 +78,7 @@ def test_two_rank_assembly_equals_one_rank():
     for p in procs:
         p.join(timeout=120)
     assert all(p.exitcode == 0 for p in procs)
-    ef, ev = q.get(timeout=5)
+    ef, ev, rows, volume, full = q.get(timeout=5)
     assert ef <= 1e-14 and ev <= 1e-14
+    assert rows == 5 * 5 * 3
+    assert volume < full / 3  # the interface, not the whole arrays

@@ -30,7 +30,9 @@
 // stresses and contractions; the eight element contributions of an entry
 // are summed in FP32 (at most three roundings) and widened to FP64 exactly.
 // Vertex coordinates enter as FP32 hi/lo pairs split on the host, so the
-// element edge vectors keep their FP64 accuracy.
+// element edge vectors keep their FP64 accuracy.  The point sums of the
+// contraction run as two interleaved partial sums (even and odd points) in
+// packed FP32x2 FMAs (fma.rn.f32x2: two IEEE FMAs per instruction).
 #include <algorithm>
 #include <cstdint>
 
@@ -48,21 +50,23 @@ constexpr int kNodes = kTile * kTile;       // 16 owned nodes per layer
 constexpr int kThreads = kNodes * 8;        // eight lanes per node
 constexpr int kRowMax = 243;                // 3 rows x 81 entries (interior node)
 
-// Element record in shared memory, laid out so that the eight lanes of a
-// node (eight different elements, eight different vertices B of them) and
-// the eight points q of one element each hit eight different bank groups:
-//   G: grad N (physical) of the vertex with lattice bits B at point q, in
-//      float4 slot 8 q + (B ^ q);
-//   S: (s00 s11 s22 s01 | s02 s12 f0 f1 | f2 - - -) of point q in slots
-//      3 q + j + rot, rot = the element's lattice parity (x | y << 1 | z << 2),
-//      which differs between the eight elements around a node;
-//   W: w_q det J_q at float 4 rot + q.
-// The record size is a multiple of 128 B (whole bank rows).
-constexpr int kRecG = 0;
-constexpr int kRecS = 64 * 16;
+// Element record in shared memory.  Points go in pairs p = (2 qp, 2 qp + 1);
+// vertex B (lattice bits x | y << 1 | z << 2) of pair qp sits in slot
+// 9 qp + B, so for a fixed pair the eight vertices (the eight lanes of a node
+// read eight different ones) and for a fixed vertex the four pairs fall in
+// different bank groups, and every address is a lane base plus an immediate.
+//   XY: (gx_q0, gx_q1, gy_q0, gy_q1) physical gradients, float4 slots;
+//   Z:  (gz_q0, gz_q1), float2 slots;
+//   S:  (s00 s11 s22 s01 | s02 s12 f0 f1 | f2 - - -) of point q in float4
+//       slots 3 q + j + rot, rot = the element's lattice parity
+//       (x | y << 1 | z << 2), different for the eight elements of a node;
+//   W:  w_q det J_q at float 4 rot + q.
+constexpr int kRecXY = 0;
+constexpr int kRecZ = kRecXY + 36 * 16;
+constexpr int kRecS = kRecZ + 36 * 8;
 constexpr int kRecW = kRecS + 31 * 16;
 constexpr int kRecBytes = ((kRecW + 36 * 4) + 127) / 128 * 128;
-static_assert(kRecBytes == 1664, "element record");
+static_assert(kRecBytes == 1536, "element record");
 
 // Node record of a plane: coordinates (FP32 hi, lo), u, u_dot.
 struct __align__(16) PlaneNode {
@@ -70,14 +74,20 @@ struct __align__(16) PlaneNode {
 };
 
 // shared memory layout
-constexpr int kSmRefGrad = 0;                                    // [q][v] float4 (dN^/dxi, N)
-constexpr int kSmRefW = kSmRefGrad + 64 * 16;                    // [q] w_q
+constexpr int kSmRefG = 0;                                       // [q][B] float4 (dN^/dxi, N), slot 9 q + B
+constexpr int kSmRefN = kSmRefG + 72 * 16;                       // [qp][B] float2 (N(q0), N(q1)), slot 9 qp + B
+constexpr int kSmRefW = kSmRefN + 36 * 8;                        // [q] w_q
 constexpr int kSmPlane = kSmRefW + 8 * 4;                        // 2 x 36 PlaneNode
 constexpr int kSmPlaneInfo = kSmPlane + 2 * kPlane * kPlane * 64;  // owned-node info of the 2 planes
 constexpr int kInfoBytes = 48;                                   // rowstart (8) lid (4) nnb (4) npos (32)
 constexpr int kSmElem = kSmPlaneInfo + 2 * kNodes * kInfoBytes;
 constexpr int kSmStage = kSmElem + 2 * kElems * kRecBytes;       // [node][243] float
 constexpr int kSmBytes = kSmStage + kNodes * kRowMax * 4;
+
+// Which lane writes which exchanged slot (bit 8 e + c): every neighbour block
+// is held by 2^(zero bits of c) lanes after the butterflies; this table picks
+// one of them so that no lane writes more than four blocks of the 27.
+constexpr unsigned long long kWriters = 0x92c2a4e08cc9b8e8ull;
 
 // shards Hexahedron<8> vertex v <-> lattice offset bits (x | y << 1 | z << 2);
 // the map is an involution on these eight codes
@@ -87,6 +97,16 @@ __device__ __forceinline__ int vbits(int v) {
 }
 
 __device__ __forceinline__ float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+
+// Two IEEE FP32 FMAs in one instruction: (a.x b.x + c.x, a.y b.y + c.y).
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(r)
+      : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)),
+        "l"(*reinterpret_cast<unsigned long long*>(&c)));
+  return *reinterpret_cast<float2*>(&r);
+}
 
 // Loads plane node records of node layer kk for the task's 6 x 6 window and
 // the owned nodes' row information.
@@ -127,47 +147,57 @@ __device__ __forceinline__ void load_plane(const LatticeArgs& A, int64_t i0, int
 }
 
 // Geometry, physical gradients and point stresses of the 5 x 5 elements of
-// element layer ek (vertices in plane slots ek & 1 and (ek + 1) & 1).
-// Reference table rg: (dN^/dxi, N) of the vertex with lattice bits B at point
-// q in slot 8 q + (B ^ q).
+// element layer ek (vertices in plane slots ek & 1 and (ek + 1) & 1); one
+// thread per (element, point pair).
+template <bool MASS>
 __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t ek,
                                               unsigned char* smem) {
   if (ek < 0 || ek >= A.nz) return;
-  const float4* rg = reinterpret_cast<const float4*>(smem + kSmRefGrad);
+  const float4* rg = reinterpret_cast<const float4*>(smem + kSmRefG);
   const float* rw = reinterpret_cast<const float*>(smem + kSmRefW);
   const PlaneNode* plo = reinterpret_cast<const PlaneNode*>(smem + kSmPlane) + (int)(ek & 1) * kPlane * kPlane;
   const PlaneNode* phi = reinterpret_cast<const PlaneNode*>(smem + kSmPlane) + (int)((ek + 1) & 1) * kPlane * kPlane;
   unsigned char* rec0 = smem + kSmElem + (int)(ek & 1) * kElems * kRecBytes;
-  for (int task = threadIdx.x; task < kElems * 8; task += blockDim.x) {
-    const int el = task >> 3, q = task & 7;
-    const int ex = el % kElem, ey = el / kElem;
-    const int64_t gx = i0 - 1 + ex, gy = j0 - 1 + ey;
-    if (gx < 0 || gx >= A.nx || gy < 0 || gy >= A.ny) continue;
-    const int rot = (int)(gx & 1) | ((int)(gy & 1) << 1) | ((int)(ek & 1) << 2);
-    unsigned char* rec = rec0 + el * kRecBytes;
-    // vertex with lattice bits B at plane (ex + Bx, ey + By), layer Bz
-    float dX[8][3], U[8][3], UD[8][3];
-    float x0h[3], x0l[3];
+  const int task = threadIdx.x;
+  if (task >= kElems * 4) return;
+  const int el = task >> 2, qp = task & 3;
+  const int ex = el % kElem, ey = el / kElem;
+  const int64_t gx = i0 - 1 + ex, gy = j0 - 1 + ey;
+  if (gx < 0 || gx >= A.nx || gy < 0 || gy >= A.ny) return;
+  const int rot = (int)(gx & 1) | ((int)(gy & 1) << 1) | ((int)(ek & 1) << 2);
+  unsigned char* rec = rec0 + el * kRecBytes;
+  // vertex with lattice bits B at plane (ex + Bx, ey + By), layer Bz
+  float dX[8][3], U[8][3], UD[8][3];
+  float x0h[3], x0l[3];
 #pragma unroll
-    for (int B = 0; B < 8; ++B) {
-      const PlaneNode& p = ((B >> 2) ? phi : plo)[(ex + (B & 1)) + kPlane * (ey + ((B >> 1) & 1))];
-      const float4 h = p.xh, l = p.xl, u = p.u, ud = p.ud;
-      if (B == 0) {
-        x0h[0] = h.x; x0h[1] = h.y; x0h[2] = h.z;
-        x0l[0] = l.x; x0l[1] = l.y; x0l[2] = l.z;
-      }
-      dX[B][0] = (h.x - x0h[0]) + (l.x - x0l[0]);
-      dX[B][1] = (h.y - x0h[1]) + (l.y - x0l[1]);
-      dX[B][2] = (h.z - x0h[2]) + (l.z - x0l[2]);
-      U[B][0] = u.x; U[B][1] = u.y; U[B][2] = u.z;
+  for (int B = 0; B < 8; ++B) {
+    const PlaneNode& p = ((B >> 2) ? phi : plo)[(ex + (B & 1)) + kPlane * (ey + ((B >> 1) & 1))];
+    const float4 h = p.xh, l = p.xl, u = p.u;
+    if (B == 0) {
+      x0h[0] = h.x; x0h[1] = h.y; x0h[2] = h.z;
+      x0l[0] = l.x; x0l[1] = l.y; x0l[2] = l.z;
+    }
+    dX[B][0] = (h.x - x0h[0]) + (l.x - x0l[0]);
+    dX[B][1] = (h.y - x0h[1]) + (l.y - x0l[1]);
+    dX[B][2] = (h.z - x0h[2]) + (l.z - x0l[2]);
+    U[B][0] = u.x; U[B][1] = u.y; U[B][2] = u.z;
+    if constexpr (MASS) {
+      const float4 ud = p.ud;
       UD[B][0] = ud.x; UD[B][1] = ud.y; UD[B][2] = ud.z;
     }
+  }
+  float gp[2][8][3];  // physical gradients at the two points
+  const float lam = A.lam, mu = A.mu;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int q = 2 * qp + h;
+    const float4* rq = rg + 9 * q;
     float J[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) J[k] = 0.f;
 #pragma unroll
     for (int B = 1; B < 8; ++B) {
-      const float4 g = rg[q * 8 + (B ^ q)];
+      const float4 g = rq[B];
       J[0] += dX[B][0] * g.x; J[1] += dX[B][0] * g.y; J[2] += dX[B][0] * g.z;
       J[3] += dX[B][1] * g.x; J[4] += dX[B][1] * g.y; J[5] += dX[B][1] * g.z;
       J[6] += dX[B][2] * g.x; J[7] += dX[B][2] * g.y; J[8] += dX[B][2] * g.z;
@@ -184,25 +214,22 @@ __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, 
     float Gu[9], acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < 9; ++k) Gu[k] = 0.f;
-    float4* G = reinterpret_cast<float4*>(rec + kRecG) + q * 8;
 #pragma unroll
     for (int B = 0; B < 8; ++B) {
-      const float4 g = rg[q * 8 + (B ^ q)];
+      const float4 g = rq[B];
       // grad_i = sum_j Jinv(j, i) grad^_j
-      const float gx0 = Ji[0] * g.x + Ji[3] * g.y + Ji[6] * g.z;
-      const float gy0 = Ji[1] * g.x + Ji[4] * g.y + Ji[7] * g.z;
-      const float gz0 = Ji[2] * g.x + Ji[5] * g.y + Ji[8] * g.z;
-      G[B ^ q] = f4(gx0, gy0, gz0, 0.f);
+      gp[h][B][0] = Ji[0] * g.x + Ji[3] * g.y + Ji[6] * g.z;
+      gp[h][B][1] = Ji[1] * g.x + Ji[4] * g.y + Ji[7] * g.z;
+      gp[h][B][2] = Ji[2] * g.x + Ji[5] * g.y + Ji[8] * g.z;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        Gu[3 * c + 0] += gx0 * U[B][c];
-        Gu[3 * c + 1] += gy0 * U[B][c];
-        Gu[3 * c + 2] += gz0 * U[B][c];
-        acc[c] += g.w * UD[B][c];
+        Gu[3 * c + 0] += gp[h][B][0] * U[B][c];
+        Gu[3 * c + 1] += gp[h][B][1] * U[B][c];
+        Gu[3 * c + 2] += gp[h][B][2] * U[B][c];
+        if constexpr (MASS) acc[c] += g.w * UD[B][c];
       }
     }
     const float tr = Gu[0] + Gu[4] + Gu[8];
-    const float lam = A.lam, mu = A.mu;
     float4* S = reinterpret_cast<float4*>(rec + kRecS) + 3 * q + rot;
     S[0] = f4(mu * (Gu[0] + Gu[0]) + lam * tr, mu * (Gu[4] + Gu[4]) + lam * tr, mu * (Gu[8] + Gu[8]) + lam * tr,
               mu * (Gu[1] + Gu[3]));
@@ -210,12 +237,20 @@ __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, 
     S[2] = f4(A.rho * acc[2] - A.body[2], 0.f, 0.f, 0.f);
     reinterpret_cast<float*>(rec + kRecW)[4 * rot + q] = rw[q] * det;
   }
+  float4* XY = reinterpret_cast<float4*>(rec + kRecXY) + 9 * qp;
+  float2* Z = reinterpret_cast<float2*>(rec + kRecZ) + 9 * qp;
+#pragma unroll
+  for (int B = 0; B < 8; ++B) {
+    XY[B] = f4(gp[0][B][0], gp[1][B][0], gp[0][B][1], gp[1][B][1]);
+    Z[B] = make_float2(gp[0][B][2], gp[1][B][2]);
+  }
 }
 
 // The rows of the 16 owned nodes of node layer k.
+template <bool MASS>
 __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t k,
                                            unsigned char* smem) {
-  const float4* rg = reinterpret_cast<const float4*>(smem + kSmRefGrad);
+  const float2* rn = reinterpret_cast<const float2*>(smem + kSmRefN);
   const int lane = threadIdx.x & 31;
   const int ln = threadIdx.x >> 3;     // owned node of this lane
   const int e = threadIdx.x & 7;       // element around it: offset bits (x | y << 1 | z << 2)
@@ -230,54 +265,77 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
   const int rot = (int)(gx & 1) | ((int)(gy & 1) << 1) | ((int)(gz & 1) << 2);
   const unsigned char* rec =
       smem + kSmElem + ((int)((k - 1 + ez) & 1) * kElems + (lx + ex) + kElem * (ly + ey)) * kRecBytes;
-  const float4* G = reinterpret_cast<const float4*>(rec + kRecG);
+  const float4* XY = reinterpret_cast<const float4*>(rec + kRecXY);
+  const float2* Z = reinterpret_cast<const float2*>(rec + kRecZ);
   const float4* S = reinterpret_cast<const float4*>(rec + kRecS) + rot;
   const float4* W4 = reinterpret_cast<const float4*>(rec + kRecW) + rot;
 
-  // the lane's own weighted gradients and values: W_q grad N_a(q), W_q N_a(q)
-  float wg[8][3], wn[8];
   float r[3] = {0.f, 0.f, 0.f};
   float blk[8][9];
   if (valid) {
     const float4 wa = W4[0], wb = W4[1];
-    const float Wq[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
-    const float sgn = Wq[0] < 0.f ? -1.f : 1.f;  // computeCellMeasure: |.| by the first point's sign
+    const float sgn = wa.x < 0.f ? -1.f : 1.f;  // computeCellMeasure: |.| by the first point's sign
+    const float Wq[8] = {wa.x * sgn, wa.y * sgn, wa.z * sgn, wa.w * sgn, wb.x * sgn, wb.y * sgn, wb.z * sgn, wb.w * sgn};
+    // the lane's own weighted gradients and values as point pairs:
+    // wg[qp][i] = (W grad_i N_a)(q0, q1), wn[qp] = (W N_a)(q0, q1)
+    float2 wg[4][3], wn[4];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const float w = Wq[q] * sgn;
-      const float4 g = G[q * 8 + (lbits ^ q)];
-      wg[q][0] = w * g.x; wg[q][1] = w * g.y; wg[q][2] = w * g.z;
-      wn[q] = w * rg[q * 8 + (lbits ^ q)].w;
-      const float4 s0 = S[q * 3], s1 = S[q * 3 + 1], s2 = S[q * 3 + 2];
-      // residual row a: grad N_a . sigma + N_a (rho acc - b)
-      r[0] += wg[q][0] * s0.x + wg[q][1] * s0.w + wg[q][2] * s1.x + wn[q] * s1.z;
-      r[1] += wg[q][0] * s0.w + wg[q][1] * s0.y + wg[q][2] * s1.y + wn[q] * s1.w;
-      r[2] += wg[q][0] * s1.x + wg[q][1] * s1.y + wg[q][2] * s0.z + wn[q] * s2.x;
+    for (int qp = 0; qp < 4; ++qp) {
+      const float4 xy = XY[9 * qp + lbits];
+      const float2 z = Z[9 * qp + lbits];
+      const float w0 = Wq[2 * qp], w1 = Wq[2 * qp + 1];
+      wg[qp][0] = make_float2(w0 * xy.x, w1 * xy.y);
+      wg[qp][1] = make_float2(w0 * xy.z, w1 * xy.w);
+      wg[qp][2] = make_float2(w0 * z.x, w1 * z.y);
+      const float2 na = rn[9 * qp + lbits];
+      wn[qp] = make_float2(w0 * na.x, w1 * na.y);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = 2 * qp + h;
+        const float g0 = h ? wg[qp][0].y : wg[qp][0].x, g1 = h ? wg[qp][1].y : wg[qp][1].x;
+        const float g2 = h ? wg[qp][2].y : wg[qp][2].x, n = h ? wn[qp].y : wn[qp].x;
+        const float4 s0 = S[q * 3], s1 = S[q * 3 + 1], s2 = S[q * 3 + 2];
+        // residual row a: grad N_a . sigma + N_a (rho acc - b)
+        r[0] += g0 * s0.x + g1 * s0.w + g2 * s1.x + n * s1.z;
+        r[1] += g0 * s0.w + g1 * s0.y + g2 * s1.y + n * s1.w;
+        r[2] += g0 * s1.x + g1 * s1.y + g2 * s0.z + n * s2.x;
+      }
     }
-    const float lam = A.lam, mu = A.mu, beta = A.beta, am = A.alpha * A.rho;
+    const float bl = A.beta * A.lam, bm = A.beta * A.mu, am = A.alpha * A.rho;
     // slot c holds the block of the element vertex with bits c ^ lbits (bit per
     // axis: 0 = the node's own lattice line, 1 = this element's neighbour line)
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const int bb = c ^ lbits;
-      float P[9], M = 0.f;
+      const float4* xyb = XY + bb;
+      const float2* zb = Z + bb;
+      float2 P[9], M = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int t = 0; t < 9; ++t) P[t] = 0.f;
+      for (int t = 0; t < 9; ++t) P[t] = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float4 g = G[q * 8 + (bb ^ q)];
-        P[0] += wg[q][0] * g.x; P[1] += wg[q][0] * g.y; P[2] += wg[q][0] * g.z;
-        P[3] += wg[q][1] * g.x; P[4] += wg[q][1] * g.y; P[5] += wg[q][1] * g.z;
-        P[6] += wg[q][2] * g.x; P[7] += wg[q][2] * g.y; P[8] += wg[q][2] * g.z;
-        M += wn[q] * rg[q * 8 + (bb ^ q)].w;
+      for (int qp = 0; qp < 4; ++qp) {
+        const float4 xy = xyb[9 * qp];
+        const float2 z = zb[9 * qp];
+        const float2 gxp = make_float2(xy.x, xy.y), gyp = make_float2(xy.z, xy.w);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          P[3 * i + 0] = ffma2(wg[qp][i], gxp, P[3 * i + 0]);
+          P[3 * i + 1] = ffma2(wg[qp][i], gyp, P[3 * i + 1]);
+          P[3 * i + 2] = ffma2(wg[qp][i], z, P[3 * i + 2]);
+        }
+        if constexpr (MASS) M = ffma2(wn[qp], rn[9 * qp + bb], M);
       }
-      const float tp = P[0] + P[4] + P[8];
+      float Ps[9];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) Ps[t] = P[t].x + P[t].y;
+      const float tp = Ps[0] + Ps[4] + Ps[8];
+      const float md = MASS ? am * (M.x + M.y) : 0.f;
 #pragma unroll
       for (int cc = 0; cc < 3; ++cc)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          float kv = beta * (lam * P[3 * cc + d] + mu * P[3 * d + cc]);
-          if (cc == d) kv += beta * mu * tp + am * M;
+          float kv = bl * Ps[3 * cc + d] + bm * Ps[3 * d + cc];
+          if (cc == d) kv += bm * tp + md;
           blk[c][3 * cc + d] = kv;
         }
     }
@@ -302,15 +360,15 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
     for (int t = 0; t < 3; ++t) r[t] += __shfl_xor_sync(0xffffffffu, r[t], 1 << ax);
   }
   // stage the node's rows: slot c of lane e is neighbour offset
-  // d_a = 0 (bit 0) or 2 e_a - 1 (bit 1); the lane with e_a = 0 on every
-  // shared axis writes it
+  // d_a = 0 (bit 0) or 2 e_a - 1 (bit 1); kWriters names the lane that writes it
   float* stage = reinterpret_cast<float*>(smem + kSmStage) + ln * kRowMax;
   if (nnb > 0) {
     const uint8_t* npos = info + 16;
     const int rl = 3 * nnb;  // entries of one row
+    const unsigned wmask = (unsigned)(kWriters >> (8 * e)) & 0xffu;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      if ((e & ~c & 7) != 0) continue;
+      if (!((wmask >> c) & 1u)) continue;
       const int dx = (c & 1) ? 2 * ex - 1 : 0, dy = (c & 2) ? 2 * ey - 1 : 0, dz = (c & 4) ? 2 * ez - 1 : 0;
       const int p = npos[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
       if (p == 0xff) continue;
@@ -339,17 +397,23 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
   }
 }
 
+template <bool MASS>
 __global__ void __launch_bounds__(kThreads, 2) k_lattice_gather(LatticeArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  // reference tables (hex8, 2 x 2 x 2 Gauss): [q][v] (dN^/dxi, N), w_q
+  // reference tables (hex8, 2 x 2 x 2 Gauss) from the packed FP64 tables
+  // [w | geo_val | geo_grad | val | grad]: (dN^/dxi, N) of the vertex with
+  // lattice bits B at point q, the values N at point pairs, and w_q
   {
-    const double* ref = A.ref;  // [w | geo_val | geo_grad | val | grad]
-    float4* rg = reinterpret_cast<float4*>(smem + kSmRefGrad);
+    const double* ref = A.ref;
+    float4* rg = reinterpret_cast<float4*>(smem + kSmRefG);
+    float* rn = reinterpret_cast<float*>(smem + kSmRefN);
     float* rw = reinterpret_cast<float*>(smem + kSmRefW);
     for (int i = threadIdx.x; i < 64; i += blockDim.x) {  // i = q * 8 + v (shards vertex v)
       const int q = i >> 3, B = vbits(i & 7);
       const double* gr = ref + 8 + 64 + 192 + 64 + 3 * i;
-      rg[q * 8 + (B ^ q)] = f4(narrow(gr[0]), narrow(gr[1]), narrow(gr[2]), narrow(ref[8 + 64 + 192 + i]));
+      const float n = narrow(ref[8 + 64 + 192 + i]);
+      rg[9 * q + B] = f4(narrow(gr[0]), narrow(gr[1]), narrow(gr[2]), n);
+      rn[2 * (9 * (q >> 1) + B) + (q & 1)] = n;
     }
     for (int i = threadIdx.x; i < 8; i += blockDim.x) rw[i] = narrow(ref[i]);
   }
@@ -366,14 +430,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_lattice_gather(LatticeArgs A) {
     load_plane(A, i0, j0, k0 - 1, smem, (int)((k0 - 1) & 1));
     load_plane(A, i0, j0, k0, smem, (int)(k0 & 1));
     __syncthreads();
-    element_layer(A, i0, j0, k0 - 1, smem);
+    element_layer<MASS>(A, i0, j0, k0 - 1, smem);
     for (int64_t k = k0; k < k1; ++k) {
       __syncthreads();  // node layer k - 1 done with plane slot (k + 1) & 1
       load_plane(A, i0, j0, k + 1, smem, (int)((k + 1) & 1));
       __syncthreads();
-      element_layer(A, i0, j0, k, smem);
+      element_layer<MASS>(A, i0, j0, k, smem);
       __syncthreads();
-      node_layer(A, i0, j0, k, smem);
+      node_layer<MASS>(A, i0, j0, k, smem);
     }
   }
 }
@@ -386,6 +450,25 @@ __global__ void k_lattice_gather_u(const LatticeNode* nodes, int64_t n, const do
     u[g] = f4(narrow(x[l]), narrow(x[l + 1]), narrow(x[l + 2]), 0.f);
     if (xdot) ud[g] = f4(narrow(xdot[l]), narrow(xdot[l + 1]), narrow(xdot[l + 2]), 0.f);
   }
+}
+
+template <bool MASS>
+cudaError_t launch_main(const LatticeArgs& A, int sms, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_lattice_gather<MASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lattice_gather<MASS>, kThreads, kSmBytes);
+  if (e != cudaSuccess) return e;
+  const int64_t ntask = ((A.nx + kTile) / kTile) * ((A.ny + kTile) / kTile) * ((A.nz + A.zchunk) / A.zchunk);
+  int64_t grid = (int64_t)(per_sm > 0 ? per_sm : 1) * sms;
+  if (A.grid > 0 && A.grid < grid) grid = A.grid;
+  if (grid > ntask) grid = ntask;
+  k_lattice_gather<MASS><<<(unsigned)grid, kThreads, kSmBytes, s>>>(A);
+  return cudaGetLastError();
 }
 
 }  // namespace
@@ -406,21 +489,9 @@ cudaError_t launch_lattice_gather(LatticeArgs A, float4* u_work, float4* ud_work
   }
   A.u = reinterpret_cast<const float*>(u_work);
   A.ud = xdot ? reinterpret_cast<const float*>(ud_work) : nullptr;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_lattice_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lattice_gather, kThreads, kSmBytes);
-  if (e != cudaSuccess) return e;
-  const int64_t ntask = ((A.nx + kTile) / kTile) * ((A.ny + kTile) / kTile) * ((A.nz + A.zchunk) / A.zchunk);
-  int64_t grid = (int64_t)(per_sm > 0 ? per_sm : 1) * sms;
-  if (A.grid > 0 && A.grid < grid) grid = A.grid;
-  if (grid > ntask) grid = ntask;
-  k_lattice_gather<<<(unsigned)grid, kThreads, kSmBytes, s>>>(A);
-  return cudaGetLastError();
+  // the time-derivative (mass) terms only where they contribute
+  const bool mass = A.rho != 0.f && (A.alpha != 0.f || xdot != nullptr);
+  return mass ? launch_main<true>(A, sms, s) : launch_main<false>(A, sms, s);
 }
 
 }  // namespace tx
