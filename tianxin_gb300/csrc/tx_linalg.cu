@@ -206,41 +206,70 @@ __global__ void __launch_bounds__(kThreads) k_spmv(int64_t n, const int64_t* __r
 // row end re-reads block j and zeroes its x values (a select, not an FP64
 // multiply: GB300's FP64 pipe is the scarce unit here, one FMA an entry), and
 // a column index outside [0, n_ent) reads entity 0.
+// One pass of UU blocks a lane (blocks j, j + G, ..., j + (UU - 1) G); CHECK:
+// slots may lie past the row end (the last pass of a row).
+template <typename T, int NF, int G, int UU, bool CHECK>
+__device__ __forceinline__ void entity_pass(int64_t j, int64_t b, int64_t deg, int64_t rs,
+                                            const int32_t* __restrict__ ecol, const T* __restrict__ v0,
+                                            const T* __restrict__ x, int64_t n_ent, T (&s)[NF]) {
+  bool in[UU];
+  int64_t m[UU];
+  T v[UU][NF][NF];
+#pragma unroll
+  for (int u = 0; u < UU; ++u) {
+    const int64_t jj = j + u * G;
+    in[u] = !CHECK || jj < deg;
+    const int64_t jc = in[u] ? jj : j;
+    const uint32_t mm = (uint32_t)__ldcs(ecol + b + jc);
+    m[u] = (uint64_t)mm < (uint64_t)n_ent ? (int64_t)mm : 0;
+#pragma unroll
+    for (int c = 0; c < NF; ++c)
+#pragma unroll
+      for (int d = 0; d < NF; ++d) v[u][c][d] = __ldcs(v0 + c * rs + NF * jc + d);
+  }
+#pragma unroll
+  for (int u = 0; u < UU; ++u) {
+    T xm[NF];
+#pragma unroll
+    for (int d = 0; d < NF; ++d) xm[d] = __ldg(x + NF * m[u] + d);
+    if (in[u]) {  // a pass slot past the row end issues no FMAs
+#pragma unroll
+      for (int c = 0; c < NF; ++c)
+#pragma unroll
+        for (int d = 0; d < NF; ++d) s[c] += v[u][c][d] * xm[d];
+    }
+  }
+}
+
+// Full passes of U blocks a lane while the whole pass lies inside the row,
+// then one last pass of just enough blocks a lane for the rest: an interior
+// elasticity entity (27 blocks) on 4 lanes x 4 blocks takes 16 + 12 slots
+// instead of 16 + 16, so the FP64 pipe (one FMA a lane-slot) idles on one
+// slot in 28 rather than five in 32.  Every load address lies inside its
+// array whatever the data: a slot past the row end re-reads block j (and
+// issues no FMAs), and a column index outside [0, n_ent) reads entity 0.
 template <typename T, int NF, int G, int U>
 __device__ __forceinline__ void entity_dot(int64_t b, int64_t deg, int sub, const int32_t* __restrict__ ecol,
                                            const T* __restrict__ vals, const T* __restrict__ x, int64_t n_ent,
                                            T (&s)[NF]) {
   const T* v0 = vals + (int64_t)NF * NF * b;
   const int64_t rs = (int64_t)NF * deg;  // distance between the entity's rows
-  for (int64_t j = sub; j < deg; j += G * U) {
-    bool in[U];
-    int64_t m[U];
-    T v[U][NF][NF];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int64_t jj = j + u * G;
-      in[u] = jj < deg;
-      const int64_t jc = in[u] ? jj : j;
-      const uint32_t mm = (uint32_t)__ldcs(ecol + b + jc);
-      m[u] = (uint64_t)mm < (uint64_t)n_ent ? (int64_t)mm : 0;
-#pragma unroll
-      for (int c = 0; c < NF; ++c)
-#pragma unroll
-        for (int d = 0; d < NF; ++d) v[u][c][d] = __ldcs(v0 + c * rs + NF * jc + d);
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      T xm[NF];
-#pragma unroll
-      for (int d = 0; d < NF; ++d) xm[d] = __ldg(x + NF * m[u] + d);
-      if (in[u]) {  // a pass slot past the row end issues no FMAs
-#pragma unroll
-        for (int c = 0; c < NF; ++c)
-#pragma unroll
-          for (int d = 0; d < NF; ++d) s[c] += v[u][c][d] * xm[d];
-      }
-    }
+  const int64_t full = deg / (G * U) * (G * U);
+  int64_t j = sub;
+  for (; j < full; j += G * U) entity_pass<T, NF, G, U, false>(j, b, deg, rs, ecol, v0, x, n_ent, s);
+  const int64_t rest = deg - full;  // blocks left for the last pass: fewer than G * U
+  if (rest <= 0) return;
+  const int64_t uu = (rest + G - 1) / G;
+  if constexpr (U >= 4) {
+    if (uu >= 4) { entity_pass<T, NF, G, 4, true>(j, b, deg, rs, ecol, v0, x, n_ent, s); return; }
   }
+  if constexpr (U >= 3) {
+    if (uu == 3) { entity_pass<T, NF, G, 3, true>(j, b, deg, rs, ecol, v0, x, n_ent, s); return; }
+  }
+  if constexpr (U >= 2) {
+    if (uu == 2) { entity_pass<T, NF, G, 2, true>(j, b, deg, rs, ecol, v0, x, n_ent, s); return; }
+  }
+  entity_pass<T, NF, G, 1, true>(j, b, deg, rs, ecol, v0, x, n_ent, s);
 }
 
 // Sums the G lanes' partial rows of one entity (NF = 3) by reduce-scatter:
@@ -310,7 +339,8 @@ __global__ void __launch_bounds__(kThreads, entity_min_blocks(G, U, sizeof(T))) 
     const T sc = entity_reduce<T, NF, G>(s, sub);
     if (r < n_ent && sub < NF) {
       const int64_t row = (int64_t)NF * r + sub;
-      y[row] = beta == T(0) ? alpha * sc : alpha * sc + beta * y[row];
+      // y = A x needs no multiply (each FP64 operation costs a pipe slot here)
+      y[row] = beta == T(0) ? (alpha == T(1) ? sc : alpha * sc) : alpha * sc + beta * y[row];
     }
   }
 }
