@@ -529,8 +529,9 @@ def run_ours(a):
             "e2e": e2e,
             "gpu_launches": (3 if gather else 2) * a.steps,
             "autotune": {"mixed": {k: v for k, v in tuned.items() if k != "candidates"},
+                         "mixed_candidates": "(variant, scatter_direct, gather, cta_threads, grid_cap, ms)",
                          "mixed_candidates_ms": [(c.get("variant"), c.get("scatter_direct"), c.get("gather", False),
-                                                  c.get("grid_cap"), round(c["ms"], 3))
+                                                  c.get("cta_threads", 0), c.get("grid_cap"), round(c["ms"], 3))
                                                  for c in tuned.get("candidates", [])],
                          "fp64": {k: v for k, v in tuned64.items() if k != "candidates"}},
             "clocks": clk,
