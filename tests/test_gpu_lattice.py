@@ -92,3 +92,19 @@ def test_lattice_gather_with_dirichlet_model_evaluator(cuda):
     me.evalModel(torch.from_numpy(x_h).cuda(), f=f, W=W, mixed=True, deterministic=True)
     assert rel(f.cpu().numpy(), f_ref) <= TOL_MIXED
     assert rel(W.values.cpu().numpy(), v_ref) <= TOL_MIXED
+
+
+def test_lattice_gather_regular_lattice_zero_entries(cuda):
+    # no jitter: some couplings of the regular lattice cancel to exact zeros, which the copy-out widens exactly
+    o, dof, lof = setup((5, 4, 6), (1.0, 0.25, 0.0, 0.0, -1.0, 0.0), jitter=0.0)
+    x_h = np.random.default_rng(6).uniform(-1, 1, o.n_dofs)
+    f_ref, v_ref = o.evaluate(x_h)
+    x = torch.from_numpy(x_h).cuda()
+    ae = tx.AssemblyEngine(lof)
+    f, W = lof.getTpetraVector(), lof.getTpetraMatrix()
+    ae.evaluate(x, f=f, W=W, mixed=True, gather=True)
+    wg = W.values.cpu().numpy()
+    assert rel(f.cpu().numpy(), f_ref) <= TOL_MIXED and rel(wg, v_ref) <= TOL_MIXED
+    assert np.isfinite(wg).all()
+    tiny = np.abs(v_ref) <= 1e-14 * np.abs(v_ref).max()
+    assert np.abs(wg[tiny]).max() <= 1e-6 * np.abs(v_ref).max()

@@ -393,7 +393,24 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
     if (nb == 0) continue;
     double* dst = A.vals + *reinterpret_cast<const int64_t*>(inf);
     const float* src = reinterpret_cast<const float*>(smem + kSmStage) + (wn0 + m) * kRowMax;
-    for (int t = lane; t < 9 * nb; t += 32) __stcs(dst + t, widen(src[t]));
+    // exact FP32 -> FP64 widening by integer operations for zeros and normal
+    // numbers (exponent rebiased, fraction moved up; no call, so no register
+    // saving around the loop); a subnormal, infinity or NaN anywhere in the
+    // node's rows (a lane flag, one vote a node) sends those entries through
+    // the hardware conversion afterwards
+    bool rare = false;
+    for (int t = lane; t < 9 * nb; t += 32) {
+      const uint32_t b = __float_as_uint(src[t]), a = b & 0x7fffffffu;
+      rare |= (a != 0u) & (a - 0x00800000u >= 0x7f000000u);
+      const uint32_t hi = a ? (b & 0x80000000u) | ((a >> 3) + 0x38000000u) : b;
+      __stcs(dst + t, __hiloint2double((int)hi, (int)(b << 29)));
+    }
+    if (__any_sync(0xffffffffu, rare))
+      for (int t = lane; t < 9 * nb; t += 32) {
+        const float v = src[t];
+        const uint32_t a = __float_as_uint(v) & 0x7fffffffu;
+        if (a != 0u && a - 0x00800000u >= 0x7f000000u) __stcs(dst + t, (double)v);
+      }
   }
 }
 
