@@ -455,15 +455,7 @@ int eval_lattice(tx_handle h, const tx_eval_args& a, const tx::EvalParams& P) {
   const tx::Mesh& m = h->mesh;
   tx::LatticeArgs L;
   L.nx = m.NX; L.ny = m.NY; L.nz = m.NZ;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // z chunks: about eight tasks per resident CTA (two per SM), so the last wave is short
-  const int64_t cols = ((m.NX + 4) / 4) * ((m.NY + 4) / 4);
-  const int64_t want = 8 * 2 * (int64_t)sms;
-  const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(m.NZ + 1, (want + cols - 1) / cols));
-  L.zchunk = (m.NZ + 1 + chunks - 1) / chunks;
-  L.grid = h->grid_cap;
+  L.grid = h->grid_cap;  // the z chunk length is picked by the launcher for its grid
   L.nodes = h->d_lat;
   L.ref = h->blocks[0].ref;
   L.lam = (float)P.lam; L.mu = (float)P.mu; L.rho = (float)P.p[5];

@@ -103,7 +103,7 @@ struct __align__(16) LatticeNode {
 static_assert(sizeof(LatticeNode) == 80, "LatticeNode layout");
 struct LatticeArgs {
   int64_t nx = 0, ny = 0, nz = 0;   // bricks per direction
-  int64_t zchunk = 0;               // node layers per task
+  int64_t zchunk = 0;               // node layers per task (set by launch_lattice_gather)
   int grid = 0;                     // CTA cap (0: one wave of resident CTAs)
   const LatticeNode* nodes = nullptr;
   const float* u = nullptr;         // [nodes][4] FP32 (set by the launcher)

@@ -9,22 +9,28 @@
 // the rows are gathered instead: a CTA owns a 4 x 4 column of nodes and
 // walks it up the z axis one node layer at a time.  At layer k it
 //
-//   1. computes the geometry and point stresses of the 5 x 5 elements of
-//      element layer k (its own 4 x 4 and a one-element halo) into a ring of
-//      two element layers in shared memory;
+//   1. computes the geometry, physical gradients and residual rows of the
+//      5 x 5 elements of element layer k (its own 4 x 4 and a one-element
+//      halo) into a ring of two element layers in shared memory (1 KB an
+//      element; four lanes an element, two points each, the residual shares
+//      summed across the four lanes);
 //   2. assembles the rows of its 16 nodes of layer k from the 8 elements
 //      around each node (element layers k - 1 and k): eight lanes per node,
 //      one element each; each lane forms its element's 3 x 24 block-row of
 //      the node (the closed form of the AD Jacobian, as in the per-element
-//      kernel) and the eight lanes sum the blocks that land on the same
-//      neighbour with three butterfly exchanges (x, y, z), a fixed order;
+//      kernel) one 3 x 3 block at a time, and the eight lanes sum the blocks
+//      that land on the same neighbour with up to three butterfly exchanges
+//      (x, y, z: a fixed order) before the next block is formed, so one
+//      block is live in registers (three CTAs of 128 threads a SM);
 //   3. stages the node's 3 rows (81 values each in the interior) in shared
-//      memory in CRS order and writes them with coalesced stores.
+//      memory in CRS order and writes them with coalesced 16-byte stores.
 //
 // f and the CRS values are written exactly once (no zeroing, no atomics, no
 // read-modify-write of the 4 GB matrix) and every run gives the same bits.
 // Halo elements are recomputed by the neighbouring columns (25 element
 // geometries per 16 nodes); the Jacobian rows themselves are formed once.
+// Tasks (a node column's z chunk) go to the CTAs round-robin; the chunk
+// length is picked at launch for the grid.
 //
 // Precision: the mixed evaluation type (TX_EVAL_MIXED): FP32 geometry,
 // stresses and contractions; the eight element contributions of an entry
@@ -49,24 +55,29 @@ constexpr int kElems = kElem * kElem;       // 25 elements per layer
 constexpr int kNodes = kTile * kTile;       // 16 owned nodes per layer
 constexpr int kThreads = kNodes * 8;        // eight lanes per node
 constexpr int kRowMax = 243;                // 3 rows x 81 entries (interior node)
+constexpr int kStageRow = 248;              // staged floats a node: one parity slot, 243 entries, float4 tail
 
-// Element record in shared memory.  Points go in pairs p = (2 qp, 2 qp + 1);
-// vertex B (lattice bits x | y << 1 | z << 2) of pair qp sits in slot
-// 9 qp + B, so for a fixed pair the eight vertices (the eight lanes of a node
-// read eight different ones) and for a fixed vertex the four pairs fall in
-// different bank groups, and every address is a lane base plus an immediate.
+// Element record in shared memory, 1 KB.  Points go in pairs p = (2 qp,
+// 2 qp + 1); vertex B (lattice bits x | y << 1 | z << 2) of pair qp sits in
+// slot 9 qp + B, so for a fixed pair the eight vertices (the eight lanes of a
+// node read eight different ones) and for a fixed vertex the four pairs fall
+// in different bank groups, and every address is a lane base plus an
+// immediate.
 //   XY: (gx_q0, gx_q1, gy_q0, gy_q1) physical gradients, float4 slots;
-//   Z:  (gz_q0, gz_q1), float2 slots;
-//   S:  (s00 s11 s22 s01 | s02 s12 f0 f1 | f2 - - -) of point q in float4
-//       slots 3 q + j + rot, rot = the element's lattice parity
-//       (x | y << 1 | z << 2), different for the eight elements of a node;
-//   W:  w_q det J_q at float 4 rot + q.
+//   Z:  (gz_q0, gz_q1), float2 slot 8 qp + B, 64 bytes further on in
+//       elements of odd lattice x (two nodes of a warp read the same slot of
+//       two x-neighbouring elements in one 64-bit load: 16 banks apart);
+//   R:  float4 slot B: the element's residual row of vertex B (summed over
+//       the points) and, in .w, the signed weight W_q = s w_q det J_q of point
+//       q = B ^ rot, rot the parity bits of the element's lattice position (s
+//       the sign of det J at the first point): the eight elements around a
+//       node have eight different parities, so the eight lanes of a node read
+//       W_q from eight different slots.
 constexpr int kRecXY = 0;
 constexpr int kRecZ = kRecXY + 36 * 16;
-constexpr int kRecS = kRecZ + 36 * 8;
-constexpr int kRecW = kRecS + 31 * 16;
-constexpr int kRecBytes = ((kRecW + 36 * 4) + 127) / 128 * 128;
-static_assert(kRecBytes == 1536, "element record");
+constexpr int kRecR = kRecZ + 32 * 8 + 64;
+constexpr int kRecBytes = ((kRecR + 8 * 16) + 127) / 128 * 128;
+static_assert(kRecBytes == 1024, "element record");
 
 // Node record of a plane: coordinates (FP32 hi, lo), u, u_dot.
 struct __align__(16) PlaneNode {
@@ -82,7 +93,7 @@ constexpr int kSmPlaneInfo = kSmPlane + 2 * kPlane * kPlane * 64;  // owned-node
 constexpr int kInfoBytes = 48;                                   // rowstart (8) lid (4) nnb (4) npos (32)
 constexpr int kSmElem = kSmPlaneInfo + 2 * kNodes * kInfoBytes;
 constexpr int kSmStage = kSmElem + 2 * kElems * kRecBytes;       // [node][243] float
-constexpr int kSmBytes = kSmStage + kNodes * kRowMax * 4;
+constexpr int kSmBytes = kSmStage + kNodes * kStageRow * 4;
 
 // Which lane writes which exchanged slot (bit 8 e + c): every neighbour block
 // is held by 2^(zero bits of c) lanes after the butterflies; this table picks
@@ -146,9 +157,12 @@ __device__ __forceinline__ void load_plane(const LatticeArgs& A, int64_t i0, int
   }
 }
 
-// Geometry, physical gradients and point stresses of the 5 x 5 elements of
+// Geometry, physical gradients and residual rows of the 5 x 5 elements of
 // element layer ek (vertices in plane slots ek & 1 and (ek + 1) & 1); one
-// thread per (element, point pair).
+// thread per (element, point pair), the four threads of an element adjacent
+// lanes of one warp.  Each thread forms its two points' share of the
+// element's 8 x 3 residual rows, W_q (grad N_B . sigma_q + N_B (rho acc_q -
+// b)), and two butterflies over the four lanes sum the shares.
 template <bool MASS>
 __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t ek,
                                               unsigned char* smem) {
@@ -163,7 +177,8 @@ __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, 
   const int el = task >> 2, qp = task & 3;
   const int ex = el % kElem, ey = el / kElem;
   const int64_t gx = i0 - 1 + ex, gy = j0 - 1 + ey;
-  if (gx < 0 || gx >= A.nx || gy < 0 || gy >= A.ny) return;
+  if (gx < 0 || gx >= A.nx || gy < 0 || gy >= A.ny) return;  // the element's four lanes alike
+  const unsigned m4 = 0xfu << (threadIdx.x & 28);              // those four lanes
   const int rot = (int)(gx & 1) | ((int)(gy & 1) << 1) | ((int)(ek & 1) << 2);
   unsigned char* rec = rec0 + el * kRecBytes;
   // vertex with lattice bits B at plane (ex + Bx, ey + By), layer Bz
@@ -186,64 +201,127 @@ __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, 
       UD[B][0] = ud.x; UD[B][1] = ud.y; UD[B][2] = ud.z;
     }
   }
-  float gp[2][8][3];  // physical gradients at the two points
+  // the two points' inverse Jacobians and accelerations first (dX and UD
+  // then dead), then per point: gradients, stress, residual shares
+  float Ji[2][9], det[2], acc[2][3];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float4* rq = rg + 9 * (2 * qp + h);
+    float J[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) J[k] = 0.f;
+    acc[h][0] = acc[h][1] = acc[h][2] = 0.f;
+#pragma unroll
+    for (int B = 0; B < 8; ++B) {
+      const float4 g = rq[B];
+      if (B > 0) {
+        J[0] += dX[B][0] * g.x; J[1] += dX[B][0] * g.y; J[2] += dX[B][0] * g.z;
+        J[3] += dX[B][1] * g.x; J[4] += dX[B][1] * g.y; J[5] += dX[B][1] * g.z;
+        J[6] += dX[B][2] * g.x; J[7] += dX[B][2] * g.y; J[8] += dX[B][2] * g.z;
+      }
+      if constexpr (MASS) {
+        acc[h][0] += g.w * UD[B][0]; acc[h][1] += g.w * UD[B][1]; acc[h][2] += g.w * UD[B][2];
+      }
+    }
+    const float c00 = J[4] * J[8] - J[5] * J[7];
+    const float c01 = J[5] * J[6] - J[3] * J[8];
+    const float c02 = J[3] * J[7] - J[4] * J[6];
+    det[h] = J[0] * c00 + J[1] * c01 + J[2] * c02;
+    const float id = 1.0f / det[h];
+    Ji[h][0] = c00 * id; Ji[h][1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[h][2] = (J[1] * J[5] - J[2] * J[4]) * id;
+    Ji[h][3] = c01 * id; Ji[h][4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[h][5] = (J[2] * J[3] - J[0] * J[5]) * id;
+    Ji[h][6] = c02 * id; Ji[h][7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[h][8] = (J[0] * J[4] - J[1] * J[3]) * id;
+  }
+  float wd[2];      // w_q det J_q at the two points
+  float res[8][3];  // the two points' share of the residual rows (unsigned weights)
+  float g0[8][3];   // physical gradients at the first point, stored with the second's
+#pragma unroll
+  for (int B = 0; B < 8; ++B) res[B][0] = res[B][1] = res[B][2] = 0.f;
+  float4* XY = reinterpret_cast<float4*>(rec + kRecXY) + 9 * qp;
+  float2* Z = reinterpret_cast<float2*>(rec + kRecZ + 64 * (int)(gx & 1)) + 8 * qp;
   const float lam = A.lam, mu = A.mu;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int q = 2 * qp + h;
     const float4* rq = rg + 9 * q;
-    float J[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) J[k] = 0.f;
-#pragma unroll
-    for (int B = 1; B < 8; ++B) {
-      const float4 g = rq[B];
-      J[0] += dX[B][0] * g.x; J[1] += dX[B][0] * g.y; J[2] += dX[B][0] * g.z;
-      J[3] += dX[B][1] * g.x; J[4] += dX[B][1] * g.y; J[5] += dX[B][1] * g.z;
-      J[6] += dX[B][2] * g.x; J[7] += dX[B][2] * g.y; J[8] += dX[B][2] * g.z;
-    }
-    const float c00 = J[4] * J[8] - J[5] * J[7];
-    const float c01 = J[5] * J[6] - J[3] * J[8];
-    const float c02 = J[3] * J[7] - J[4] * J[6];
-    const float det = J[0] * c00 + J[1] * c01 + J[2] * c02;
-    const float id = 1.0f / det;
-    float Ji[9];
-    Ji[0] = c00 * id; Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
-    Ji[3] = c01 * id; Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[5] = (J[2] * J[3] - J[0] * J[5]) * id;
-    Ji[6] = c02 * id; Ji[7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[8] = (J[0] * J[4] - J[1] * J[3]) * id;
-    float Gu[9], acc[3] = {0.f, 0.f, 0.f};
+    float gp[8][3];  // physical gradients at point q
+    float Gu[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) Gu[k] = 0.f;
 #pragma unroll
     for (int B = 0; B < 8; ++B) {
       const float4 g = rq[B];
       // grad_i = sum_j Jinv(j, i) grad^_j
-      gp[h][B][0] = Ji[0] * g.x + Ji[3] * g.y + Ji[6] * g.z;
-      gp[h][B][1] = Ji[1] * g.x + Ji[4] * g.y + Ji[7] * g.z;
-      gp[h][B][2] = Ji[2] * g.x + Ji[5] * g.y + Ji[8] * g.z;
+      gp[B][0] = Ji[h][0] * g.x + Ji[h][3] * g.y + Ji[h][6] * g.z;
+      gp[B][1] = Ji[h][1] * g.x + Ji[h][4] * g.y + Ji[h][7] * g.z;
+      gp[B][2] = Ji[h][2] * g.x + Ji[h][5] * g.y + Ji[h][8] * g.z;
+      if (h == 0) {
+        g0[B][0] = gp[B][0]; g0[B][1] = gp[B][1]; g0[B][2] = gp[B][2];
+      } else {
+        // slots 9 qp + B (gx_q0, gx_q1, gy_q0, gy_q1) and 8 qp + B (gz_q0, gz_q1)
+        XY[B] = f4(g0[B][0], gp[B][0], g0[B][1], gp[B][1]);
+        Z[B] = make_float2(g0[B][2], gp[B][2]);
+      }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        Gu[3 * c + 0] += gp[h][B][0] * U[B][c];
-        Gu[3 * c + 1] += gp[h][B][1] * U[B][c];
-        Gu[3 * c + 2] += gp[h][B][2] * U[B][c];
-        if constexpr (MASS) acc[c] += g.w * UD[B][c];
+        Gu[3 * c + 0] += gp[B][0] * U[B][c];
+        Gu[3 * c + 1] += gp[B][1] * U[B][c];
+        Gu[3 * c + 2] += gp[B][2] * U[B][c];
       }
     }
     const float tr = Gu[0] + Gu[4] + Gu[8];
-    float4* S = reinterpret_cast<float4*>(rec + kRecS) + 3 * q + rot;
-    S[0] = f4(mu * (Gu[0] + Gu[0]) + lam * tr, mu * (Gu[4] + Gu[4]) + lam * tr, mu * (Gu[8] + Gu[8]) + lam * tr,
-              mu * (Gu[1] + Gu[3]));
-    S[1] = f4(mu * (Gu[2] + Gu[6]), mu * (Gu[5] + Gu[7]), A.rho * acc[0] - A.body[0], A.rho * acc[1] - A.body[1]);
-    S[2] = f4(A.rho * acc[2] - A.body[2], 0.f, 0.f, 0.f);
-    reinterpret_cast<float*>(rec + kRecW)[4 * rot + q] = rw[q] * det;
-  }
-  float4* XY = reinterpret_cast<float4*>(rec + kRecXY) + 9 * qp;
-  float2* Z = reinterpret_cast<float2*>(rec + kRecZ) + 9 * qp;
+    wd[h] = rw[q] * det[h];
+    // W-scaled stress and point force (rho acc - b)
+    const float s00 = wd[h] * (mu * (Gu[0] + Gu[0]) + lam * tr), s11 = wd[h] * (mu * (Gu[4] + Gu[4]) + lam * tr);
+    const float s22 = wd[h] * (mu * (Gu[8] + Gu[8]) + lam * tr), s01 = wd[h] * (mu * (Gu[1] + Gu[3]));
+    const float s02 = wd[h] * (mu * (Gu[2] + Gu[6])), s12 = wd[h] * (mu * (Gu[5] + Gu[7]));
+    const float f0 = wd[h] * (A.rho * acc[h][0] - A.body[0]), f1 = wd[h] * (A.rho * acc[h][1] - A.body[1]);
+    const float f2 = wd[h] * (A.rho * acc[h][2] - A.body[2]);
 #pragma unroll
-  for (int B = 0; B < 8; ++B) {
-    XY[B] = f4(gp[0][B][0], gp[1][B][0], gp[0][B][1], gp[1][B][1]);
-    Z[B] = make_float2(gp[0][B][2], gp[1][B][2]);
+    for (int B = 0; B < 8; ++B) {
+      const float a0 = gp[B][0], a1 = gp[B][1], a2 = gp[B][2], n = rq[B].w;
+      res[B][0] += a0 * s00 + a1 * s01 + a2 * s02 + n * f0;
+      res[B][1] += a0 * s01 + a1 * s11 + a2 * s12 + n * f1;
+      res[B][2] += a0 * s02 + a1 * s12 + a2 * s22 + n * f2;
+    }
   }
+  // computeCellMeasure: the weights take the sign of the first point's det J
+  const int l0 = threadIdx.x & 28;
+  const float sg = __shfl_sync(m4, wd[0], l0) < 0.f ? -1.f : 1.f;
+  // sum the four point pairs' shares (lanes 4 el .. 4 el + 3) by halving
+  // exchanges: across lane bit 1 the lane keeps vertices 0-3 or 4-7, across
+  // bit 0 the lower or upper two of those, so lane qp ends with the sums of
+  // vertices 2 qp and 2 qp + 1
+  float h4[4][3];
+  {
+    const bool up = qp & 2;
+#pragma unroll
+    for (int B = 0; B < 4; ++B)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float keep = up ? res[B + 4][c] : res[B][c], send = up ? res[B][c] : res[B + 4][c];
+        h4[B][c] = keep + __shfl_xor_sync(m4, send, 2);
+      }
+  }
+  float h2[2][3];
+  {
+    const bool up = qp & 1;
+#pragma unroll
+    for (int B = 0; B < 2; ++B)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float keep = up ? h4[B + 2][c] : h4[B][c], send = up ? h4[B][c] : h4[B + 2][c];
+        h2[B][c] = keep + __shfl_xor_sync(m4, send, 1);
+      }
+  }
+  // slots 2 qp and 2 qp + 1 hold W of points 2 qp ^ rot and (2 qp ^ rot) ^ 1,
+  // both held by lane 4 el + ((2 qp ^ rot) >> 1)
+  const int src = l0 + (((2 * qp) ^ rot) >> 1);
+  const float wa = sg * __shfl_sync(m4, wd[0], src), wb = sg * __shfl_sync(m4, wd[1], src);
+  const bool odd = rot & 1;
+  float4* R = reinterpret_cast<float4*>(rec + kRecR);
+  R[2 * qp] = f4(sg * h2[0][0], sg * h2[0][1], sg * h2[0][2], odd ? wb : wa);
+  R[2 * qp + 1] = f4(sg * h2[1][0], sg * h2[1][1], sg * h2[1][2], odd ? wa : wb);
 }
 
 // The rows of the 16 owned nodes of node layer k.
@@ -266,46 +344,47 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
   const unsigned char* rec =
       smem + kSmElem + ((int)((k - 1 + ez) & 1) * kElems + (lx + ex) + kElem * (ly + ey)) * kRecBytes;
   const float4* XY = reinterpret_cast<const float4*>(rec + kRecXY);
-  const float2* Z = reinterpret_cast<const float2*>(rec + kRecZ);
-  const float4* S = reinterpret_cast<const float4*>(rec + kRecS) + rot;
-  const float4* W4 = reinterpret_cast<const float4*>(rec + kRecW) + rot;
+  const float2* Z = reinterpret_cast<const float2*>(rec + kRecZ + 64 * (int)(gx & 1));
+  const float4* R = reinterpret_cast<const float4*>(rec + kRecR);
 
   float r[3] = {0.f, 0.f, 0.f};
-  float blk[8][9];
+  // the lane's own weighted gradients and values as point pairs:
+  // wg[qp][i] = (W grad_i N_a)(q0, q1), wn[qp] = (W N_a)(q0, q1)
+  float2 wg[4][3], wn[4];
   if (valid) {
-    const float4 wa = W4[0], wb = W4[1];
-    const float sgn = wa.x < 0.f ? -1.f : 1.f;  // computeCellMeasure: |.| by the first point's sign
-    const float Wq[8] = {wa.x * sgn, wa.y * sgn, wa.z * sgn, wa.w * sgn, wb.x * sgn, wb.y * sgn, wb.z * sgn, wb.w * sgn};
-    // the lane's own weighted gradients and values as point pairs:
-    // wg[qp][i] = (W grad_i N_a)(q0, q1), wn[qp] = (W N_a)(q0, q1)
-    float2 wg[4][3], wn[4];
+    float Wq[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Wq[q] = R[q ^ rot].w;  // W_q sits in slot q ^ rot: eight lanes, eight slots
 #pragma unroll
     for (int qp = 0; qp < 4; ++qp) {
       const float4 xy = XY[9 * qp + lbits];
-      const float2 z = Z[9 * qp + lbits];
+      const float2 z = Z[8 * qp + lbits];
       const float w0 = Wq[2 * qp], w1 = Wq[2 * qp + 1];
       wg[qp][0] = make_float2(w0 * xy.x, w1 * xy.y);
       wg[qp][1] = make_float2(w0 * xy.z, w1 * xy.w);
       wg[qp][2] = make_float2(w0 * z.x, w1 * z.y);
-      const float2 na = rn[9 * qp + lbits];
-      wn[qp] = make_float2(w0 * na.x, w1 * na.y);
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int q = 2 * qp + h;
-        const float g0 = h ? wg[qp][0].y : wg[qp][0].x, g1 = h ? wg[qp][1].y : wg[qp][1].x;
-        const float g2 = h ? wg[qp][2].y : wg[qp][2].x, n = h ? wn[qp].y : wn[qp].x;
-        const float4 s0 = S[q * 3], s1 = S[q * 3 + 1], s2 = S[q * 3 + 2];
-        // residual row a: grad N_a . sigma + N_a (rho acc - b)
-        r[0] += g0 * s0.x + g1 * s0.w + g2 * s1.x + n * s1.z;
-        r[1] += g0 * s0.w + g1 * s0.y + g2 * s1.y + n * s1.w;
-        r[2] += g0 * s1.x + g1 * s1.y + g2 * s0.z + n * s2.x;
+      if constexpr (MASS) {
+        const float2 na = rn[9 * qp + lbits];
+        wn[qp] = make_float2(w0 * na.x, w1 * na.y);
       }
     }
-    const float bl = A.beta * A.lam, bm = A.beta * A.mu, am = A.alpha * A.rho;
-    // slot c holds the block of the element vertex with bits c ^ lbits (bit per
-    // axis: 0 = the node's own lattice line, 1 = this element's neighbour line)
+    const float4 ra = R[lbits];  // the element's residual row of the node's vertex
+    r[0] = ra.x; r[1] = ra.y; r[2] = ra.z;
+  }
+  const float bl = A.beta * A.lam, bm = A.beta * A.mu, am = A.alpha * A.rho;
+  // entries start at float (rowstart & 1) of the node's stage row, so that
+  // stage float4 j maps to an even, 16-byte aligned pair of FP64 entries
+  float* stage = reinterpret_cast<float*>(smem + kSmStage) + ln * kStageRow +
+                 (int)(*reinterpret_cast<const int64_t*>(info) & 1);
+  const uint8_t* npos = info + 16;
+  const int rl = 3 * nnb;  // entries of one row
+  const unsigned wmask = nnb > 0 ? (unsigned)(kWriters >> (8 * e)) & 0xffu : 0u;
+  // slot c holds the block of the element vertex with bits c ^ lbits (bit per
+  // axis: 0 = the node's own lattice line, 1 = this element's neighbour line)
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
+  for (int c = 0; c < 8; ++c) {
+    float kv[9];
+    if (valid) {
       const int bb = c ^ lbits;
       const float4* xyb = XY + bb;
       const float2* zb = Z + bb;
@@ -315,7 +394,7 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
 #pragma unroll
       for (int qp = 0; qp < 4; ++qp) {
         const float4 xy = xyb[9 * qp];
-        const float2 z = zb[9 * qp];
+        const float2 z = zb[8 * qp];
         const float2 gxp = make_float2(xy.x, xy.y), gyp = make_float2(xy.z, xy.w);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -334,88 +413,101 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
       for (int cc = 0; cc < 3; ++cc)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          float kv = bl * Ps[3 * cc + d] + bm * Ps[3 * d + cc];
-          if (cc == d) kv += bm * tp + md;
-          blk[c][3 * cc + d] = kv;
+          float v = bl * Ps[3 * cc + d] + bm * Ps[3 * d + cc];
+          if (cc == d) v += bm * tp + md;
+          kv[3 * cc + d] = v;
         }
+    } else {
+#pragma unroll
+      for (int t = 0; t < 9; ++t) kv[t] = 0.f;
     }
-  } else {
+    // butterflies, x then y then z: on each axis where slot c has bit 0 (the
+    // neighbour on the node's own line) the block is shared by the two
+    // elements on either side; both lanes end with the same sum (a + b == b + a
+    // in IEEE arithmetic)
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-#pragma unroll
-      for (int t = 0; t < 9; ++t) blk[c][t] = 0.f;
-  }
-  // butterflies: on each axis the slot with bit 0 (neighbour on the node's own
-  // line) is shared by the two elements on either side; both lanes end with
-  // the same sum (a + b == b + a in IEEE arithmetic)
-#pragma unroll
-  for (int ax = 0; ax < 3; ++ax) {
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
+    for (int ax = 0; ax < 3; ++ax) {
       if (c & (1 << ax)) continue;
 #pragma unroll
-      for (int t = 0; t < 9; ++t) blk[c][t] += __shfl_xor_sync(0xffffffffu, blk[c][t], 1 << ax);
+      for (int t = 0; t < 9; ++t) kv[t] += __shfl_xor_sync(0xffffffffu, kv[t], 1 << ax);
     }
-#pragma unroll
-    for (int t = 0; t < 3; ++t) r[t] += __shfl_xor_sync(0xffffffffu, r[t], 1 << ax);
-  }
-  // stage the node's rows: slot c of lane e is neighbour offset
-  // d_a = 0 (bit 0) or 2 e_a - 1 (bit 1); kWriters names the lane that writes it
-  float* stage = reinterpret_cast<float*>(smem + kSmStage) + ln * kRowMax;
-  if (nnb > 0) {
-    const uint8_t* npos = info + 16;
-    const int rl = 3 * nnb;  // entries of one row
-    const unsigned wmask = (unsigned)(kWriters >> (8 * e)) & 0xffu;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      if (!((wmask >> c) & 1u)) continue;
+    // stage slot c: neighbour offset d_a = 0 (bit 0) or 2 e_a - 1 (bit 1);
+    // kWriters names the lane that writes it
+    if ((wmask >> c) & 1u) {
       const int dx = (c & 1) ? 2 * ex - 1 : 0, dy = (c & 2) ? 2 * ey - 1 : 0, dz = (c & 4) ? 2 * ez - 1 : 0;
       const int p = npos[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
-      if (p == 0xff) continue;
+      if (p != 0xff) {
 #pragma unroll
-      for (int cc = 0; cc < 3; ++cc)
+        for (int cc = 0; cc < 3; ++cc)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) stage[cc * rl + 3 * p + d] = blk[c][3 * cc + d];
-    }
-    if (e == 0 && A.f) {
-      const int32_t lid = reinterpret_cast<const int32_t*>(info)[2];
-#pragma unroll
-      for (int t = 0; t < 3; ++t) A.f[3 * (int64_t)lid + t] = widen(r[t]);
+          for (int d = 0; d < 3; ++d) stage[cc * rl + 3 * p + d] = kv[3 * cc + d];
+      }
     }
   }
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+    for (int t = 0; t < 3; ++t) r[t] += __shfl_xor_sync(0xffffffffu, r[t], 1 << ax);
+  if (nnb > 0 && e == 0 && A.f) {
+    const int32_t lid = reinterpret_cast<const int32_t*>(info)[2];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) A.f[3 * (int64_t)lid + t] = widen(r[t]);
+  }
   __syncwarp();
-  // the warp's four nodes: coalesced FP64 stores of each node's 3 rows
+  // the warp's four nodes: coalesced FP64 stores of each node's 3 rows, a
+  // float4 of the stage (four entries, two 16-byte stores) per lane and step
   const int wn0 = (threadIdx.x >> 5) * 4;
 #pragma unroll 1
   for (int m = 0; m < 4; ++m) {
     const unsigned char* inf = smem + kSmPlaneInfo + ((int)(k & 1) * kNodes + wn0 + m) * kInfoBytes;
     const int nb = reinterpret_cast<const int32_t*>(inf)[3];
     if (nb == 0) continue;
-    double* dst = A.vals + *reinterpret_cast<const int64_t*>(inf);
-    const float* src = reinterpret_cast<const float*>(smem + kSmStage) + (wn0 + m) * kRowMax;
+    const int64_t rs = *reinterpret_cast<const int64_t*>(inf);
+    const int o = (int)(rs & 1), n = 9 * nb, end = o + n;
+    double* dst = A.vals + (rs - o);  // even: 16-byte aligned
+    const float4* src = reinterpret_cast<const float4*>(smem + kSmStage + (wn0 + m) * kStageRow * 4);
     // exact FP32 -> FP64 widening by integer operations for zeros and normal
-    // numbers (exponent rebiased, fraction moved up; no call, so no register
-    // saving around the loop); a subnormal, infinity or NaN anywhere in the
-    // node's rows (a lane flag, one vote a node) sends those entries through
-    // the hardware conversion afterwards
-    bool rare = false;
-    for (int t = lane; t < 9 * nb; t += 32) {
-      const uint32_t b = __float_as_uint(src[t]), a = b & 0x7fffffffu;
-      rare |= (a != 0u) & (a - 0x00800000u >= 0x7f000000u);
-      const uint32_t hi = a ? (b & 0x80000000u) | ((a >> 3) + 0x38000000u) : b;
-      __stcs(dst + t, __hiloint2double((int)hi, (int)(b << 29)));
-    }
-    if (__any_sync(0xffffffffu, rare))
-      for (int t = lane; t < 9 * nb; t += 32) {
-        const float v = src[t];
-        const uint32_t a = __float_as_uint(v) & 0x7fffffffu;
-        if (a != 0u && a - 0x00800000u >= 0x7f000000u) __stcs(dst + t, (double)v);
+    // numbers: the exponent rebiased (not for a zero: times min(|b|, 1)),
+    // the fraction moved up; a subnormal, infinity or NaN anywhere in the
+    // node's rows (lane extremes of |b| and |b| - 1, one vote a node) sends
+    // those entries through the hardware conversion afterwards
+    uint32_t mx = 0u, mn = 0xffffffffu;
+    for (int j = lane; 4 * j < end; j += 32) {
+      const float4 v4 = src[j];
+      const float v[4] = {v4.x, v4.y, v4.z, v4.w};
+      double d[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int p = 4 * j + i;
+        const uint32_t b = __float_as_uint(v[i]);
+        const uint32_t a = (p >= o && p < end) ? b & 0x7fffffffu : 0u;
+        mx = max(mx, a);
+        mn = min(mn, a - 1u);
+        const uint32_t hi = min(a, 1u) * 0x38000000u + ((uint32_t)((int32_t)b >> 3) & 0x8fffffffu);
+        d[i] = __hiloint2double((int)hi, (int)(b << 29));
       }
+      if (4 * j >= o && 4 * j + 4 <= end) {
+        __stcs(reinterpret_cast<double2*>(dst) + 2 * j, make_double2(d[0], d[1]));
+        __stcs(reinterpret_cast<double2*>(dst) + 2 * j + 1, make_double2(d[2], d[3]));
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (4 * j + i >= o && 4 * j + i < end) __stcs(dst + 4 * j + i, d[i]);
+      }
+    }
+    if (__any_sync(0xffffffffu, mx >= 0x7f800000u || mn < 0x007fffffu)) {
+      const float* sf = reinterpret_cast<const float*>(src);
+      for (int p = o + lane; p < end; p += 32) {
+        const float v = sf[p];
+        const uint32_t a = __float_as_uint(v) & 0x7fffffffu;
+        if (a >= 0x7f800000u || (a != 0u && a < 0x00800000u)) __stcs(dst + p, (double)v);
+      }
+    }
   }
 }
 
 template <bool MASS>
-__global__ void __launch_bounds__(kThreads, 2) k_lattice_gather(LatticeArgs A) {
+__global__ void __launch_bounds__(kThreads, 3) k_lattice_gather(LatticeArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   // reference tables (hex8, 2 x 2 x 2 Gauss) from the packed FP64 tables
   // [w | geo_val | geo_grad | val | grad]: (dN^/dxi, N) of the vertex with
@@ -469,6 +561,23 @@ __global__ void k_lattice_gather_u(const LatticeNode* nodes, int64_t n, const do
   }
 }
 
+// Node layers per task: tasks (a node column's z chunk) go to the CTAs
+// round-robin, so the kernel lasts as long as the CTA with the most tasks;
+// each task adds one prologue element layer (about half a node layer's
+// work).  Picks the chunk with the fewest half-layers on the heaviest CTA,
+// the longer chunk on a tie.
+int64_t choose_zchunk(int64_t nx, int64_t ny, int64_t nz, int64_t grid) {
+  const int64_t cols = ((nx + kTile) / kTile) * ((ny + kTile) / kTile), layers = nz + 1;
+  int64_t best = layers, best_cost = -1;
+  for (int64_t zc = 1; zc <= layers; ++zc) {
+    const int64_t ntask = cols * ((layers + zc - 1) / zc);
+    const int64_t g = std::min<int64_t>(std::max<int64_t>(grid, 1), ntask);
+    const int64_t cost = (ntask + g - 1) / g * (2 * zc + 1);
+    if (best_cost < 0 || cost <= best_cost) best_cost = cost, best = zc;
+  }
+  return best;
+}
+
 template <bool MASS>
 cudaError_t launch_main(const LatticeArgs& A, int sms, cudaStream_t s) {
   static bool attr = false;
@@ -480,11 +589,13 @@ cudaError_t launch_main(const LatticeArgs& A, int sms, cudaStream_t s) {
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lattice_gather<MASS>, kThreads, kSmBytes);
   if (e != cudaSuccess) return e;
-  const int64_t ntask = ((A.nx + kTile) / kTile) * ((A.ny + kTile) / kTile) * ((A.nz + A.zchunk) / A.zchunk);
   int64_t grid = (int64_t)(per_sm > 0 ? per_sm : 1) * sms;
   if (A.grid > 0 && A.grid < grid) grid = A.grid;
+  LatticeArgs B = A;
+  B.zchunk = choose_zchunk(A.nx, A.ny, A.nz, grid);
+  const int64_t ntask = ((A.nx + kTile) / kTile) * ((A.ny + kTile) / kTile) * ((A.nz + B.zchunk) / B.zchunk);
   if (grid > ntask) grid = ntask;
-  k_lattice_gather<MASS><<<(unsigned)grid, kThreads, kSmBytes, s>>>(A);
+  k_lattice_gather<MASS><<<(unsigned)grid, kThreads, kSmBytes, s>>>(B);
   return cudaGetLastError();
 }
 
