@@ -567,11 +567,17 @@ int tx_set_spmv_entity_shape(tx_handle h, int32_t lanes, int32_t unroll);
 /* Assembly kernel of the per-block mixed evaluation: 0 automatic (the
  * warp-per-element kernel where the element family has one, hex8 elasticity;
  * the CTA-staged kernel elsewhere), 1 always the CTA-staged kernel, 2 the
- * warp-per-element kernel where available.  Results agree to the FP32
- * summation order; the autotuner's third knob. */
+ * warp-per-element kernel where available, 3 the tensor-core kernel where
+ * available (hex8 elasticity R+J: the element contractions P = sum_q W grad N
+ * grad N^T and M = sum_q W N N^T as tcgen05 TF32 MMAs with hi/lo splitting,
+ * relative error about 1e-6; a bounded MMA wait that gives up is reported by
+ * tx_synchronize as TX_ETIMEDOUT).  Results agree to the FP32 summation order
+ * (the tensor-core kernel to its splitting error); the autotuner's third
+ * knob.  The reference has one AD kernel per integrator and no such choice. */
 #define TX_VARIANT_AUTO 0
 #define TX_VARIANT_CTA 1
 #define TX_VARIANT_WARP 2
+#define TX_VARIANT_TENSOR 3
 int tx_set_assembly_variant(tx_handle h, int32_t variant);
 /* Tile shape of the CTA-staged Jacobian kernel: threads a CTA, 64, 128 (the
  * default; 0 restores it) or 256.  Each element takes TPE threads (its basis
@@ -618,6 +624,9 @@ int tx_eval_noalloc(tx_handle h, const tx_eval_args* args);
 /* Stream the handle's work is ordered on (cudaStream_t as void*); set NULL
  * to use the legacy default stream. */
 int tx_set_stream(tx_handle h, void* stream);
+/* Waits for the handle's stream; TX_ETIMEDOUT when a bounded device wait of
+ * the work since the last call gave up (the tensor-core kernel's MMA waits),
+ * TX_ECUDA on a CUDA error. */
 int tx_synchronize(tx_handle h);
 
 #ifdef __cplusplus

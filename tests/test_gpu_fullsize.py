@@ -7,8 +7,8 @@ at full size:
 * elasticity hex8 128^3 (2,097,152 elements, 6,440,067 DOFs, 513,599,625 CRS
   entries): owned GIDs, element GID/LID vectors, Dirichlet set and the CRS
   graph bit-exact; FP64 residual and Jacobian within 1e-12 of the oracle's
-  (relative to the largest entry); the mixed Jacobian, atomic and
-  owner-computes lattice forms, within its stated 2e-5;
+  (relative to the largest entry); the mixed Jacobian, atomic, owner-computes
+  lattice and tensor-core forms, within its stated 2e-5;
   the GPU's converged solution has an oracle-computed FP64 residual
   ||f(x)|| <= 1e-10 ||f(0)||, as the reference's fe_assembly test checks
   ||b - Ax|| (dof-mgr/test/fe_assembly/test_fe_assembly_HEX.hpp:672-677);
@@ -29,6 +29,7 @@ import numpy as np
 import pytest
 import torch
 
+import tianxin_gb300 as tx
 from oracle import oracle as O
 from tianxin_gb300 import _abi as A
 from tianxin_gb300 import workloads as WL
@@ -86,14 +87,18 @@ def test_elasticity_128_residual_jacobian_against_oracle(c2):
     o.dirichlet_apply(bd, np.zeros(len(bd)), x_h, f_ref, v_ref)
     x = torch.from_numpy(x_h).cuda()
     f, W = w.lof.getTpetraVector(), w.me.create_W_op()
-    # FP64 and mixed atomic forms, and the mixed owner-computes lattice form (deterministic evaluations take
-    # the gather form, which on this lattice is k_lattice_gather)
+    # FP64 and mixed atomic forms, the mixed owner-computes lattice form (deterministic evaluations take
+    # the gather form, which on this lattice is k_lattice_gather) and the tensor-core contractions
     assert w.me.ae.gather_form() == "lattice"
-    for mixed, det, tol in ((False, False, TOL_FP64), (True, False, TOL_MIXED), (True, True, TOL_MIXED)):
+    for mixed, det, variant, tol in ((False, False, 0, TOL_FP64), (True, False, 0, TOL_MIXED),
+                                     (True, True, 0, TOL_MIXED), (True, False, 3, TOL_MIXED)):
+        w.me.ae.setVariant(variant)
         w.me.evalModel(x, f=f, W=W, mixed=mixed, deterministic=det)
+        tx.synchronize(w.dof)
         ef = rel(f.cpu().numpy(), f_ref)
         ew = rel(W.values.cpu().numpy(), v_ref)
-        assert ef <= tol and ew <= tol, (mixed, det, ef, ew)
+        assert ef <= tol and ew <= tol, (mixed, det, variant, ef, ew)
+    w.me.ae.setVariant(0)
 
 
 def test_elasticity_128_converged_solution_oracle_residual(c2):

@@ -85,12 +85,15 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                                                   scatter_direct=direct), reps)
                     results.append(({"workset": ws, "grid_cap": 0, "scatter_direct": direct}, t))
         else:
-            # kernel variant (warp per element / CTA-staged / CTA direct scatter / two-phase) x CTA tile
+            # kernel variant (warp per element / CTA-staged / CTA direct scatter / tensor-core contractions /
+            # two-phase) x CTA tile
             # shape (threads a CTA of the staged kernel: elements per CTA) x CTA cap
             kernels = [(2, False, False, 0), (1, False, False, 0), (1, True, False, 0)] if mixed else \
                 [(1, False, False, 0), (1, True, False, 0)]
             if W is not None:
                 kernels += [(1, False, False, 64), (1, False, False, 256)]
+                if mixed:  # the element contractions on the tensor cores (hex8 elasticity; elsewhere a repeat)
+                    kernels.append((3, False, False, 0))
             if W is not None and ae.gather_supported():
                 kernels.append((1, False, True, 0))
 

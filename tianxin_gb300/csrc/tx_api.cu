@@ -134,7 +134,8 @@ struct tx_handle_s {
   std::vector<ResponseSet> responses;
   tx::SpmvShape spmv;     // SpMV launch shape ({0, 0}: automatic)
   tx::SpmvShape spmv_eb;  // the same for the entity-block form
-  int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element
+  int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element, 3 tensor cores
+  int* d_wait_status = nullptr;  // bounded device waits that gave up (bit 0: the tensor-core kernel's MMA waits)
   int cta_threads = 0; // threads a CTA of the staged Jacobian kernel (0: 128); tx_set_cta_threads
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
@@ -201,6 +202,7 @@ struct tx_handle_s {
       if (g) cudaGraphExecDestroy(g);
     free_dofs();
     cudaFree(d_coords);
+    cudaFree(d_wait_status);
   }
 };
 
@@ -569,9 +571,18 @@ int eval_blocks(tx_handle h, const tx_eval_args& a, const CoefOverride* ov = nul
     cudaError_t e = cudaSuccess;
     const bool tiled = !det && stage && P.vals && !P.tan && h->cta_threads != 0 &&
                        tx::tile_shape_supported(db.kind, h->cta_threads);
-    const bool wpe = !det && !tiled && mixed && stage && h->variant != 1 && h->cta_threads == 0 &&
+    const bool tens = !det && !tiled && mixed && stage && P.vals && h->variant == 3 && h->cta_threads == 0 &&
+                      tx::tc_supported(V, P);
+    const bool wpe = !det && !tiled && !tens && mixed && stage && h->variant != 1 && h->cta_threads == 0 &&
                      tx::wpe_supported(V, P);
-    if (tiled) {
+    if (tens && !h->d_wait_status) {
+      if (cudaMalloc((void**)&h->d_wait_status, sizeof(int)) != cudaSuccess ||
+          cudaMemset(h->d_wait_status, 0, sizeof(int)) != cudaSuccess)
+        return fail(h, TX_ECUDA, "tx_eval: status word of the tensor-core kernel");
+    }
+    if (tens) {
+      e = tx::launch_assemble_tc(V, P, e0, e1, h->d_wait_status, h->stream, h->grid_cap);
+    } else if (tiled) {
       e = tx::launch_assemble_tile(V, P, mixed, h->cta_threads, e0, e1, h->stream, h->grid_cap);
     } else if (wpe) {
       e = tx::launch_assemble_wpe(V, P, e0, e1, h->stream, h->grid_cap);
@@ -1435,7 +1446,7 @@ int tx_set_cta_threads(tx_handle h, int32_t threads) {
 
 int tx_set_assembly_variant(tx_handle h, int32_t variant) {
   if (!h) return TX_EINVAL;
-  if (variant < 0 || variant > 2) return fail(h, TX_EINVAL, "tx_set_assembly_variant: 0, 1 or 2");
+  if (variant < 0 || variant > 3) return fail(h, TX_EINVAL, "tx_set_assembly_variant: 0, 1, 2 or 3");
   h->variant = variant;
   return TX_OK;
 }
@@ -1627,6 +1638,15 @@ int tx_synchronize(tx_handle h) {
   if (!h) return TX_EINVAL;
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_synchronize: ") + cudaGetErrorString(e));
+  if (h->d_wait_status) {
+    int st = 0;
+    e = cudaMemcpy(&st, h->d_wait_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_synchronize: ") + cudaGetErrorString(e));
+    if (st) {
+      cudaMemset(h->d_wait_status, 0, sizeof(int));
+      return fail(h, TX_ETIMEDOUT, "tx_synchronize: a tensor-core MMA wait gave up; the results of that evaluation are incomplete");
+    }
+  }
   return TX_OK;
 }
 

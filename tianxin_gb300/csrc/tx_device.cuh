@@ -86,6 +86,13 @@ bool tile_shape_supported(int kind, int threads);
 cudaError_t launch_assemble_tile(const BlockView& B, const EvalParams& P, bool mixed, int threads, int64_t e_lo,
                                  int64_t e_hi, cudaStream_t s, int grid_cap);
 
+// Mixed R+J of hex8 elasticity with the element contraction on the tensor
+// cores (tcgen05 TF32, hi/lo split; tx_assemble_tc.cu), atomic scatter.  A
+// bounded MMA wait that gives up sets bit 0 of *status.
+bool tc_supported(const BlockView& B, const EvalParams& P);
+cudaError_t launch_assemble_tc(const BlockView& B, const EvalParams& P, int64_t e_lo, int64_t e_hi, int* status,
+                               cudaStream_t s, int grid_cap);
+
 // ---- owner-computes lattice assembly (tx_lattice.cu)
 // One node of a single-block hex8 brick lattice, in node GID order: FP32
 // hi/lo coordinates (x = hi + lo), its entity LID, the first CRS value of

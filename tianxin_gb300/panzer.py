@@ -658,7 +658,8 @@ class AssemblyEngine:
         check(self.dof.h, self.dof.lib.tx_set_grid_cap(self.dof.h, max_ctas), "tx_set_grid_cap")
 
     def setVariant(self, variant):
-        """Assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element (hex8 elasticity, mixed)."""
+        """Assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element (hex8 elasticity, mixed), 3 the
+        element contractions on the tensor cores (hex8 elasticity, mixed R+J; tcgen05 TF32 with hi/lo splitting)."""
         check(self.dof.h, self.dof.lib.tx_set_assembly_variant(self.dof.h, variant), "tx_set_assembly_variant")
 
     def setCtaThreads(self, threads):
