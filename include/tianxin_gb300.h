@@ -628,6 +628,12 @@ int tx_set_stream(tx_handle h, void* stream);
  * the work since the last call gave up (the tensor-core kernel's MMA waits),
  * TX_ECUDA on a CUDA error. */
 int tx_synchronize(tx_handle h);
+/* Failure-path check of the bounded device waits: launches one warp that
+ * waits on an mbarrier nothing arrives at, gives up after a few thousand
+ * polls and sets the handle's status word, so the next tx_synchronize returns
+ * TX_ETIMEDOUT (and the one after it TX_OK).  No counterpart in the
+ * reference; no GPU fault or hang is involved. */
+int tx_selftest_wait_timeout(tx_handle h);
 
 #ifdef __cplusplus
 }

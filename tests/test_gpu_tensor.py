@@ -61,3 +61,14 @@ def test_tensor_core_contractions_against_oracle(cuda, n, params):
     fc, wc = out[1]
     assert rel(wt, wc) <= TOL_CUDA_CORES and rel(ft, fc) <= TOL_CUDA_CORES
     assert np.abs(wt - wc).max() > 0.0  # a different kernel ran: TF32 products, not FP32 FMAs
+
+
+def test_bounded_wait_gives_up_and_reports(cuda):
+    # the give-up path of the bounded mbarrier waits: nothing arrives, the wait ends, tx_synchronize reports it once
+    conn = tx.CartesianConnManager(2, 2, 2)
+    dof = tx.DOFManager(conn, A.equation_set(A.TX_PHYS_ELASTICITY))
+    lib = dof.lib
+    assert lib.tx_selftest_wait_timeout(dof.h) == 0
+    assert lib.tx_synchronize(dof.h) == A.TX_ETIMEDOUT
+    assert b"gave up" in lib.tx_last_error(dof.h)
+    assert lib.tx_synchronize(dof.h) == 0

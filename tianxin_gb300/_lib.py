@@ -74,6 +74,7 @@ SIGNATURES = {
     "tx_dirichlet_dofs_node_set": (C.c_int, [P, I32, U32, C.POINTER(I64), P]),
     "tx_set_stream": (C.c_int, [P, P]),
     "tx_synchronize": (C.c_int, [P]),
+    "tx_selftest_wait_timeout": (C.c_int, [P]),
 }
 
 _lib = None

@@ -1634,6 +1634,18 @@ int tx_set_stream(tx_handle h, void* stream) {
   return TX_OK;
 }
 
+int tx_selftest_wait_timeout(tx_handle h) {
+  if (!h) return TX_EINVAL;
+  if (!h->d_wait_status) {
+    if (cudaMalloc((void**)&h->d_wait_status, sizeof(int)) != cudaSuccess ||
+        cudaMemset(h->d_wait_status, 0, sizeof(int)) != cudaSuccess)
+      return fail(h, TX_ECUDA, "tx_selftest_wait_timeout: status word");
+  }
+  cudaError_t e = tx::launch_wait_selftest(h->d_wait_status, h->stream);
+  if (e != cudaSuccess) return fail(h, TX_ECUDA, std::string("tx_selftest_wait_timeout: ") + cudaGetErrorString(e));
+  return TX_OK;
+}
+
 int tx_synchronize(tx_handle h) {
   if (!h) return TX_EINVAL;
   cudaError_t e = cudaStreamSynchronize(h->stream);

@@ -291,7 +291,25 @@ __global__ void __launch_bounds__(kThreads, 4)
   }
 }
 
+// A wait on an mbarrier nothing arrives at: the bounded wait gives up after
+// max_polls polls and sets bit 0 of *status, as the assembly kernel does.
+__global__ void k_wait_selftest(int* status, uint32_t max_polls) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::mbar_init_fence();
+  }
+  __syncthreads();
+  const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(&bar, 0, max_polls));
+  if (!ok && threadIdx.x == 0) atomicOr(status, 1);
+}
+
 }  // namespace
+
+cudaError_t launch_wait_selftest(int* status, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(status, 1u << 12);
+  return cudaGetLastError();
+}
 
 bool tc_supported(const BlockView& B, const EvalParams& P) {
   return B.topo == TX_TOPO_HEX && B.basis == TX_HGRAD_C1 && B.nq == 8 && B.nb == 8 && B.nv == 8 &&

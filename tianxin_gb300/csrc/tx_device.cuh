@@ -92,6 +92,9 @@ cudaError_t launch_assemble_tile(const BlockView& B, const EvalParams& P, bool m
 bool tc_supported(const BlockView& B, const EvalParams& P);
 cudaError_t launch_assemble_tc(const BlockView& B, const EvalParams& P, int64_t e_lo, int64_t e_hi, int* status,
                                cudaStream_t s, int grid_cap);
+// One warp waiting on an mbarrier that never completes: the bounded wait's
+// give-up path (sets bit 0 of *status).
+cudaError_t launch_wait_selftest(int* status, cudaStream_t s);
 
 // ---- owner-computes lattice assembly (tx_lattice.cu)
 // One node of a single-block hex8 brick lattice, in node GID order: FP32
