@@ -12,8 +12,8 @@
 //   1. computes the geometry, physical gradients and residual rows of the
 //      5 x 5 elements of element layer k (its own 4 x 4 and a one-element
 //      halo) into a ring of two element layers in shared memory (1 KB an
-//      element; four lanes an element, two points each, the residual shares
-//      summed across the four lanes);
+//      element; four lanes an element, two points each as the two halves of
+//      packed FP32x2 FMAs, the residual shares summed across the four lanes);
 //   2. assembles the rows of its 16 nodes of layer k from the 8 elements
 //      around each node (element layers k - 1 and k): eight lanes per node,
 //      one element each; each lane forms its element's 3 x 24 block-row of
@@ -85,8 +85,8 @@ struct __align__(16) PlaneNode {
 };
 
 // shared memory layout
-constexpr int kSmRefG = 0;                                       // [q][B] float4 (dN^/dxi, N), slot 9 q + B
-constexpr int kSmRefN = kSmRefG + 72 * 16;                       // [qp][B] float2 (N(q0), N(q1)), slot 9 qp + B
+constexpr int kSmRefP = 0;  // [qp][B] 2 float4 (gx_q0, gx_q1, gy_q0, gy_q1), (gz_q0, gz_q1, N_q0, N_q1), slots 2 (9 qp + B)
+constexpr int kSmRefN = kSmRefP + 72 * 16;                       // [qp][B] float2 (N(q0), N(q1)), slot 9 qp + B
 constexpr int kSmRefW = kSmRefN + 36 * 8;                        // [q] w_q
 constexpr int kSmPlane = kSmRefW + 8 * 4;                        // 2 x 36 PlaneNode
 constexpr int kSmPlaneInfo = kSmPlane + 2 * kPlane * kPlane * 64;  // owned-node info of the 2 planes
@@ -167,7 +167,6 @@ template <bool MASS>
 __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t ek,
                                               unsigned char* smem) {
   if (ek < 0 || ek >= A.nz) return;
-  const float4* rg = reinterpret_cast<const float4*>(smem + kSmRefG);
   const float* rw = reinterpret_cast<const float*>(smem + kSmRefW);
   const PlaneNode* plo = reinterpret_cast<const PlaneNode*>(smem + kSmPlane) + (int)(ek & 1) * kPlane * kPlane;
   const PlaneNode* phi = reinterpret_cast<const PlaneNode*>(smem + kSmPlane) + (int)((ek + 1) & 1) * kPlane * kPlane;
@@ -201,88 +200,125 @@ __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, 
       UD[B][0] = ud.x; UD[B][1] = ud.y; UD[B][2] = ud.z;
     }
   }
-  // the two points' inverse Jacobians and accelerations first (dX and UD
-  // then dead), then per point: gradients, stress, residual shares
-  float Ji[2][9], det[2], acc[2][3];
+  // The two points of the pair run as the two halves of packed FP32x2 FMAs
+  // (fma.rn.f32x2); per vertex B the reference table holds (gx, gy | gz, N)
+  // of both points.
+  const float4* rp = reinterpret_cast<const float4*>(smem + kSmRefP) + 2 * 9 * qp;
+  const float2 zero2 = make_float2(0.f, 0.f);
+  float2 J2[9], acc2[3] = {zero2, zero2, zero2};
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const float4* rq = rg + 9 * (2 * qp + h);
-    float J[9];
+  for (int k = 0; k < 9; ++k) J2[k] = zero2;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) J[k] = 0.f;
-    acc[h][0] = acc[h][1] = acc[h][2] = 0.f;
+  for (int B = 0; B < 8; ++B) {
+    const float4 p0 = rp[2 * B], p1 = rp[2 * B + 1];
+    const float2 gx = make_float2(p0.x, p0.y), gy = make_float2(p0.z, p0.w), gz = make_float2(p1.x, p1.y);
+    if (B > 0) {
 #pragma unroll
-    for (int B = 0; B < 8; ++B) {
-      const float4 g = rq[B];
-      if (B > 0) {
-        J[0] += dX[B][0] * g.x; J[1] += dX[B][0] * g.y; J[2] += dX[B][0] * g.z;
-        J[3] += dX[B][1] * g.x; J[4] += dX[B][1] * g.y; J[5] += dX[B][1] * g.z;
-        J[6] += dX[B][2] * g.x; J[7] += dX[B][2] * g.y; J[8] += dX[B][2] * g.z;
-      }
-      if constexpr (MASS) {
-        acc[h][0] += g.w * UD[B][0]; acc[h][1] += g.w * UD[B][1]; acc[h][2] += g.w * UD[B][2];
+      for (int i = 0; i < 3; ++i) {
+        const float2 d = make_float2(dX[B][i], dX[B][i]);
+        J2[3 * i + 0] = ffma2(d, gx, J2[3 * i + 0]);
+        J2[3 * i + 1] = ffma2(d, gy, J2[3 * i + 1]);
+        J2[3 * i + 2] = ffma2(d, gz, J2[3 * i + 2]);
       }
     }
+    if constexpr (MASS) {
+      const float2 nn = make_float2(p1.z, p1.w);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc2[c] = ffma2(nn, make_float2(UD[B][c], UD[B][c]), acc2[c]);
+    }
+  }
+  float2 Ji2[9];
+  float det[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float J[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) J[k] = h ? J2[k].y : J2[k].x;
     const float c00 = J[4] * J[8] - J[5] * J[7];
     const float c01 = J[5] * J[6] - J[3] * J[8];
     const float c02 = J[3] * J[7] - J[4] * J[6];
     det[h] = J[0] * c00 + J[1] * c01 + J[2] * c02;
     const float id = 1.0f / det[h];
-    Ji[h][0] = c00 * id; Ji[h][1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[h][2] = (J[1] * J[5] - J[2] * J[4]) * id;
-    Ji[h][3] = c01 * id; Ji[h][4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[h][5] = (J[2] * J[3] - J[0] * J[5]) * id;
-    Ji[h][6] = c02 * id; Ji[h][7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[h][8] = (J[0] * J[4] - J[1] * J[3]) * id;
-  }
-  float wd[2];      // w_q det J_q at the two points
-  float res[8][3];  // the two points' share of the residual rows (unsigned weights)
-  float g0[8][3];   // physical gradients at the first point, stored with the second's
+    float Ji[9];
+    Ji[0] = c00 * id; Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+    Ji[3] = c01 * id; Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[5] = (J[2] * J[3] - J[0] * J[5]) * id;
+    Ji[6] = c02 * id; Ji[7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[8] = (J[0] * J[4] - J[1] * J[3]) * id;
 #pragma unroll
-  for (int B = 0; B < 8; ++B) res[B][0] = res[B][1] = res[B][2] = 0.f;
+    for (int k = 0; k < 9; ++k) {
+      if (h == 0) Ji2[k].x = Ji[k];
+      else Ji2[k].y = Ji[k];
+    }
+  }
+  // physical gradients grad_i = sum_j Jinv(j, i) grad^_j of both points, stored as
+  // slots 9 qp + B (gx_q0, gx_q1, gy_q0, gy_q1) and 8 qp + B (gz_q0, gz_q1);
+  // displacement gradients Gu[3 c + i] = du_c / dx_i
   float4* XY = reinterpret_cast<float4*>(rec + kRecXY) + 9 * qp;
   float2* Z = reinterpret_cast<float2*>(rec + kRecZ + 64 * (int)(gx & 1)) + 8 * qp;
+  float2 Gu2[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Gu2[k] = zero2;
+#pragma unroll
+  for (int B = 0; B < 8; ++B) {
+    const float4 p0 = rp[2 * B], p1 = rp[2 * B + 1];
+    const float2 hx = make_float2(p0.x, p0.y), hy = make_float2(p0.z, p0.w), hz = make_float2(p1.x, p1.y);
+    float2 g[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g[i] = ffma2(Ji2[i], hx, ffma2(Ji2[3 + i], hy, ffma2(Ji2[6 + i], hz, zero2)));
+    XY[B] = f4(g[0].x, g[0].y, g[1].x, g[1].y);
+    Z[B] = g[2];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 uu = make_float2(U[B][c], U[B][c]);
+      Gu2[3 * c + 0] = ffma2(g[0], uu, Gu2[3 * c + 0]);
+      Gu2[3 * c + 1] = ffma2(g[1], uu, Gu2[3 * c + 1]);
+      Gu2[3 * c + 2] = ffma2(g[2], uu, Gu2[3 * c + 2]);
+    }
+  }
+  // W-scaled stress rows and point force (rho acc - b), both points
+  float wd[2];  // w_q det J_q at the two points
+  float2 S[3][3], F[3];
   const float lam = A.lam, mu = A.mu;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
-    const int q = 2 * qp + h;
-    const float4* rq = rg + 9 * q;
-    float gp[8][3];  // physical gradients at point q
     float Gu[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Gu[k] = 0.f;
-#pragma unroll
-    for (int B = 0; B < 8; ++B) {
-      const float4 g = rq[B];
-      // grad_i = sum_j Jinv(j, i) grad^_j
-      gp[B][0] = Ji[h][0] * g.x + Ji[h][3] * g.y + Ji[h][6] * g.z;
-      gp[B][1] = Ji[h][1] * g.x + Ji[h][4] * g.y + Ji[h][7] * g.z;
-      gp[B][2] = Ji[h][2] * g.x + Ji[h][5] * g.y + Ji[h][8] * g.z;
-      if (h == 0) {
-        g0[B][0] = gp[B][0]; g0[B][1] = gp[B][1]; g0[B][2] = gp[B][2];
-      } else {
-        // slots 9 qp + B (gx_q0, gx_q1, gy_q0, gy_q1) and 8 qp + B (gz_q0, gz_q1)
-        XY[B] = f4(g0[B][0], gp[B][0], g0[B][1], gp[B][1]);
-        Z[B] = make_float2(g0[B][2], gp[B][2]);
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        Gu[3 * c + 0] += gp[B][0] * U[B][c];
-        Gu[3 * c + 1] += gp[B][1] * U[B][c];
-        Gu[3 * c + 2] += gp[B][2] * U[B][c];
-      }
-    }
+    for (int k = 0; k < 9; ++k) Gu[k] = h ? Gu2[k].y : Gu2[k].x;
+    const float w = rw[2 * qp + h] * det[h];
+    wd[h] = w;
     const float tr = Gu[0] + Gu[4] + Gu[8];
-    wd[h] = rw[q] * det[h];
-    // W-scaled stress and point force (rho acc - b)
-    const float s00 = wd[h] * (mu * (Gu[0] + Gu[0]) + lam * tr), s11 = wd[h] * (mu * (Gu[4] + Gu[4]) + lam * tr);
-    const float s22 = wd[h] * (mu * (Gu[8] + Gu[8]) + lam * tr), s01 = wd[h] * (mu * (Gu[1] + Gu[3]));
-    const float s02 = wd[h] * (mu * (Gu[2] + Gu[6])), s12 = wd[h] * (mu * (Gu[5] + Gu[7]));
-    const float f0 = wd[h] * (A.rho * acc[h][0] - A.body[0]), f1 = wd[h] * (A.rho * acc[h][1] - A.body[1]);
-    const float f2 = wd[h] * (A.rho * acc[h][2] - A.body[2]);
+    float s[3][3];
+    s[0][0] = w * (mu * (Gu[0] + Gu[0]) + lam * tr);
+    s[1][1] = w * (mu * (Gu[4] + Gu[4]) + lam * tr);
+    s[2][2] = w * (mu * (Gu[8] + Gu[8]) + lam * tr);
+    s[0][1] = s[1][0] = w * (mu * (Gu[1] + Gu[3]));
+    s[0][2] = s[2][0] = w * (mu * (Gu[2] + Gu[6]));
+    s[1][2] = s[2][1] = w * (mu * (Gu[5] + Gu[7]));
+    const float a[3] = {h ? acc2[0].y : acc2[0].x, h ? acc2[1].y : acc2[1].x, h ? acc2[2].y : acc2[2].x};
 #pragma unroll
-    for (int B = 0; B < 8; ++B) {
-      const float a0 = gp[B][0], a1 = gp[B][1], a2 = gp[B][2], n = rq[B].w;
-      res[B][0] += a0 * s00 + a1 * s01 + a2 * s02 + n * f0;
-      res[B][1] += a0 * s01 + a1 * s11 + a2 * s12 + n * f1;
-      res[B][2] += a0 * s02 + a1 * s12 + a2 * s22 + n * f2;
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        if (h == 0) S[c][i].x = s[c][i];
+        else S[c][i].y = s[c][i];
+      }
+      const float fc = w * (A.rho * a[c] - A.body[c]);
+      if (h == 0) F[c].x = fc;
+      else F[c].y = fc;
+    }
+  }
+  // the two points' share of the residual rows: grad N_B . sigma_c + N_B f_c,
+  // gradients read back from the record, the halves summed
+  float res[8][3];
+#pragma unroll
+  for (int B = 0; B < 8; ++B) {
+    const float4 xy = XY[B];
+    const float2 z = Z[B];
+    const float4 p1 = rp[2 * B + 1];
+    const float2 g0 = make_float2(xy.x, xy.y), g1 = make_float2(xy.z, xy.w), nn = make_float2(p1.z, p1.w);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 t = ffma2(g0, S[c][0], ffma2(g1, S[c][1], ffma2(z, S[c][2], ffma2(nn, F[c], zero2))));
+      res[B][c] = t.x + t.y;
     }
   }
   // computeCellMeasure: the weights take the sign of the first point's det J
@@ -514,15 +550,19 @@ __global__ void __launch_bounds__(kThreads, 3) k_lattice_gather(LatticeArgs A) {
   // lattice bits B at point q, the values N at point pairs, and w_q
   {
     const double* ref = A.ref;
-    float4* rg = reinterpret_cast<float4*>(smem + kSmRefG);
+    float* rp = reinterpret_cast<float*>(smem + kSmRefP);
     float* rn = reinterpret_cast<float*>(smem + kSmRefN);
     float* rw = reinterpret_cast<float*>(smem + kSmRefW);
     for (int i = threadIdx.x; i < 64; i += blockDim.x) {  // i = q * 8 + v (shards vertex v)
-      const int q = i >> 3, B = vbits(i & 7);
+      const int q = i >> 3, B = vbits(i & 7), h = q & 1;
       const double* gr = ref + 8 + 64 + 192 + 64 + 3 * i;
       const float n = narrow(ref[8 + 64 + 192 + i]);
-      rg[9 * q + B] = f4(narrow(gr[0]), narrow(gr[1]), narrow(gr[2]), n);
-      rn[2 * (9 * (q >> 1) + B) + (q & 1)] = n;
+      float* slot = rp + 8 * (9 * (q >> 1) + B);  // two float4: x x y y | z z N N, point h in the h-th of each pair
+      slot[h] = narrow(gr[0]);
+      slot[2 + h] = narrow(gr[1]);
+      slot[4 + h] = narrow(gr[2]);
+      slot[6 + h] = n;
+      rn[2 * (9 * (q >> 1) + B) + h] = n;
     }
     for (int i = threadIdx.x; i < 8; i += blockDim.x) rw[i] = narrow(ref[i]);
   }
