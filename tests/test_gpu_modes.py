@@ -122,7 +122,7 @@ def test_warp_per_element_kernel_matches_cta_kernel_and_oracle(cuda, jitter):
     ae.setVariant(0)
 
 
-def test_warp_variant_falls_back_where_no_warp_kernel(cuda):
+def test_warp_and_tensor_variants_fall_back_where_no_such_kernel(cuda):
     o, dof, lof = build((3, 3, 3), (1, 1, 1), A.TX_TOPO_TET, A.TX_PHYS_POISSON, A.TX_HGRAD_C1)
     rng = np.random.default_rng(1)
     x, xd, aux = (rng.uniform(-1, 1, o.n_dofs) for _ in range(3))
@@ -132,8 +132,11 @@ def test_warp_variant_falls_back_where_no_warp_kernel(cuda):
     ae.setVariant(1)
     f1, v1 = run(dof, lof, x, xd, aux, mixed=True)
     assert rel(v2, v1) <= 1e-6 and rel(f2, f1) <= 1e-6
+    ae.setVariant(3)  # no tensor-core kernel for tet Poisson either: the CTA-staged kernel
+    f3, v3 = run(dof, lof, x, xd, aux, mixed=True)
+    assert rel(v3, v1) <= 1e-6 and rel(f3, f1) <= 1e-6
     with pytest.raises(tx.TxError):
-        ae.setVariant(3)
+        ae.setVariant(4)
 
 
 # ------------------------------------------------------------ two-phase (gather) evaluation
