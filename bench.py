@@ -371,20 +371,6 @@ def run_ours(a):
     else:
         sh64 = autotune.tune_spmv(W, W.values, xs, ys)
     t_s64 = time_spmv(W.values, xs, ys, reps)
-    # the FP64 entity-block product with 0-2 of each entity's rows on the FP64 pipe and the others in
-    # double-FP32 arithmetic (tx_set_spmv_fp64_rows): times and the largest deviation from the FP64 product
-    split_cands = []
-    if sh64["form"] == "entity" and not a.spmv_shape:
-        y_fp64 = ys.clone()
-        for rows in (2, 1, 0):
-            W.setFp64Rows(rows)
-            for shape in ((3, 3), (4, 4), (8, 2), (8, 4), (16, 2)):
-                W.setEntityApplyShape(*shape)
-                t = time_spmv(W.values, xs, ys, reps)
-                dev = float(((ys - y_fp64).abs().max() / y_fp64.abs().max()).item())
-                split_cands.append((rows, shape, t, dev))
-        W.setFp64Rows(3)
-        W.setEntityApplyShape(*sh64["shape"])
     sh32 = fix_shape(parts[-1]) if a.spmv_shape else autotune.tune_spmv(W, v32, xs32, ys32)
     t_s32 = time_spmv(v32, xs32, ys32, reps)  # the FP32 form and shape stay set for the solver's inner SpMV
     n_ent = N // 3
@@ -398,16 +384,6 @@ def run_ours(a):
 
     b64, b32 = spmv_bytes(sh64["form"], 8), spmv_bytes(sh32["form"], 4)
     crs64, crs32 = spmv_bytes("crs", 8), spmv_bytes("crs", 4)
-
-    split = None
-    if split_cands:
-        rows, shape, t, dev = min(split_cands, key=lambda c: c[2])
-        split = {"fp64_rows": rows, "shape": shape, "ms": 1e3 * t, "gbs": b64 / t / 1e9, "bytes": b64,
-                 "maxrel_vs_fp64": dev,
-                 "arithmetic": "rows on the FP64 pipe: fp64_rows of 3 an entity; the others double-FP32 "
-                               "(hi/lo split by integer operations, exact products, compensated sums)",
-                 "candidates": "(fp64_rows, shape, ms, maxrel_vs_fp64)",
-                 "candidates_ms": [(r, sh, round(1e3 * tt, 3), d) for r, sh, tt, d in split_cands]}
 
     def best_crs_ms(sh):
         ts = [t for c, t in sh["candidates"] if c[0] == "crs"]
@@ -544,8 +520,7 @@ def run_ours(a):
                      "crs_equivalent_gbs": {"f64": crs64 / t_s64 / 1e9, "f32": crs32 / t_s32 / 1e9},
                      "best_crs_form_ms": {"f64": best_crs_ms(sh64), "f32": best_crs_ms(sh32)},
                      "shape_candidates_ms": {"f64": [(c, round(t, 3)) for c, t in sh64["candidates"]],
-                                             "f32": [(c, round(t, 3)) for c, t in sh32["candidates"]]},
-                     "f64_split": None if split is None else split | {"frac": split["gbs"] / peak}},
+                                             "f32": [(c, round(t, 3)) for c, t in sh32["candidates"]]}},
             "solve": solve,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind, "kernel": kernel_name,

@@ -564,18 +564,6 @@ int tx_set_spmv_shape(tx_handle h, int32_t lanes, int32_t unroll);
  * entities a warp, two lanes idle), 4 or 8 (1/2/4) or 16/32 (1/2); (0, 0) =
  * FP64 4 lanes, 4 blocks, FP32 16 lanes, 2. */
 int tx_set_spmv_entity_shape(tx_handle h, int32_t lanes, int32_t unroll);
-/* Arithmetic of the FP64 entity-block tx_spmv (TX_SPMV_F64 |
- * TX_SPMV_ENTITY_BLOCKS): the first `rows` of each entity's three rows run
- * as FP64 FMAs, the others in double-FP32 arithmetic on the FP32 pipes (each
- * FP64 value split into two FP32 values by integer operations, exact FP32
- * products with their error terms, compensated sums), which carries about
- * 2^-46 of the sum of a row's term magnitudes instead of FP64's 2^-53; values
- * outside [2^-74, 2^128) in magnitude take the FP64 FMA.  3 (the default) is
- * plain FP64.  GB300 issues about two FP64 FMAs a clock an SM, so with 3 the
- * product is bound by the FP64 pipe rather than by HBM; fewer FP64 rows move
- * the work to the FP32 pipes.  Values, vectors and results stay FP64.  No
- * counterpart in the reference (Tpetra's apply is FP64 throughout). */
-int tx_set_spmv_fp64_rows(tx_handle h, int32_t rows);
 /* Assembly kernel of the per-block mixed evaluation: 0 automatic (the
  * warp-per-element kernel where the element family has one, hex8 elasticity;
  * the CTA-staged kernel elsewhere), 1 always the CTA-staged kernel, 2 the

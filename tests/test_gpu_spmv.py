@@ -197,38 +197,3 @@ def test_spmv_vector_shape_on_unaligned_arrays(cuda):
                      d_x.data_ptr(), y.data_ptr(), 1.0, 0.0)
     assert rc == 0
     assert np.abs(y.cpu().numpy() - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
-
-
-def test_spmv_fp64_rows_split_double_fp32(cuda):
-    # FP64 entity-block product with 0-2 of each entity's rows in double-FP32 arithmetic: within 1e-13 of the
-    # largest |y| like the FP64 forms; values outside [2^-74, 2^128) take the FP64 FMA
-    g = GRAPHS["elasticity_hex8"]
-    conn = tx.CartesianConnManager(*g["n"], *g["blocks"], topology=g["topo"], jitter=0.1, seed=5)
-    dof = tx.DOFManager(conn, A.equation_set(g["phys"], g["basis"], params=g["params"]))
-    W = tx.TpetraLinearObjFactory(dof).getTpetraMatrix()
-    rng = np.random.default_rng(3)
-    vals = rng.uniform(-1, 1, dof.nnz) * np.exp(rng.uniform(-20, 20, dof.nnz))
-    vals[::97] = 0.0
-    vals[5::211] = 1e-30  # below 2^-74: the FP64 FMA
-    vals[7::307] = -3e40  # above 2^128
-    x = rng.uniform(-1, 1, dof.n_dofs)
-    x[::53] = 0.0
-    W.values.copy_(torch.from_numpy(vals))
-    y_ref = _csr_ref(W.rowptr.cpu().numpy(), W.colind.cpu().numpy(), vals, x)
-    mag = _csr_ref(W.rowptr.cpu().numpy(), W.colind.cpu().numpy(), np.abs(vals), np.abs(x))
-    xd = torch.from_numpy(x).cuda()
-    W.setApplyForm("entity")
-    try:
-        for rows in (0, 1, 2, 3):
-            W.setFp64Rows(rows)
-            for lanes, unroll in ((3, 3), (4, 4), (8, 2), (16, 1)):
-                W.setEntityApplyShape(lanes, unroll)
-                y = W.apply(xd).cpu().numpy()
-                # each row within 2^-44 of the sum of its terms' magnitudes
-                assert (np.abs(y - y_ref) <= 2.0 ** -44 * mag + 1e-300).all(), (rows, lanes, unroll)
-                assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max(), (rows, lanes, unroll)
-    finally:
-        W.setFp64Rows(3)
-        W.setEntityApplyShape(0, 0)
-    with pytest.raises(tx.TxError):
-        W.setFp64Rows(4)

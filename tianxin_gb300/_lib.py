@@ -46,7 +46,6 @@ SIGNATURES = {
     "tx_set_grid_cap": (C.c_int, [P, I32]),
     "tx_set_spmv_shape": (C.c_int, [P, I32, I32]),
     "tx_set_spmv_entity_shape": (C.c_int, [P, I32, I32]),
-    "tx_set_spmv_fp64_rows": (C.c_int, [P, I32]),
     "tx_set_assembly_variant": (C.c_int, [P, I32]),
     "tx_set_cta_threads": (C.c_int, [P, C.c_int32]),
     "tx_graph_capture_begin": (C.c_int, [P]),

@@ -137,7 +137,6 @@ struct tx_handle_s {
   int variant = 0;     // assembly kernel: 0 automatic, 1 CTA-staged, 2 warp per element, 3 tensor cores
   int* d_wait_status = nullptr;  // bounded device waits that gave up (bit 0: the tensor-core kernel's MMA waits)
   int cta_threads = 0; // threads a CTA of the staged Jacobian kernel (0: 128); tx_set_cta_threads
-  int spmv_fp64_rows = 3;  // rows of an entity on the FP64 pipe in the FP64 entity-block tx_spmv; tx_set_spmv_fp64_rows
   std::vector<cudaGraphExec_t> graphs;  // tx_graph_capture_end; destroyed slots are null
   bool capturing = false;
   // two-phase evaluation: entity -> (block, element, local basis) incidence
@@ -1078,8 +1077,8 @@ int tx_spmv(tx_handle h, int32_t precision, int64_t n_rows, const int64_t* rowpt
   const tx::EntityGraph* eg = entity ? entity_graph(h, n_rows, egs) : nullptr;
   cudaError_t e;
   if (eg && precision == TX_SPMV_F64)
-    e = tx::launch_spmv_entity_f64_split(*eg, (const double*)vals, (const double*)x, (double*)y, alpha, beta,
-                                         h->spmv_fp64_rows, h->stream, h->spmv_eb);
+    e = tx::launch_spmv_entity_f64(*eg, (const double*)vals, (const double*)x, (double*)y, alpha, beta, h->stream,
+                                   h->spmv_eb);
   else if (eg && precision == TX_SPMV_F32)
     e = tx::launch_spmv_entity_f32(*eg, (const float*)vals, (const float*)x, (float*)y, (float)alpha, (float)beta,
                                    h->stream, h->spmv_eb);
@@ -1449,13 +1448,6 @@ int tx_set_assembly_variant(tx_handle h, int32_t variant) {
   if (!h) return TX_EINVAL;
   if (variant < 0 || variant > 3) return fail(h, TX_EINVAL, "tx_set_assembly_variant: 0, 1, 2 or 3");
   h->variant = variant;
-  return TX_OK;
-}
-
-int tx_set_spmv_fp64_rows(tx_handle h, int32_t rows) {
-  if (!h) return TX_EINVAL;
-  if (rows < 0 || rows > 3) return fail(h, TX_EINVAL, "tx_set_spmv_fp64_rows: 0, 1, 2 or 3");
-  h->spmv_fp64_rows = rows;
   return TX_OK;
 }
 

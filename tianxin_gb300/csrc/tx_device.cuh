@@ -164,11 +164,6 @@ cudaError_t launch_spmv_entity_f64(const EntityGraph& eg, const double* vals, co
                                    double b, cudaStream_t s, SpmvShape shape = SpmvShape());
 cudaError_t launch_spmv_entity_f32(const EntityGraph& eg, const float* vals, const float* x, float* y, float a,
                                    float b, cudaStream_t s, SpmvShape shape = SpmvShape());
-// The FP64 entity-block product with the first fp64_rows (0-3) of each
-// entity's three rows on the FP64 pipe and the rest in double-FP32 arithmetic
-// (about 2^-46 of a row's term magnitudes); 3 is launch_spmv_entity_f64.
-cudaError_t launch_spmv_entity_f64_split(const EntityGraph& eg, const double* vals, const double* x, double* y,
-                                         double a, double b, int fp64_rows, cudaStream_t s, SpmvShape shape = SpmvShape());
 // Warp-per-element mixed assembly (hex8 elasticity, FP32 element math, atomic
 // FP64 scatter): the same results as launch_assemble's staged FP32 kernel up to
 // the summation order.

@@ -345,144 +345,6 @@ __global__ void __launch_bounds__(kThreads, entity_min_blocks(G, U, sizeof(T))) 
   }
 }
 
-// ---- FP64 product with part of each entity's rows in double-FP32 arithmetic
-// GB300 issues about two FP64 FMAs a clock an SM against 128 FP32 lanes, so
-// the FP64 entity-block product above is bound by its FP64 pipe (one FMA an
-// entry), not by HBM.  Here the first R of an entity's three rows keep FP64
-// FMAs and the other 3 - R rows run on the FP32 pipes: each FP64 value is split
-// into hi + lo (two FP32 values, by integer operations), the product
-// (ah + al)(bh + bl) is formed as an exact FP32 product plus its error term
-// and the cross terms (al bl, ~2^-48 of the product, dropped), and the sums
-// are compensated (TwoSum), so a row carries about 2^-46 of the sum of its
-// terms' magnitudes instead of FP64's 2^-53.  Values outside [2^-74, 2^128)
-// in magnitude (and inf/NaN) take the FP64 FMA.
-
-// v = h + l to 2^-48 |v|: h the leading 24 significant bits (truncated), l the
-// next 29 rounded to FP32; false (h, l unusable) outside [2^-74, 2^128) in
-// magnitude, except zero (h = l = 0).
-__device__ __forceinline__ bool split_f64(double v, float& h, float& l) {
-  const uint32_t hi = (uint32_t)__double2hiint(v), lo = (uint32_t)__double2loint(v);
-  const uint32_t a = hi & 0x7fffffffu, e = a >> 20, sg = hi & 0x80000000u;
-  const bool zero = (a | lo) == 0u;
-  h = __uint_as_float(zero ? sg : (__funnelshift_l(lo, a - 0x38000000u, 3) | sg));
-  l = zero ? 0.f : __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), __uint_as_float(sg | ((e - 948u) << 23)));
-  return zero || e - 949u <= 1150u - 949u;
-}
-
-// (sh, sl) += (ah + al)(bh + bl): the FP32 product, its rounding error and the
-// cross terms, added with a TwoSum (intrinsics: no contraction into FMAs).
-__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float bh, float bl) {
-  const float p = __fmul_rn(ah, bh);
-  float pe = __fmaf_rn(ah, bh, -p);
-  pe = __fmaf_rn(ah, bl, pe);
-  pe = __fmaf_rn(al, bh, pe);
-  const float t = __fadd_rn(sh, p);
-  const float bp = __fsub_rn(t, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-  sh = t;
-  sl = __fadd_rn(sl, __fadd_rn(err, pe));
-}
-
-template <int G, int UU, bool CHECK, int R>
-__device__ __forceinline__ void entity_pass_split(int64_t j, int64_t b, int64_t deg, int64_t rs,
-                                                  const int32_t* __restrict__ ecol, const double* __restrict__ v0,
-                                                  const double* __restrict__ x, int64_t n_ent, double (&s)[3],
-                                                  float (&sh)[3], float (&sl)[3]) {
-  bool in[UU];
-  int64_t m[UU];
-  double v[UU][3][3];
-#pragma unroll
-  for (int u = 0; u < UU; ++u) {
-    const int64_t jj = j + u * G;
-    in[u] = !CHECK || jj < deg;
-    const int64_t jc = in[u] ? jj : j;
-    const uint32_t mm = (uint32_t)__ldcs(ecol + b + jc);
-    m[u] = (uint64_t)mm < (uint64_t)n_ent ? (int64_t)mm : 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) v[u][c][d] = __ldcs(v0 + c * rs + 3 * jc + d);
-  }
-#pragma unroll
-  for (int u = 0; u < UU; ++u) {
-    double xm[3];
-    float xh[3], xl[3];
-    bool xo[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      xm[d] = __ldg(x + 3 * m[u] + d);
-      xo[d] = split_f64(xm[d], xh[d], xl[d]);
-    }
-    if (in[u]) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          if (c < R) {
-            s[c] += v[u][c][d] * xm[d];
-          } else {
-            float vh, vl;
-            if (split_f64(v[u][c][d], vh, vl) && xo[d]) df_fma(sh[c], sl[c], vh, vl, xh[d], xl[d]);
-            else s[c] += v[u][c][d] * xm[d];
-          }
-        }
-    }
-  }
-}
-
-template <int G, int U, int R>
-__device__ __forceinline__ void entity_dot_split(int64_t b, int64_t deg, int sub, const int32_t* __restrict__ ecol,
-                                                 const double* __restrict__ vals, const double* __restrict__ x,
-                                                 int64_t n_ent, double (&s)[3], float (&sh)[3], float (&sl)[3]) {
-  const double* v0 = vals + 9 * b;
-  const int64_t rs = 3 * deg;
-  const int64_t full = deg / (G * U) * (G * U);
-  int64_t j = sub;
-  for (; j < full; j += G * U) entity_pass_split<G, U, false, R>(j, b, deg, rs, ecol, v0, x, n_ent, s, sh, sl);
-  const int64_t rest = deg - full;
-  if (rest <= 0) return;
-  const int64_t uu = (rest + G - 1) / G;
-  if constexpr (U >= 4) {
-    if (uu >= 4) { entity_pass_split<G, 4, true, R>(j, b, deg, rs, ecol, v0, x, n_ent, s, sh, sl); return; }
-  }
-  if constexpr (U >= 3) {
-    if (uu == 3) { entity_pass_split<G, 3, true, R>(j, b, deg, rs, ecol, v0, x, n_ent, s, sh, sl); return; }
-  }
-  if constexpr (U >= 2) {
-    if (uu == 2) { entity_pass_split<G, 2, true, R>(j, b, deg, rs, ecol, v0, x, n_ent, s, sh, sl); return; }
-  }
-  entity_pass_split<G, 1, true, R>(j, b, deg, rs, ecol, v0, x, n_ent, s, sh, sl);
-}
-
-template <int G, int U, int R>
-__global__ void __launch_bounds__(kThreads, 2) k_spmv_eb_split(int64_t n_ent, const int64_t* __restrict__ erp,
-                                                     const int32_t* __restrict__ ecol,
-                                                     const double* __restrict__ vals, const double* __restrict__ x,
-                                                     double* __restrict__ y, double alpha, double beta) {
-  constexpr int GPW = 32 / G;
-  const int lane = threadIdx.x & 31;
-  const int g = lane / G < GPW ? lane / G : GPW;
-  const int sub = lane - (lane / G) * G;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t base = warp * GPW; base < n_ent; base += nwarps * GPW) {
-    const int64_t r = g < GPW ? base + g : n_ent;
-    double s[3] = {0.0, 0.0, 0.0};
-    float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
-    const int64_t rc = r < n_ent ? r : n_ent - 1;
-    const int64_t b = __ldg(erp + rc);
-    entity_dot_split<G, U, R>(b, r < n_ent ? __ldg(erp + rc + 1) - b : 0, sub, ecol, vals, x, n_ent, s, sh, sl);
-    // the FP32 pairs join their rows' FP64 sums (exact widening, two FP64 additions a row)
-#pragma unroll
-    for (int c = R; c < 3; ++c) s[c] = (s[c] + widen(sh[c])) + widen(sl[c]);
-    const double sc = entity_reduce<double, 3, G>(s, sub);
-    if (r < n_ent && sub < 3) {
-      const int64_t row = 3 * r + sub;
-      y[row] = beta == 0.0 ? (alpha == 1.0 ? sc : alpha * sc) : alpha * sc + beta * y[row];
-    }
-  }
-}
-
 // The automatic shape, from timings of every shape on the 128^3 elasticity
 // operator (80 entries a row): narrow row groups win (8 lanes, FP64 1.52 ms
 // against 3.84 ms for a warp per row), FP32 gains from four loads per lane.
@@ -944,24 +806,6 @@ cudaError_t launch_spmv_entity_f64(const EntityGraph& eg, const double* vals, co
                                    double b, cudaStream_t s, SpmvShape shape) {
   if (eg.n_ent <= 0) return cudaSuccess;
   return with_entity_shape(resolve_entity_shape(shape, false), EntitySpmvLaunch<double>{eg, vals, x, y, a, b, s});
-}
-struct EntitySplitLaunch {
-  EntityGraph eg; const double* vals; const double* x; double* y; double a, b; cudaStream_t s; int rows;
-  template <int L, int U>
-  cudaError_t run() const {
-    const unsigned grid = grid_for(eg.n_ent, (kThreads / 32) * (32 / L), 152 * 64);
-    if (rows == 0) k_spmv_eb_split<L, U, 0><<<grid, kThreads, 0, s>>>(eg.n_ent, eg.erp, eg.ecol, vals, x, y, a, b);
-    else if (rows == 1) k_spmv_eb_split<L, U, 1><<<grid, kThreads, 0, s>>>(eg.n_ent, eg.erp, eg.ecol, vals, x, y, a, b);
-    else k_spmv_eb_split<L, U, 2><<<grid, kThreads, 0, s>>>(eg.n_ent, eg.erp, eg.ecol, vals, x, y, a, b);
-    return cudaGetLastError();
-  }
-};
-cudaError_t launch_spmv_entity_f64_split(const EntityGraph& eg, const double* vals, const double* x, double* y,
-                                         double a, double b, int fp64_rows, cudaStream_t s, SpmvShape shape) {
-  if (eg.n_ent <= 0) return cudaSuccess;
-  if (fp64_rows >= 3) return launch_spmv_entity_f64(eg, vals, x, y, a, b, s, shape);
-  if (fp64_rows < 0) return cudaErrorInvalidValue;
-  return with_entity_shape(resolve_entity_shape(shape, false), EntitySplitLaunch{eg, vals, x, y, a, b, s, fp64_rows});
 }
 cudaError_t launch_spmv_entity_f32(const EntityGraph& eg, const float* vals, const float* x, float* y, float a,
                                    float b, cudaStream_t s, SpmvShape shape) {

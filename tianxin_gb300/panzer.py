@@ -342,11 +342,6 @@ class CrsMatrix:
         check(self.dof.h, self.dof.lib.tx_set_spmv_entity_shape(self.dof.h, lanes, unroll),
               "tx_set_spmv_entity_shape")
 
-    def setFp64Rows(self, rows=3):
-        """Rows of each entity on the FP64 pipe in the FP64 entity-block apply (3: plain FP64); the others in
-        double-FP32 arithmetic on the FP32 pipes (about 2^-46 of a row's term magnitudes)."""
-        check(self.dof.h, self.dof.lib.tx_set_spmv_fp64_rows(self.dof.h, rows), "tx_set_spmv_fp64_rows")
-
     def setApplyForm(self, form):
         """"entity" (the handle's graph only) or "crs"."""
         if form not in ("entity", "crs") or (form == "entity" and not self.on_handle_graph):
