@@ -410,10 +410,17 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
   const float bl = A.beta * A.lam, bm = A.beta * A.mu, am = A.alpha * A.rho;
   // entries start at float (rowstart & 1) of the node's stage row, so that
   // stage float4 j maps to an even, 16-byte aligned pair of FP64 entries
-  float* stage = reinterpret_cast<float*>(smem + kSmStage) + ln * kStageRow +
-                 (int)(*reinterpret_cast<const int64_t*>(info) & 1);
+  const int so = (int)(*reinterpret_cast<const int64_t*>(info) & 1);
+  float* stage = reinterpret_cast<float*>(smem + kSmStage) + ln * kStageRow + so;
   const uint8_t* npos = info + 16;
   const int rl = 3 * nnb;  // entries of one row
+  // zeros around the node's entries: the parity slot and the float4 tail
+  if (e == 7 && nnb > 0) {
+    if (so) stage[-1] = 0.f;  // (the slot no writer touches)
+    stage[9 * nnb] = 0.f;
+    stage[9 * nnb + 1] = 0.f;
+    stage[9 * nnb + 2] = 0.f;
+  }
   const unsigned wmask = nnb > 0 ? (unsigned)(kWriters >> (8 * e)) & 0xffu : 0u;
   // slot c holds the block of the element vertex with bits c ^ lbits (bit per
   // axis: 0 = the node's own lattice line, 1 = this element's neighbour line)
@@ -493,7 +500,8 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
   // the warp's four nodes: coalesced FP64 stores of each node's 3 rows, a
   // float4 of the stage (four entries, two 16-byte stores) per lane and step
   const int wn0 = (threadIdx.x >> 5) * 4;
-#pragma unroll 1
+  // two nodes' loads and stores in flight
+#pragma unroll 2
   for (int m = 0; m < 4; ++m) {
     const unsigned char* inf = smem + kSmPlaneInfo + ((int)(k & 1) * kNodes + wn0 + m) * kInfoBytes;
     const int nb = reinterpret_cast<const int32_t*>(inf)[3];
@@ -502,11 +510,14 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
     const int o = (int)(rs & 1), n = 9 * nb, end = o + n;
     double* dst = A.vals + (rs - o);  // even: 16-byte aligned
     const float4* src = reinterpret_cast<const float4*>(smem + kSmStage + (wn0 + m) * kStageRow * 4);
-    // exact FP32 -> FP64 widening by integer operations for zeros and normal
-    // numbers: the exponent rebiased (not for a zero: times min(|b|, 1)),
-    // the fraction moved up; a subnormal, infinity or NaN anywhere in the
-    // node's rows (lane extremes of |b| and |b| - 1, one vote a node) sends
-    // those entries through the hardware conversion afterwards
+    // exact FP32 -> FP64 widening: one entry of four by the hardware
+    // conversion (on the FP64 pipe, which this kernel leaves idle; more than
+    // one in four makes it the bottleneck), three by integer operations for
+    // zeros and normal numbers: the exponent rebiased (not for a zero: times
+    // min(|b|, 1)), the fraction moved up; a subnormal, infinity or NaN among
+    // those (lane extremes of |b| and |b| - 1, one vote a node) sends them
+    // through the hardware conversion afterwards.  The stage holds zeros
+    // around the node's entries, so the extremes need no range test.
     uint32_t mx = 0u, mn = 0xffffffffu;
     for (int j = lane; 4 * j < end; j += 32) {
       const float4 v4 = src[j];
@@ -514,9 +525,12 @@ __device__ __forceinline__ void node_layer(const LatticeArgs& A, int64_t i0, int
       double d[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int p = 4 * j + i;
+        if (i == 0) {
+          d[0] = (double)v[0];
+          continue;
+        }
         const uint32_t b = __float_as_uint(v[i]);
-        const uint32_t a = (p >= o && p < end) ? b & 0x7fffffffu : 0u;
+        const uint32_t a = b & 0x7fffffffu;  // zeros around the entries
         mx = max(mx, a);
         mn = min(mn, a - 1u);
         const uint32_t hi = min(a, 1u) * 0x38000000u + ((uint32_t)((int32_t)b >> 3) & 0x8fffffffu);
