@@ -249,7 +249,9 @@ def run_reference(a):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": workload_desc(a.n) | {"parallelism": "cpu", "sample_elements": n ** 3},
+            "config": workload_desc(a.n) | {"workload": workload_desc(a.n)["workload"] +
+                                            f"; each step a {n}^3 sample ({n ** 3} elements) of it",
+                                            "parallelism": "cpu", "sample_elements": n ** 3},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
