@@ -160,9 +160,10 @@ __device__ __forceinline__ void load_plane(const LatticeArgs& A, int64_t i0, int
 // Geometry, physical gradients and residual rows of the 5 x 5 elements of
 // element layer ek (vertices in plane slots ek & 1 and (ek + 1) & 1); one
 // thread per (element, point pair), the four threads of an element adjacent
-// lanes of one warp.  Each thread forms its two points' share of the
-// element's 8 x 3 residual rows, W_q (grad N_B . sigma_q + N_B (rho acc_q -
-// b)), and two butterflies over the four lanes sum the shares.
+// lanes of one warp, the pair's two points the two halves of packed FP32x2
+// FMAs.  Each thread forms its two points' share of the element's 8 x 3
+// residual rows, W_q (grad N_B . sigma_q + N_B (rho acc_q - b)), and two
+// halving exchanges over the four lanes sum the shares.
 template <bool MASS>
 __device__ __forceinline__ void element_layer(const LatticeArgs& A, int64_t i0, int64_t j0, int64_t ek,
                                               unsigned char* smem) {
