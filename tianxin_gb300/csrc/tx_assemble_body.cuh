@@ -451,18 +451,31 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               accumulate<ATOMIC>(P.vals + rp[c] + pb + d, widen(v));
             }
           };
-          // Scalar physics with many points (hex27: 27 x 27 entries over 27
-          // points): the point loop outside, so the row's own weighted
-          // gradient and the point's flux factors are read once a point and
-          // the NB entries of the row accumulate in registers (one broadcast
-          // load and four FMAs an entry and point instead of about ten loads);
+          // Scalar physics whose point tables stay in shared memory (hex27: 27 x
+          // 27 entries over 27 points; H(curl): 12 x 12 over 8): the point loop
+          // outside, so the row's own weighted gradient (or curl and value) and
+          // the point's flux factors are read once a point and the NB entries
+          // of the row accumulate in registers (one or two broadcast loads and
+          // four to eight FMAs an entry and point instead of about ten loads);
           // each entry's sum still runs over the points in order.
-          constexpr bool QOUTER = !CACHE && (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT);
+          constexpr bool QOUTER = !CACHE && (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT || PHYS == TX_PHYS_MAXWELL);
           if constexpr (QOUTER) {
             Real kg[NB], km[NB];
 #pragma unroll
             for (int b = 0; b < NB; ++b) kg[b] = km[b] = Real(0);
             for (int q = 0; q < NQ; ++q) {
+              if constexpr (PHYS == TX_PHYS_MAXWELL) {
+                // curl-curl and mass entries: the row's curl and value at q read once
+                const Real w = sW[q];
+                const R4<Real> ca = ld4(sG + q * GQS + a * 4), va = ld4(sV + q * GQS + a * 4);
+#pragma unroll
+                for (int b = 0; b < NB; ++b) {
+                  const R4<Real> cb = ld4(sG + q * GQS + b * 4), vb = ld4(sV + q * GQS + b * 4);
+                  kg[b] += w * (ca.x * cb.x + ca.y * cb.y + ca.z * cb.z);
+                  km[b] += w * (va.x * vb.x + va.y * vb.y + va.z * vb.z);
+                }
+                continue;
+              }
               const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2);
               if constexpr (PHYS == TX_PHYS_HEAT) {
                 const Real* qf = sQF + q * NQF;
@@ -488,6 +501,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               if constexpr (TAN) eb = __ldg(B.dconn + e * NB + b);
               if constexpr (PHYS == TX_PHYS_HEAT) {
                 put(0, b, 0, pb, beta * kg[b]);
+              } else if constexpr (PHYS == TX_PHYS_MAXWELL) {
+                put(0, b, 0, pb, beta * (pr[0] * kg[b] + pr[1] * km[b]));
               } else {
                 put(0, b, 0, pb, (beta * pr[0]) * kg[b] + (beta * pr[1] + alpha * pr[2]) * km[b]);
               }
