@@ -70,7 +70,8 @@ struct Cfg {
   // odd word strides: threads that write one row/point each spread over all banks
   // sG/sV: per point q and basis b one 4-vector (x, y, z, N) at q * GQS + b * 4;
   // GQS / 4 odd: the quarter-warp of a 128-bit access covers all banks
-  static constexpr int GQS = NB * 4 + 4;
+  static constexpr int GQS = NB * 4 + (NB % 2 == 0 ? 4 : 0);  // NB float4 slots, padded to an odd count
+  static_assert((GQS / 4) % 2 == 1, "odd point stride in float4 slots");
   static constexpr int NE_ = (PHYS == TX_PHYS_ELASTICITY ? 3 : 1) * NB;
   static constexpr int KRS = NE_ | 1;       // sK:    [row * KRS + col]
   // shared: reference part
