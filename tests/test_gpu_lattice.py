@@ -108,3 +108,24 @@ def test_lattice_gather_regular_lattice_zero_entries(cuda):
     assert np.isfinite(wg).all()
     tiny = np.abs(v_ref) <= 1e-14 * np.abs(v_ref).max()
     assert np.abs(wg[tiny]).max() <= 1e-6 * np.abs(v_ref).max()
+
+
+@pytest.mark.parametrize("n,params,alpha", [
+    ((1, 7, 3), (1.0, 0.3, 0.0, 0.0, -1.0, 0.0), 0.75),      # one element wide: most node tiles half empty
+    ((2, 2, 64), (1.0, 0.3, 0.0, 0.0, -1.0, 0.0), 0.75),     # tall: many z chunks of one node column
+    ((7, 5, 4), (1.0, 0.3, 0.1, 0.2, 0.3, 2.0), 0.0),        # density with alpha = 0: mass terms in R only
+], ids=["1x7x3", "2x2x64", "7x5x4_alpha0"])
+def test_lattice_gather_edge_shapes_against_oracle(cuda, n, params, alpha):
+    o, dof, lof = setup(n, params, seed=8)
+    rng = np.random.default_rng(11)
+    x_h = rng.uniform(-1, 1, o.n_dofs)
+    xd_h = rng.uniform(-1, 1, o.n_dofs)
+    f_ref, v_ref = o.evaluate(x_h, xd_h, alpha=alpha, beta=1.0)
+    f, W = lof.getTpetraVector(), lof.getTpetraMatrix()
+    f.fill_(-5.0)
+    W.initializeMatrix(9.0)
+    ae = tx.AssemblyEngine(lof)
+    assert ae.gather_form() == "lattice"
+    ae.evaluate(torch.from_numpy(x_h).cuda(), torch.from_numpy(xd_h).cuda(), alpha=alpha, beta=1.0, f=f, W=W,
+                mixed=True, gather=True)
+    assert rel(f.cpu().numpy(), f_ref) <= TOL_MIXED and rel(W.values.cpu().numpy(), v_ref) <= TOL_MIXED
