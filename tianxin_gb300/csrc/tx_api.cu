@@ -24,9 +24,12 @@ struct DevBlock {
   uint8_t* epos = nullptr;
   int8_t* esign = nullptr;
   double* ref = nullptr;
+  float* ref32 = nullptr;
   int32_t* color_perm = nullptr;
   std::vector<int64_t> color_offsets;
-  tx::BlockView view() const { return tx::BlockView{topo, basis, nq, nb, nv, n_elem, vconn, dconn, epos, esign, ref}; }
+  tx::BlockView view() const {
+    return tx::BlockView{topo, basis, nq, nb, nv, n_elem, vconn, dconn, epos, esign, ref, ref32};
+  }
 };
 
 // Pinned staging for small per-call tables (kernel parameters of batched
@@ -181,7 +184,7 @@ struct tx_handle_s {
     cudaFree(d_lat); cudaFree(d_lat_u); cudaFree(d_lat_ud);
     d_lat = nullptr; d_lat_u = nullptr; d_lat_ud = nullptr;
     for (auto& b : blocks) {
-      cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref);
+      cudaFree(b.vconn); cudaFree(b.dconn); cudaFree(b.epos); cudaFree(b.esign); cudaFree(b.ref); cudaFree(b.ref32);
       cudaFree(b.color_perm);
     }
     cudaFree(d_items); cudaFree(d_counter);
@@ -914,7 +917,9 @@ int tx_dof_build(tx_handle h, const tx_equation_set_desc* eq) {
       ck(upload(d.dconn, B.dconn), "upload dconn");
       ck(upload(d.epos, B.epos), "upload epos");
       ck(upload(d.esign, B.esign), "upload esign");
-      ck(upload(d.ref, B.ref.packed()), "upload reference tables");
+      const std::vector<double> ref = B.ref.packed();
+      ck(upload(d.ref, ref), "upload reference tables");
+      ck(upload(d.ref32, std::vector<float>(ref.begin(), ref.end())), "upload FP32 reference tables");
       ck(upload(d.color_perm, B.color_perm), "upload colouring");
     }
     ck(upload(h->d_erowptr, D.erowptr), "upload entity rowptr");

@@ -16,7 +16,8 @@ constexpr int kBatchThreads = 128;
 template <int T, int BS, int Q, int PH, typename Real, bool JAC, bool STAGE>
 __device__ __noinline__ void batched_item(const BlockView& B, const EvalParams& P, int64_t e0, int64_t e1,
                                           unsigned char* smem) {
-  assemble_body<T, BS, Q, PH, Real, JAC, true, kBatchThreads, STAGE>(B, P, nullptr, e0, e1, 0, 1, smem);
+  assemble_body<T, BS, Q, PH, Real, JAC, true, kBatchThreads, STAGE, false, false, true>(B, P, nullptr, e0, e1, 0, 1,
+                                                                                        smem);
 }
 
 // Persistent kernel: CTAs take work items (element chunks of any block of
@@ -57,7 +58,7 @@ size_t smem_of_kind(int kind) {
   switch (kind) {
 #define TX_SZ(K, T, BS, Q, PH) \
   case K:                      \
-    return Cfg<T, BS, Q, PH, Real, kBatchThreads, STAGE>::SMEM;
+    return Cfg<T, BS, Q, PH, Real, kBatchThreads, STAGE, true>::SMEM;
     TX_FOR_EACH_KIND(TX_SZ)
 #undef TX_SZ
     default:

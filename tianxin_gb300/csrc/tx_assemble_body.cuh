@@ -55,8 +55,10 @@ constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 // STAGE_: element residual/Jacobian staged in shared memory, then scattered
 // by the whole CTA with consecutive threads on consecutive entries of a CRS
 // row (few L2 sectors per warp reduction) instead of one row per thread.
+// GREF_: the persistent kernel's form, whose shared memory is sized for the
+// largest family of the launch (hex27 tables in global memory: see RG).
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, int THREADS_ = (Family<TOPO, BASIS>::NB > 16 ? 128 : 256),
-          bool STAGE_ = false>
+          bool STAGE_ = false, bool GREF_ = false>
 struct Cfg {
   static constexpr int NV = Family<TOPO, BASIS>::NV;
   static constexpr int NB = Family<TOPO, BASIS>::NB;
@@ -74,13 +76,21 @@ struct Cfg {
   static_assert((GQS / 4) % 2 == 1, "odd point stride in float4 slots");
   static constexpr int NE_ = (PHYS == TX_PHYS_ELASTICITY ? 3 : 1) * NB;
   static constexpr int KRS = NE_ | 1;       // sK:    [row * KRS + col]
-  // shared: reference part
+  // hex27 (27 basis functions at 27 points) in the persistent kernel: the
+  // reference tables and the element's epos stay in global memory (read
+  // through L1), so that a CTA's shared memory (four elements' point tables,
+  // 54 KB) lets four CTAs share an SM, for the hex27 items and for the other
+  // families' items of the same launch.  (The per-block kernel keeps them in
+  // shared memory: at three CTAs an SM its L1 holds more of the gathers.)
+  static constexpr bool RG = GREF_ && NB > 16;
+  // shared: reference part (geometry values only where sources need absolute coordinates)
   static constexpr size_t R_GEO_GRAD = 0;
-  static constexpr size_t R_GEO_VAL = align16(R_GEO_GRAD + sizeof(Real) * NQ * NV * 3);
-  static constexpr size_t R_W = align16(R_GEO_VAL + sizeof(double) * NQ * NV);
+  static constexpr size_t R_GEO_VAL = align16(R_GEO_GRAD + (RG ? 0 : sizeof(Real) * NQ * NV * 3));
+  static constexpr size_t R_W =
+      align16(R_GEO_VAL + (RG && PHYS != TX_PHYS_POISSON ? 0 : sizeof(double) * NQ * NV));
   static constexpr size_t R_VAL = align16(R_W + sizeof(Real) * NQ);
-  static constexpr size_t R_GRAD = align16(R_VAL + sizeof(Real) * NQ * NB * NVAL);
-  static constexpr size_t R_END = align16(R_GRAD + sizeof(Real) * NQ * NB * 3);
+  static constexpr size_t R_GRAD = align16(R_VAL + (RG ? 0 : sizeof(Real) * NQ * NB * NVAL));
+  static constexpr size_t R_END = align16(R_GRAD + (RG ? 0 : sizeof(Real) * NQ * NB * 3));
   // shared: per element part
   static constexpr bool XABS = PHYS == TX_PHYS_POISSON;                // sources need absolute coordinates
   static constexpr size_t E_X = 0;                                      // vertex coordinates (FP64)
@@ -107,7 +117,7 @@ struct Cfg {
   static constexpr size_t E_EP = align16(E_LA + sizeof(int32_t) * (STAGE ? NB : 0));
   // per-element stride = 32 B past a multiple of 128 B: the four elements of a
   // warp start 8 banks apart, so same-offset accesses do not conflict
-  static constexpr size_t E_RAW = align16(E_EP + (STAGE ? NB * NB : 0));
+  static constexpr size_t E_RAW = align16(E_EP + (STAGE && !RG ? NB * NB : 0));
   static constexpr size_t E_END = ((E_RAW + 127 - 32) / 128) * 128 + 32;
   static constexpr size_t SMEM = R_END + EPB * E_END;
 };
@@ -128,19 +138,32 @@ __device__ __forceinline__ Real source_at(int kind, double c, double s0, const d
 // the coloured (deterministic) scatter: no two elements processed by one
 // launch share a row, so plain read-modify-write is race free.
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, int THREADS,
-          bool STAGE = false, bool TAN = false, bool SCR = false>
+          bool STAGE = false, bool TAN = false, bool SCR = false, bool GREF = false>
 __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalParams& P, const int32_t* perm,
                                               int64_t e_lo, int64_t e_hi, int64_t grp0, int64_t grp_stride,
                                               unsigned char* smem) {
-  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS, STAGE>;
+  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, THREADS, STAGE, GREF>;
   constexpr int NV = C::NV, NB = C::NB, NF = C::NF, TPE = C::TPE, EPB = C::EPB, NQF = C::NQF, NE = C::NE;
   constexpr int GQS = C::GQS, KRS = C::KRS;
   constexpr bool HC = C::HC;
-  Real* r_geo_grad = reinterpret_cast<Real*>(smem + C::R_GEO_GRAD);
-  double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
   Real* r_w = reinterpret_cast<Real*>(smem + C::R_W);
-  Real* r_val = reinterpret_cast<Real*>(smem + C::R_VAL);
-  Real* r_grad = reinterpret_cast<Real*>(smem + C::R_GRAD);
+  double* r_geo_val = reinterpret_cast<double*>(smem + C::R_GEO_VAL);
+  const Real* r_geo_grad;
+  const Real* r_val;
+  const Real* r_grad;
+  if constexpr (C::RG) {
+    // the packed tables in global memory, in the arithmetic's type
+    const Real* g;
+    if constexpr (sizeof(Real) == 4) g = reinterpret_cast<const Real*>(B.ref32);
+    else g = reinterpret_cast<const Real*>(B.ref);
+    r_geo_grad = g + NQ + NQ * NV;
+    r_val = r_geo_grad + NQ * NV * 3;
+    r_grad = r_val + NQ * NB * C::NVAL;
+  } else {
+    r_geo_grad = reinterpret_cast<const Real*>(smem + C::R_GEO_GRAD);
+    r_val = reinterpret_cast<const Real*>(smem + C::R_VAL);
+    r_grad = reinterpret_cast<const Real*>(smem + C::R_GRAD);
+  }
 
   // reference tables: [w | geo_val | geo_grad | val | grad] in FP64
   {
@@ -148,13 +171,19 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
     // FP32 copies by integer narrowing (off the FP64 pipe)
     for (int i = threadIdx.x; i < NQ; i += blockDim.x) r_w[i] = to_real<Real>(ref[i]);
     ref += NQ;
-    for (int i = threadIdx.x; i < NQ * NV; i += blockDim.x) r_geo_val[i] = ref[i];
+    if constexpr (!C::RG || C::XABS)
+      for (int i = threadIdx.x; i < NQ * NV; i += blockDim.x) r_geo_val[i] = ref[i];
     ref += NQ * NV;
-    for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) r_geo_grad[i] = to_real<Real>(ref[i]);
-    ref += NQ * NV * 3;
-    for (int i = threadIdx.x; i < NQ * NB * C::NVAL; i += blockDim.x) r_val[i] = to_real<Real>(ref[i]);
-    ref += NQ * NB * C::NVAL;
-    for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) r_grad[i] = to_real<Real>(ref[i]);
+    if constexpr (!C::RG) {
+      Real* s_geo_grad = reinterpret_cast<Real*>(smem + C::R_GEO_GRAD);
+      Real* s_val = reinterpret_cast<Real*>(smem + C::R_VAL);
+      Real* s_grad = reinterpret_cast<Real*>(smem + C::R_GRAD);
+      for (int i = threadIdx.x; i < NQ * NV * 3; i += blockDim.x) s_geo_grad[i] = to_real<Real>(ref[i]);
+      ref += NQ * NV * 3;
+      for (int i = threadIdx.x; i < NQ * NB * C::NVAL; i += blockDim.x) s_val[i] = to_real<Real>(ref[i]);
+      ref += NQ * NB * C::NVAL;
+      for (int i = threadIdx.x; i < NQ * NB * 3; i += blockDim.x) s_grad[i] = to_real<Real>(ref[i]);
+    }
   }
 
   const int le = threadIdx.x / TPE;
@@ -219,7 +248,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
             // that the scatter's lane (column block k) finds its row positions together
 #pragma unroll
             for (int c = 0; c < NF; ++c) sRP[b * NF + c] = (int64_t)(P.vals + __ldg(P.rowptr + NF * ent + c));
-            for (int k = 0; k < NB; ++k) sEP[k * NB + b] = __ldg(B.epos + (e * NB + b) * NB + k);
+            if constexpr (!C::RG)
+              for (int k = 0; k < NB; ++k) sEP[k * NB + b] = __ldg(B.epos + (e * NB + b) * NB + k);
           }
         }
       }
@@ -642,6 +672,12 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
             const int64_t* rps = reinterpret_cast<const int64_t*>(e2 + C::E_RP) + sub;
             const uint8_t* eps = reinterpret_cast<const uint8_t*>(e2 + C::E_EP) + cb * NB;
             const Real* kk = reinterpret_cast<const Real*>(e2 + C::E_K) + sub * KRS + col;
+            // hex27: the element's epos from global memory, column cb of row a at epos[e][a][cb]
+            const uint8_t* epg = nullptr;
+            if constexpr (C::RG) {
+              const int64_t ei2 = g0 + l2;
+              epg = B.epos + ((perm ? (int64_t)__ldg(perm + ei2) : ei2) * NB) * NB + cb;
+            }
             if constexpr (RPW == 1 && NB == 8) {
               // one pass per row: the lane's 8 byte offsets (one per row vertex) in registers
               const uint2 w = *reinterpret_cast<const uint2*>(eps);
@@ -660,7 +696,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               for (int k = 0; k < NR; ++k) {
                 const int row = sub + k * RPW;
                 if (NE % RPW == 0 || row < NE) {
-                  double* p = reinterpret_cast<double*>(rps[k * RPW]) + (NF * eps[row / NF] + cd);
+                  const int pos = C::RG ? (int)__ldg(epg + (row / NF) * NB) : (int)eps[row / NF];
+                  double* p = reinterpret_cast<double*>(rps[k * RPW]) + (NF * pos + cd);
                   if constexpr (ATOMIC) red_global(p, widen(kk[k * RPW * KRS]));
                   else *p += widen(kk[k * RPW * KRS]);
                 }

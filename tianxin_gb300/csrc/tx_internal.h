@@ -50,6 +50,7 @@ struct BlockView {
   const uint8_t* epos;    // [E][nb][nb] block position of entity b in row of entity a
   const int8_t* esign;    // [E][nb]  HCURL edge signs (nullptr otherwise)
   const double* ref;      // packed RefTables
+  const float* ref32 = nullptr;  // the same tables in FP32 (read from global memory by the hex27 kernels)
 };
 
 struct Handle;  // defined in tx_api.cu
