@@ -22,11 +22,13 @@ __device__ __noinline__ void batched_item(const BlockView& B, const EvalParams& 
 
 // Persistent kernel: CTAs take work items (element chunks of any block of
 // any mesh, any family) from an atomic counter until the list is empty.
-// STAGE: Jacobians through the staged, row-coalesced scatter (FP32 builds
-// held to four resident CTAs like the per-block staged kernels), else each
+// STAGE: Jacobians through the staged, row-coalesced scatter, else each
 // thread reduces its own rows.
+// FP32 staged builds ask for five resident CTAs (at most 102 registers; some
+// families' item functions then spill a little): the work items' gathers are
+// latency-bound, and the fifth CTA takes the 256-mesh batch from 7.7 to 6.8 ms.
 template <typename Real, bool JAC, bool STAGE>
-__global__ void __launch_bounds__(kBatchThreads, min_blocks<Real, STAGE>())
+__global__ void __launch_bounds__(kBatchThreads, min_blocks<Real, STAGE>() + (sizeof(Real) == 4 && STAGE ? 1 : 0))
 k_assemble_batched(const BlockView* __restrict__ views, const EvalParams* __restrict__ params,
                    const WorkItem* __restrict__ items, int n_items, int* counter) {
   extern __shared__ __align__(16) unsigned char smem[];
