@@ -12,12 +12,16 @@ constexpr int kBatchThreads = 128;
 // One work item of one element family, compiled out of line so that every
 // family keeps its own register allocation inside the persistent kernel
 // (inlined into one switch, the families' code shared one allocation of
-// 238-255 registers).
+// 238-255 registers).  The block view and parameters stay in global memory
+// and are read through the pointers: copied by value into the caller, each
+// thread kept its own 330-byte copy on its stack (local memory, rewritten for
+// every work item and re-read inside the element loops; 7 % of the 256-mesh
+// batch's time).
 template <int T, int BS, int Q, int PH, typename Real, bool JAC, bool STAGE>
-__device__ __noinline__ void batched_item(const BlockView& B, const EvalParams& P, int64_t e0, int64_t e1,
-                                          unsigned char* smem) {
-  assemble_body<T, BS, Q, PH, Real, JAC, true, kBatchThreads, STAGE, false, false, true>(B, P, nullptr, e0, e1, 0, 1,
-                                                                                        smem);
+__device__ __noinline__ void batched_item(const BlockView* __restrict__ B, const EvalParams* __restrict__ P,
+                                          int64_t e0, int64_t e1, unsigned char* smem) {
+  assemble_body<T, BS, Q, PH, Real, JAC, true, kBatchThreads, STAGE, false, false, true>(*B, *P, nullptr, e0, e1, 0,
+                                                                                        1, smem);
 }
 
 // Persistent kernel: CTAs take work items (element chunks of any block of
@@ -40,12 +44,10 @@ k_assemble_batched(const BlockView* __restrict__ views, const EvalParams* __rest
     __syncthreads();
     if (it >= n_items) break;
     const WorkItem w = items[it];
-    const BlockView B = views[w.view];
-    const EvalParams P = params[w.view];
     switch (w.kind) {
-#define TX_CASE(K, T, BS, Q, PH)                                                                 \
-  case K:                                                                                        \
-    batched_item<T, BS, Q, PH, Real, JAC, STAGE>(B, P, w.e0, w.e1, smem);                           \
+#define TX_CASE(K, T, BS, Q, PH)                                                                     \
+  case K:                                                                                            \
+    batched_item<T, BS, Q, PH, Real, JAC, STAGE>(views + w.view, params + w.view, w.e0, w.e1, smem); \
     break;
       TX_FOR_EACH_KIND(TX_CASE)
 #undef TX_CASE
