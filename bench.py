@@ -31,6 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Jacobian-assembly elems/s + SpMV GB/s on 1 GB300, mixed vs FP64 at <=1e-10 rel"
 UNIT = "elements/s"
+E2E_WINDOWS = 5
 
 
 def args():
@@ -443,26 +444,38 @@ def run_ours(a):
         for k in range(2):
             hev.step(xh, fh, Wh)
         hev.synchronize()
-        barrier()
+        # The host link is shared with the machine's other work: a window of K2 steps now and then runs at a
+        # fraction of its usual rate, so the leg times E2E_WINDOWS windows and reports the median window (every
+        # window's step time is listed beside it).
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record(stream)
-        for k in range(K2):
-            hev.step(xh, fh, Wh)
-        hev.synchronize()
-        e.record(stream)
-        barrier()
-        te = maxall(s.elapsed_time(e) / 1e3)
-        # the host link alone: the same step's bytes copied back with nothing else running (its bound)
-        s.record(stream)
-        for k in range(2):
-            fh.copy_(f, non_blocking=True)
-            Wh.copy_(W.values, non_blocking=True)
-        e.record(stream)
-        e.synchronize()
-        link_s = s.elapsed_time(e) / 2e3
+        win = []
+        for _ in range(E2E_WINDOWS):
+            barrier()
+            s.record(stream)
+            for k in range(K2):
+                hev.step(xh, fh, Wh)
+            hev.synchronize()
+            e.record(stream)
+            barrier()
+            win.append(maxall(s.elapsed_time(e) / 1e3))
+        te = sorted(win)[len(win) // 2]
+        # the host link alone: the same step's bytes copied back with nothing else running (its bound; median of
+        # three)
+        links = []
+        for _ in range(3):
+            s.record(stream)
+            for k in range(2):
+                fh.copy_(f, non_blocking=True)
+                Wh.copy_(W.values, non_blocking=True)
+            e.record(stream)
+            e.synchronize()
+            links.append(s.elapsed_time(e) / 2e3)
+        link_s = sorted(links)[1]
         d2h = 8 * N + 8 * nnz
         e2e = {"value": ws * E * K2 / te, "unit": UNIT, "h2d_bytes_per_step": 8 * N,
-               "d2h_bytes_per_step": d2h, "steps": K2,
+               "d2h_bytes_per_step": d2h, "steps": K2, "windows": E2E_WINDOWS,
+               "statistic": f"median of {E2E_WINDOWS} windows of {K2} steps",
+               "window_ms_per_step": [round(t / K2 * 1e3, 3) for t in win],
                "link_d2h_gbs": d2h / link_s / 1e9, "link_bound_frac": link_s / (te / K2),
                "path": "host x -> tx_eval(mixed) + Dirichlet -> host f and CRS values (HostEvaluator: copy-back "
                        "of step k overlapped with the assembly of step k+1)"}

@@ -66,10 +66,15 @@ def _time(fn, reps=3):
     return s.elapsed_time(e) / reps
 
 
-def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=False, verbose=False):
-    """Pick and apply the fastest configuration for ae's handle; returns it."""
+def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=False, verbose=False, x_dot=None,
+         alpha=0.0):
+    """Pick and apply the fastest configuration for ae's handle; returns it.  x_dot and alpha are timed as
+    given (the mass terms of a transient Jacobian run only with alpha != 0 or x_dot)."""
     dof = ae.dof
-    key = _key(dof, mixed, "persistent" if persistent else "block")
+    mode = "persistent" if persistent else "block"
+    if x_dot is not None or alpha != 0.0:
+        mode += "+mass"
+    key = _key(dof, mixed, mode)
     cache = _load()
     if key in cache and not force:
         cfg = cache[key]
@@ -81,8 +86,8 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
             for direct in (False, True):  # staged or per-thread Jacobian scatter
                 for ws in (128, 256, 512, 1024, 2048):
                     ae.setWorksetSize(ws, ws)
-                    t = _time(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, persistent=True,
-                                                  scatter_direct=direct), reps)
+                    t = _time(lambda: ae.evaluate(x, x_dot=x_dot, aux=aux, alpha=alpha, f=f, W=W, mixed=mixed,
+                                                  persistent=True, scatter_direct=direct), reps)
                     results.append(({"workset": ws, "grid_cap": 0, "scatter_direct": direct}, t))
         else:
             # kernel variant (warp per element / CTA-staged / CTA direct scatter / tensor-core contractions /
@@ -102,7 +107,8 @@ def tune(ae, x, f, W, mixed=True, persistent=False, aux=None, reps=3, force=Fals
                     W.initializeMatrix(0.0)
                     if f is not None:
                         f.zero_()
-                ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, scatter_direct=direct, gather=gather)
+                ae.evaluate(x, x_dot=x_dot, aux=aux, alpha=alpha, f=f, W=W, mixed=mixed, scatter_direct=direct,
+                            gather=gather)
 
             for variant, direct, gather, threads in kernels:
                 ae.setVariant(variant)

@@ -146,22 +146,25 @@ def _time_kernel(fn, prep, reps):
     return total / reps
 
 
-def _assembly_legs(w, ae, x, f, W, peak_gbs, reps, persistent=False, aux=None):
-    """FP64 and mixed R+J of one workload: each precision's tuned kernel, timed alone (zeroing outside)."""
+def _assembly_legs(w, ae, x, f, W, peak_gbs, reps, persistent=False, aux=None, x_dot=None, alpha=0.0):
+    """FP64 and mixed R+J of one workload: each precision's tuned kernel, timed alone (zeroing outside);
+    x_dot and alpha as given (a transient Jacobian's mass terms)."""
     from . import autotune
     E, N = w.n_elements, w.dof.n_dofs
     bytes_ = assembly_bytes(_lattice_vertices(w), N, w.dof.nnz, _conn_entries(w))
     out = {"elements": E, "dofs": N, "nnz": w.dof.nnz, "algorithmic_bytes": bytes_}
     for tag, mixed in (("fp64", False), ("mixed", True)):
         # per-block launches: the tuned kernel; the persistent launch keeps the workload's worksets
-        cfg = {} if persistent else autotune.tune(ae, x, f, W, mixed=mixed, aux=aux, force=True, reps=2)
+        cfg = {} if persistent else autotune.tune(ae, x, f, W, mixed=mixed, aux=aux, force=True, reps=2,
+                                                  x_dot=x_dot, alpha=alpha)
         gather = ae.gather and not persistent
 
         def prep():
             if not gather:
                 f.zero_()
                 W.initializeMatrix(0.0)
-        ms = _time_kernel(lambda: ae.evaluate(x, aux=aux, f=f, W=W, mixed=mixed, persistent=persistent), prep, reps)
+        ms = _time_kernel(lambda: ae.evaluate(x, x_dot=x_dot, aux=aux, alpha=alpha, f=f, W=W, mixed=mixed,
+                                              persistent=persistent), prep, reps)
         form = ("lattice" if gather and mixed and ae.gather_form() == "lattice" else "two-phase" if gather
                 else "persistent" if persistent else "staged" if cfg.get("variant") != 2 else "warp")
         gbs = bytes_ / ms / 1e6
@@ -227,9 +230,12 @@ def measure_configs(peak_gbs, reps=5):
     g = torch.Generator(device="cuda").manual_seed(4)
     u0 = torch.randn(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g) * 1e-3
     f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
-    r = _assembly_legs(w, ae, u0, f, W, peak_gbs, reps)
-    del f, W
-    nm = NewmarkElastodynamics(w.me, 1e-3, 0.25, 0.5, mixed=True, outer=3, inner=24)
+    # K_eff = K + c rho M, c = 1 / (beta dt^2) of the step below: the evaluation the Newmark step assembles
+    dt, nb_beta = 1e-3, 0.25
+    zero = torch.zeros_like(u0)
+    r = _assembly_legs(w, ae, u0, f, W, peak_gbs, reps, x_dot=zero, alpha=1.0 / (nb_beta * dt * dt))
+    del f, W, zero
+    nm = NewmarkElastodynamics(w.me, dt, nb_beta, 0.5, mixed=True, outer=3, inner=24)
     nm.initialize(u0)
     nm.capture()
     nm.step()
