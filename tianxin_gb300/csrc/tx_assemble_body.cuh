@@ -442,6 +442,27 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
             r[0] += w * (ga[0] * qf[0] + ga[1] * qf[1] + ga[2] * qf[2] + va[0] * qf[3] + va[1] * qf[4] + va[2] * qf[5]);
           }
         }
+        // heat Jacobian entries, k(T) W grad N_a . grad N_b + N_b W (dk/dT grad T . grad N_a): the row's point
+        // factors (k(T) W grad N_a, W dk/dT grad T . grad N_a) formed once a point, so that an entry takes four
+        // FMAs a point; in registers for small rules (the row's gradients are dead after the residual)
+        constexpr bool HCACHE = CACHE && PHYS == TX_PHYS_HEAT;
+        Real hq[HCACHE ? NQ : 1][4];
+        if constexpr (HCACHE) {
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) {
+            const Real* qf = sQF + q * NQF;
+            const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2);
+            hq[q][0] = qf[7] * g0; hq[q][1] = qf[7] * g1; hq[q][2] = qf[7] * g2;
+            hq[q][3] = g0 * qf[4] + g1 * qf[5] + g2 * qf[6];
+          }
+        }
+        auto HQ = [&](int q, int i) -> Real {
+          if constexpr (HCACHE) return hq[q][i];
+          else {
+            const Real* qf = sQF + q * NQF;
+            return i < 3 ? qf[7] * WG(q, i) : WG(q, 0) * qf[4] + WG(q, 1) * qf[5] + WG(q, 2) * qf[6];
+          }
+        };
         if constexpr (STAGE) {
           if constexpr (SCR) {  // two-phase: the element residual to scratch
 #pragma unroll
@@ -499,29 +520,41 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 // curl-curl and mass entries: the row's curl and value at q read once
                 const Real w = sW[q];
                 const R4<Real> ca = ld4(sG + q * GQS + a * 4), va = ld4(sV + q * GQS + a * 4);
+                const Real c0 = w * ca.x, c1 = w * ca.y, c2 = w * ca.z;
+                const Real v0 = w * va.x, v1 = w * va.y, v2 = w * va.z;
 #pragma unroll
                 for (int b = 0; b < NB; ++b) {
                   const R4<Real> cb = ld4(sG + q * GQS + b * 4), vb = ld4(sV + q * GQS + b * 4);
-                  kg[b] += w * (ca.x * cb.x + ca.y * cb.y + ca.z * cb.z);
-                  km[b] += w * (va.x * vb.x + va.y * vb.y + va.z * vb.z);
+                  Real sc = kg[b], sv = km[b];
+                  sc += c0 * cb.x; sc += c1 * cb.y; sc += c2 * cb.z;
+                  sv += v0 * vb.x; sv += v1 * vb.y; sv += v2 * vb.z;
+                  kg[b] = sc;
+                  km[b] = sv;
                 }
                 continue;
               }
               const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2);
               if constexpr (PHYS == TX_PHYS_HEAT) {
+                // k(T) grad N_a . grad N_b + N_b (dk/dT grad T . grad N_a): the point's factors applied to the
+                // row's gradient once, then four FMAs an entry
                 const Real* qf = sQF + q * NQF;
                 const Real k7 = qf[7], sa = g0 * qf[4] + g1 * qf[5] + g2 * qf[6];
+                const Real h0 = k7 * g0, h1 = k7 * g1, h2 = k7 * g2;
 #pragma unroll
                 for (int b = 0; b < NB; ++b) {
                   const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                  kg[b] += k7 * (g0 * gb.x + g1 * gb.y + g2 * gb.z) + gb.w * sa;
+                  Real s = kg[b];
+                  s += h0 * gb.x; s += h1 * gb.y; s += h2 * gb.z; s += sa * gb.w;
+                  kg[b] = s;
                 }
               } else {
                 const Real wn = WN(q);
 #pragma unroll
                 for (int b = 0; b < NB; ++b) {
                   const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                  kg[b] += g0 * gb.x + g1 * gb.y + g2 * gb.z;
+                  Real s = kg[b];
+                  s += g0 * gb.x; s += g1 * gb.y; s += g2 * gb.z;
+                  kg[b] = s;
                   km[b] += wn * gb.w;
                 }
               }
@@ -550,7 +583,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 #pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
                 const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                kg += WG(q, 0) * gb.x + WG(q, 1) * gb.y + WG(q, 2) * gb.z;
+                kg += WG(q, 0) * gb.x; kg += WG(q, 1) * gb.y; kg += WG(q, 2) * gb.z;
                 km += WN(q) * gb.w;
               }
               put(0, b, 0, pb, ca * kg + cm * km);
@@ -559,9 +592,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 #pragma unroll(CACHE ? NQ : 1)
               for (int q = 0; q < NQ; ++q) {
                 const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                const Real* qf = sQF + q * NQF;
-                const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2);
-                kab += qf[7] * (g0 * gb.x + g1 * gb.y + g2 * gb.z) + gb.w * (g0 * qf[4] + g1 * qf[5] + g2 * qf[6]);
+                kab += HQ(q, 0) * gb.x; kab += HQ(q, 1) * gb.y; kab += HQ(q, 2) * gb.z; kab += HQ(q, 3) * gb.w;
               }
               put(0, b, 0, pb, beta * kab);
             } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
