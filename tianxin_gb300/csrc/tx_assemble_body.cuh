@@ -395,7 +395,17 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
     __syncthreads();
     // ---------------------------------------------------------- 4 rows + scatter
     // staged form: this thread's Jacobian block-row waits in registers until
-    // every thread of the CTA has finished reading the point tables it reuses
+    // every thread of the CTA has finished reading the point tables it reuses.
+    // SYM (FP64): the element matrix of elasticity and of Poisson is
+    // symmetric (K_ba = K_ab^T), so row a forms only the blocks of b = a,
+    // a + 1, ..., a + NB / 2 (mod NB; the last one for a < NB / 2 only),
+    // NB / 2 + 1 of NB, and the staging writes each block and its transpose.
+    // The FP32 build forms every block, so that all its kernel forms (staged,
+    // coloured, direct, warp per element) give the same element matrices bit
+    // for bit; K_ab^T and a separately formed K_ba differ by rounding.
+    constexpr bool SYM = sizeof(Real) == 8 && STAGE && JAC && !TAN && !SCR && NQ <= 8 && !HC && NB % 2 == 0 &&
+                         (PHYS == TX_PHYS_ELASTICITY || PHYS == TX_PHYS_POISSON);
+    constexpr int NSLOT = SYM ? NB / 2 + 1 : NB;  // blocks a row forms
     Real kreg[STAGE && JAC ? NF * NE : 1];
     const int my_a = (valid && t < NB) ? t : -1;
     if (valid) {
@@ -573,8 +583,10 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               }
             }
           }
-#pragma unroll(STAGE ? NB : 1)
-          for (int b = 0; b < (QOUTER ? 0 : NB); ++b) {
+#pragma unroll(STAGE ? NSLOT : 1)
+          for (int sl = 0; sl < (QOUTER ? 0 : NSLOT); ++sl) {
+            if (SYM && sl == NB / 2 && a >= NB / 2) continue;  // the opposite block: formed by the lower row
+            const int b = SYM ? (a + sl < NB ? a + sl : a + sl - NB) : sl;
             const int64_t pb = (STAGE || TAN) ? 0 : (int64_t)NF * __ldg(ep + b);
             if constexpr (TAN) eb = __ldg(B.dconn + e * NB + b);
             if constexpr (PHYS == TX_PHYS_POISSON) {
@@ -587,7 +599,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 kg += WG(q, 0) * gb.x; kg += WG(q, 1) * gb.y; kg += WG(q, 2) * gb.z;
                 km += WN(q) * gb.w;
               }
-              put(0, b, 0, pb, ca * kg + cm * km);
+              if constexpr (SYM) kreg[sl] = ca * kg + cm * km;
+              else put(0, b, 0, pb, ca * kg + cm * km);
             } else if constexpr (PHYS == TX_PHYS_HEAT) {
               Real kab = 0;
 #pragma unroll(CACHE ? NQ : 1)
@@ -627,7 +640,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 for (int d = 0; d < 3; ++d) {
                   Real k = bl * Pm[3 * c + d] + bm * Pm[3 * d + c];
                   if (c == d) k += dg;
-                  put(c, b, d, pb, k);
+                  if constexpr (SYM) kreg[sl * 9 + 3 * c + d] = k;
+                  else put(c, b, d, pb, k);
                 }
             } else {  // MAXWELL
               const Real imu = pr[0], sig = pr[1];
@@ -680,10 +694,26 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
       if constexpr (JAC) {
         __syncthreads();  // point tables are dead from here: the staged rows overwrite them
         if (my_a >= 0) {
+          if constexpr (SYM) {
 #pragma unroll
-          for (int c = 0; c < NF; ++c)
+            for (int sl = 0; sl < NSLOT; ++sl) {
+              if (sl == NB / 2 && my_a >= NB / 2) continue;
+              const int b = my_a + sl < NB ? my_a + sl : my_a + sl - NB;
 #pragma unroll
-            for (int k = 0; k < NE; ++k) sK[(my_a * NF + c) * KRS + k] = kreg[c * NE + k];
+              for (int c = 0; c < NF; ++c)
+#pragma unroll
+                for (int d = 0; d < NF; ++d) {
+                  const Real v = kreg[(sl * NF + c) * NF + d];
+                  sK[(my_a * NF + c) * KRS + b * NF + d] = v;
+                  if (sl != 0) sK[(b * NF + d) * KRS + my_a * NF + c] = v;  // K_ba = K_ab^T
+                }
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < NF; ++c)
+#pragma unroll
+              for (int k = 0; k < NE; ++k) sK[(my_a * NF + c) * KRS + k] = kreg[c * NE + k];
+          }
         }
       }
       // consecutive threads take consecutive entries of an element row
