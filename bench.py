@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Jacobian-assembly elems/s + SpMV GB/s on 1 GB300, mixed vs FP64 at <=1e-10 rel"
 UNIT = "elements/s"
-E2E_WINDOWS = 5
+E2E_WINDOWS = 7
 
 
 def args():
@@ -417,6 +417,7 @@ def run_ours(a):
     # ---- solve: mixed Jacobian + FP64 matrix-free residual, block-Jacobi CG (FP32) inside FP64 refinement
     solve = None
     if not a.no_solve:
+        autotune.tune(me.ae, x, f, W, mixed=True)  # the Jacobian of the timed mixed step (the FP64 leg tuned its own)
         xsol = lof.getTpetraVector()
         me.evalModel(xsol, f=f, W=W, mixed=True)
         barrier()

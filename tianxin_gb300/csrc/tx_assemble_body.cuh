@@ -314,15 +314,20 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         Real* qf = sQF + q * NQF;
         if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
           Real u = 0, ud = 0, g[3] = {0, 0, 0};
-          for (int b = 0; b < NB; ++b) {
-            const R4<Real> gq = ld4(sG + q * GQS + b * 4);
-            const Real ub = sU[b];
-            u += gq.w * ub;
-            ud += gq.w * sUD[b];
-            g[0] += gq.x * ub;
-            g[1] += gq.y * ub;
-            g[2] += gq.z * ub;
-          }
+          // the time derivative only when one is given (its values are zeros otherwise)
+          auto values = [&](auto td) {
+            for (int b = 0; b < NB; ++b) {
+              const R4<Real> gq = ld4(sG + q * GQS + b * 4);
+              const Real ub = sU[b];
+              u += gq.w * ub;
+              if constexpr (decltype(td)::value) ud += gq.w * sUD[b];
+              g[0] += gq.x * ub;
+              g[1] += gq.y * ub;
+              g[2] += gq.z * ub;
+            }
+          };
+          if (P.xdot) values(std::true_type{});
+          else values(std::false_type{});
           if constexpr (PHYS == TX_PHYS_POISSON) {
             const Real k = pr[0], c = pr[1], m = pr[2];
             Real s = pr[3];
@@ -348,17 +353,22 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           Real Gu[9], acc[3] = {0, 0, 0};
 #pragma unroll
           for (int k = 0; k < 9; ++k) Gu[k] = 0;
-          for (int b = 0; b < NB; ++b) {
-            const R4<Real> gb = ld4(sG + q * GQS + b * 4);
+          // the acceleration only when a time derivative is given (its values are zeros otherwise)
+          auto values = [&](auto td) {
+            for (int b = 0; b < NB; ++b) {
+              const R4<Real> gb = ld4(sG + q * GQS + b * 4);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              const Real ub = sU[c * NB + b];
-              Gu[3 * c + 0] += gb.x * ub;
-              Gu[3 * c + 1] += gb.y * ub;
-              Gu[3 * c + 2] += gb.z * ub;
-              acc[c] += gb.w * sUD[c * NB + b];
+              for (int c = 0; c < 3; ++c) {
+                const Real ub = sU[c * NB + b];
+                Gu[3 * c + 0] += gb.x * ub;
+                Gu[3 * c + 1] += gb.y * ub;
+                Gu[3 * c + 2] += gb.z * ub;
+                if constexpr (decltype(td)::value) acc[c] += gb.w * sUD[c * NB + b];
+              }
             }
-          }
+          };
+          if (P.xdot) values(std::true_type{});
+          else values(std::false_type{});
           const Real tr = Gu[0] + Gu[4] + Gu[8];
           qf[0] = mu * (Gu[0] + Gu[0]) + lam * tr;  // s00
           qf[1] = mu * (Gu[4] + Gu[4]) + lam * tr;  // s11
