@@ -413,8 +413,9 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
     // The FP32 build forms every block, so that all its kernel forms (staged,
     // coloured, direct, warp per element) give the same element matrices bit
     // for bit; K_ab^T and a separately formed K_ba differ by rounding.
-    constexpr bool SYM = sizeof(Real) == 8 && STAGE && JAC && !TAN && !SCR && NQ <= 8 && !HC && NB % 2 == 0 &&
-                         (PHYS == TX_PHYS_ELASTICITY || PHYS == TX_PHYS_POISSON);
+    constexpr bool SYM = sizeof(Real) == 8 && STAGE && JAC && !TAN && !SCR && NB % 2 == 0 &&
+                         (((PHYS == TX_PHYS_ELASTICITY || PHYS == TX_PHYS_POISSON) && NQ <= 8 && !HC) ||
+                          PHYS == TX_PHYS_MAXWELL);
     constexpr int NSLOT = SYM ? NB / 2 + 1 : NB;  // blocks a row forms
     Real kreg[STAGE && JAC ? NF * NE : 1];
     const int my_a = (valid && t < NB) ? t : -1;
@@ -533,6 +534,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           // each entry's sum still runs over the points in order.
           constexpr bool QOUTER = !CACHE && (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT || PHYS == TX_PHYS_MAXWELL);
           if constexpr (QOUTER) {
+            // SYM (FP64 Maxwell): accumulator j holds the entry of b = a + j (mod NB), NB / 2 + 1 of them
             Real kg[NB], km[NB];
 #pragma unroll
             for (int b = 0; b < NB; ++b) kg[b] = km[b] = Real(0);
@@ -544,8 +546,9 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                 const Real c0 = w * ca.x, c1 = w * ca.y, c2 = w * ca.z;
                 const Real v0 = w * va.x, v1 = w * va.y, v2 = w * va.z;
 #pragma unroll
-                for (int b = 0; b < NB; ++b) {
-                  const R4<Real> cb = ld4(sG + q * GQS + b * 4), vb = ld4(sV + q * GQS + b * 4);
+                for (int b = 0; b < NSLOT; ++b) {
+                  const int bc = SYM ? (a + b < NB ? a + b : a + b - NB) : b;
+                  const R4<Real> cb = ld4(sG + q * GQS + bc * 4), vb = ld4(sV + q * GQS + bc * 4);
                   Real sc = kg[b], sv = km[b];
                   sc += c0 * cb.x; sc += c1 * cb.y; sc += c2 * cb.z;
                   sv += v0 * vb.x; sv += v1 * vb.y; sv += v2 * vb.z;
@@ -582,6 +585,10 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
             }
 #pragma unroll
             for (int b = 0; b < NB; ++b) {
+              if constexpr (SYM) {  // Maxwell: the formed entries, in accumulator order
+                if (b < NSLOT) kreg[b] = beta * (pr[0] * kg[b] + pr[1] * km[b]);
+                continue;
+              }
               const int64_t pb = (STAGE || TAN) ? 0 : (int64_t)NF * __ldg(ep + b);
               if constexpr (TAN) eb = __ldg(B.dconn + e * NB + b);
               if constexpr (PHYS == TX_PHYS_HEAT) {
