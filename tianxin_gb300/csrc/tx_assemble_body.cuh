@@ -417,15 +417,15 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
                          (((PHYS == TX_PHYS_ELASTICITY || PHYS == TX_PHYS_POISSON) && NQ <= 8 && !HC) ||
                           PHYS == TX_PHYS_MAXWELL);
     constexpr int NSLOT = SYM ? NB / 2 + 1 : NB;  // blocks a row forms
-    // HSYM (FP64 heat, point-outer rows): K_ab = S_ab + N_b . s_a with S_ab =
-    // sum_q k W grad N_a . grad N_b symmetric and s_a(q) = W dk/dT grad T .
-    // grad N_a; row a forms S for b = a, ..., a + (NB - 1) / 2 (mod NB; NB
-    // odd: every pair once) and the N_b term for every column, 69 instead of
-    // 108 FMAs a point for hex27, and the staging adds each S entry to both
-    // of its places.
-    constexpr bool HSYM = sizeof(Real) == 8 && STAGE && JAC && !TAN && !SCR && PHYS == TX_PHYS_HEAT &&
-                          !(NQ <= 8 && !HC) && NB % 2 == 1;
-    constexpr int NSH = (NB + 1) / 2;
+    // HSYM (FP64 heat): K_ab = S_ab + N_b . s_a with S_ab = sum_q k W grad
+    // N_a . grad N_b symmetric and s_a(q) = W dk/dT grad T . grad N_a; row a
+    // forms S for b = a, ..., a + NB / 2 (mod NB; for NB even the last one
+    // for a < NB / 2 only: every pair once) and the N_b term for every
+    // column (hex27: 69 instead of 108 FMAs a point; tet10: 12 x 6 + 4 x 10
+    // instead of 16 x 10 an element row), and the staging adds each S entry
+    // to both of its places.
+    constexpr bool HSYM = sizeof(Real) == 8 && STAGE && JAC && !TAN && !SCR && PHYS == TX_PHYS_HEAT;
+    constexpr int NSH = NB / 2 + 1;
     Real kreg[STAGE && JAC ? NF * NE : 1];
     Real ksym[HSYM ? NSH : 1];
     const int my_a = (valid && t < NB) ? t : -1;
@@ -646,13 +646,34 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
               if constexpr (SYM) kreg[sl] = ca * kg + cm * km;
               else put(0, b, 0, pb, ca * kg + cm * km);
             } else if constexpr (PHYS == TX_PHYS_HEAT) {
-              Real kab = 0;
+              if constexpr (HSYM) {
+                // the N_b term of every column; the rows' symmetric part once, with the first column
+                Real kn = 0;
 #pragma unroll(CACHE ? NQ : 1)
-              for (int q = 0; q < NQ; ++q) {
-                const R4<Real> gb = ld4(sG + q * GQS + b * 4);
-                kab += HQ(q, 0) * gb.x; kab += HQ(q, 1) * gb.y; kab += HQ(q, 2) * gb.z; kab += HQ(q, 3) * gb.w;
+                for (int q = 0; q < NQ; ++q) kn += HQ(q, 3) * sG[q * GQS + b * 4 + 3];
+                put(0, b, 0, pb, beta * kn);
+                if (sl == 0) {
+#pragma unroll
+                  for (int j = 0; j < NSH; ++j) {
+                    const int bc = a + j < NB ? a + j : a + j - NB;
+                    Real ks = 0;
+#pragma unroll(CACHE ? NQ : 1)
+                    for (int q = 0; q < NQ; ++q) {
+                      const R4<Real> gb = ld4(sG + q * GQS + bc * 4);
+                      ks += HQ(q, 0) * gb.x; ks += HQ(q, 1) * gb.y; ks += HQ(q, 2) * gb.z;
+                    }
+                    ksym[j] = beta * ks;
+                  }
+                }
+              } else {
+                Real kab = 0;
+#pragma unroll(CACHE ? NQ : 1)
+                for (int q = 0; q < NQ; ++q) {
+                  const R4<Real> gb = ld4(sG + q * GQS + b * 4);
+                  kab += HQ(q, 0) * gb.x; kab += HQ(q, 1) * gb.y; kab += HQ(q, 2) * gb.z; kab += HQ(q, 3) * gb.w;
+                }
+                put(0, b, 0, pb, beta * kab);
               }
-              put(0, b, 0, pb, beta * kab);
             } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
               Real Pm[9], M = 0;
 #pragma unroll
@@ -765,6 +786,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
           if (my_a >= 0) {
 #pragma unroll
             for (int j = 1; j < NSH; ++j) {
+              if (NB % 2 == 0 && j == NB / 2 && my_a >= NB / 2) continue;  // the opposite column: the lower row's
               const int b = my_a + j < NB ? my_a + j : my_a + j - NB;
               sK[my_a * KRS + b] += ksym[j];  // S_ab, and S_ba = S_ab: no other row adds to either
               sK[b * KRS + my_a] += ksym[j];
