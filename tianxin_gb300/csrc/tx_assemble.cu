@@ -10,6 +10,12 @@ namespace tx {
 namespace {
 
 // SCR: the first phase of the two-phase evaluation (element rows to scratch).
+// FP64 hex27: the reference tables and the elements' epos read from global memory (through L1) instead of
+// shared memory, which halves the CTA's shared memory (139.7 -> 97 KB) and lets two CTAs share an SM (the
+// FP32 build keeps them in shared memory: there the fourth CTA's smaller L1 cost more than it gained).
+template <typename Real>
+constexpr bool global_ref() { return sizeof(Real) == 8; }
+
 // tet10 (FP32): five CTAs an SM (at most 102 registers; it needs 96 without spills) rather than four: its
 // gathers are latency-bound, and the fifth CTA takes C3's tet10 block from 0.79 to about 0.68 ms.
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false,
@@ -20,8 +26,8 @@ __global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STA
 k_assemble(const BlockView B, const EvalParams P, const int32_t* perm, int64_t e_lo, int64_t e_hi) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
-  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, T, STAGE, TAN, SCR>(B, P, perm, e_lo, e_hi, blockIdx.x,
-                                                                              gridDim.x, smem);
+  assemble_body<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, T, STAGE, TAN, SCR, global_ref<Real>()>(
+      B, P, perm, e_lo, e_hi, blockIdx.x, gridDim.x, smem);
 }
 
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false,
@@ -29,7 +35,7 @@ template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool A
 cudaError_t launch_one(const BlockView& B, const EvalParams& P, const int32_t* perm, int64_t e_lo, int64_t e_hi,
                        cudaStream_t s, int grid_cap) {
   constexpr int T = block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>();
-  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, T, STAGE>;
+  using C = Cfg<TOPO, BASIS, NQ, PHYS, Real, T, STAGE, global_ref<Real>()>;
   auto kern = k_assemble<TOPO, BASIS, NQ, PHYS, Real, JAC, ATOMIC, STAGE, TAN, SCR>;
   static int max_blocks_per_sm = -1;
   static int num_sms = 0;
