@@ -31,8 +31,13 @@ __device__ __noinline__ void batched_item(const BlockView* __restrict__ B, const
 // FP32 staged builds ask for five resident CTAs (at most 102 registers; some
 // families' item functions then spill a little): the work items' gathers are
 // latency-bound, and the fifth CTA takes the 256-mesh batch from 7.7 to 6.8 ms.
+// FP64 builds ask for three (at most 168 registers): where shared memory
+// allows a third CTA (the 256-mesh batch: FP64 48.6 -> 47.6 ms), the FP64 pipe
+// gets a third warp a scheduler; the hex27 items' shared memory still allows
+// two.
 template <typename Real, bool JAC, bool STAGE>
-__global__ void __launch_bounds__(kBatchThreads, min_blocks<Real, STAGE>() + (sizeof(Real) == 4 && STAGE ? 1 : 0))
+__global__ void __launch_bounds__(kBatchThreads, min_blocks<Real, STAGE>() + (sizeof(Real) == 4 && STAGE ? 1 : 0) +
+                                                     (sizeof(Real) == 8 ? 2 : 0))
 k_assemble_batched(const BlockView* __restrict__ views, const EvalParams* __restrict__ params,
                    const WorkItem* __restrict__ items, int n_items, int* counter) {
   extern __shared__ __align__(16) unsigned char smem[];
