@@ -17,7 +17,7 @@ template <typename Real>
 constexpr bool global_ref() { return sizeof(Real) == 8; }
 
 // tet10 (FP32): five CTAs an SM (at most 102 registers; it needs 96 without spills) rather than four: its
-// gathers are latency-bound, and the fifth CTA takes C3's tet10 block from 0.79 to about 0.68 ms.
+// gathers are latency-bound, and the fifth CTA takes the 48^3 tet10 heat block from 0.79 to about 0.68 ms.
 template <int TOPO, int BASIS, int NQ, int PHYS, typename Real, bool JAC, bool ATOMIC, bool STAGE, bool TAN = false,
           bool SCR = false>
 __global__ void __launch_bounds__(block_threads<TOPO, BASIS, NQ, PHYS, Real, STAGE>(),

@@ -679,8 +679,8 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 #pragma unroll
               for (int k = 0; k < 9; ++k) Pm[k] = 0;
               // FP64: the mass entries only where they contribute (alpha rho != 0), one FMA in ten fewer on the
-              // FP64 pipe otherwise (C2's FP64 kernel 39.4 -> 35.7 ms with the folded coefficients below); the
-              // FP32 build keeps one loop (two cost its staged kernel 2 %)
+              // FP64 pipe otherwise (the 128^3 elasticity FP64 kernel 39.4 -> 35.7 ms with the folded coefficients
+              // below); the FP32 build keeps one loop (two cost its staged kernel 2 %)
               auto contract = [&](auto with_mass) {
 #pragma unroll(CACHE ? NQ : 1)
                 for (int q = 0; q < NQ; ++q) {

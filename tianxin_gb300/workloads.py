@@ -203,14 +203,14 @@ def measure_configs(peak_gbs, reps=5):
     from .newmark import NewmarkElastodynamics
     from .panzer import AssemblyEngine, Batch
     out = {}
-    # C1: Poisson hex8 16^3 (launch-latency bound at this size)
+    # Poisson hex8 16^3 (launch-latency bound at this size)
     w = poisson_hex8(16)
     ae, x = AssemblyEngine(w.lof), w.lof.getTpetraVector()
     x.uniform_(-1.0, 1.0)
     f, W = w.lof.getTpetraVector(), w.lof.getTpetraMatrix()
     out["poisson_hex8_16"] = _assembly_legs(w, ae, x, f, W, peak_gbs, reps)
     del w, ae, x, f, W
-    # C3: nonlinear heat, hex27 48^3 + tet10 48^3, uneven worksets in one persistent launch
+    # nonlinear heat, hex27 48^3 + tet10 48^3, uneven worksets in one persistent launch
     w = heat_hex27_tet10(48)
     ae = AssemblyEngine(w.lof)
     ae.setWorksetSize(256, 1024, seed=11)
@@ -224,7 +224,7 @@ def measure_configs(peak_gbs, reps=5):
     del w, ae, x, f, W
     gc.collect()
     torch.cuda.empty_cache()
-    # C4: elastodynamics hex8 96^3: K_eff assembly and the graph-captured Newmark step
+    # elastodynamics hex8 96^3: K_eff assembly and the graph-captured Newmark step
     w = elastodynamics_hex8(96)
     ae = AssemblyEngine(w.lof)
     g = torch.Generator(device="cuda").manual_seed(4)
@@ -251,7 +251,7 @@ def measure_configs(peak_gbs, reps=5):
     del w, ae, u0, nm
     gc.collect()
     torch.cuda.empty_cache()
-    # C5: 256 independent meshes in one persistent launch
+    # 256 independent meshes in one persistent launch
     ws = mixed_batch(256)
     g = torch.Generator(device="cuda").manual_seed(5)
     xs = [torch.rand(w.dof.n_dofs, dtype=torch.float64, device="cuda", generator=g) for w in ws]
