@@ -263,7 +263,7 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
 #pragma unroll
         for (int k = 0; k < 9; ++k) J[k] = Real(0);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
+        for (int v = 1; v < NV; ++v) {  // X[0] - X[0] = 0: vertex 0 adds nothing
           const Real dx = sDX[3 * v + 0], dy = sDX[3 * v + 1], dz = sDX[3 * v + 2];
           const Real* gg = r_geo_grad + (q * NV + v) * 3;
 #pragma unroll
@@ -461,12 +461,13 @@ __device__ __forceinline__ void assemble_body(const BlockView& B, const EvalPara
         for (int q = 0; q < NQ; ++q) {
           const Real* qf = sQF + q * NQF;
           if constexpr (PHYS == TX_PHYS_POISSON || PHYS == TX_PHYS_HEAT) {
-            r[0] += WG(q, 0) * qf[0] + WG(q, 1) * qf[1] + WG(q, 2) * qf[2] + WN(q) * qf[3];
+            // FMA chains: four operations a point and row instead of five
+            r[0] += WG(q, 0) * qf[0]; r[0] += WG(q, 1) * qf[1]; r[0] += WG(q, 2) * qf[2]; r[0] += WN(q) * qf[3];
           } else if constexpr (PHYS == TX_PHYS_ELASTICITY) {
             const Real g0 = WG(q, 0), g1 = WG(q, 1), g2 = WG(q, 2), n = WN(q);
-            r[0] += g0 * qf[0] + g1 * qf[3] + g2 * qf[4] + n * qf[6];
-            r[1] += g0 * qf[3] + g1 * qf[1] + g2 * qf[5] + n * qf[7];
-            r[2] += g0 * qf[4] + g1 * qf[5] + g2 * qf[2] + n * qf[8];
+            r[0] += g0 * qf[0]; r[0] += g1 * qf[3]; r[0] += g2 * qf[4]; r[0] += n * qf[6];
+            r[1] += g0 * qf[3]; r[1] += g1 * qf[1]; r[1] += g2 * qf[5]; r[1] += n * qf[7];
+            r[2] += g0 * qf[4]; r[2] += g1 * qf[5]; r[2] += g2 * qf[2]; r[2] += n * qf[8];
           } else {
             const Real w = sW[q];
             const Real* ga = sG + q * GQS + a * 4;
