@@ -60,6 +60,20 @@ def dist_env():
     return ws, rank, local
 
 
+def e2e_summary(windows_s, links_s, steps, elements, h2d, d2h):
+    """The e2e object from the timed windows (seconds for `steps` steps each, max over ranks) and the link-only
+    copies (seconds per step's copy-back): the median window is the value, every window is listed."""
+    te = sorted(windows_s)[len(windows_s) // 2]
+    link_s = sorted(links_s)[len(links_s) // 2]
+    return {"value": elements * steps / te, "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": steps, "windows": len(windows_s),
+            "statistic": f"median of {len(windows_s)} windows of {steps} steps",
+            "window_ms_per_step": [round(t / steps * 1e3, 3) for t in windows_s],
+            "link_d2h_gbs": d2h / link_s / 1e9, "link_bound_frac": link_s / (te / steps),
+            "path": "host x -> tx_eval(mixed) + Dirichlet -> host f and CRS values (HostEvaluator: copy-back "
+                    "of step k overlapped with the assembly of step k+1)"}
+
+
 def workload_desc(n):
     return {"workload": f"elasticity hex8 {n}^3 (E=1, nu=0.3, b=(0,0,-1), clamp z=0, 2x2x2 Gauss, jitter 0.05h)",
             "elements": n ** 3, "dofs": 3 * (n + 1) ** 3, "nnz": 9 * (3 * n + 1) ** 3}
@@ -459,7 +473,6 @@ def run_ours(a):
             e.record(stream)
             barrier()
             win.append(maxall(s.elapsed_time(e) / 1e3))
-        te = sorted(win)[len(win) // 2]
         # the host link alone: the same step's bytes copied back with nothing else running (its bound; median of
         # three)
         links = []
@@ -471,15 +484,7 @@ def run_ours(a):
             e.record(stream)
             e.synchronize()
             links.append(s.elapsed_time(e) / 2e3)
-        link_s = sorted(links)[1]
-        d2h = 8 * N + 8 * nnz
-        e2e = {"value": ws * E * K2 / te, "unit": UNIT, "h2d_bytes_per_step": 8 * N,
-               "d2h_bytes_per_step": d2h, "steps": K2, "windows": E2E_WINDOWS,
-               "statistic": f"median of {E2E_WINDOWS} windows of {K2} steps",
-               "window_ms_per_step": [round(t / K2 * 1e3, 3) for t in win],
-               "link_d2h_gbs": d2h / link_s / 1e9, "link_bound_frac": link_s / (te / K2),
-               "path": "host x -> tx_eval(mixed) + Dirichlet -> host f and CRS values (HostEvaluator: copy-back "
-                       "of step k overlapped with the assembly of step k+1)"}
+        e2e = e2e_summary(win, links, K2, ws * E, 8 * N, 8 * N + 8 * nnz)
         del Wh, hev
 
     # the mixed path against the FP64 path at full size (after the timed legs): both Jacobians (FP32 element

@@ -34,3 +34,19 @@ def test_reference_arm_line():
 def test_reference_arm_other_ranks_are_silent():
     p = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert p.returncode == 0 and not p.stdout.strip()
+
+
+def test_e2e_summary_takes_the_median_window():
+    # seven windows of five steps, two of them slowed by other traffic on the host link: the median window sets
+    # the value, every window is listed, the link-only copy is the median of its samples
+    import bench
+    steps, elements, h2d, d2h = 5, 2_097_152, 51_520_536, 4_160_317_536
+    win = [0.1105, 0.1105, 0.2930, 0.1104, 0.1105, 0.2956, 0.1106]
+    links = [0.0215, 0.0780, 0.0216]
+    d = bench.e2e_summary(win, links, steps, elements, h2d, d2h)
+    assert d["value"] == elements * steps / 0.1105 and d["unit"] == bench.UNIT
+    assert d["windows"] == 7 and d["steps"] == 5 and d["statistic"] == "median of 7 windows of 5 steps"
+    assert d["window_ms_per_step"] == [22.1, 22.1, 58.6, 22.08, 22.1, 59.12, 22.12]
+    assert d["h2d_bytes_per_step"] == h2d and d["d2h_bytes_per_step"] == d2h
+    assert abs(d["link_d2h_gbs"] - d2h / 0.0216 / 1e9) < 1e-9
+    assert abs(d["link_bound_frac"] - 0.0216 / (0.1105 / 5)) < 1e-12
