@@ -215,10 +215,11 @@ int tx_graph_build(tx_handle h, int64_t* rowptr, int32_t* colind);
  * gather -> IntegrationValues2/BasisValues2 -> integrators -> scatter.
  * crs_vals == NULL gives the Residual evaluation type.  Uses the handle's
  * graph (rowptr/colind of tx_graph_build).  In FP64 (without TX_EVAL_MIXED)
- * the element matrices of elasticity, Poisson and Nedelec Maxwell blocks are
- * formed symmetric: block (b, a) is the transpose of block (a, b) bit for
- * bit, so the assembled Jacobian is symmetric up to the order of the FP64
- * sums into each entry. */
+ * with the staged scatter (without TX_EVAL_SCATTER_DIRECT) the element
+ * matrices of elasticity, Poisson and Nedelec Maxwell blocks are formed
+ * symmetric: block (b, a) is the transpose of block (a, b) bit for bit, so
+ * the assembled Jacobian is symmetric up to the order of the FP64 sums into
+ * each entry. */
 int tx_eval(tx_handle h, const tx_eval_args* args);
 
 /* *supported = 1 when TX_EVAL_GATHER holds this handle's rows (after
